@@ -1,0 +1,196 @@
+"""Seeded synthetic workloads for the batched narrowphase.
+
+Every random number comes from ``Generator(Philox(seed)).random()`` and is
+transformed here (Box-Muller, Shoemake quaternions, inverse CDFs), so a seed
+gives the same batch on every numpy version and host.
+
+Workloads (sizes as the project's benchmark configurations state them):
+
+* ``plain_small``   4096 convex pairs, hulls of 32 points on the unit sphere
+  scaled by r ~ U[0.05, 0.5] m, translation uniform in a 1 m cube, uniform
+  random rotation.
+* ``mixed``         pairs of shapes drawn uniformly from box / sphere /
+  capsule / cylinder / convex; half extents, radii and half lengths
+  ~ U[0.02, 0.4] m; convex hulls of V ~ log-uniform[8, 256] sphere points;
+  about 40 % of the pairs overlap.
+* ``pareto``        convex pairs with V ~ Pareto(alpha = 1.5, x_m = 4) clipped
+  to [4, 1024]; about 30 % overlap.
+
+Overlap control: the translation of shape b is a uniform direction times
+g * (rho_a + rho_b), rho the bounding-sphere radius and g ~ U[0, g_max]; g_max
+was calibrated once with the FP64 oracle so that the overlap fraction lands on
+the target (the achieved fraction is measured and reported by the bench).
+"""
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .layout import BOX, CAPSULE, CONVEX, CYLINDER, PAIR_DTYPE, SHAPE_DTYPE, SPHERE
+
+SEED_BASE = 20240611
+MIXED_G_MAX = 1.92   # calibrated: 40 % overlap on the mixed workload
+PARETO_G_MAX = 1.66  # calibrated: 30 % overlap on the pareto workload
+
+
+@dataclass
+class Batch:
+    name: str
+    shapes: np.ndarray           # SHAPE_DTYPE [n_shapes]
+    vertices: np.ndarray         # float32 [n_vertices, 4] (x, y, z, 0)
+    pairs: np.ndarray            # PAIR_DTYPE [n_pairs]
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def n_pairs(self):
+        return len(self.pairs)
+
+    def subset(self, idx):
+        """Pairs ``idx`` with only the shapes and vertices they use, re-indexed."""
+        idx = np.asarray(idx)
+        p = self.pairs[idx].copy()
+        used = np.unique(np.concatenate([p["shape_a"], p["shape_b"]]))
+        remap = np.full(len(self.shapes), -1, np.int64)
+        remap[used] = np.arange(len(used))
+        s = self.shapes[used].copy()
+        counts = s["vert_count"].astype(np.int64)
+        is_cvx = s["type"] == CONVEX
+        counts[~is_cvx] = 0
+        new_off = np.concatenate([[0], np.cumsum(counts)[:-1]])
+        chunks = [self.vertices[o:o + c] for o, c in zip(s["vert_offset"].astype(np.int64), counts) if c > 0]
+        verts = np.concatenate(chunks) if chunks else np.zeros((0, 4), np.float32)
+        s["vert_offset"] = np.where(is_cvx, new_off, 0)
+        p["shape_a"] = remap[p["shape_a"]]
+        p["shape_b"] = remap[p["shape_b"]]
+        return Batch(self.name + "[subset]", s, np.ascontiguousarray(verts, np.float32), p, dict(self.meta))
+
+
+def _rng(seed):
+    return np.random.Generator(np.random.Philox(seed))
+
+
+def _normals(rng, shape):
+    """Standard normals by Box-Muller from uniforms."""
+    n = int(np.prod(shape))
+    m = (n + 1) // 2
+    u1 = rng.random(m)
+    u2 = rng.random(m)
+    rad = np.sqrt(-2.0 * np.log1p(-u1))
+    z = np.concatenate([rad * np.cos(2 * np.pi * u2), rad * np.sin(2 * np.pi * u2)])[:n]
+    return z.reshape(shape)
+
+
+def unit_vectors(rng, n):
+    v = _normals(rng, (n, 3))
+    nrm = np.linalg.norm(v, axis=1, keepdims=True)
+    nrm[nrm == 0] = 1.0
+    return v / nrm
+
+
+def random_rotations(rng, n):
+    """Uniform random rotations (Shoemake's quaternion method), row-major 3x3."""
+    u1, u2, u3 = rng.random(n), rng.random(n), rng.random(n)
+    a, b = np.sqrt(1 - u1), np.sqrt(u1)
+    x, y = a * np.sin(2 * np.pi * u2), a * np.cos(2 * np.pi * u2)
+    z, w = b * np.sin(2 * np.pi * u3), b * np.cos(2 * np.pi * u3)
+    R = np.empty((n, 9))
+    R[:, 0] = 1 - 2 * (y * y + z * z)
+    R[:, 1] = 2 * (x * y - z * w)
+    R[:, 2] = 2 * (x * z + y * w)
+    R[:, 3] = 2 * (x * y + z * w)
+    R[:, 4] = 1 - 2 * (x * x + z * z)
+    R[:, 5] = 2 * (y * z - x * w)
+    R[:, 6] = 2 * (x * z - y * w)
+    R[:, 7] = 2 * (y * z + x * w)
+    R[:, 8] = 1 - 2 * (x * x + y * y)
+    return R
+
+
+def log_uniform_counts(rng, n, lo, hi):
+    u = rng.random(n)
+    v = np.floor(np.exp(np.log(lo) + u * (np.log(hi + 1) - np.log(lo)))).astype(np.int64)
+    return np.clip(v, lo, hi)
+
+
+def pareto_counts(rng, n, alpha=1.5, xm=4, hi=1024):
+    u = rng.random(n)
+    v = np.floor(xm * (1.0 - u) ** (-1.0 / alpha)).astype(np.int64)
+    return np.clip(v, xm, hi)
+
+
+def _make_shapes(rng, types, lo, hi, counts):
+    """Shapes of the given types; convex hull vertex counts from ``counts``."""
+    n = len(types)
+    s = np.zeros(n, SHAPE_DTYPE)
+    s["type"] = types
+    half = rng.random((n, 3)) * (hi - lo) + lo
+    r = rng.random(n) * (hi - lo) + lo
+    hl = rng.random(n) * (hi - lo) + lo
+    rho = np.zeros(n)
+    isb, iss, isc, isy, isx = (types == t for t in (BOX, SPHERE, CAPSULE, CYLINDER, CONVEX))
+    s["param"][isb, :3] = 2 * half[isb]
+    rho[isb] = np.linalg.norm(half[isb], axis=1)
+    s["param"][iss, 0] = r[iss]
+    rho[iss] = r[iss]
+    s["param"][isc, 0] = r[isc]
+    s["param"][isc, 1] = 2 * hl[isc]
+    rho[isc] = r[isc] + hl[isc]
+    s["param"][isy, 0] = r[isy]
+    s["param"][isy, 1] = 2 * hl[isy]
+    rho[isy] = np.sqrt(r[isy] ** 2 + hl[isy] ** 2)
+    rho[isx] = r[isx]
+    cvx_idx = np.nonzero(isx)[0]
+    cnt = np.zeros(n, np.int64)
+    cnt[cvx_idx] = counts(len(cvx_idx))
+    off = np.concatenate([[0], np.cumsum(cnt)[:-1]])
+    s["vert_offset"] = np.where(isx, off, 0)
+    s["vert_count"] = cnt
+    nv = int(cnt.sum())
+    verts = np.zeros((nv, 4), np.float32)
+    if nv:
+        pts = unit_vectors(rng, nv) * np.repeat(r, cnt)[:, None]
+        verts[:, :3] = pts
+        # interior point (vertex mean) for MPR-style queries, in param[0:3]
+        sums = np.add.reduceat(verts[:, :3].astype(np.float64), off[cvx_idx], axis=0)
+        s["param"][cvx_idx, :3] = sums / cnt[cvx_idx, None]
+    s["param"][:, 3] = rho
+    return s, verts, rho
+
+
+def _pairs(rng, n, rho, translation):
+    p = np.zeros(n, PAIR_DTYPE)
+    p["shape_a"] = np.arange(0, 2 * n, 2)
+    p["shape_b"] = np.arange(1, 2 * n, 2)
+    p["rot"] = random_rotations(rng, n)
+    if translation == "cube":
+        p["trans"] = rng.random((n, 3)) - 0.5
+    else:
+        g_max = float(translation)
+        d = unit_vectors(rng, n)
+        g = rng.random(n) * g_max
+        p["trans"] = d * (g * (rho[0::2] + rho[1::2]))[:, None]
+    return p
+
+
+def plain_small(n_pairs=4096, seed=SEED_BASE + 0):
+    rng = _rng(seed)
+    types = np.full(2 * n_pairs, CONVEX, np.int32)
+    s, v, rho = _make_shapes(rng, types, 0.05, 0.5, lambda k: np.full(k, 32, np.int64))
+    p = _pairs(rng, n_pairs, rho, "cube")
+    return Batch("plain_small", s, v, p, {"seed": seed, "vertices_per_hull": 32})
+
+
+def mixed(n_pairs=1_000_000, seed=SEED_BASE + 1, g_max=MIXED_G_MAX):
+    rng = _rng(seed)
+    choice = np.array([BOX, SPHERE, CAPSULE, CYLINDER, CONVEX], np.int32)
+    types = choice[np.minimum((rng.random(2 * n_pairs) * 5).astype(np.int64), 4)]
+    s, v, rho = _make_shapes(rng, types, 0.02, 0.4, lambda k: log_uniform_counts(rng, k, 8, 256))
+    p = _pairs(rng, n_pairs, rho, g_max)
+    return Batch("mixed", s, v, p, {"seed": seed, "g_max": g_max})
+
+
+def pareto(n_pairs=4_000_000, seed=SEED_BASE + 4, g_max=PARETO_G_MAX):
+    rng = _rng(seed)
+    types = np.full(2 * n_pairs, CONVEX, np.int32)
+    s, v, rho = _make_shapes(rng, types, 0.02, 0.4, lambda k: pareto_counts(rng, k))
+    p = _pairs(rng, n_pairs, rho, g_max)
+    return Batch("pareto", s, v, p, {"seed": seed, "g_max": g_max})

@@ -1,0 +1,149 @@
+"""ORACLE — test infrastructure only.
+
+ctypes access to the FP64 CPU restatement of mind-fcl's convex query engine
+(oracle/orc_convex.hpp, built into oracle/liboracle.so) and, where it was
+built, to the reference itself (oracle/_ref/libfcl_ref.so, see
+oracle/build_ref.sh).  Only tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline leg import this package; the product never does.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libfcl_ref.so")
+
+RESULT_DTYPE = np.dtype(
+    [("distance", "<f8"), ("p0", "<f8", (3,)), ("p1", "<f8", (3,)), ("normal", "<f8", (3,)),
+     ("ok", "<i4"), ("gjk_status", "<i4"), ("epa_status", "<i4"), ("gjk_iters", "<i4"),
+     ("epa_iters", "<i4"), ("reserved", "<i4")]
+)
+assert RESULT_DTYPE.itemsize == 104
+
+_CXXFLAGS = ["-O3", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared"]
+
+
+def build(force=False):
+    """Compile the restatement (always) and the reference driver (only where the
+    reference sources exist)."""
+    srcs = [os.path.join(HERE, f) for f in ("oracle.cpp", "orc_convex.hpp", "orc_mesh.hpp") if
+            os.path.exists(os.path.join(HERE, f))]
+    if force or not os.path.exists(LIB_PATH) or any(os.path.getmtime(s) > os.path.getmtime(LIB_PATH) for s in srcs):
+        subprocess.check_call(["g++", *_CXXFLAGS, os.path.join(HERE, "oracle.cpp"), "-o", LIB_PATH, "-lpthread"])
+    ref_root = os.environ.get("REF_ROOT", "/root/reference")
+    if os.path.isdir(os.path.join(ref_root, "include", "fcl", "cvx_collide")):
+        subprocess.check_call(["bash", os.path.join(HERE, "build_ref.sh")])
+
+
+_lib = None
+_ref = None
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        lib = ctypes.CDLL(LIB_PATH)
+        vp, i, d = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+        lib.orc_signed_distance.argtypes = [vp, i, vp, vp, i, vp, vp, i, i, d, i, i, d]
+        lib.orc_signed_distance.restype = i
+        lib.orc_collide.argtypes = [vp, i, vp, vp, i, i, vp, i]
+        lib.orc_collide.restype = i
+        lib.orc_time_signed_distance.argtypes = [vp, i, vp, vp, i, vp, i]
+        lib.orc_time_signed_distance.restype = d
+        if hasattr(lib, "orc_mesh_collide"):
+            lib.orc_mesh_collide.restype = i
+        _lib = lib
+    return _lib
+
+
+def ref_available():
+    return os.path.exists(REF_PATH)
+
+
+def _load_ref():
+    global _ref
+    if _ref is None:
+        lib = ctypes.CDLL(REF_PATH)
+        vp, i = ctypes.c_void_p, ctypes.c_int
+        lib.ref_signed_distance.argtypes = [vp, i, vp, vp, i, vp, vp, i]
+        lib.ref_signed_distance.restype = i
+        lib.ref_collide.argtypes = [vp, i, vp, vp, i, i, vp, i]
+        lib.ref_collide.restype = i
+        _ref = lib
+    return _ref
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def _prep(batch):
+    s = np.ascontiguousarray(batch.shapes)
+    v = np.ascontiguousarray(batch.vertices, np.float32)
+    if len(v) == 0:
+        v = np.zeros((1, 4), np.float32)
+    p = np.ascontiguousarray(batch.pairs)
+    return s, v, p
+
+
+def default_threads():
+    return max(1, os.cpu_count() or 1)
+
+
+def signed_distance(batch, guess=None, threads=None, gjk_max_iter=0, gjk_tol=0.0, epa_max_faces=0,
+                    epa_max_iter=0, epa_tol=0.0):
+    """GJKSolver::shapeSignedDistance per pair (restatement)."""
+    lib = _load()
+    s, v, p = _prep(batch)
+    out = np.zeros(len(p), RESULT_DTYPE)
+    g = None if guess is None else np.ascontiguousarray(guess, np.float32)
+    rc = lib.orc_signed_distance(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), _ptr(g), _ptr(out),
+                                 threads or default_threads(), gjk_max_iter, gjk_tol, epa_max_faces, epa_max_iter,
+                                 epa_tol)
+    assert rc == 0
+    return out
+
+
+def collide(batch, want_contact=False, threads=None):
+    """fcl::collide on convex pairs (restatement): MPR boolean, or GJK+EPA contact."""
+    lib = _load()
+    s, v, p = _prep(batch)
+    out = np.zeros(len(p), RESULT_DTYPE)
+    rc = lib.orc_collide(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), int(want_contact), _ptr(out),
+                         threads or default_threads())
+    assert rc == 0
+    return out
+
+
+def time_signed_distance(batch, threads=None):
+    """Seconds the restatement takes for the whole batch (wall clock, C++ side)."""
+    lib = _load()
+    s, v, p = _prep(batch)
+    out = np.zeros(len(p), RESULT_DTYPE)
+    return lib.orc_time_signed_distance(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), _ptr(out),
+                                        threads or default_threads()), out
+
+
+def ref_signed_distance(batch, guess=None, threads=None):
+    """The reference's own GJK/EPA (oracle/_ref) on the same inputs."""
+    lib = _load_ref()
+    s, v, p = _prep(batch)
+    out = np.zeros(len(p), RESULT_DTYPE)
+    g = None if guess is None else np.ascontiguousarray(guess, np.float32)
+    assert lib.ref_signed_distance(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), _ptr(g), _ptr(out),
+                                   threads or default_threads()) == 0
+    return out
+
+
+def ref_collide(batch, want_contact=False, threads=None):
+    lib = _load_ref()
+    s, v, p = _prep(batch)
+    out = np.zeros(len(p), RESULT_DTYPE)
+    assert lib.ref_collide(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), int(want_contact), _ptr(out),
+                           threads or default_threads()) == 0
+    return out
