@@ -1,0 +1,294 @@
+"""Benchmark: batched signed-distance queries (GJK distance + EPA penetration)
+on the mixed-primitive workload — 1M pairs of sphere / box / capsule /
+cylinder / convex shapes (convex hulls of log-uniform 8..256 sphere points,
+sizes U[0.02, 0.4] m, ~40 % overlapping) — on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+A step is one signed-distance query over the whole batch: the GJK pass over
+all pairs, then the EPA pass over the overlapping ones.  ``value`` times steps
+with the pairs and shapes already in HBM (the device entry point);
+``e2e`` times the host entry point (fclg_distance) from pinned host memory,
+H2D of the pair list and D2H of the results included, shapes uploaded once
+beforehand as a caller constructs its geometry objects once.  The inputs
+(~0.6 GB of pairs, shapes and hull vertices) exceed the 129 MB L2, so no L2
+flush is needed between steps.
+
+``--impl reference`` times the reference's CPU implementation of the same
+query (its GJKSolver::shapeSignedDistance path) on the host cores: the
+FP64 restatement in oracle/, which is bit-identical to the reference's own
+GJK / EPA (tests/test_oracle.py), on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "mind-fcl_gb300"))
+
+import numpy as np  # noqa: E402
+
+BASELINE_METRIC = "convex pair queries/s (GJK+EPA) & BVH collides/s, warm-start vs plain, 1 GB300"
+UNIT = "pair queries/s"
+N_PAIRS = 1_000_000
+# compulsory bytes per query of this workload: hull vertices (12 B each) of the
+# convex shapes, 16 B of parameters per primitive, 48 B pose, 2 x 8 B shape
+# descriptors and a 64 B result record, averaged over the shape mix
+ALGO_BYTES_PER_QUERY = 498.0
+CPU_SAMPLE_PAIRS = 100_000
+WORKLOAD = ("mixed primitive batch: 1M pairs of sphere/box/capsule/cylinder/convex (convex V log-uniform "
+            "[8,256]), sizes U[0.02,0.4] m, ~40% overlap; GJK distance for separated pairs, EPA depth + "
+            "normal for overlapping pairs")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="fclg", choices=["fclg", "reference"])
+    ap.add_argument("--pairs", type=int, default=N_PAIRS)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(batch, threads):
+    """The reference CPU path (FP64 restatement) on a bounded sample, all host threads."""
+    import oracle
+    oracle.build()
+    sample = batch.subset(np.arange(min(CPU_SAMPLE_PAIRS, batch.n_pairs)))
+    oracle.signed_distance(sample.subset(np.arange(2000)), threads=threads)  # warm the code path
+    secs, _ = oracle.time_signed_distance(sample, threads=threads)
+    return sample.n_pairs / secs, sample.n_pairs, secs
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    from fclg import workloads
+    batch = workloads.mixed(args.pairs)
+    threads = os.cpu_count() or 1
+    import oracle
+    oracle.build()
+    sample = batch.subset(np.arange(min(CPU_SAMPLE_PAIRS // 2, batch.n_pairs)))
+    for _ in range(max(args.warmup, 1)):
+        oracle.time_signed_distance(sample.subset(np.arange(min(5000, sample.n_pairs))), threads=threads)
+    total = 0.0
+    for _ in range(args.steps):
+        secs, _ = oracle.time_signed_distance(sample, threads=threads)
+        total += secs
+    value = sample.n_pairs * args.steps / total
+    line = {
+        "impl": "reference", "metric": BASELINE_METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "pairs_per_step": sample.n_pairs, "seed": batch.meta["seed"]},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "first %d pairs of the 1M mixed batch per step" % sample.n_pairs},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+
+    from fclg import workloads
+    from fclg.api import Context
+    batch = workloads.mixed(args.pairs, seed=workloads.SEED_BASE + 1 + rank)  # weak scaling: own batch per rank
+    n = batch.n_pairs
+    ctx = Context(local)
+    ctx.set_batch(batch)
+    stream = torch.cuda.current_stream(dev)
+    d_pairs = torch.from_numpy(batch.pairs.view(np.uint8).copy()).to(dev)
+    d_res = torch.empty(n * 48, dtype=torch.uint8, device=dev)
+
+    def step():
+        ctx.distance_device(d_pairs.data_ptr(), n, d_res.data_ptr(), None, stream.cuda_stream)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+
+    # ---- device-resident throughput (value)
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    launches0 = ctx.launch_count
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    launches = ctx.launch_count - launches0
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = n * world / (ms * 1e-3)
+
+    # ---- per-pass kernel times for the roofline (same steps, events on the launch stream)
+    ctx.set_profiling(True)
+    ctx.pass_times(reset=True)
+    for _ in range(max(3, args.steps // 2)):
+        step()
+    torch.cuda.synchronize(dev)
+    gjk_ms, epa_ms, nq = ctx.pass_times(reset=True)
+    ctx.set_profiling(False)
+    gjk_ms /= max(nq, 1)
+    epa_ms /= max(nq, 1)
+    res = d_res.cpu().numpy().view(np.dtype([("distance", "<f4"), ("rest", "V44")]))
+    overlap = float(np.mean(res["distance"] < 0))
+
+    # ---- end to end through the host entry point, pinned buffers
+    h_pairs = torch.from_numpy(batch.pairs.view(np.uint8).copy()).pin_memory()
+    h_res = torch.empty(n * 48, dtype=torch.uint8).pin_memory()
+    lib = ctx.lib
+    import ctypes
+
+    def e2e_step():
+        rc = lib.fclg_distance(ctx.h, ctypes.c_void_p(h_pairs.data_ptr()), n, None, ctypes.c_void_p(h_res.data_ptr()))
+        if rc != 0:
+            raise RuntimeError("fclg_distance failed: %s" % lib.fclg_last_error(ctx.h).decode())
+
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    barrier()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = n * world / (e2e_ms * 1e-3)
+
+    if rank == 0:
+        peak, peak_kind = peaks()
+        dominant = "epa_pass" if epa_ms >= gjk_ms else "gjk_pass"
+        # algorithmic bytes of the whole query per step over the dominant pass time and over the step
+        achieved = ALGO_BYTES_PER_QUERY * n / (max(gjk_ms, epa_ms) * 1e-3) / 1e9
+        threads = os.cpu_count() or 1
+        cpu_v, cpu_n, cpu_s = cpu_baseline(batch, threads)
+        line = {
+            "metric": BASELINE_METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (FP64 EPA face solve, GJK tetrahedron tests)",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "pairs_per_gpu": n, "overlap_fraction": overlap,
+                       "seed": batch.meta["seed"], "l2": "inputs larger than L2 (no flush)",
+                       "gjk_pass_ms": gjk_ms, "epa_pass_ms": epa_ms},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "kernel": dominant,
+                         "peak_source": peak_kind,
+                         "algorithmic_bytes": "498 B/query x %d queries per launch" % n},
+            "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": "first %d pairs of the batch, FP64 restatement (%.2f s)" % (cpu_n, cpu_s)},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 64, "d2h_bytes_per_step": n * 48},
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line))
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,154 @@
+/*
+ * fclg — batched narrowphase for one GB300 (sm_103a): the C ABI.
+ *
+ * Replaces, for batches of shape pairs, the reference's per-pair narrowphase
+ * entry points (paths relative to the mind-fcl project root):
+ *   fcl::collide(geom1, tf1, geom2, tf2, CollisionRequest, CollisionResult&)
+ *       include/fcl/narrowphase/collision.h:54-58,
+ *       include/fcl/narrowphase/collision_interface-inl.h:13-32
+ *   detail::GJKSolver<S>::shapeSignedDistance / shapeIntersect
+ *       include/fcl/narrowphase/detail/gjk_solver.h:53-177,
+ *       include/fcl/narrowphase/detail/gjk_solver-inl.h:70-148, 810-874
+ *   fcl::collide on two BVHModel<OBBRSS> (OrientedNodeBVHSolver::MeshIntersect)
+ *       include/fcl/narrowphase/detail/traversal/collision/bvh_solver-inl.h:74-164
+ *
+ * Conventions
+ *   - Plain pointers and sizes only.  Every function returns FCLG_OK (0) or a
+ *     negative FCLG_E_* code; fclg_last_error() describes the last failure of
+ *     a context.  A context is used by one host thread at a time.
+ *   - Shape records follow the fcl geometry classes (Box stores full side
+ *     lengths, Capsule / Cylinder radius and full length lz); type codes are
+ *     the reference's GJKShapeType values (cvx_collide/gjk_shape.h:9-28).
+ *   - A pair carries the pose of shape b expressed in shape a's frame
+ *     (MinkowskiDiff::toshape0, gjk_solver-inl.h:84-85); every output point
+ *     and normal is in shape a's frame.
+ *   - Tolerances and limits default to what fcl::collide hands the solver
+ *     (collision_request-inl.h:54-60, gjk_solver-inl.h:1120-1130).
+ *   - *_device entry points take device pointers and a cudaStream_t (as
+ *     void*) and are asynchronous; the others take host pointers and return
+ *     when the results are in host memory.
+ */
+#ifndef FCLG_H_
+#define FCLG_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  FCLG_OK = 0,
+  FCLG_E_INVALID = -1,      /* bad argument (null pointer, index out of range, bad size) */
+  FCLG_E_CUDA = -2,         /* a CUDA call failed; see fclg_last_error */
+  FCLG_E_NO_SHAPES = -3,    /* query before fclg_set_shapes */
+  FCLG_E_NO_DEVICE = -4,    /* no usable sm_103 device */
+  FCLG_E_TOO_LARGE = -5     /* batch exceeds a fixed capacity */
+};
+
+/* GJKShapeType values, cvx_collide/gjk_shape.h:9-28 */
+enum { FCLG_BOX = 0, FCLG_SPHERE = 1, FCLG_CAPSULE = 3, FCLG_CYLINDER = 5, FCLG_CONVEX = 100 };
+
+typedef struct fclg_shape { /* 32 bytes */
+  int32_t type;
+  uint32_t vert_offset;  /* convex: first vertex in the vertex pool */
+  uint32_t vert_count;   /* convex: number of hull vertices */
+  uint32_t reserved;
+  float param[4];        /* box: side x, y, z; sphere: radius; capsule, cylinder: radius, lz;
+                            convex: interior point (vertex mean) x, y, z; [3]: bounding radius */
+} fclg_shape;
+
+typedef struct fclg_pair { /* 64 bytes */
+  uint32_t shape_a, shape_b;
+  float rot[9];          /* rotation of b's frame in a's frame, row-major */
+  float trans[3];        /* origin of b in a's frame */
+  uint32_t flags, reserved;
+} fclg_pair;
+
+typedef struct fclg_result { /* 48 bytes */
+  float distance;        /* signed: separation > 0, -penetration depth < 0 */
+  float normal[3];       /* unit; moving b along +normal increases the signed distance.  When
+                            penetrating this is normalize(p_a - p_b), the reference's contact
+                            normal (gjk_solver-inl.h:117-121) */
+  float p_a[3];          /* witness point on a */
+  float p_b[3];          /* witness point on b */
+  int32_t status;        /* bits 0-7 GJK_Status (cvx_collide/gjk.h:13-28); bits 8-15 EPA_Status+1
+                            (cvx_collide/epa.h:14), 0 when EPA did not run */
+  uint16_t iterations;   /* GJK (+distance) iterations, plus EPA expansions */
+  uint8_t collide;       /* boolean collide flag */
+  uint8_t ok;            /* the query produced a valid distance (shapeSignedDistance's return) */
+} fclg_result;
+
+typedef struct fclg_request {
+  uint32_t gjk_max_iterations;  /* 0: 128 */
+  uint32_t epa_max_faces;       /* 0: 256 (GJKSolver::epa_max_face_num) */
+  uint32_t epa_max_iterations;  /* 0: 255 */
+  uint32_t flags;               /* FCLG_REQ_* */
+  float gjk_tolerance;          /* 0: 1e-6 (CollisionRequest::binaryCollisionTolerance) */
+  float epa_tolerance;          /* 0: 1e-6 (CollisionRequest::distanceTolerance) */
+  float reserved[2];
+} fclg_request;
+
+enum {
+  FCLG_REQ_BOOLEAN_ONLY = 1u << 0,  /* collide flag only: no distance, no EPA */
+  FCLG_REQ_NO_EPA = 1u << 1,        /* separation distance only; overlapping pairs get distance 0 */
+  FCLG_REQ_WARM_START = 1u << 2     /* seed GJK with the learned direction model (fclg_warmstart_*) */
+};
+
+typedef struct fclg_context fclg_context;
+
+/* Context on a device (sm_103 required).  Owns device copies of the shapes and
+   the scratch of the query passes. */
+int fclg_create(fclg_context** ctx, int device);
+void fclg_destroy(fclg_context* ctx);
+const char* fclg_last_error(const fclg_context* ctx);
+/* Library version and the compute capability it was built for (e.g. 1030). */
+int fclg_version(void);
+int fclg_built_arch(void);
+
+/* Shapes and hull vertices (float x, y, z, pad per vertex), copied to the
+   device.  Replaces constructing fcl::Box / Sphere / Capsule / Cylinder /
+   Convex objects (geometry/shape/*.h). */
+int fclg_set_shapes(fclg_context* ctx, const fclg_shape* shapes, uint32_t n_shapes, const float* vertices_xyzw,
+                    uint64_t n_vertices);
+/* Same, with the arrays already on the device; the context borrows them. */
+int fclg_set_shapes_device(fclg_context* ctx, const fclg_shape* d_shapes, uint32_t n_shapes,
+                           const float* d_vertices_xyzw, uint64_t n_vertices);
+
+/* Signed distance per pair: GJK separation distance and witness points for
+   separated pairs, -EPA depth, witness points and contact normal for
+   overlapping ones (GJKSolver::shapeSignedDistance, gjk_solver-inl.h:810-874;
+   the reference exposes no fcl::distance for it).  req may be NULL. */
+int fclg_distance(fclg_context* ctx, const fclg_pair* pairs, uint32_t n_pairs, const fclg_request* req,
+                  fclg_result* results);
+int fclg_distance_device(fclg_context* ctx, const fclg_pair* d_pairs, uint32_t n_pairs, const fclg_request* req,
+                         fclg_result* d_results, void* stream);
+
+/* Collision per pair (fcl::collide on a shape pair): the boolean flag, and with
+   penetration (req NULL or without FCLG_REQ_BOOLEAN_ONLY) one contact per
+   colliding pair — depth, normal, p_a / p_b — as useDefaultPenetration gives. */
+int fclg_collide(fclg_context* ctx, const fclg_pair* pairs, uint32_t n_pairs, const fclg_request* req,
+                 fclg_result* results);
+int fclg_collide_device(fclg_context* ctx, const fclg_pair* d_pairs, uint32_t n_pairs, const fclg_request* req,
+                        fclg_result* d_results, void* stream);
+
+/* Launch shape of the two query passes (lanes per pair of the GJK pass,
+   CTAs of the EPA pass); 0 keeps the built-in choice.  For tuning. */
+int fclg_set_launch(fclg_context* ctx, int gjk_lanes, int epa_ctas_per_sm);
+
+/* Kernel launches issued by this context since creation (for accounting). */
+uint64_t fclg_launch_count(const fclg_context* ctx);
+
+/* Per-pass timing: when enabled, every query records CUDA events around its
+   GJK and EPA passes on the query's stream; fclg_pass_times synchronises on
+   them and returns the summed milliseconds of each pass and the number of
+   queries timed since the last reset (reset = 1 clears the sums). */
+int fclg_set_profiling(fclg_context* ctx, int enable);
+int fclg_pass_times(fclg_context* ctx, double* gjk_ms, double* epa_ms, uint64_t* queries, int reset);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FCLG_H_ */

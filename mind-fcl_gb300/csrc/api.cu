@@ -1,0 +1,347 @@
+// The C ABI of include/fclg.h: contexts, shape upload, and the batched
+// collide / distance queries over the two kernel passes of convex_query.cu.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fclg.h"
+#include "kernels.h"
+
+struct fclg_context {
+  int device = 0;
+  int num_sms = 0;
+  std::string err;
+  cudaStream_t stream = nullptr;
+  // shapes
+  void* own_shapes = nullptr;
+  void* own_verts = nullptr;
+  const int4* shapes = nullptr;
+  const float4* verts = nullptr;
+  uint32_t n_shapes = 0;
+  uint64_t n_verts = 0;
+  // scratch handed from the GJK pass to the EPA pass
+  uint32_t* epa_count = nullptr;
+  uint32_t* epa_list = nullptr;
+  float4* epa_rec = nullptr;
+  size_t epa_cap = 0;
+  // device staging of the host-pointer entry points
+  void* io_pairs = nullptr;
+  void* io_results = nullptr;
+  size_t io_cap = 0;
+  // launch shape
+  int gjk_lanes = 1;
+  int epa_ctas_per_sm = 3;
+  uint64_t launches = 0;
+  // optional per-pass timing
+  bool profiling = false;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  bool ev_pending = false;
+  bool ev_epa = false;
+  double gjk_ms = 0, epa_ms = 0;
+  uint64_t timed = 0;
+};
+
+namespace {
+
+int fail(fclg_context* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cuda_fail(fclg_context* c, cudaError_t e, const char* what) {
+  return fail(c, FCLG_E_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define FCLG_CUDA(ctx, call)                                   \
+  do {                                                         \
+    cudaError_t e_ = (call);                                   \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call);   \
+  } while (0)
+
+int validate_shapes(fclg_context* c, const fclg_shape* s, uint32_t n, uint64_t n_verts) {
+  for (uint32_t i = 0; i < n; ++i) {
+    const int t = s[i].type;
+    if (t == FCLG_CONVEX) {
+      if (s[i].vert_count == 0 || (uint64_t)s[i].vert_offset + s[i].vert_count > n_verts) {
+        char b[160];
+        snprintf(b, sizeof b, "shape %u: convex vertex range [%u, +%u) outside the %llu-vertex pool", i,
+                 s[i].vert_offset, s[i].vert_count, (unsigned long long)n_verts);
+        return fail(c, FCLG_E_INVALID, b);
+      }
+    } else if (t != FCLG_BOX && t != FCLG_SPHERE && t != FCLG_CAPSULE && t != FCLG_CYLINDER) {
+      char b[96];
+      snprintf(b, sizeof b, "shape %u: unsupported type %d", i, t);
+      return fail(c, FCLG_E_INVALID, b);
+    }
+  }
+  return FCLG_OK;
+}
+
+void release_shapes(fclg_context* c) {
+  if (c->own_shapes) cudaFree(c->own_shapes);
+  if (c->own_verts) cudaFree(c->own_verts);
+  c->own_shapes = c->own_verts = nullptr;
+  c->shapes = nullptr;
+  c->verts = nullptr;
+  c->n_shapes = 0;
+  c->n_verts = 0;
+}
+
+int ensure_epa(fclg_context* c, size_t n) {
+  if (n <= c->epa_cap) return FCLG_OK;
+  if (c->epa_list) cudaFree(c->epa_list);
+  if (c->epa_rec) cudaFree(c->epa_rec);
+  c->epa_list = nullptr;
+  c->epa_rec = nullptr;
+  c->epa_cap = 0;
+  const size_t cap = std::max<size_t>(n, 1024);
+  FCLG_CUDA(c, cudaMalloc(&c->epa_list, cap * sizeof(uint32_t)));
+  FCLG_CUDA(c, cudaMalloc(&c->epa_rec, cap * fclg::kEpaRecordBytes));
+  c->epa_cap = cap;
+  return FCLG_OK;
+}
+
+int ensure_io(fclg_context* c, size_t n) {
+  if (n <= c->io_cap) return FCLG_OK;
+  if (c->io_pairs) cudaFree(c->io_pairs);
+  if (c->io_results) cudaFree(c->io_results);
+  c->io_pairs = c->io_results = nullptr;
+  c->io_cap = 0;
+  const size_t cap = std::max<size_t>(n, 1024);
+  FCLG_CUDA(c, cudaMalloc(&c->io_pairs, cap * sizeof(fclg_pair)));
+  FCLG_CUDA(c, cudaMalloc(&c->io_results, cap * sizeof(fclg_result)));
+  c->io_cap = cap;
+  return FCLG_OK;
+}
+
+fclg::QueryParams make_params(const fclg_request* req, bool distance_query) {
+  fclg::QueryParams p;
+  p.gjk_tol = (req && req->gjk_tolerance > 0.f) ? req->gjk_tolerance : 1e-6f;
+  p.epa_tol = (req && req->epa_tolerance > 0.f) ? req->epa_tolerance : 1e-6f;
+  p.gjk_max_iter = (req && req->gjk_max_iterations) ? (int)req->gjk_max_iterations : 128;
+  p.epa_max_iter = (req && req->epa_max_iterations) ? (int)req->epa_max_iterations : 255;
+  p.epa_max_faces = (req && req->epa_max_faces) ? (int)req->epa_max_faces : 256;
+  const uint32_t fl = req ? req->flags : 0u;
+  const bool boolean_only = (fl & FCLG_REQ_BOOLEAN_ONLY) != 0;
+  p.want_distance = (distance_query || !boolean_only) ? 1 : 0;
+  p.want_epa = (!boolean_only && !(fl & FCLG_REQ_NO_EPA)) ? 1 : 0;
+  return p;
+}
+
+int collect_times(fclg_context* c) {
+  if (!c->ev_pending) return FCLG_OK;
+  FCLG_CUDA(c, cudaEventSynchronize(c->ev[c->ev_epa ? 2 : 1]));
+  float a = 0, b = 0;
+  FCLG_CUDA(c, cudaEventElapsedTime(&a, c->ev[0], c->ev[1]));
+  if (c->ev_epa) FCLG_CUDA(c, cudaEventElapsedTime(&b, c->ev[1], c->ev[2]));
+  c->gjk_ms += a;
+  c->epa_ms += b;
+  c->timed += 1;
+  c->ev_pending = false;
+  return FCLG_OK;
+}
+
+int run_query(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_request* req, fclg_result* d_results,
+              cudaStream_t st, bool distance_query) {
+  if (!c) return FCLG_E_INVALID;
+  if (n == 0) return FCLG_OK;
+  if (!d_pairs || !d_results) return fail(c, FCLG_E_INVALID, "null pair or result pointer");
+  if (!c->shapes) return fail(c, FCLG_E_NO_SHAPES, "no shapes set");
+  FCLG_CUDA(c, cudaSetDevice(c->device));
+  const fclg::QueryParams prm = make_params(req, distance_query);
+  if (prm.want_epa) {
+    const int rc = ensure_epa(c, n);
+    if (rc) return rc;
+  }
+  fclg::BatchArgs b;
+  b.shapes = c->shapes;
+  b.verts = c->verts;
+  b.pairs = reinterpret_cast<const float4*>(d_pairs);
+  b.guess = nullptr;
+  b.results = reinterpret_cast<float4*>(d_results);
+  b.n_pairs = n;
+  b.n_shapes = c->n_shapes;
+  fclg::EpaQueue q{c->epa_count, c->epa_list, c->epa_rec};
+  if (c->profiling) {
+    const int rc = collect_times(c);
+    if (rc) return rc;
+  }
+  if (prm.want_epa) FCLG_CUDA(c, cudaMemsetAsync(c->epa_count, 0, sizeof(uint32_t), st));
+  if (c->profiling) FCLG_CUDA(c, cudaEventRecord(c->ev[0], st));
+  FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes, st));
+  c->launches += 1;
+  if (c->profiling) FCLG_CUDA(c, cudaEventRecord(c->ev[1], st));
+  if (prm.want_epa) {
+    FCLG_CUDA(c, fclg::launch_epa(b, prm, q, c->num_sms * c->epa_ctas_per_sm, st));
+    c->launches += 1;
+    if (c->profiling) FCLG_CUDA(c, cudaEventRecord(c->ev[2], st));
+  }
+  if (c->profiling) {
+    c->ev_pending = true;
+    c->ev_epa = prm.want_epa != 0;
+  }
+  return FCLG_OK;
+}
+
+int run_host_query(fclg_context* c, const fclg_pair* pairs, uint32_t n, const fclg_request* req,
+                   fclg_result* results, bool distance_query) {
+  if (!c) return FCLG_E_INVALID;
+  if (n == 0) return FCLG_OK;
+  if (!pairs || !results) return fail(c, FCLG_E_INVALID, "null pair or result pointer");
+  int rc = ensure_io(c, n);
+  if (rc) return rc;
+  FCLG_CUDA(c, cudaMemcpyAsync(c->io_pairs, pairs, (size_t)n * sizeof(fclg_pair), cudaMemcpyHostToDevice, c->stream));
+  rc = run_query(c, static_cast<const fclg_pair*>(c->io_pairs), n, req, static_cast<fclg_result*>(c->io_results),
+                 c->stream, distance_query);
+  if (rc) return rc;
+  FCLG_CUDA(c, cudaMemcpyAsync(results, c->io_results, (size_t)n * sizeof(fclg_result), cudaMemcpyDeviceToHost,
+                               c->stream));
+  FCLG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return FCLG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fclg_version(void) { return 100; }
+
+int fclg_built_arch(void) { return 1030; }
+
+int fclg_create(fclg_context** out, int device) {
+  if (!out) return FCLG_E_INVALID;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) return FCLG_E_NO_DEVICE;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return FCLG_E_NO_DEVICE;
+  if (prop.major * 10 + prop.minor != 103) return FCLG_E_NO_DEVICE;
+  fclg_context* c = new fclg_context();
+  c->device = device;
+  c->num_sms = prop.multiProcessorCount;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc(&c->epa_count, sizeof(uint32_t)) != cudaSuccess || fclg::prepare_epa() != cudaSuccess) {
+    fclg_destroy(c);
+    return FCLG_E_CUDA;
+  }
+  *out = c;
+  return FCLG_OK;
+}
+
+void fclg_destroy(fclg_context* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  release_shapes(c);
+  if (c->epa_count) cudaFree(c->epa_count);
+  if (c->epa_list) cudaFree(c->epa_list);
+  if (c->epa_rec) cudaFree(c->epa_rec);
+  if (c->io_pairs) cudaFree(c->io_pairs);
+  if (c->io_results) cudaFree(c->io_results);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  for (auto& e : c->ev)
+    if (e) cudaEventDestroy(e);
+  delete c;
+}
+
+const char* fclg_last_error(const fclg_context* c) { return c ? c->err.c_str() : "null context"; }
+
+int fclg_set_shapes(fclg_context* c, const fclg_shape* shapes, uint32_t n_shapes, const float* vertices,
+                    uint64_t n_vertices) {
+  if (!c) return FCLG_E_INVALID;
+  if (!shapes || n_shapes == 0) return fail(c, FCLG_E_INVALID, "no shapes");
+  if (n_vertices > 0 && !vertices) return fail(c, FCLG_E_INVALID, "null vertex pointer");
+  int rc = validate_shapes(c, shapes, n_shapes, n_vertices);
+  if (rc) return rc;
+  FCLG_CUDA(c, cudaSetDevice(c->device));
+  release_shapes(c);
+  FCLG_CUDA(c, cudaMalloc(&c->own_shapes, (size_t)n_shapes * sizeof(fclg_shape)));
+  FCLG_CUDA(c, cudaMalloc(&c->own_verts, std::max<uint64_t>(n_vertices, 1) * 4 * sizeof(float)));
+  FCLG_CUDA(c, cudaMemcpy(c->own_shapes, shapes, (size_t)n_shapes * sizeof(fclg_shape), cudaMemcpyHostToDevice));
+  if (n_vertices)
+    FCLG_CUDA(c, cudaMemcpy(c->own_verts, vertices, n_vertices * 4 * sizeof(float), cudaMemcpyHostToDevice));
+  c->shapes = static_cast<const int4*>(c->own_shapes);
+  c->verts = static_cast<const float4*>(c->own_verts);
+  c->n_shapes = n_shapes;
+  c->n_verts = n_vertices;
+  return FCLG_OK;
+}
+
+int fclg_set_shapes_device(fclg_context* c, const fclg_shape* d_shapes, uint32_t n_shapes, const float* d_vertices,
+                           uint64_t n_vertices) {
+  if (!c) return FCLG_E_INVALID;
+  if (!d_shapes || n_shapes == 0 || !d_vertices) return fail(c, FCLG_E_INVALID, "null shape or vertex pointer");
+  FCLG_CUDA(c, cudaSetDevice(c->device));
+  // validate the table once on the host: kernels trust vertex ranges
+  std::vector<fclg_shape> h(n_shapes);
+  FCLG_CUDA(c, cudaMemcpy(h.data(), d_shapes, (size_t)n_shapes * sizeof(fclg_shape), cudaMemcpyDeviceToHost));
+  const int rc = validate_shapes(c, h.data(), n_shapes, n_vertices);
+  if (rc) return rc;
+  release_shapes(c);
+  c->shapes = reinterpret_cast<const int4*>(d_shapes);
+  c->verts = reinterpret_cast<const float4*>(d_vertices);
+  c->n_shapes = n_shapes;
+  c->n_verts = n_vertices;
+  return FCLG_OK;
+}
+
+int fclg_distance(fclg_context* c, const fclg_pair* pairs, uint32_t n, const fclg_request* req,
+                  fclg_result* results) {
+  return run_host_query(c, pairs, n, req, results, true);
+}
+
+int fclg_distance_device(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_request* req,
+                         fclg_result* d_results, void* stream) {
+  return run_query(c, d_pairs, n, req, d_results, static_cast<cudaStream_t>(stream), true);
+}
+
+int fclg_collide(fclg_context* c, const fclg_pair* pairs, uint32_t n, const fclg_request* req, fclg_result* results) {
+  return run_host_query(c, pairs, n, req, results, false);
+}
+
+int fclg_collide_device(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_request* req,
+                        fclg_result* d_results, void* stream) {
+  return run_query(c, d_pairs, n, req, d_results, static_cast<cudaStream_t>(stream), false);
+}
+
+int fclg_set_launch(fclg_context* c, int gjk_lanes, int epa_ctas_per_sm) {
+  if (!c) return FCLG_E_INVALID;
+  if (gjk_lanes) {
+    if (gjk_lanes != 1 && gjk_lanes != 2 && gjk_lanes != 4 && gjk_lanes != 8 && gjk_lanes != 16 && gjk_lanes != 32)
+      return fail(c, FCLG_E_INVALID, "gjk_lanes must be 1, 2, 4, 8, 16 or 32");
+    c->gjk_lanes = gjk_lanes;
+  }
+  if (epa_ctas_per_sm) {
+    if (epa_ctas_per_sm < 1 || epa_ctas_per_sm > 32) return fail(c, FCLG_E_INVALID, "epa_ctas_per_sm out of range");
+    c->epa_ctas_per_sm = epa_ctas_per_sm;
+  }
+  return FCLG_OK;
+}
+
+uint64_t fclg_launch_count(const fclg_context* c) { return c ? c->launches : 0; }
+
+int fclg_set_profiling(fclg_context* c, int enable) {
+  if (!c) return FCLG_E_INVALID;
+  FCLG_CUDA(c, cudaSetDevice(c->device));
+  if (enable && !c->ev[0])
+    for (auto& e : c->ev) FCLG_CUDA(c, cudaEventCreate(&e));
+  c->profiling = enable != 0;
+  return FCLG_OK;
+}
+
+int fclg_pass_times(fclg_context* c, double* gjk_ms, double* epa_ms, uint64_t* queries, int reset) {
+  if (!c) return FCLG_E_INVALID;
+  const int rc = collect_times(c);
+  if (rc) return rc;
+  if (gjk_ms) *gjk_ms = c->gjk_ms;
+  if (epa_ms) *epa_ms = c->epa_ms;
+  if (queries) *queries = c->timed;
+  if (reset) {
+    c->gjk_ms = c->epa_ms = 0;
+    c->timed = 0;
+  }
+  return FCLG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,193 @@
+// The two passes of a convex query batch.
+//
+//  gjk_pass   one group of LANES lanes per pair: GJK boolean and, for
+//             separated pairs, the GJK separation distance; overlapping pairs
+//             are appended (warp-aggregated atomics) to a compact work list
+//             with their final simplex.
+//  epa_pass   persistent grid, one warp per listed pair: EPA from the simplex.
+//
+// Both passes are stream-ordered and need no host round trip between them:
+// the EPA grid reads the list length from device memory, so the pair of
+// launches can be captured into a CUDA graph.
+#include "epa.cuh"
+#include "gjk.cuh"
+#include "kernels.h"
+
+namespace fclg {
+
+namespace {
+
+__device__ __forceinline__ void write_simplex(float4* __restrict__ rec, uint32_t slot, const Simplex& s, int iters) {
+  float f[28];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    f[1 + 6 * i + 0] = s.a[i].x;
+    f[1 + 6 * i + 1] = s.a[i].y;
+    f[1 + 6 * i + 2] = s.a[i].z;
+    f[1 + 6 * i + 3] = s.b[i].x;
+    f[1 + 6 * i + 4] = s.b[i].y;
+    f[1 + 6 * i + 5] = s.b[i].z;
+  }
+  f[0] = __int_as_float(s.rank);
+  f[25] = __int_as_float(iters);
+  f[26] = 0.f;
+  f[27] = 0.f;
+  float4* r = rec + 7 * (size_t)slot;
+#pragma unroll
+  for (int k = 0; k < 7; ++k) r[k] = make_float4(f[4 * k], f[4 * k + 1], f[4 * k + 2], f[4 * k + 3]);
+}
+
+__device__ __forceinline__ uint32_t aggregated_slot(uint32_t* counter) {
+  const unsigned m = __activemask();
+  const unsigned lane = threadIdx.x & 31u;
+  const int leader = __ffs(m) - 1;
+  uint32_t base = 0;
+  if ((int)lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
+  base = __shfl_sync(m, base, leader);
+  return base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ void store_invalid(float4* out, uint32_t pid) {
+  store_result(out, pid, -1.f, mk3(0, 0, 1), mk3(0, 0, 0), mk3(0, 0, 0), kGjkFailed, 0, false, false);
+}
+
+}  // namespace
+
+template <int LANES>
+__global__ void __launch_bounds__(256) gjk_pass(BatchArgs b, QueryParams prm, EpaQueue q) {
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t pid = tid / LANES;
+  if (pid >= b.n_pairs) return;
+  const Group<LANES> g = Group<LANES>::make();
+  const PairDev pr = load_pair(b.pairs, pid);
+  if (pr.a >= b.n_shapes || pr.b >= b.n_shapes) {
+    if (g.lane == 0) store_invalid(b.results, pid);
+    return;
+  }
+  MinkowskiSupport<LANES> sup;
+  sup.A = load_shape(b.shapes, pr.a);
+  sup.B = load_shape(b.shapes, pr.b);
+  sup.pose = pr.pose;
+  sup.verts = b.verts;
+  sup.g = g;
+  f3 guess = mk3(1.f, 0.f, 0.f);
+  if (b.guess) guess = mk3(__ldg(b.guess + 3 * (size_t)pid), __ldg(b.guess + 3 * (size_t)pid + 1),
+                           __ldg(b.guess + 3 * (size_t)pid + 2));
+  Simplex s;
+  const GjkOut o = gjk_evaluate(sup, -guess, prm.gjk_tol, prm.gjk_max_iter, prm.want_distance != 0, s);
+  if (g.lane != 0) return;
+  if (o.status == kGjkIntersect) {
+    if (prm.want_epa) {
+      const uint32_t slot = aggregated_slot(q.count);
+      q.list[slot] = pid;
+      write_simplex(q.rec, slot, s, o.iterations);
+      return;
+    }
+    store_result(b.results, pid, 0.f, mk3(0, 0, 1), mk3(0, 0, 0), mk3(0, 0, 0), kGjkIntersect,
+                 (uint32_t)o.iterations, true, true);
+    return;
+  }
+  if (!prm.want_distance) {
+    store_result(b.results, pid, 0.f, mk3(0, 0, 1), mk3(0, 0, 0), mk3(0, 0, 0), o.status, (uint32_t)o.iterations,
+                 false, o.status == kGjkSeparated);
+    return;
+  }
+  // shapeSignedDistance: valid only for a separation certificate with valid points
+  const bool ok = (o.status == kGjkSeparated) && o.point_valid;
+  const f3 dv = o.p1 - o.p0;
+  const float dist = ok ? nrm(dv) : -1.f;
+  f3 nrmv = normalized(dv);
+  if (!(sqn(nrmv) > 0.f)) nrmv = mk3(0, 0, 1);
+  store_result(b.results, pid, dist, nrmv, o.p0, o.p1, o.status, (uint32_t)o.iterations, false, ok);
+}
+
+template <int FMAX, int VMAX, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) epa_pass(BatchArgs b, QueryParams prm, EpaQueue q) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  EpaSmem<FMAX, VMAX>& P = reinterpret_cast<EpaSmem<FMAX, VMAX>*>(smem_raw)[threadIdx.x >> 5];
+  const unsigned lane = threadIdx.x & 31u;
+  const uint32_t n = *q.count;
+  const uint32_t gw = blockIdx.x * WARPS + (threadIdx.x >> 5);
+  const uint32_t nw = gridDim.x * WARPS;
+  const int max_faces = prm.epa_max_faces < FMAX ? prm.epa_max_faces : FMAX;
+  for (uint32_t item = gw; item < n; item += nw) {
+    const uint32_t pid = q.list[item];
+    const float4* r = q.rec + 7 * (size_t)item;
+    float f[28];
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+      const float4 v = r[k];
+      f[4 * k] = v.x;
+      f[4 * k + 1] = v.y;
+      f[4 * k + 2] = v.z;
+      f[4 * k + 3] = v.w;
+    }
+    const int rank = __float_as_int(f[0]);
+    const int gjk_iters = __float_as_int(f[25]);
+    f3 spa[4], spb[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      spa[i] = mk3(f[1 + 6 * i], f[2 + 6 * i], f[3 + 6 * i]);
+      spb[i] = mk3(f[4 + 6 * i], f[5 + 6 * i], f[6 + 6 * i]);
+    }
+    const PairDev pr = load_pair(b.pairs, pid);
+    MinkowskiSupport<32> sup;
+    sup.A = load_shape(b.shapes, pr.a);
+    sup.B = load_shape(b.shapes, pr.b);
+    sup.pose = pr.pose;
+    sup.verts = b.verts;
+    sup.g = Group<32>::make();
+    EpaWarp<FMAX, VMAX> E{P, sup, prm.epa_tol, lane, 0, 0, 0};
+    const EpaResult er = E.run(rank < 1 ? 1 : (rank > 4 ? 4 : rank), spa, spb, prm.epa_max_iter, max_faces);
+    if (lane == 0) {
+      const int32_t status = kGjkIntersect | ((er.status + 1) << 8);
+      const uint32_t iters = (uint32_t)(gjk_iters + er.iterations);
+      if (er.status != kEpaFailed) {
+        f3 nv = er.p0 - er.p1;
+        nv = (sqn(nv) > 0.f) ? normalized(nv) : mk3(0, 0, 1);
+        store_result(b.results, pid, -er.depth, nv, er.p0, er.p1, status, iters, true, true);
+      } else {
+        store_result(b.results, pid, -1.f, mk3(0, 0, 1), mk3(0, 0, 0), mk3(0, 0, 0), status, iters, true, false);
+      }
+    }
+    __syncwarp();
+  }
+}
+
+constexpr int kEpaFmax = 256;
+constexpr int kEpaVmax = 192;
+constexpr int kEpaWarps = 4;
+
+size_t epa_smem_bytes() { return (size_t)kEpaWarps * sizeof(EpaSmem<kEpaFmax, kEpaVmax>); }
+
+cudaError_t launch_gjk(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q, int lanes, cudaStream_t st) {
+  if (b.n_pairs == 0) return cudaSuccess;
+  const int threads = 256;
+  const uint64_t total = (uint64_t)b.n_pairs * (uint64_t)lanes;
+  const unsigned blocks = (unsigned)((total + threads - 1) / threads);
+  switch (lanes) {
+    case 1: gjk_pass<1><<<blocks, threads, 0, st>>>(b, prm, q); break;
+    case 2: gjk_pass<2><<<blocks, threads, 0, st>>>(b, prm, q); break;
+    case 4: gjk_pass<4><<<blocks, threads, 0, st>>>(b, prm, q); break;
+    case 8: gjk_pass<8><<<blocks, threads, 0, st>>>(b, prm, q); break;
+    case 16: gjk_pass<16><<<blocks, threads, 0, st>>>(b, prm, q); break;
+    case 32: gjk_pass<32><<<blocks, threads, 0, st>>>(b, prm, q); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t prepare_epa() {
+  return cudaFuncSetAttribute(epa_pass<kEpaFmax, kEpaVmax, kEpaWarps>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)epa_smem_bytes());
+}
+
+cudaError_t launch_epa(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q, int blocks, cudaStream_t st) {
+  if (b.n_pairs == 0) return cudaSuccess;
+  epa_pass<kEpaFmax, kEpaVmax, kEpaWarps><<<blocks, kEpaWarps * 32, epa_smem_bytes(), st>>>(b, prm, q);
+  return cudaGetLastError();
+}
+
+int epa_max_faces_supported() { return kEpaFmax; }
+
+}  // namespace fclg

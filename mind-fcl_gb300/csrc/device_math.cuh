@@ -1,0 +1,125 @@
+// Small vector types and the packed records the kernels read and write.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fclg {
+
+struct f3 {
+  float x, y, z;
+};
+__device__ __forceinline__ f3 mk3(float x, float y, float z) { return f3{x, y, z}; }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ f3 operator-(f3 a) { return mk3(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ f3 operator*(f3 a, float s) { return mk3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ f3 operator*(float s, f3 a) { return mk3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float dot(f3 a, f3 b) { return fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)); }
+__device__ __forceinline__ f3 cross(f3 a, f3 b) {
+  return mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float sqn(f3 a) { return dot(a, a); }
+__device__ __forceinline__ float nrm(f3 a) { return sqrtf(sqn(a)); }
+// Leaves a zero vector unchanged (the reference's Eigen normalize()).
+__device__ __forceinline__ f3 normalized(f3 a) {
+  const float n2 = sqn(a);
+  return n2 > 0.f ? a * rsqrtf(n2) : a;
+}
+
+struct d3 {
+  double x, y, z;
+};
+__device__ __forceinline__ d3 tod(f3 a) { return d3{(double)a.x, (double)a.y, (double)a.z}; }
+__device__ __forceinline__ d3 operator-(d3 a, d3 b) { return d3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ d3 operator+(d3 a, d3 b) { return d3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ d3 operator*(d3 a, double s) { return d3{a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ double dot(d3 a, d3 b) { return fma(a.z, b.z, fma(a.y, b.y, a.x * b.x)); }
+__device__ __forceinline__ d3 cross(d3 a, d3 b) {
+  return d3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+
+// Shape types: the reference's GJKShapeType values (gjk_shape.h:9-28).
+enum : int32_t { kBox = 0, kSphere = 1, kCapsule = 3, kCylinder = 5, kConvex = 100 };
+
+// One shape as the kernels use it, decoded from the 32-byte fclg_shape.
+struct ShapeDev {
+  int32_t type;
+  uint32_t vofs, nv;
+  float p0, p1, p2;  // box: half extents; sphere: r; capsule/cylinder: r, half length
+};
+
+__device__ __forceinline__ ShapeDev load_shape(const int4* __restrict__ shapes, uint32_t i) {
+  const int4 h = __ldg(shapes + 2 * (size_t)i);
+  const float4 p = __ldg(reinterpret_cast<const float4*>(shapes) + 2 * (size_t)i + 1);
+  ShapeDev s;
+  s.type = h.x;
+  s.vofs = (uint32_t)h.y;
+  s.nv = (uint32_t)h.z;
+  if (s.type == kBox) {
+    s.p0 = 0.5f * p.x; s.p1 = 0.5f * p.y; s.p2 = 0.5f * p.z;
+  } else {
+    s.p0 = p.x; s.p1 = 0.5f * p.y; s.p2 = 0.f;
+  }
+  return s;
+}
+
+// Pose of shape b in shape a's frame (the reference's MinkowskiDiff::toshape0).
+struct Pose {
+  float r[9];
+  f3 t;
+  __device__ __forceinline__ f3 rot(f3 v) const {
+    return mk3(fmaf(r[2], v.z, fmaf(r[1], v.y, r[0] * v.x)), fmaf(r[5], v.z, fmaf(r[4], v.y, r[3] * v.x)),
+               fmaf(r[8], v.z, fmaf(r[7], v.y, r[6] * v.x)));
+  }
+  __device__ __forceinline__ f3 rotT(f3 v) const {
+    return mk3(fmaf(r[6], v.z, fmaf(r[3], v.y, r[0] * v.x)), fmaf(r[7], v.z, fmaf(r[4], v.y, r[1] * v.x)),
+               fmaf(r[8], v.z, fmaf(r[5], v.y, r[2] * v.x)));
+  }
+  __device__ __forceinline__ f3 apply(f3 v) const { return rot(v) + t; }
+};
+
+struct PairDev {
+  uint32_t a, b;
+  Pose pose;
+};
+
+__device__ __forceinline__ PairDev load_pair(const float4* __restrict__ pairs, uint32_t i) {
+  const float4 q0 = __ldg(pairs + 4 * (size_t)i + 0);
+  const float4 q1 = __ldg(pairs + 4 * (size_t)i + 1);
+  const float4 q2 = __ldg(pairs + 4 * (size_t)i + 2);
+  const float4 q3 = __ldg(pairs + 4 * (size_t)i + 3);
+  PairDev p;
+  p.a = __float_as_uint(q0.x);
+  p.b = __float_as_uint(q0.y);
+  p.pose.r[0] = q0.z; p.pose.r[1] = q0.w;
+  p.pose.r[2] = q1.x; p.pose.r[3] = q1.y; p.pose.r[4] = q1.z; p.pose.r[5] = q1.w;
+  p.pose.r[6] = q2.x; p.pose.r[7] = q2.y; p.pose.r[8] = q2.z;
+  p.pose.t = mk3(q2.w, q3.x, q3.y);
+  return p;
+}
+
+// Status word of a result: bits 0-7 GJK_Status, bits 8-15 EPA_Status + 1.
+enum : int32_t { kGjkIntersect = 0, kGjkSeparated = 1, kGjkNoProgress = 2, kGjkIterLimit = 3, kGjkFailed = 4 };
+enum : int32_t { kEpaFailed = 0, kEpaOK = 1, kEpaTouching = 2, kEpaIterLimit = 3, kEpaMallocFailed = 4 };
+
+// 48-byte fclg_result written as three float4 stores.
+__device__ __forceinline__ void store_result(float4* __restrict__ out, uint32_t i, float dist, f3 n, f3 pa, f3 pb,
+                                             int32_t status, uint32_t iters, bool collide, bool ok) {
+  const uint32_t tail = (iters > 0xFFFFu ? 0xFFFFu : iters) | ((collide ? 1u : 0u) << 16) | ((ok ? 1u : 0u) << 24);
+  out[3 * (size_t)i + 0] = make_float4(dist, n.x, n.y, n.z);
+  out[3 * (size_t)i + 1] = make_float4(pa.x, pa.y, pa.z, pb.x);
+  out[3 * (size_t)i + 2] = make_float4(pb.y, pb.z, __int_as_float(status), __uint_as_float(tail));
+}
+
+// Scalar parameters of a query batch (GJKSolver fields, gjk_solver.h:122-163).
+struct QueryParams {
+  float gjk_tol;
+  float epa_tol;
+  int gjk_max_iter;
+  int epa_max_iter;
+  int epa_max_faces;
+  int want_distance;  // 1: signed distance (GJK distance / EPA); 0: boolean only
+  int want_epa;       // run EPA on overlapping pairs
+};
+
+}  // namespace fclg

@@ -1,0 +1,543 @@
+// EPA penetration depth / witness points, one warp per overlapping pair, with
+// the polytope held in the warp's slice of shared memory.
+//
+// Algorithm (epa.hpp:133-237 and the polytope code it drives): repeatedly take
+// the face nearest the origin, evaluate the support along its outward normal,
+// stop when the support point is within the tolerance of that face's plane,
+// else remove the patch of faces the new point sees (grown from the nearest
+// face through visible neighbours, as computeVisiblePatch's DFS does,
+// epa_polytope_expand.hpp:120-180) and fan new faces from the point to the
+// patch's horizon.  Capacity (live faces <= max_faces, the reference's
+// MallocFailed) and the iteration limit end the loop with the current nearest
+// face, as the reference does.
+//
+// GPU layout: face slots are striped over the 32 lanes for the nearest-face
+// argmin and the visibility test; horizon edges are gathered with ballot
+// prefix sums and fanned in parallel, neighbours linked through a per-vertex
+// "edge starting here" table.  Faces carry FP32 unit normals and plane
+// distances; the final closest-face solve (normal, depth, barycentric witness
+// points) runs in FP64.
+//
+// Initial polytope from the GJK simplex: epa_simplex2polytope.hpp:41-376
+// (touching detection, triangle blown up along +-normal, segment search over
+// 72 directions, tetrahedron).
+#pragma once
+#include "support.cuh"
+
+#ifndef FCLG_EPA_TRACE
+#define FCLG_EPA_TRACE(...) \
+  do {                      \
+  } while (0)
+#endif
+
+namespace fclg {
+
+constexpr uint32_t kNoFace = 0xFFFFu;
+constexpr uint32_t kNoSlot = 0xFFFFFFFFu;
+
+template <int FMAX, int VMAX>
+struct EpaSmem {
+  float4 fn[FMAX];        // outward unit normal xyz, plane distance (inf: unusable)
+  uint32_t fv[FMAX];      // vertex indices v0 | v1 << 8 | v2 << 16, counter-clockwise seen from outside;
+                          // bit 24: the origin projects inside the face
+  uint16_t fadj[FMAX][4]; // neighbour across edge k = (v_k, v_k+1)
+  uint8_t falive[FMAX];
+  uint8_t fvis[FMAX];     // 0 hidden, 1 sees the new point, 2 in the visible patch
+  float4 vw[VMAX];        // Minkowski vertex w = pa - pb
+  float4 vpa[VMAX];       // support point on shape a
+  uint32_t start_at[VMAX];
+  uint16_t hz_s[FMAX + 8];
+  uint8_t hz_e[FMAX + 8];
+  uint16_t hz_slot[FMAX + 8];
+  uint16_t freelist[FMAX];
+  uint32_t scratch[8];
+};
+
+__device__ __forceinline__ uint32_t fvert(uint32_t packed, int k) { return (packed >> (8 * k)) & 0xFFu; }
+__device__ __forceinline__ f3 ld3(const float4& q) { return mk3(q.x, q.y, q.z); }
+
+__device__ __forceinline__ float4 face_plane(f3 a, f3 b, f3 c) {
+  const f3 n = cross(b - a, c - a);
+  const float n2 = sqn(n);
+  if (!(n2 > 0.f)) return make_float4(0.f, 0.f, 0.f, INFINITY);
+  const f3 u = n * rsqrtf(n2);
+  return make_float4(u.x, u.y, u.z, dot(u, a));
+}
+
+// Whether the origin's projection onto the face plane lies inside the
+// triangle (barycentric coordinates >= -1e-4).  The reference ranks faces by
+// their distance to the origin only when this holds (pointToTriangle's
+// witness_in_simplex, epa_polytope_utils.h:88-165); among coplanar triangles
+// it is what picks the one that holds the nearest point.
+__device__ __forceinline__ uint32_t projects_inside(f3 a, f3 b, f3 c, float4 plane) {
+  if (!(plane.w < INFINITY)) return 0u;
+  const f3 u = ld3(plane);
+  const f3 p = u * plane.w;
+  const float e0 = dot(u, cross(b - a, p - a));
+  const float e1 = dot(u, cross(c - b, p - b));
+  const float e2 = dot(u, cross(a - c, p - c));
+  const float tot = e0 + e1 + e2;
+  const float slack = -1e-4f * fabsf(tot);
+  return (tot > 0.f && e0 >= slack && e1 >= slack && e2 >= slack) ? 1u : 0u;
+}
+
+struct EpaResult {
+  int status;
+  float depth;
+  f3 p0, p1;
+  int iterations;
+};
+
+// epa_polytope_utils.h:71-86 with p = origin
+__device__ __forceinline__ float origin_to_plane(f3 a, f3 b, f3 c) {
+  const f3 n = cross(a - b, b - c);
+  const float nl = nrm(n);
+  if (nl <= 0.f) {
+    const f3 ab = b - a;
+    const float len = nrm(ab);
+    if (len <= 0.f) return nrm(a);
+    return nrm(cross(mk3(0, 0, 0) - a, ab)) / len;
+  }
+  return fabsf(dot(n * (1.f / nl), a));
+}
+
+__device__ __forceinline__ float point_to_line(f3 p, f3 a, f3 b) {
+  const f3 ab = b - a;
+  const float len = nrm(ab);
+  if (len <= 0.f) return nrm(p - a);
+  return nrm(cross(p - a, ab)) / len;
+}
+__device__ __forceinline__ float point_to_plane(f3 p, f3 a, f3 b, f3 c) {
+  const f3 n = cross(a - b, b - c);
+  const float nl = nrm(n);
+  if (nl <= 0.f) return point_to_line(p, a, b);
+  return fabsf(dot(n * (1.f / nl), a - p));
+}
+
+template <int FMAX, int VMAX>
+struct EpaWarp {
+  EpaSmem<FMAX, VMAX>& P;
+  const MinkowskiSupport<32>& sup;
+  float tol;
+  unsigned lane;
+  int nv, hw, live;
+
+  __device__ __forceinline__ f3 W(uint32_t i) const { return ld3(P.vw[i]); }
+
+  // Vertices pushed by lane 0; callers __syncwarp before reading them.
+  __device__ __forceinline__ void push_vertex(f3 pa, f3 pb) {
+    if (lane == 0) {
+      const f3 w = pa - pb;
+      P.vw[nv] = make_float4(w.x, w.y, w.z, 0.f);
+      P.vpa[nv] = make_float4(pa.x, pa.y, pa.z, 0.f);
+    }
+    ++nv;
+  }
+
+  // Build the initial polytope from faces (index triples into the vertices
+  // already pushed), oriented away from the vertex centroid; lane 0 only.
+  // Returns false when the faces do not close up.
+  __device__ bool build_faces(const int (*tri)[3], int nf) {
+    bool ok = true;
+    if (lane == 0) {
+      f3 c = mk3(0, 0, 0);
+      for (int i = 0; i < nv; ++i) c = c + W(i);
+      c = c * (1.f / (float)nv);
+      for (int f = 0; f < nf; ++f) {
+        int i = tri[f][0], j = tri[f][1], k = tri[f][2];
+        const f3 n = cross(W(j) - W(i), W(k) - W(i));
+        if (dot(n, W(i) - c) < 0.f) { const int t = j; j = k; k = t; }
+        const float4 pl = face_plane(W(i), W(j), W(k));
+        P.fv[f] = (uint32_t)i | ((uint32_t)j << 8) | ((uint32_t)k << 16) | (projects_inside(W(i), W(j), W(k), pl) << 24);
+        P.fn[f] = pl;
+        P.falive[f] = 1;
+      }
+      for (int f = 0; f < nf && ok; ++f) {
+        for (int e = 0; e < 3 && ok; ++e) {
+          const uint32_t u = fvert(P.fv[f], e), v = fvert(P.fv[f], (e + 1) % 3);
+          int found = -1;
+          for (int g = 0; g < nf && found < 0; ++g) {
+            if (g == f) continue;
+            for (int h = 0; h < 3; ++h)
+              if (fvert(P.fv[g], h) == v && fvert(P.fv[g], (h + 1) % 3) == u) { found = g; break; }
+          }
+          if (found < 0) ok = false;
+          else P.fadj[f][e] = (uint16_t)found;
+        }
+      }
+    }
+    hw = nf;
+    live = nf;
+    return __shfl_sync(0xFFFFFFFFu, (int)ok, 0) != 0;
+  }
+
+  // formNewTetrahedronPolytope, epa_simplex2polytope.hpp:143-174
+  __device__ bool tetra() {
+    const int tri[4][3] = {{0, 1, 2}, {0, 3, 1}, {1, 3, 2}, {2, 3, 0}};
+    return build_faces(tri, 4);
+  }
+
+  // Final closest-face solve in FP64 (epa.hpp:425-498); falls back to the
+  // last support pair like assignPenetrationPair (epa.hpp:340-365).
+  __device__ void finalize(uint32_t fvp, f3 cand_pa, f3 cand_pb, EpaResult& r) const {
+    const uint32_t ia = fvert(fvp, 0), ib = fvert(fvp, 1), ic = fvert(fvp, 2);
+    const d3 a = tod(W(ia)), b = tod(W(ib)), c = tod(W(ic));
+    const d3 n = cross(b - a, c - a);
+    const double n2 = dot(n, n);
+    bool ok = n2 > 0.0;
+    if (ok) {
+      const d3 u = n * (1.0 / sqrt(n2));
+      const double dist = dot(u, a);
+      const d3 p = u * dist;
+      const double area = sqrt(n2);
+      const d3 dl0 = a - b, dl1 = b - c, dl2 = c - a;
+      double wgt[3];
+      const d3 q0 = cross(dl1, b - p), q1 = cross(dl2, c - p), q2 = cross(dl0, a - p);
+      wgt[0] = sqrt(dot(q0, q0)) / area;
+      wgt[1] = sqrt(dot(q1, q1)) / area;
+      const double chk = sqrt(dot(q2, q2)) / area;
+      wgt[2] = 1.0 - wgt[0] - wgt[1];
+      if (fabs(chk - wgt[2]) > 0.01) ok = false;
+      if (ok) {
+        const d3 pa0 = tod(ld3(P.vpa[ia])), pa1 = tod(ld3(P.vpa[ib])), pa2 = tod(ld3(P.vpa[ic]));
+        const d3 pb0 = pa0 - a, pb1 = pa1 - b, pb2 = pa2 - c;
+        const d3 x0 = (pa0 * wgt[0] + pa1 * wgt[1]) + pa2 * wgt[2];
+        const d3 x1 = (pb0 * wgt[0] + pb1 * wgt[1]) + pb2 * wgt[2];
+        r.p0 = mk3((float)x0.x, (float)x0.y, (float)x0.z);
+        r.p1 = mk3((float)x1.x, (float)x1.y, (float)x1.z);
+        r.depth = (float)fabs(dist);
+        return;
+      }
+    }
+    r.p0 = cand_pa;
+    r.p1 = cand_pb;
+    r.depth = nrm(cand_pa - cand_pb);
+  }
+
+  __device__ void touching(f3 pa, f3 pb, EpaResult& r) const {
+    const f3 m = (pa + pb) * 0.5f;
+    r.status = kEpaTouching;
+    r.depth = 0.f;
+    r.p0 = m;
+    r.p1 = m;
+  }
+
+  // simplexToPolytope3, epa_simplex2polytope.hpp:112-141: vertices 0..2 pushed.
+  __device__ bool from_triangle(EpaResult& r, bool& done) {
+    const f3 a = W(0), b = W(1), c = W(2);
+    f3 n = cross(b - a, c - a);
+    if (!(sqn(n) > 0.f)) { r.status = kEpaFailed; done = true; return false; }
+    n = normalized(n);
+    f3 pa0, pb0, pa1, pb1;
+    sup(n, pa0, pb0);
+    sup(-n, pa1, pb1);
+    const float d0 = point_to_plane(pa0 - pb0, a, b, c);
+    const float d1 = point_to_plane(pa1 - pb1, a, b, c);
+    if (d0 <= tol) { touching(pa0, pb0, r); done = true; return false; }
+    if (d1 <= tol) { touching(pa1, pb1, r); done = true; return false; }
+    if (d0 > d1) push_vertex(pa0, pb0);
+    else push_vertex(pa1, pb1);
+    __syncwarp();
+    return tetra();
+  }
+
+  // simplexToPolytope2, epa_simplex2polytope.hpp:176-376: vertices 0, 1 pushed.
+  __device__ bool from_segment(EpaResult& r, bool& done) {
+    const f3 a = W(0), b = W(1);
+    const float thr = tol, thr2 = tol * tol;
+    const f3 ab = b - a;
+    if (sqn(ab) < thr2) { r.status = kEpaFailed; done = true; return false; }
+    const f3 abu = normalized(ab);
+    f3 dinit = mk3(abu.y, -abu.x, 0.f);
+    bool okd = sqn(dinit) > thr2;
+    if (!okd) { dinit = mk3(abu.z, 0.f, -abu.x); okd = sqn(dinit) > thr2; }
+    if (!okd) { dinit = mk3(0.f, abu.z, -abu.y); okd = sqn(dinit) > thr2; }
+    if (!okd) { r.status = kEpaFailed; done = true; return false; }
+    dinit = normalized(dinit);
+    f3 dcur = dinit, pa, pb;
+    bool found = false;
+    for (int i = 0; i < 72; ++i) {
+      sup(dcur, pa, pb);
+      const f3 v = pa - pb;
+      if (point_to_line(v, a, b) > thr) { found = true; break; }
+      const float step = 2.0f * 3.145926f / 72.0f;  // the reference's constant
+      dcur = normalized(dcur + cross(abu, v) * step);
+    }
+    if (!found) {
+      sup(dinit, pa, pb);
+      touching(pa, pb, r);
+      done = true;
+      return false;
+    }
+    const f3 v0 = pa - pb, v0pa = pa, v0pb = pb;
+    f3 pa1, pb1;
+    sup(-dcur, pa1, pb1);
+    const f3 v1 = pa1 - pb1;
+    if (point_to_line(v1, a, b) < thr) { touching(pa1, pb1, r); done = true; return false; }
+    const f3 nn = cross(v0 - a, v1 - a);
+    if (sqn(nn) < thr2) { r.status = kEpaFailed; done = true; return false; }
+    const f3 d2 = normalized(nn);
+    f3 pa2, pb2, pa3, pb3;
+    sup(d2, pa2, pb2);
+    if (point_to_line(pa2 - pb2, a, b) < thr) { touching(pa2, pb2, r); done = true; return false; }
+    sup(-d2, pa3, pb3);
+    if (point_to_line(pa3 - pb3, a, b) < thr) { touching(pa3, pb3, r); done = true; return false; }
+    // The reference's double pyramid: ring a, v0, b, v1 (slots 0, 2, 1, 3)
+    // with apexes v2 (slot 4) and v3 (slot 5).
+    push_vertex(v0pa, v0pb);
+    push_vertex(pa1, pb1);
+    push_vertex(pa2, pb2);
+    push_vertex(pa3, pb3);
+    __syncwarp();
+    const int tri[8][3] = {{4, 0, 2}, {4, 2, 1}, {4, 1, 3}, {4, 3, 0}, {5, 0, 2}, {5, 2, 1}, {5, 1, 3}, {5, 3, 0}};
+    return build_faces(tri, 8);
+  }
+
+  // Warp argmin of the plane distance over live faces the origin projects
+  // into (ties: lowest slot); over all live faces when none qualifies.
+  __device__ __forceinline__ void nearest(int& best_slot, float& best_d) const {
+    float bd = INFINITY, ad = INFINITY;
+    int bs = 0x7FFFFFFF, as = 0x7FFFFFFF;
+    for (int s = (int)lane; s < hw; s += 32) {
+      if (P.falive[s]) {
+        const float d = P.fn[s].w;
+        if (d < ad) { ad = d; as = s; }
+        if ((P.fv[s] >> 24) && d < bd) { bd = d; bs = s; }
+      }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const float od = __shfl_xor_sync(0xFFFFFFFFu, bd, off);
+      const int os = __shfl_xor_sync(0xFFFFFFFFu, bs, off);
+      if (od < bd || (od == bd && os < bs)) { bd = od; bs = os; }
+      const float oa = __shfl_xor_sync(0xFFFFFFFFu, ad, off);
+      const int oas = __shfl_xor_sync(0xFFFFFFFFu, as, off);
+      if (oa < ad || (oa == ad && oas < as)) { ad = oa; as = oas; }
+    }
+    if (bs == 0x7FFFFFFF) { bs = as; bd = ad; }
+    best_slot = __shfl_sync(0xFFFFFFFFu, bs, 0);
+    best_d = __shfl_sync(0xFFFFFFFFu, bd, 0);
+  }
+
+  // One expansion with the new vertex nv-1; returns 0 ok, 1 capacity, 2 broken topology.
+  __device__ int expand(int start, int max_faces) {
+    const uint32_t vnew = (uint32_t)(nv - 1);
+    const f3 w = W(vnew);
+    for (int s = (int)lane; s < hw; s += 32) {
+      uint8_t v = 0;
+      if (P.falive[s]) {
+        const float4 q = P.fn[s];
+        v = (dot(ld3(q), w - W(fvert(P.fv[s], 0))) >= 0.f) ? 1 : 0;
+      }
+      P.fvis[s] = v;
+    }
+    __syncwarp();
+    if (lane == 0) P.fvis[start] = 2;
+    __syncwarp();
+    for (int round = 0; round < FMAX; ++round) {
+      bool changed = false;
+      for (int s = (int)lane; s < hw; s += 32) {
+        if (P.fvis[s] == 1) {
+          if (P.fvis[P.fadj[s][0]] == 2 || P.fvis[P.fadj[s][1]] == 2 || P.fvis[P.fadj[s][2]] == 2) {
+            P.fvis[s] = 2;
+            changed = true;
+          }
+        }
+      }
+      __syncwarp();
+      if (!__any_sync(0xFFFFFFFFu, changed)) break;
+    }
+    // Gather: free slots (dead or now removed) and horizon edges, in slot order.
+    int n_free = 0, n_hz = 0, n_rem = 0;
+    for (int base = 0; base < hw; base += 32) {
+      const int s = base + (int)lane;
+      bool fr = false, rem = false;
+      int h = 0;
+      uint32_t hmask = 0;
+      if (s < hw) {
+        rem = P.fvis[s] == 2;
+        fr = rem || !P.falive[s];
+        if (rem) {
+#pragma unroll
+          for (int k = 0; k < 3; ++k)
+            if (P.fvis[P.fadj[s][k]] != 2) { hmask |= 1u << k; ++h; }
+        }
+      }
+      const unsigned fb = __ballot_sync(0xFFFFFFFFu, fr);
+      const unsigned lt = (1u << lane) - 1u;
+      if (fr) P.freelist[n_free + __popc(fb & lt)] = (uint16_t)s;
+      n_free += __popc(fb);
+      n_rem += __popc(__ballot_sync(0xFFFFFFFFu, rem));
+      // horizon prefix sum
+      int incl = h;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const int t = __shfl_up_sync(0xFFFFFFFFu, incl, off);
+        if ((int)lane >= off) incl += t;
+      }
+      const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+      int k = n_hz + incl - h;
+      if (k + h <= FMAX + 8) {
+        for (int e = 0; e < 3; ++e)
+          if (hmask & (1u << e)) { P.hz_s[k] = (uint16_t)s; P.hz_e[k] = (uint8_t)e; ++k; }
+      }
+      n_hz += total;
+    }
+    const int new_live = live - n_rem + n_hz;
+    const int fresh = n_hz > n_free ? n_hz - n_free : 0;
+    if (n_hz < 3 || n_hz > FMAX + 8) return 2;
+    if (new_live > max_faces || hw + fresh > FMAX) return 1;
+    __syncwarp();
+    // Phase A: read the horizon edges' endpoints and outside neighbours (the
+    // removed faces' slots are overwritten below).
+    uint32_t ha[(FMAX + 8 + 31) / 32], hb[(FMAX + 8 + 31) / 32], hg[(FMAX + 8 + 31) / 32];
+    int j = 0;
+    for (int k = (int)lane; k < n_hz; k += 32, ++j) {
+      const uint32_t s = P.hz_s[k], e = P.hz_e[k];
+      ha[j] = fvert(P.fv[s], (int)e);
+      hb[j] = fvert(P.fv[s], (int)((e + 1) % 3));
+      hg[j] = P.fadj[s][e];
+      P.hz_slot[k] = (k < n_free) ? P.freelist[k] : (uint16_t)(hw + (k - n_free));
+    }
+    __syncwarp();
+    for (int s = (int)lane; s < hw; s += 32)
+      if (P.fvis[s] == 2) P.falive[s] = 0;
+    j = 0;
+    for (int k = (int)lane; k < n_hz; k += 32, ++j) {
+      P.start_at[ha[j]] = kNoSlot;
+      P.start_at[hb[j]] = kNoSlot;
+    }
+    __syncwarp();
+    // Phase B: write the fan (a, b, new) and re-point the outside neighbours.
+    bool err = false;
+    j = 0;
+    for (int k = (int)lane; k < n_hz; k += 32, ++j) {
+      const uint32_t t = P.hz_slot[k];
+      const uint32_t a = ha[j], b = hb[j], g = hg[j];
+      const float4 pl = face_plane(W(a), W(b), w);
+      P.fv[t] = a | (b << 8) | (vnew << 16) | (projects_inside(W(a), W(b), w, pl) << 24);
+      P.fn[t] = pl;
+      P.falive[t] = 1;
+      P.fadj[t][0] = (uint16_t)g;
+      const uint32_t gv = P.fv[g];
+      int gj = -1;
+#pragma unroll
+      for (int h = 0; h < 3; ++h)
+        if (fvert(gv, h) == b && fvert(gv, (h + 1) % 3) == a) gj = h;
+      if (gj < 0) err = true;
+      else P.fadj[g][gj] = (uint16_t)t;
+      if (atomicCAS(&P.start_at[a], kNoSlot, t) != kNoSlot) err = true;
+    }
+    __syncwarp();
+    // Phase C: link consecutive fan faces.
+    j = 0;
+    for (int k = (int)lane; k < n_hz; k += 32, ++j) {
+      const uint32_t t = P.hz_slot[k];
+      const uint32_t u = P.start_at[hb[j]];
+      if (u == kNoSlot) { err = true; continue; }
+      P.fadj[t][1] = (uint16_t)u;
+      P.fadj[u][2] = (uint16_t)t;
+    }
+    __syncwarp();
+    if (__any_sync(0xFFFFFFFFu, err)) return 2;
+    live = new_live;
+    hw += fresh;
+    return 0;
+  }
+
+  // Runs EPA from the GJK simplex (rank, pa[], pb[]).
+  __device__ EpaResult run(int rank, const f3* spa, const f3* spb, int max_iter, int max_faces) {
+    EpaResult r;
+    r.status = kEpaFailed;
+    r.depth = 0.f;
+    r.p0 = r.p1 = mk3(0, 0, 0);
+    r.iterations = 0;
+    nv = 0;
+    hw = 0;
+    live = 0;
+    const float tol2 = tol * tol;
+    for (int i = 0; i < rank; ++i) {
+      if (sqn(spa[i] - spb[i]) <= tol2) { touching(spa[i], spb[i], r); return r; }
+    }
+    for (int i = 0; i < rank; ++i) push_vertex(spa[i], spb[i]);
+    __syncwarp();
+    bool done = false, ok = false;
+    if (rank == 4) {
+      const int faces[4][3] = {{0, 1, 2}, {0, 2, 3}, {0, 1, 3}, {1, 2, 3}};
+      int tri = -1;
+      for (int f = 0; f < 4 && tri < 0; ++f)
+        if (origin_to_plane(W(faces[f][0]), W(faces[f][1]), W(faces[f][2])) < tol) tri = f;
+      if (tri < 0) {
+        ok = tetra();
+      } else {
+        const f3 qa[3] = {spa[faces[tri][0]], spa[faces[tri][1]], spa[faces[tri][2]]};
+        const f3 qb[3] = {spb[faces[tri][0]], spb[faces[tri][1]], spb[faces[tri][2]]};
+        nv = 0;
+        __syncwarp();
+        for (int i = 0; i < 3; ++i) push_vertex(qa[i], qb[i]);
+        __syncwarp();
+        ok = from_triangle(r, done);
+      }
+    } else if (rank == 3) {
+      ok = from_triangle(r, done);
+    } else if (rank == 2) {
+      ok = from_segment(r, done);
+    } else {
+      r.status = kEpaTouching;
+      r.p0 = spa[0];
+      r.p1 = spb[0];
+      return r;
+    }
+    if (done) return r;
+    if (!ok) { r.status = kEpaFailed; return r; }
+    __syncwarp();
+    for (int it = 0;; ) {
+      int bs;
+      float bd;
+      nearest(bs, bd);
+      if (bs == 0x7FFFFFFF || !(bd < INFINITY)) { r.status = kEpaFailed; return r; }
+      const f3 n = ld3(P.fn[bs]);
+      const uint32_t bfv = P.fv[bs];  // the slot may be reused by the expansion below
+      f3 pa, pb;
+      sup(n, pa, pb);
+      const float delta = dot(n, pa - pb) - bd;
+      FCLG_EPA_TRACE(P, it, bs, bd, delta, live, hw, nv);
+      if (delta <= tol) {
+        finalize(bfv, pa, pb, r);
+        r.status = kEpaOK;
+        return r;
+      }
+      if (nv >= VMAX) {
+        finalize(bfv, pa, pb, r);
+        r.status = kEpaMallocFailed;
+        return r;
+      }
+      push_vertex(pa, pb);
+      __syncwarp();
+      const int ex = expand(bs, max_faces);
+      if (ex == 1) {
+        finalize(bfv, pa, pb, r);
+        r.status = kEpaMallocFailed;
+        return r;
+      }
+      if (ex == 2) {
+        // The new point's visible patch has no simple horizon at FP32
+        // resolution (near-coplanar faces, delta is already tiny): end with
+        // the current nearest face, whose plane is within delta of the
+        // support.
+        finalize(bfv, pa, pb, r);
+        r.status = kEpaOK;
+        return r;
+      }
+      ++it;
+      r.iterations = it;
+      if (it >= max_iter) {
+        finalize(bfv, pa, pb, r);
+        r.status = kEpaIterLimit;
+        return r;
+      }
+    }
+  }
+};
+
+}  // namespace fclg

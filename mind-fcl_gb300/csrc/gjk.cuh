@@ -1,0 +1,435 @@
+// GJK boolean + GJK separation distance in FP32, one pair per group of LANES
+// lanes.  The control flow restates the reference's GJK (gjk.hpp:10-363) and
+// its minimum-distance loop (gjk_distance.hpp:10-559) branch for branch, so
+// that the flag, the status and the witness points agree with the FP64
+// reference except where FP32 rounding moves a decision that sits within a
+// few ulps of its threshold.  The tetrahedron orientation tests of
+// simplexProjection4 (the degenerate-simplex determinants) run in FP64.
+//
+// All lanes of a group run this scalar code redundantly on identical values;
+// only the support evaluations split work across the group.
+#pragma once
+#include "support.cuh"
+
+#ifndef FCLG_GJK_TRACE
+#define FCLG_GJK_TRACE(...) \
+  do {                      \
+  } while (0)
+#endif
+
+namespace fclg {
+
+struct Simplex {
+  f3 w[4];   // Minkowski-difference vertex = a - b
+  f3 a[4];   // support point on shape a (a's frame)
+  f3 b[4];   // support point on shape b (a's frame)
+  int rank;
+  __device__ __forceinline__ void set(int i, f3 pa, f3 pb) {
+    a[i] = pa;
+    b[i] = pb;
+    w[i] = pa - pb;
+  }
+  __device__ __forceinline__ void copy(int dst, int src) {
+    w[dst] = w[src];
+    a[dst] = a[src];
+    b[dst] = b[src];
+  }
+};
+
+enum class Proj { Failed, Continue, Intersect, ZeroVolume };
+enum class Upd { NoImprovement, OK, Failed };
+
+struct GjkOut {
+  int status;      // GJK_Status
+  bool point_valid;
+  f3 p0, p1;       // witness points (a's frame) when separated
+  int iterations;  // boolean + distance loop iterations
+};
+
+// gjk.hpp:161-197
+__device__ __forceinline__ Proj project2(Simplex& s, f3& d) {
+  const f3 a = s.w[1], b = s.w[0];
+  const f3 a_to_b = b - a;
+  const float ao_dot_ab = -dot(a_to_b, a);
+  const f3 ab_cross_ao = cross(a, a_to_b);
+  if (ao_dot_ab > 0.f && sqn(ab_cross_ao) <= 0.f) return Proj::Intersect;
+  if (ao_dot_ab <= 0.f) {
+    s.copy(0, 1);
+    s.rank = 1;
+    d = -normalized(a);
+    return Proj::Continue;
+  }
+  d = normalized(cross(ab_cross_ao, a_to_b));
+  return Proj::Continue;
+}
+
+// gjk.hpp:199-278
+__device__ __forceinline__ Proj project3(Simplex& s, f3& d, float tol) {
+  const f3 a = s.w[2], b = s.w[1], c = s.w[0];
+  const f3 a_to_b = b - a, a_to_c = c - a;
+  const bool sep_b = dot(a, a_to_b) >= 0.f;
+  const bool sep_c = dot(a, a_to_c) >= 0.f;
+  if (sep_b && sep_c) {
+    s.copy(0, 2);
+    s.rank = 1;
+    d = normalized(-a);
+    return Proj::Continue;
+  }
+  const f3 n = cross(a_to_b, a_to_c);
+  const f3 ac_normal = cross(n, a_to_c);
+  if (dot(a, ac_normal) <= 0.f) {
+    s.copy(1, 2);
+    s.rank = 2;
+    d = normalized(cross(cross(a, a_to_c), a_to_c));
+    return Proj::Continue;
+  }
+  const f3 ab_normal = cross(a_to_b, n);
+  if (dot(a, ab_normal) <= 0.f) {
+    s.copy(0, 1);
+    s.copy(1, 2);
+    s.rank = 2;
+    d = normalized(cross(cross(a, a_to_b), a_to_b));
+    return Proj::Continue;
+  }
+  const float area = nrm(n);
+  if (area < tol * tol) return Proj::Failed;
+  const f3 nu = n * (1.f / area);
+  const float nu_dot_a = dot(nu, a);
+  if (fabsf(nu_dot_a) < tol) return Proj::Intersect;
+  d = (nu_dot_a <= 0.f) ? nu : -nu;
+  return Proj::Continue;
+}
+
+// gjk.hpp:280-360; orientation tests in FP64.
+__device__ __forceinline__ Proj project4(Simplex& s, f3& dir, float tol) {
+  const d3 a = tod(s.w[3]), b = tod(s.w[2]), c = tod(s.w[1]), dd = tod(s.w[0]);
+  const d3 ab = b - a, ac = c - a, ad = dd - a;
+  d3 abc = cross(ab, ac), acd = cross(ac, ad), abd = cross(ab, ad);
+  const double abc_ad = dot(abc, ad), acd_ab = dot(acd, ab), abd_ac = dot(abd, ac);
+  if (fabs(abc_ad) <= 0.0) return Proj::ZeroVolume;
+  if (abc_ad > 0) abc = abc * -1.0;
+  if (acd_ab > 0) acd = acd * -1.0;
+  if (abd_ac > 0) abd = abd * -1.0;
+  const bool d_side = dot(a, abc) > 0;
+  const bool c_side = dot(a, abd) > 0;
+  const bool b_side = dot(a, acd) > 0;
+  if (d_side && c_side && b_side) return Proj::Intersect;
+  if (!b_side) {
+    s.copy(2, 3);
+  } else if (!c_side) {
+    s.copy(1, 2);
+    s.copy(2, 3);
+  } else {
+    s.copy(0, 1);
+    s.copy(1, 2);
+    s.copy(2, 3);
+  }
+  s.rank = 3;
+  return project3(s, dir, tol);
+}
+
+// gjk_distance.hpp:128-153 (on simplex slots 1 = newest, 0)
+__device__ __forceinline__ void update2(Simplex& s, f3& out, float tol) {
+  const f3 s1 = s.w[1], s2 = s.w[0];
+  const f3 s1_to_s2 = s2 - s1;
+  const float len2 = sqn(s1_to_s2);
+  const float t = -dot(s1, s1_to_s2);
+  if (t <= 0.f || len2 <= tol * tol) {
+    out = s1;
+    s.copy(0, 1);
+    s.rank = 1;
+  } else if (t >= len2) {
+    out = s2;
+    s.rank = 1;
+  } else {
+    const float w2 = t / len2;
+    out = w2 * s2 + (1.f - w2) * s1;
+  }
+}
+
+// gjk_distance.hpp:155-286 (slot 2 newest)
+__device__ __forceinline__ void update3(Simplex& s, f3& out, float tol) {
+  const f3 s1 = s.w[2], s2 = s.w[1], s3 = s.w[0];
+  const f3 s1_to_s2 = s2 - s1, s1_to_s3 = s3 - s1;
+  const bool sep2 = dot(s1, s1_to_s2) >= 0.f;
+  const bool sep3 = dot(s1, s1_to_s3) >= 0.f;
+  if (sep2 && sep3) {
+    out = s1;
+    s.copy(0, 2);
+    s.rank = 1;
+    return;
+  }
+  const f3 n = cross(s1_to_s2, s1_to_s3);
+  const float area2 = sqn(n);
+  const bool zero_area = area2 <= 0.f;
+  const bool s12_sep = dot(s1, cross(n, s1_to_s2)) > 0.f;
+  if (!sep2 && s12_sep) {
+    s.copy(0, 1);
+    s.copy(1, 2);
+    s.rank = 2;
+    update2(s, out, tol);
+    return;
+  }
+  const bool s13_sep = dot(s1, cross(n, s1_to_s3)) < 0.f;
+  if (!sep3 && s13_sep) {
+    s.copy(1, 2);
+    s.rank = 2;
+    update2(s, out, tol);
+    return;
+  }
+  float best = -1.f;
+  f3 best_pt = mk3(0, 0, 0), pt;
+  Simplex best_s = s, c;
+  if (zero_area || s12_sep) {
+    c = s;
+    c.copy(0, 1);
+    c.copy(1, 2);
+    c.rank = 2;
+    update2(c, pt, tol);
+    const float dd = sqn(pt);
+    if (best < 0.f || dd < best) { best = dd; best_s = c; best_pt = pt; }
+  }
+  if (zero_area || s13_sep) {
+    c = s;
+    c.copy(1, 2);
+    c.rank = 2;
+    update2(c, pt, tol);
+    const float dd = sqn(pt);
+    if (best < 0.f || dd < best) { best = dd; best_s = c; best_pt = pt; }
+  }
+  const bool s23_sep = dot(s2, cross(n, s3 - s2)) > 0.f;
+  if (zero_area || s23_sep) {
+    c = s;
+    c.rank = 2;
+    update2(c, pt, tol);
+    const float dd = sqn(pt);
+    if (best < 0.f || dd < best) { best = dd; best_s = c; best_pt = pt; }
+  }
+  if (best < 0.f) {
+    out = n * (dot(s1, n) / area2);
+  } else {
+    s = best_s;
+    out = best_pt;
+  }
+}
+
+// gjk_distance.hpp:288-373 (slot 3 newest): best of faces (3,2,1), (3,2,0), (3,1,0).
+__device__ __forceinline__ Upd update4(Simplex& s, f3& out, float tol) {
+  float best = -1.f;
+  f3 best_pt = mk3(0, 0, 0), pt;
+  Simplex best_s = s, c;
+  c = s;
+  c.copy(0, 1); c.copy(1, 2); c.copy(2, 3);
+  c.rank = 3;
+  update3(c, pt, tol);
+  float dd = sqn(pt);
+  if (best < 0.f || dd < best) { best = dd; best_pt = pt; best_s = c; }
+  c = s;
+  c.copy(1, 2); c.copy(2, 3);
+  c.rank = 3;
+  update3(c, pt, tol);
+  dd = sqn(pt);
+  if (best < 0.f || dd < best) { best = dd; best_pt = pt; best_s = c; }
+  c = s;
+  c.copy(2, 3);
+  c.rank = 3;
+  update3(c, pt, tol);
+  dd = sqn(pt);
+  if (best < 0.f || dd < best) { best = dd; best_pt = pt; best_s = c; }
+  if (best < 0.f) return Upd::NoImprovement;
+  s = best_s;
+  out = best_pt;
+  return Upd::OK;
+}
+
+__device__ __forceinline__ Upd update_simplex(Simplex& s, f3& out, float tol) {
+  if (s.rank == 1) { out = s.w[0]; return Upd::OK; }
+  if (s.rank == 2) { update2(s, out, tol); return Upd::OK; }
+  if (s.rank == 3) { update3(s, out, tol); return Upd::OK; }
+  if (s.rank == 4) return update4(s, out, tol);
+  return Upd::Failed;
+}
+
+// gjk_distance.hpp:375-470; the stored support points replace the
+// reference's re-evaluation of support0/support1 at the stored directions.
+__device__ __forceinline__ bool extract_no_sub(const Simplex& s, f3& p0, f3& p1) {
+  constexpr float kBaryTol = 1e-3f;
+  if (s.rank == 4 || s.rank < 1) return false;
+  if (s.rank == 1) {
+    p0 = s.a[0];
+    p1 = s.b[0];
+    return true;
+  }
+  if (s.rank == 2) {
+    const f3 s1_to_s2 = s.w[1] - s.w[0];
+    const float len2 = sqn(s1_to_s2);
+    if (len2 <= 0.f) {
+      p0 = s.a[0];
+      p1 = s.b[0];
+      return true;
+    }
+    const float w2 = -dot(s.w[0], s1_to_s2) / len2;
+    if (w2 > 1.f + kBaryTol) { p0 = s.a[1]; p1 = s.b[1]; return false; }
+    if (w2 < -kBaryTol) { p0 = s.a[0]; p1 = s.b[0]; return false; }
+    const float w1 = 1.f - w2;
+    p0 = s.a[0] * w1 + s.a[1] * w2;
+    p1 = s.b[0] * w1 + s.b[1] * w2;
+    return true;
+  }
+  const f3 s1_to_s2 = s.w[1] - s.w[0], s1_to_s3 = s.w[2] - s.w[0];
+  const f3 n = cross(s1_to_s2, s1_to_s3);
+  const float area2 = sqn(n);
+  if (area2 <= 0.f) return false;
+  const f3 proj = n * (dot(s.w[0], n) / area2);
+  const float area = sqrtf(area2);
+  const float w2 = nrm(cross(s1_to_s3, s.w[0] - proj)) / area;
+  const float w3 = nrm(cross(s1_to_s2, s.w[0] - proj)) / area;
+  const float w1 = 1.f - w2 - w3;
+  if (w1 < -kBaryTol || w2 < -kBaryTol || w3 < -kBaryTol) return false;
+  p0 = (s.a[0] * w1 + s.a[1] * w2) + s.a[2] * w3;
+  p1 = (s.b[0] * w1 + s.b[1] * w2) + s.b[2] * w3;
+  return true;
+}
+
+// gjk_distance.hpp:472-559
+__device__ __forceinline__ bool extract_try_sub(const Simplex& s, f3& p0, f3& p1) {
+  if (s.rank >= 4) return false;
+  if (s.rank <= 2) {
+    extract_no_sub(s, p0, p1);
+    return true;
+  }
+  float best = -1.f;
+  f3 b0 = mk3(0, 0, 0), b1 = mk3(0, 0, 0), c0, c1;
+  Simplex c = s;
+  if (extract_no_sub(c, c0, c1)) {
+    const float dd = sqn(c0 - c1);
+    if (best < 0.f || dd < best) { best = dd; b0 = c0; b1 = c1; }
+  }
+  c = s;
+  c.rank = 2;
+  extract_no_sub(c, c0, c1);
+  float dd = sqn(c0 - c1);
+  if (best < 0.f || dd < best) { best = dd; b0 = c0; b1 = c1; }
+  c = s;
+  c.copy(1, 2);
+  c.rank = 2;
+  extract_no_sub(c, c0, c1);
+  dd = sqn(c0 - c1);
+  if (best < 0.f || dd < best) { best = dd; b0 = c0; b1 = c1; }
+  c = s;
+  c.copy(0, 1);
+  c.copy(1, 2);
+  c.rank = 2;
+  extract_no_sub(c, c0, c1);
+  dd = sqn(c0 - c1);
+  if (best < 0.f || dd < best) { best = dd; b0 = c0; b1 = c1; }
+  p0 = b0;
+  p1 = b1;
+  return true;
+}
+
+// gjk_distance.hpp:10-105: minimum distance from a separating vertex.
+template <class Sup>
+__device__ __forceinline__ bool min_distance(const Sup& sup, Simplex& s, float tol, int max_iter, f3& p0, f3& p1,
+                                             int& iters) {
+  f3 cur;
+  if (update_simplex(s, cur, tol) != Upd::OK) return false;
+  float book = nrm(cur);
+  if (book <= tol) return extract_no_sub(s, p0, p1);
+  f3 next = cur * (-1.f / book);
+  const float tol2 = tol * tol;
+  for (int it = 0; it < max_iter; ++it) {
+    ++iters;
+    f3 pa, pb;
+    sup(next, pa, pb);
+    const f3 w = pa - pb;
+    FCLG_GJK_TRACE(it, -1, dot(next, w - cur), 0.f);
+    if (dot(next, w - cur) < tol) return extract_no_sub(s, p0, p1);
+    bool dup = false;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (j < s.rank && sqn(s.w[j] - w) < tol2) dup = true;
+    if (dup) return extract_no_sub(s, p0, p1);
+    // s.rank is 1..3 here
+    if (s.rank == 1) s.set(1, pa, pb);
+    else if (s.rank == 2) s.set(2, pa, pb);
+    else s.set(3, pa, pb);
+    s.rank += 1;
+    const Upd st = update_simplex(s, cur, tol);
+    if (st == Upd::NoImprovement) return extract_no_sub(s, p0, p1);
+    if (st != Upd::OK) return false;
+    const float nd = nrm(cur);
+    FCLG_GJK_TRACE(it, s.rank, nd, book - nd);
+    if (book - nd < tol) return extract_no_sub(s, p0, p1);
+    if (nd < tol) return extract_no_sub(s, p0, p1);
+    book = nd;
+    next = cur * (-1.f / book);
+  }
+  return false;
+}
+
+// gjk.hpp:10-140.  want_distance selects the MinSeparationDistanceOutput path.
+template <class Sup>
+__device__ __forceinline__ GjkOut gjk_evaluate(const Sup& sup, f3 guess, float tol, int max_iter, bool want_distance,
+                                               Simplex& s) {
+  GjkOut o;
+  o.point_valid = false;
+  o.iterations = 0;
+  o.p0 = o.p1 = mk3(0, 0, 0);
+  f3 d = guess;
+  if (sqn(d) <= 0.f) d = mk3(1, 0, 0);
+  d = normalized(d);
+  const float tol2 = tol * tol;
+  f3 pa, pb;
+  sup(d, pa, pb);
+  s.set(0, pa, pb);
+  s.rank = 1;
+  if (sqn(s.w[0]) <= tol2) { o.status = kGjkIntersect; return o; }
+  bool separated = dot(s.w[0], d) < 0.f;
+  int undetermined = -1;
+  if (!separated) {
+    d = -d;
+    int it = 0;
+    for (; it < max_iter; ++it) {
+      o.iterations = it + 1;
+      sup(d, pa, pb);
+      const f3 w = pa - pb;
+      if (dot(w, d) < 0.f) {
+        s.set(0, pa, pb);  // the separating vertex seeds the distance simplex
+        s.rank = 1;
+        separated = true;
+        break;
+      }
+      bool dup = false;
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (j < s.rank && sqn(s.w[j] - w) < tol2) dup = true;
+      if (dup) { undetermined = kGjkNoProgress; break; }
+      if (s.rank == 1) s.set(1, pa, pb);
+      else if (s.rank == 2) s.set(2, pa, pb);
+      else s.set(3, pa, pb);
+      s.rank += 1;
+      if (sqn(w) <= tol2) { o.status = kGjkIntersect; return o; }
+      Proj st;
+      if (s.rank == 2) st = project2(s, d);
+      else if (s.rank == 3) st = project3(s, d, tol);
+      else st = project4(s, d, tol);
+      if (st == Proj::Failed) { o.status = kGjkFailed; return o; }
+      if (st == Proj::Intersect) { o.status = kGjkIntersect; return o; }
+      if (st == Proj::ZeroVolume) { undetermined = kGjkNoProgress; break; }
+    }
+    if (!separated && undetermined < 0) undetermined = kGjkIterLimit;
+  } else {
+    s.rank = 1;
+  }
+  if (separated) {
+    o.status = kGjkSeparated;
+    if (want_distance) o.point_valid = min_distance(sup, s, tol, max_iter, o.p0, o.p1, o.iterations);
+    return o;
+  }
+  o.status = undetermined;
+  if (want_distance) o.point_valid = extract_try_sub(s, o.p0, o.p1);
+  return o;
+}
+
+}  // namespace fclg

@@ -1,0 +1,113 @@
+// Support mappings of the five shape types and of their Minkowski difference,
+// evaluated cooperatively by a group of LANES lanes (LANES = 1: one thread per
+// pair; 32: one warp per pair).
+//
+// Primitive supports restate gjk_shape.hpp:44-51 (box), :65-71 (sphere),
+// :101-117 (capsule), :161-177 (cylinder) in FP32.  The convex support is the
+// argmax of d.v over the hull's vertices (convex-inl.h:133-149): every lane of
+// the group scans a strided slice of the vertex list with vectorised float4
+// loads, then a shuffle butterfly reduces (value, index) pairs, lowest index
+// winning ties as the reference's first-maximum scan does.
+#pragma once
+#include "device_math.cuh"
+
+namespace fclg {
+
+template <int LANES>
+struct Group {
+  unsigned lane;   // lane within the group
+  unsigned mask;   // member mask of the group within the warp
+  unsigned base;   // warp lane of the group's first lane
+  __device__ __forceinline__ static Group make() {
+    Group g;
+    const unsigned wl = threadIdx.x & 31u;
+    g.lane = wl & (LANES - 1);
+    g.base = wl & ~(unsigned)(LANES - 1);
+    g.mask = (LANES == 32) ? 0xFFFFFFFFu : (((1u << LANES) - 1u) << g.base);
+    return g;
+  }
+};
+
+template <int LANES>
+__device__ __forceinline__ f3 convex_support(const float4* __restrict__ v, uint32_t nv, f3 d, const Group<LANES>& g) {
+  float best;
+  uint32_t bi;
+  if (g.lane == 0 && nv > 0) {
+    const float4 q = __ldg(v);
+    best = fmaf(d.z, q.z, fmaf(d.y, q.y, d.x * q.x));
+    bi = 0;
+  } else {
+    best = -INFINITY;
+    bi = 0xFFFFFFFFu;
+  }
+  uint32_t i = (g.lane == 0) ? LANES : g.lane;
+#pragma unroll 4
+  for (; i < nv; i += LANES) {
+    const float4 q = __ldg(v + i);
+    const float val = fmaf(d.z, q.z, fmaf(d.y, q.y, d.x * q.x));
+    if (val > best) {
+      best = val;
+      bi = i;
+    }
+  }
+  if (LANES > 1) {
+#pragma unroll
+    for (int off = LANES / 2; off > 0; off >>= 1) {
+      const float ov = __shfl_xor_sync(g.mask, best, off);
+      const uint32_t oi = __shfl_xor_sync(g.mask, bi, off);
+      if (ov > best || (ov == best && oi < bi)) {
+        best = ov;
+        bi = oi;
+      }
+    }
+    // every lane must agree, also when a NaN direction made the order partial
+    bi = __shfl_sync(g.mask, bi, g.base);
+  }
+  if (bi >= nv) bi = 0;
+  const float4 q = __ldg(v + bi);
+  return mk3(q.x, q.y, q.z);
+}
+
+template <int LANES>
+__device__ __forceinline__ f3 shape_support(const ShapeDev& s, const float4* __restrict__ verts, f3 d,
+                                            const Group<LANES>& g) {
+  switch (s.type) {
+    case kBox:
+      return mk3(d.x > 0.f ? s.p0 : -s.p0, d.y > 0.f ? s.p1 : -s.p1, d.z > 0.f ? s.p2 : -s.p2);
+    case kSphere:
+      return d * s.p0;
+    case kCapsule: {
+      const f3 v = d * s.p0;
+      const f3 pos1 = mk3(v.x, v.y, s.p1 + v.z);
+      const f3 pos2 = mk3(v.x, v.y, -s.p1 + v.z);
+      return (dot(d, pos1) > dot(d, pos2)) ? pos1 : pos2;
+    }
+    case kCylinder: {
+      const float zdist = sqrtf(fmaf(d.y, d.y, d.x * d.x));
+      const float z = d.z > 0.f ? s.p1 : -s.p1;
+      if (zdist == 0.f) return mk3(0.f, 0.f, z);
+      const float k = s.p0 / zdist;
+      return mk3(k * d.x, k * d.y, z);
+    }
+    case kConvex:
+      return convex_support<LANES>(verts + s.vofs, s.nv, d, g);
+    default:
+      return mk3(0.f, 0.f, 0.f);
+  }
+}
+
+// Support of A - B with B posed in A's frame (minkowski_diff.hpp:21-58):
+// pa = s_A(d), pb = T * s_B(-R^T d), both in A's frame.
+template <int LANES>
+struct MinkowskiSupport {
+  ShapeDev A, B;
+  Pose pose;
+  const float4* __restrict__ verts;
+  Group<LANES> g;
+  __device__ __forceinline__ void operator()(f3 d, f3& pa, f3& pb) const {
+    pa = shape_support<LANES>(A, verts, d, g);
+    pb = pose.apply(shape_support<LANES>(B, verts, pose.rotT(-d), g));
+  }
+};
+
+}  // namespace fclg

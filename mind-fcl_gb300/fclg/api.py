@@ -1,0 +1,185 @@
+"""ctypes binding of the C ABI in include/fclg.h (lib/libfclg.so).
+
+The library is the product path: there is no CPU fallback, and loading fails
+loudly when the shared library or a GB300 (sm_103) device is missing.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from .layout import PAIR_DTYPE, RESULT_DTYPE, SHAPE_DTYPE
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG, "lib", "libfclg.so")
+
+FCLG_REQ_BOOLEAN_ONLY = 1
+FCLG_REQ_NO_EPA = 2
+FCLG_REQ_WARM_START = 4
+
+# Every symbol include/fclg.h declares (checked by tests/test_abi.py).
+EXPORTS = [
+    "fclg_create", "fclg_destroy", "fclg_last_error", "fclg_version", "fclg_built_arch",
+    "fclg_set_shapes", "fclg_set_shapes_device",
+    "fclg_distance", "fclg_distance_device", "fclg_collide", "fclg_collide_device",
+    "fclg_set_launch", "fclg_launch_count", "fclg_set_profiling", "fclg_pass_times",
+]
+
+
+class FclgError(RuntimeError):
+    pass
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("gjk_max_iterations", ctypes.c_uint32), ("epa_max_faces", ctypes.c_uint32),
+                ("epa_max_iterations", ctypes.c_uint32), ("flags", ctypes.c_uint32),
+                ("gjk_tolerance", ctypes.c_float), ("epa_tolerance", ctypes.c_float),
+                ("reserved", ctypes.c_float * 2)]
+
+
+_lib = None
+
+
+def load_library(path=LIB_PATH):
+    """Loads lib/libfclg.so and declares the C signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FclgError("libfclg.so not built (%s); run __graft_entry__.build()" % path)
+    lib = ctypes.CDLL(path)
+    vp, u32, u64, i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int
+    lib.fclg_create.argtypes = [ctypes.POINTER(vp), i32]
+    lib.fclg_create.restype = i32
+    lib.fclg_destroy.argtypes = [vp]
+    lib.fclg_destroy.restype = None
+    lib.fclg_last_error.argtypes = [vp]
+    lib.fclg_last_error.restype = ctypes.c_char_p
+    lib.fclg_version.restype = i32
+    lib.fclg_built_arch.restype = i32
+    lib.fclg_set_shapes.argtypes = [vp, vp, u32, vp, u64]
+    lib.fclg_set_shapes.restype = i32
+    lib.fclg_set_shapes_device.argtypes = [vp, vp, u32, vp, u64]
+    lib.fclg_set_shapes_device.restype = i32
+    for name in ("fclg_distance", "fclg_collide"):
+        getattr(lib, name).argtypes = [vp, vp, u32, vp, vp]
+        getattr(lib, name).restype = i32
+    for name in ("fclg_distance_device", "fclg_collide_device"):
+        getattr(lib, name).argtypes = [vp, vp, u32, vp, vp, vp]
+        getattr(lib, name).restype = i32
+    lib.fclg_set_launch.argtypes = [vp, i32, i32]
+    lib.fclg_set_launch.restype = i32
+    lib.fclg_launch_count.argtypes = [vp]
+    lib.fclg_launch_count.restype = u64
+    lib.fclg_set_profiling.argtypes = [vp, i32]
+    lib.fclg_set_profiling.restype = i32
+    lib.fclg_pass_times.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                    ctypes.POINTER(u64), i32]
+    lib.fclg_pass_times.restype = i32
+    _lib = lib
+    return lib
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def make_request(flags=0, gjk_tol=0.0, epa_tol=0.0, gjk_max_iter=0, epa_max_faces=0, epa_max_iter=0):
+    r = Request()
+    r.flags = flags
+    r.gjk_tolerance = gjk_tol
+    r.epa_tolerance = epa_tol
+    r.gjk_max_iterations = gjk_max_iter
+    r.epa_max_faces = epa_max_faces
+    r.epa_max_iterations = epa_max_iter
+    return r
+
+
+class Context:
+    """One fclg_context on a device: shapes plus batched collide / distance."""
+
+    def __init__(self, device=0):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        rc = self.lib.fclg_create(ctypes.byref(h), device)
+        if rc != 0:
+            raise FclgError("fclg_create(device=%d) failed with %d (needs an sm_103 GPU)" % (device, rc))
+        self.h = h
+        self._keep = []
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fclg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise FclgError("%s failed (%d): %s" % (what, rc, self.lib.fclg_last_error(self.h).decode()))
+
+    def set_shapes(self, shapes, vertices):
+        s = np.ascontiguousarray(shapes, SHAPE_DTYPE)
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 4)
+        self._check(self.lib.fclg_set_shapes(self.h, _ptr(s), len(s), _ptr(v), len(v)), "fclg_set_shapes")
+
+    def set_shapes_device(self, d_shapes, d_vertices):
+        """d_shapes / d_vertices: CUDA tensors (uint8 or any dtype) holding the packed arrays."""
+        n_s = d_shapes.numel() * d_shapes.element_size() // SHAPE_DTYPE.itemsize
+        n_v = d_vertices.numel() * d_vertices.element_size() // 16
+        self._keep = [d_shapes, d_vertices]
+        self._check(self.lib.fclg_set_shapes_device(self.h, ctypes.c_void_p(d_shapes.data_ptr()), n_s,
+                                                    ctypes.c_void_p(d_vertices.data_ptr()), n_v),
+                    "fclg_set_shapes_device")
+
+    def set_batch(self, batch):
+        self.set_shapes(batch.shapes, batch.vertices)
+
+    def _host_query(self, fn, pairs, request, out):
+        p = np.ascontiguousarray(pairs, PAIR_DTYPE)
+        if out is None:
+            out = np.zeros(len(p), RESULT_DTYPE)
+        req = ctypes.byref(request) if request is not None else None
+        self._check(fn(self.h, _ptr(p), len(p), req, _ptr(out)), fn.__name__)
+        return out
+
+    def distance(self, pairs, request=None, out=None):
+        """Signed distance per pair (host arrays in and out)."""
+        return self._host_query(self.lib.fclg_distance, pairs, request, out)
+
+    def collide(self, pairs, request=None, out=None):
+        """fcl::collide per pair (host arrays in and out)."""
+        return self._host_query(self.lib.fclg_collide, pairs, request, out)
+
+    def _dev_query(self, fn, d_pairs, n, d_results, request, stream):
+        req = ctypes.byref(request) if request is not None else None
+        st = ctypes.c_void_p(stream) if stream else None
+        self._check(fn(self.h, ctypes.c_void_p(d_pairs), n, req, ctypes.c_void_p(d_results), st), fn.__name__)
+
+    def distance_device(self, d_pairs, n, d_results, request=None, stream=0):
+        """Asynchronous signed distance on device pointers (ints) on a CUDA stream handle."""
+        self._dev_query(self.lib.fclg_distance_device, d_pairs, n, d_results, request, stream)
+
+    def collide_device(self, d_pairs, n, d_results, request=None, stream=0):
+        self._dev_query(self.lib.fclg_collide_device, d_pairs, n, d_results, request, stream)
+
+    def set_launch(self, gjk_lanes=0, epa_ctas_per_sm=0):
+        self._check(self.lib.fclg_set_launch(self.h, gjk_lanes, epa_ctas_per_sm), "fclg_set_launch")
+
+    def set_profiling(self, enable=True):
+        self._check(self.lib.fclg_set_profiling(self.h, int(enable)), "fclg_set_profiling")
+
+    def pass_times(self, reset=True):
+        """(gjk_ms, epa_ms, queries) summed since the last reset."""
+        g, e, q = ctypes.c_double(), ctypes.c_double(), ctypes.c_uint64()
+        self._check(self.lib.fclg_pass_times(self.h, ctypes.byref(g), ctypes.byref(e), ctypes.byref(q), int(reset)),
+                    "fclg_pass_times")
+        return g.value, e.value, q.value
+
+    @property
+    def launch_count(self):
+        return int(self.lib.fclg_launch_count(self.h))

@@ -70,7 +70,7 @@ def _load_ref():
     if _ref is None:
         lib = ctypes.CDLL(REF_PATH)
         vp, i = ctypes.c_void_p, ctypes.c_int
-        lib.ref_signed_distance.argtypes = [vp, i, vp, vp, i, vp, vp, i]
+        lib.ref_signed_distance.argtypes = [vp, i, vp, vp, i, vp, vp, i, i, ctypes.c_double]
         lib.ref_signed_distance.restype = i
         lib.ref_collide.argtypes = [vp, i, vp, vp, i, i, vp, i]
         lib.ref_collide.restype = i
@@ -129,14 +129,14 @@ def time_signed_distance(batch, threads=None):
                                         threads or default_threads()), out
 
 
-def ref_signed_distance(batch, guess=None, threads=None):
+def ref_signed_distance(batch, guess=None, threads=None, gjk_max_iter=0, gjk_tol=0.0):
     """The reference's own GJK/EPA (oracle/_ref) on the same inputs."""
     lib = _load_ref()
     s, v, p = _prep(batch)
     out = np.zeros(len(p), RESULT_DTYPE)
     g = None if guess is None else np.ascontiguousarray(guess, np.float32)
     assert lib.ref_signed_distance(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), _ptr(g), _ptr(out),
-                                   threads or default_threads()) == 0
+                                   threads or default_threads(), gjk_max_iter, gjk_tol) == 0
     return out
 
 

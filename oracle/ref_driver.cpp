@@ -140,7 +140,9 @@ static void finish(RefResult& r, bool contact) {
 }
 
 int ref_signed_distance(const void* shapes, int n_shapes, const float* verts, const void* pairs, int n_pairs,
-                        const float* guess, RefResult* out, int n_threads) {
+                        const float* guess, RefResult* out, int n_threads, int gjk_max_iter, double gjk_tol) {
+  if (gjk_max_iter <= 0) gjk_max_iter = 128;
+  if (gjk_tol <= 0) gjk_tol = 1e-6;
   const Prepared p = prepare((const ShapeRec*)shapes, n_shapes, verts);
   const PairRec* pr = (const PairRec*)pairs;
   parallelFor(n_pairs, n_threads, [&](int b, int e) {
@@ -152,7 +154,7 @@ int ref_signed_distance(const void* shapes, int n_shapes, const float* verts, co
       const MinkowskiDiff<double> md = makeDiff(p, pr[i]);
       Vec g(1, 0, 0);
       if (guess) g = Vec(guess[3 * i], guess[3 * i + 1], guess[3 * i + 2]);
-      GJK<double> gjk(128, 1e-6);
+      GJK<double> gjk(gjk_max_iter, gjk_tol);
       GJKSimplex<double> s;
       GJK<double>::MinSeparationDistanceOutput mdo;
       const GJK_Status gs = gjk.Evaluate(md, s, -g, &mdo);

@@ -1,0 +1,213 @@
+"""GPU convex queries through the C ABI against the reference.
+
+Parity bar (FP32 kernels vs the FP64 reference on identical inputs):
+* collision flags agree exactly outside a 1e-6 m band around contact
+  (|signed distance| > 1e-6 by the reference);
+* separation distance: |err| <= 1e-5 m for >= 99.5 % of the pairs both sides
+  solve; the rest are pairs where the reference's own stopping rule
+  (improvement < 1e-6 per iteration, gjk_distance.hpp:78-90) fires at a
+  different iterate on a curved surface — bounded by 1e-3 m;
+* penetration depth: |err| <= 1e-5 m for >= 99 % of overlapping pairs, the
+  rest bounded by 1e-2 m (pairs where EPA hits the 256-face capacity on
+  curved shapes, where the reference itself returns its partial polytope);
+* contact normal (depth > 1e-3 m): angle error <= 1e-3 rad for >= 99 %.
+The golden cases are outputs of the reference itself (tests/golden/).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from fclg import workloads
+from fclg.layout import (BOX, CAPSULE, CONVEX, CYLINDER, PAIR_DTYPE, SHAPE_DTYPE, SPHERE, epa_status,
+                         gjk_status)
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "convex_ref.npz")
+BAND = 1e-6
+
+
+def _golden(name):
+    g = np.load(GOLDEN)
+    b = workloads.Batch(name, g[name + "/shapes"], g[name + "/vertices"], g[name + "/pairs"])
+    return b, g
+
+
+def check_parity(got, ref, sep_frac=0.995, depth_frac=0.99):
+    """Asserts the parity bar above; returns a dict of statistics."""
+    n = len(got)
+    both = (got["ok"] == 1) & (ref["ok"] == 1)
+    assert both.mean() >= 0.999, "valid fraction %.5f" % both.mean()
+    rd = ref["distance"]
+    gd = got["distance"].astype(np.float64)
+    outside = np.abs(rd) > BAND
+    flags = (gd < 0) != (rd < 0)
+    assert np.sum(flags & outside & both) == 0
+    err = np.abs(gd - rd)
+    sep = both & (rd > 0)
+    ov = both & (rd < 0)
+    st = {"n": n}
+    if sep.any():
+        e = err[sep]
+        st["sep_p99"] = float(np.percentile(e, 99))
+        assert np.mean(e <= 1e-5) >= sep_frac, "separation: %.4f within 1e-5" % np.mean(e <= 1e-5)
+        assert e.max() <= 1e-3
+    if ov.any():
+        e = err[ov]
+        st["depth_p99"] = float(np.percentile(e, 99))
+        assert np.mean(e <= 1e-5) >= depth_frac, "depth: %.4f within 1e-5" % np.mean(e <= 1e-5)
+        assert e.max() <= 1e-2
+        deep = ov & (rd < -1e-3)
+        if deep.any():
+            c = np.clip(np.sum(got["normal"][deep] * ref["normal"][deep], axis=1), -1, 1)
+            ang = np.arccos(c)
+            assert np.mean(ang <= 1e-3) >= 0.99
+    return st
+
+
+@pytest.mark.parametrize("name", ["plain_small", "mixed", "pareto"])
+def test_distance_vs_reference_golden(gpu_ctx, name):
+    b, g = _golden(name)
+    gpu_ctx.set_batch(b)
+    got = gpu_ctx.distance(b.pairs)
+    check_parity(got, g[name + "/signed_distance"])
+
+
+@pytest.mark.parametrize("name", ["plain_small", "mixed", "pareto"])
+def test_collide_vs_reference_golden(gpu_ctx, name):
+    from fclg.api import FCLG_REQ_BOOLEAN_ONLY, make_request
+    b, g = _golden(name)
+    gpu_ctx.set_batch(b)
+    got = gpu_ctx.collide(b.pairs, make_request(flags=FCLG_REQ_BOOLEAN_ONLY))
+    ref = g[name + "/collide_bool"]
+    sd = g[name + "/signed_distance"]
+    outside = np.abs(sd["distance"]) > BAND
+    assert np.sum((got["collide"] != ref["ok"]) & outside) == 0
+    # with penetration: one contact per colliding pair
+    got_c = gpu_ctx.collide(b.pairs)
+    ref_c = g[name + "/collide_contact"]
+    hit = (ref_c["ok"] == 1) & (got_c["ok"] == 1) & (ref_c["distance"] < -1e-5)
+    err = np.abs(got_c["distance"][hit] - ref_c["distance"][hit])
+    assert np.mean(err <= 1e-5) >= 0.99
+
+
+@pytest.mark.parametrize("workload,n", [("plain_small", 4096), ("mixed", 60000), ("pareto", 60000)])
+def test_distance_vs_oracle(gpu_ctx, oracle_lib, workload, n):
+    b = getattr(workloads, workload)(n)
+    gpu_ctx.set_batch(b)
+    got = gpu_ctx.distance(b.pairs)
+    ref = oracle_lib.signed_distance(b)
+    check_parity(got, ref)
+    # status words: GJK verdict identical wherever the reference is outside the band
+    outside = np.abs(ref["distance"]) > BAND
+    assert np.mean(gjk_status(got["status"])[outside] == ref["gjk_status"][outside]) > 0.999
+
+
+def test_launch_shapes_agree(gpu_ctx, oracle_lib):
+    b = workloads.mixed(20000, seed=5)
+    gpu_ctx.set_batch(b)
+    ref = oracle_lib.signed_distance(b)
+    outs = []
+    for lanes in (1, 4, 32):
+        gpu_ctx.set_launch(gjk_lanes=lanes)
+        outs.append(gpu_ctx.distance(b.pairs))
+        check_parity(outs[-1], ref)
+    gpu_ctx.set_launch(gjk_lanes=1)
+    for o in outs[1:]:
+        assert np.mean(np.abs(o["distance"] - outs[0]["distance"]) <= 1e-5) > 0.995
+
+
+def test_device_entry_point_matches_host(gpu_ctx):
+    import torch
+    b = workloads.mixed(5000, seed=6)
+    gpu_ctx.set_batch(b)
+    host = gpu_ctx.distance(b.pairs)
+    d_pairs = torch.from_numpy(b.pairs.view(np.uint8).copy()).cuda()
+    d_res = torch.empty(len(b.pairs) * 48, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.Stream()
+    gpu_ctx.distance_device(d_pairs.data_ptr(), len(b.pairs), d_res.data_ptr(), None, s.cuda_stream)
+    s.synchronize()
+    dev = d_res.cpu().numpy().view(host.dtype)
+    assert np.array_equal(dev.view(np.uint8), host.view(np.uint8))
+
+
+def _one(shape_a, shape_b, R, t, verts=None):
+    s = np.concatenate([shape_a, shape_b])
+    p = np.zeros(len(t), PAIR_DTYPE)
+    p["shape_b"] = 1
+    p["rot"] = np.asarray(R).reshape(-1, 9)
+    p["trans"] = t
+    v = np.zeros((1, 4), np.float32) if verts is None else verts
+    return workloads.Batch("edge", s, v, p)
+
+
+def _sh(t, *param, vc=0, vo=0):
+    s = np.zeros(1, SHAPE_DTYPE)
+    s["type"] = t
+    s["param"][0, :len(param)] = param
+    s["vert_count"] = vc
+    s["vert_offset"] = vo
+    return s
+
+
+def test_edge_cases(gpu_ctx, oracle_lib):
+    # empty batch
+    b = _one(_sh(SPHERE, 0.1), _sh(SPHERE, 0.1), np.eye(3)[None], np.zeros((1, 3)))
+    gpu_ctx.set_batch(b)
+    assert len(gpu_ctx.distance(b.pairs[:0])) == 0
+    # coincident spheres, face-touching boxes, separated boxes, deep box-in-box
+    eye = np.repeat(np.eye(3)[None], 4, axis=0)
+    t = np.array([[0, 0, 0], [0.2, 0, 0], [0.5, 0, 0], [0.01, 0.02, 0]], np.float64)
+    b = _one(_sh(BOX, 0.2, 0.2, 0.2), _sh(BOX, 0.2, 0.2, 0.2), eye, t)
+    gpu_ctx.set_batch(b)
+    got = gpu_ctx.distance(b.pairs)
+    ref = oracle_lib.signed_distance(b)
+    assert np.all(got["ok"] == ref["ok"])
+    assert np.allclose(got["distance"], ref["distance"], atol=1e-5)
+    # NaN pose: must return (no hang) and must not claim a valid distance
+    p = b.pairs.copy()
+    p["trans"][0] = np.nan
+    got = gpu_ctx.distance(p)
+    assert got["ok"][0] == 0 or np.isnan(got["distance"][0])
+    # out-of-range shape index: rejected per pair, not read
+    p = b.pairs.copy()
+    p["shape_b"][1] = 1000
+    got = gpu_ctx.distance(p)
+    assert got["ok"][1] == 0 and gjk_status(got["status"][1]) == 4
+    # one-vertex convex (a point) against a sphere, and a flat (coplanar) hull against a box
+    verts = np.array([[0.3, 0, 0, 0], [-0.1, -0.1, 0, 0], [0.1, -0.1, 0, 0], [0.1, 0.1, 0, 0], [-0.1, 0.1, 0, 0]],
+                     np.float32)
+    s = np.concatenate([_sh(CONVEX, vc=1, vo=0), _sh(SPHERE, 0.1), _sh(CONVEX, vc=4, vo=1), _sh(BOX, 0.1, 0.1, 0.1)])
+    p = np.zeros(3, PAIR_DTYPE)
+    p["rot"] = np.eye(3).ravel()
+    p[0]["shape_a"], p[0]["shape_b"] = 0, 1
+    p[1]["shape_a"], p[1]["shape_b"] = 2, 3
+    p[2]["shape_a"], p[2]["shape_b"] = 2, 3
+    p["trans"] = [[0, 0, 0], [0, 0, 0.3], [0.02, 0.01, 0.03]]
+    b = workloads.Batch("edge2", s, verts, p)
+    gpu_ctx.set_batch(b)
+    got = gpu_ctx.distance(b.pairs)
+    ref = oracle_lib.signed_distance(b)
+    assert np.all(got["ok"] == ref["ok"])
+    ok = ref["ok"] == 1
+    assert np.allclose(got["distance"][ok], ref["distance"][ok], atol=1e-5)
+
+
+def test_large_hulls(gpu_ctx, oracle_lib):
+    # Pareto tail: up to 1024-vertex hulls
+    b = workloads.pareto(200000, seed=12)
+    big = np.nonzero(np.maximum(b.shapes["vert_count"][b.pairs["shape_a"]],
+                                b.shapes["vert_count"][b.pairs["shape_b"]]) >= 256)[0][:3000]
+    sub = b.subset(big)
+    gpu_ctx.set_batch(sub)
+    check_parity(gpu_ctx.distance(sub.pairs), oracle_lib.signed_distance(sub))
+
+
+def test_invalid_shapes_rejected(gpu_ctx):
+    from fclg.api import FclgError
+    s = _sh(CONVEX, vc=10, vo=0)
+    with pytest.raises(FclgError, match="vertex range"):
+        gpu_ctx.set_shapes(s, np.zeros((4, 4), np.float32))
+    with pytest.raises(FclgError, match="unsupported type"):
+        gpu_ctx.set_shapes(_sh(7, 1.0), np.zeros((1, 4), np.float32))
