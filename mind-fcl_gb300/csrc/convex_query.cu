@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(WARPS * 32) epa_pass(BatchArgs b, QueryParams 
     sup.pose = pr.pose;
     sup.verts = b.verts;
     sup.g = Group<32>::make();
-    EpaWarp<FMAX, VMAX> E{P, sup, prm.epa_tol, lane, 0, 0, 0};
+    EpaWarp<FMAX, VMAX> E{P, sup, prm.epa_tol, lane, 0, 0, 0, 0, 0u};
     const EpaResult er = E.run(rank < 1 ? 1 : (rank > 4 ? 4 : rank), spa, spb, prm.epa_max_iter, max_faces);
     if (lane == 0) {
       const int32_t status = kGjkIntersect | ((er.status + 1) << 8);

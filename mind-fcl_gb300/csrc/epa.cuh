@@ -4,19 +4,29 @@
 // Algorithm (epa.hpp:133-237 and the polytope code it drives): repeatedly take
 // the face nearest the origin, evaluate the support along its outward normal,
 // stop when the support point is within the tolerance of that face's plane,
-// else remove the patch of faces the new point sees (grown from the nearest
-// face through visible neighbours, as computeVisiblePatch's DFS does,
-// epa_polytope_expand.hpp:120-180) and fan new faces from the point to the
+// else remove the patch of faces the new point sees — grown from the nearest
+// face through visible neighbours, as computeVisiblePatch's DFS does
+// (epa_polytope_expand.hpp:120-180) — and fan new faces from the point to the
 // patch's horizon.  Capacity (live faces <= max_faces, the reference's
 // MallocFailed) and the iteration limit end the loop with the current nearest
-// face, as the reference does.
+// face, as the reference does.  A face counts as seen when the point lies more
+// than the tolerance beyond its plane (the reference uses >= 0): coplanar
+// faces stay, which keeps the FP32 polytope convex where supports tie.
 //
-// GPU layout: face slots are striped over the 32 lanes for the nearest-face
-// argmin and the visibility test; horizon edges are gathered with ballot
-// prefix sums and fanned in parallel, neighbours linked through a per-vertex
-// "edge starting here" table.  Faces carry FP32 unit normals and plane
-// distances; the final closest-face solve (normal, depth, barycentric witness
-// points) runs in FP64.
+// Faces are ranked by plane distance among those the origin projects into
+// (the reference's pointToTriangle witness_in_simplex, epa_polytope_utils.h:
+// 88-165); among coplanar triangles that picks the one holding the nearest
+// point.
+//
+// GPU layout: per iteration the work is proportional to the visible patch,
+// not to the polytope: the patch grows in frontier rounds (a lane per frontier
+// face, classification claimed with a compare-and-swap on a per-iteration
+// stamp), horizon edges are gathered with a warp prefix sum, slots are
+// recycled through a free stack, and the fan is linked through a per-vertex
+// "edge starting here" table.  Only the nearest-face argmin touches every
+// slot: one shared-memory load per lane per 32 slots.  Faces carry FP32 unit
+// normals and plane distances; the final closest-face solve (normal, depth,
+// barycentric witness points) runs in FP64.
 //
 // Initial polytope from the GJK simplex: epa_simplex2polytope.hpp:41-376
 // (touching detection, triangle blown up along +-normal, segment search over
@@ -32,25 +42,24 @@
 
 namespace fclg {
 
-constexpr uint32_t kNoFace = 0xFFFFu;
 constexpr uint32_t kNoSlot = 0xFFFFFFFFu;
 
 template <int FMAX, int VMAX>
 struct EpaSmem {
-  float4 fn[FMAX];        // outward unit normal xyz, plane distance (inf: unusable)
-  uint32_t fv[FMAX];      // vertex indices v0 | v1 << 8 | v2 << 16, counter-clockwise seen from outside;
-                          // bit 24: the origin projects inside the face
-  uint16_t fadj[FMAX][4]; // neighbour across edge k = (v_k, v_k+1)
-  uint8_t falive[FMAX];
-  uint8_t fvis[FMAX];     // 0 hidden, 1 sees the new point, 2 in the visible patch
-  float4 vw[VMAX];        // Minkowski vertex w = pa - pb
-  float4 vpa[VMAX];       // support point on shape a
+  float4 fn[FMAX];         // outward unit normal xyz, plane distance (inf: dead or degenerate)
+  float fkey[FMAX];        // plane distance when the origin projects inside, else inf
+  uint32_t fv[FMAX];       // vertex indices v0 | v1 << 8 | v2 << 16, counter-clockwise seen from outside
+  uint16_t fadj[FMAX][4];  // neighbour across edge k = (v_k, v_k+1)
+  uint32_t fmark[FMAX];    // classification stamp of the current expansion
+  float4 vw[VMAX];         // Minkowski vertex w = pa - pb
+  float4 vpa[VMAX];        // support point on shape a
   uint32_t start_at[VMAX];
-  uint16_t hz_s[FMAX + 8];
-  uint8_t hz_e[FMAX + 8];
-  uint16_t hz_slot[FMAX + 8];
-  uint16_t freelist[FMAX];
-  uint32_t scratch[8];
+  uint16_t patch[FMAX];    // faces of the visible patch, in discovery order
+  uint16_t freestk[FMAX];  // recycled face slots
+  uint16_t hz_s[3 * FMAX]; // horizon edge: patch face
+  uint8_t hz_e[3 * FMAX];  //              and its edge index
+  uint16_t hz_slot[3 * FMAX];
+  uint32_t npatch;
 };
 
 __device__ __forceinline__ uint32_t fvert(uint32_t packed, int k) { return (packed >> (8 * k)) & 0xFFu; }
@@ -64,13 +73,11 @@ __device__ __forceinline__ float4 face_plane(f3 a, f3 b, f3 c) {
   return make_float4(u.x, u.y, u.z, dot(u, a));
 }
 
-// Whether the origin's projection onto the face plane lies inside the
-// triangle (barycentric coordinates >= -1e-4).  The reference ranks faces by
-// their distance to the origin only when this holds (pointToTriangle's
-// witness_in_simplex, epa_polytope_utils.h:88-165); among coplanar triangles
-// it is what picks the one that holds the nearest point.
-__device__ __forceinline__ uint32_t projects_inside(f3 a, f3 b, f3 c, float4 plane) {
-  if (!(plane.w < INFINITY)) return 0u;
+// Selection key of a face: its plane distance when the origin's projection
+// onto the plane lies inside the triangle (barycentric coordinates >= -1e-4),
+// else infinity.
+__device__ __forceinline__ float face_key(f3 a, f3 b, f3 c, float4 plane) {
+  if (!(plane.w < INFINITY)) return INFINITY;
   const f3 u = ld3(plane);
   const f3 p = u * plane.w;
   const float e0 = dot(u, cross(b - a, p - a));
@@ -78,7 +85,7 @@ __device__ __forceinline__ uint32_t projects_inside(f3 a, f3 b, f3 c, float4 pla
   const float e2 = dot(u, cross(a - c, p - c));
   const float tot = e0 + e1 + e2;
   const float slack = -1e-4f * fabsf(tot);
-  return (tot > 0.f && e0 >= slack && e1 >= slack && e2 >= slack) ? 1u : 0u;
+  return (tot > 0.f && e0 >= slack && e1 >= slack && e2 >= slack) ? plane.w : INFINITY;
 }
 
 struct EpaResult {
@@ -88,19 +95,7 @@ struct EpaResult {
   int iterations;
 };
 
-// epa_polytope_utils.h:71-86 with p = origin
-__device__ __forceinline__ float origin_to_plane(f3 a, f3 b, f3 c) {
-  const f3 n = cross(a - b, b - c);
-  const float nl = nrm(n);
-  if (nl <= 0.f) {
-    const f3 ab = b - a;
-    const float len = nrm(ab);
-    if (len <= 0.f) return nrm(a);
-    return nrm(cross(mk3(0, 0, 0) - a, ab)) / len;
-  }
-  return fabsf(dot(n * (1.f / nl), a));
-}
-
+// epa_polytope_utils.h:58-86
 __device__ __forceinline__ float point_to_line(f3 p, f3 a, f3 b) {
   const f3 ab = b - a;
   const float len = nrm(ab);
@@ -120,7 +115,8 @@ struct EpaWarp {
   const MinkowskiSupport<32>& sup;
   float tol;
   unsigned lane;
-  int nv, hw, live;
+  int nv, hw, live, fs_top;
+  uint32_t stamp;  // even; advanced by 2 per expansion, never reused by this warp
 
   __device__ __forceinline__ f3 W(uint32_t i) const { return ld3(P.vw[i]); }
 
@@ -134,9 +130,17 @@ struct EpaWarp {
     ++nv;
   }
 
-  // Build the initial polytope from faces (index triples into the vertices
-  // already pushed), oriented away from the vertex centroid; lane 0 only.
-  // Returns false when the faces do not close up.
+  __device__ __forceinline__ void write_face(uint32_t t, uint32_t a, uint32_t b, uint32_t c) {
+    const f3 A = W(a), B = W(b), C = W(c);
+    const float4 pl = face_plane(A, B, C);
+    P.fv[t] = a | (b << 8) | (c << 16);
+    P.fn[t] = pl;
+    P.fkey[t] = face_key(A, B, C, pl);
+  }
+
+  // Initial polytope from faces (index triples into the vertices already
+  // pushed), oriented away from the vertex centroid; lane 0 only.  Returns
+  // false when the faces do not close up.
   __device__ bool build_faces(const int (*tri)[3], int nf) {
     bool ok = true;
     if (lane == 0) {
@@ -147,10 +151,8 @@ struct EpaWarp {
         int i = tri[f][0], j = tri[f][1], k = tri[f][2];
         const f3 n = cross(W(j) - W(i), W(k) - W(i));
         if (dot(n, W(i) - c) < 0.f) { const int t = j; j = k; k = t; }
-        const float4 pl = face_plane(W(i), W(j), W(k));
-        P.fv[f] = (uint32_t)i | ((uint32_t)j << 8) | ((uint32_t)k << 16) | (projects_inside(W(i), W(j), W(k), pl) << 24);
-        P.fn[f] = pl;
-        P.falive[f] = 1;
+        write_face(f, i, j, k);
+        P.fmark[f] = 0;
       }
       for (int f = 0; f < nf && ok; ++f) {
         for (int e = 0; e < 3 && ok; ++e) {
@@ -168,6 +170,7 @@ struct EpaWarp {
     }
     hw = nf;
     live = nf;
+    fs_top = 0;
     return __shfl_sync(0xFFFFFFFFu, (int)ok, 0) != 0;
   }
 
@@ -184,25 +187,22 @@ struct EpaWarp {
     const d3 a = tod(W(ia)), b = tod(W(ib)), c = tod(W(ic));
     const d3 n = cross(b - a, c - a);
     const double n2 = dot(n, n);
-    bool ok = n2 > 0.0;
-    if (ok) {
+    if (n2 > 0.0) {
       const d3 u = n * (1.0 / sqrt(n2));
       const double dist = dot(u, a);
       const d3 p = u * dist;
       const double area = sqrt(n2);
       const d3 dl0 = a - b, dl1 = b - c, dl2 = c - a;
-      double wgt[3];
       const d3 q0 = cross(dl1, b - p), q1 = cross(dl2, c - p), q2 = cross(dl0, a - p);
-      wgt[0] = sqrt(dot(q0, q0)) / area;
-      wgt[1] = sqrt(dot(q1, q1)) / area;
+      const double w0 = sqrt(dot(q0, q0)) / area;
+      const double w1 = sqrt(dot(q1, q1)) / area;
       const double chk = sqrt(dot(q2, q2)) / area;
-      wgt[2] = 1.0 - wgt[0] - wgt[1];
-      if (fabs(chk - wgt[2]) > 0.01) ok = false;
-      if (ok) {
+      const double w2 = 1.0 - w0 - w1;
+      if (!(fabs(chk - w2) > 0.01)) {
         const d3 pa0 = tod(ld3(P.vpa[ia])), pa1 = tod(ld3(P.vpa[ib])), pa2 = tod(ld3(P.vpa[ic]));
         const d3 pb0 = pa0 - a, pb1 = pa1 - b, pb2 = pa2 - c;
-        const d3 x0 = (pa0 * wgt[0] + pa1 * wgt[1]) + pa2 * wgt[2];
-        const d3 x1 = (pb0 * wgt[0] + pb1 * wgt[1]) + pb2 * wgt[2];
+        const d3 x0 = (pa0 * w0 + pa1 * w1) + pa2 * w2;
+        const d3 x1 = (pb0 * w0 + pb1 * w1) + pb2 * w2;
         r.p0 = mk3((float)x0.x, (float)x0.y, (float)x0.z);
         r.p1 = mk3((float)x1.x, (float)x1.y, (float)x1.z);
         r.depth = (float)fabs(dist);
@@ -293,115 +293,124 @@ struct EpaWarp {
     return build_faces(tri, 8);
   }
 
-  // Warp argmin of the plane distance over live faces the origin projects
-  // into (ties: lowest slot); over all live faces when none qualifies.
+  // Warp argmin of the selection key (ties: lowest slot); when no face
+  // qualifies, the argmin of the plane distance over live faces.
   __device__ __forceinline__ void nearest(int& best_slot, float& best_d) const {
-    float bd = INFINITY, ad = INFINITY;
-    int bs = 0x7FFFFFFF, as = 0x7FFFFFFF;
+    float bd = INFINITY;
+    int bs = 0x7FFFFFFF;
     for (int s = (int)lane; s < hw; s += 32) {
-      if (P.falive[s]) {
-        const float d = P.fn[s].w;
-        if (d < ad) { ad = d; as = s; }
-        if ((P.fv[s] >> 24) && d < bd) { bd = d; bs = s; }
-      }
+      const float d = P.fkey[s];
+      if (d < bd) { bd = d; bs = s; }
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
       const float od = __shfl_xor_sync(0xFFFFFFFFu, bd, off);
       const int os = __shfl_xor_sync(0xFFFFFFFFu, bs, off);
       if (od < bd || (od == bd && os < bs)) { bd = od; bs = os; }
-      const float oa = __shfl_xor_sync(0xFFFFFFFFu, ad, off);
-      const int oas = __shfl_xor_sync(0xFFFFFFFFu, as, off);
-      if (oa < ad || (oa == ad && oas < as)) { ad = oa; as = oas; }
     }
-    if (bs == 0x7FFFFFFF) { bs = as; bd = ad; }
+    if (!(bd < INFINITY)) {
+      bs = 0x7FFFFFFF;
+      for (int s = (int)lane; s < hw; s += 32) {
+        const float d = P.fn[s].w;
+        if (d < bd) { bd = d; bs = s; }
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const float od = __shfl_xor_sync(0xFFFFFFFFu, bd, off);
+        const int os = __shfl_xor_sync(0xFFFFFFFFu, bs, off);
+        if (od < bd || (od == bd && os < bs)) { bd = od; bs = os; }
+      }
+    }
     best_slot = __shfl_sync(0xFFFFFFFFu, bs, 0);
     best_d = __shfl_sync(0xFFFFFFFFu, bd, 0);
   }
 
-  // One expansion with the new vertex nv-1; returns 0 ok, 1 capacity, 2 broken topology.
+  // One expansion with the new vertex nv-1 from the visible face `start`;
+  // returns 0 ok, 1 capacity, 2 broken topology.
   __device__ int expand(int start, int max_faces) {
     const uint32_t vnew = (uint32_t)(nv - 1);
     const f3 w = W(vnew);
-    for (int s = (int)lane; s < hw; s += 32) {
-      uint8_t v = 0;
-      if (P.falive[s]) {
-        const float4 q = P.fn[s];
-        v = (dot(ld3(q), w - W(fvert(P.fv[s], 0))) >= 0.f) ? 1 : 0;
-      }
-      P.fvis[s] = v;
+    stamp += 2;
+    const uint32_t kVis = stamp + 1, kHid = stamp;
+    if (lane == 0) {
+      P.fmark[start] = kVis;
+      P.patch[0] = (uint16_t)start;
+      P.npatch = 1;
     }
     __syncwarp();
-    if (lane == 0) P.fvis[start] = 2;
-    __syncwarp();
-    for (int round = 0; round < FMAX; ++round) {
-      bool changed = false;
-      for (int s = (int)lane; s < hw; s += 32) {
-        if (P.fvis[s] == 1) {
-          if (P.fvis[P.fadj[s][0]] == 2 || P.fvis[P.fadj[s][1]] == 2 || P.fvis[P.fadj[s][2]] == 2) {
-            P.fvis[s] = 2;
-            changed = true;
+    // frontier rounds
+    int lo = 0, hi = 1;
+    for (int round = 0; round < FMAX && lo < hi; ++round) {
+      for (int k = lo + (int)lane; k < hi; k += 32) {
+        const uint32_t f = P.patch[k];
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+          const uint32_t g = P.fadj[f][e];
+          const uint32_t m = P.fmark[g];
+          if (m == kVis || m == kHid) continue;
+          const float4 q = P.fn[g];
+          const bool visible = dot(ld3(q), w - W(fvert(P.fv[g], 0))) > tol;
+          if (atomicCAS(&P.fmark[g], m, visible ? kVis : kHid) == m && visible) {
+            const uint32_t slot = atomicAdd(&P.npatch, 1u);
+            if (slot < FMAX) P.patch[slot] = (uint16_t)g;
           }
         }
       }
       __syncwarp();
-      if (!__any_sync(0xFFFFFFFFu, changed)) break;
+      lo = hi;
+      hi = P.npatch < (uint32_t)FMAX ? (int)P.npatch : FMAX;
+      __syncwarp();
     }
-    // Gather: free slots (dead or now removed) and horizon edges, in slot order.
-    int n_free = 0, n_hz = 0, n_rem = 0;
-    for (int base = 0; base < hw; base += 32) {
-      const int s = base + (int)lane;
-      bool fr = false, rem = false;
+    const int n_rem = hi;
+    // horizon edges of the patch, gathered in patch order
+    int n_hz = 0;
+    for (int base = 0; base < n_rem; base += 32) {
+      const int k = base + (int)lane;
       int h = 0;
-      uint32_t hmask = 0;
-      if (s < hw) {
-        rem = P.fvis[s] == 2;
-        fr = rem || !P.falive[s];
-        if (rem) {
+      uint32_t hmask = 0, f = 0;
+      if (k < n_rem) {
+        f = P.patch[k];
 #pragma unroll
-          for (int k = 0; k < 3; ++k)
-            if (P.fvis[P.fadj[s][k]] != 2) { hmask |= 1u << k; ++h; }
-        }
+        for (int e = 0; e < 3; ++e)
+          if (P.fmark[P.fadj[f][e]] != kVis) { hmask |= 1u << e; ++h; }
       }
-      const unsigned fb = __ballot_sync(0xFFFFFFFFu, fr);
-      const unsigned lt = (1u << lane) - 1u;
-      if (fr) P.freelist[n_free + __popc(fb & lt)] = (uint16_t)s;
-      n_free += __popc(fb);
-      n_rem += __popc(__ballot_sync(0xFFFFFFFFu, rem));
-      // horizon prefix sum
       int incl = h;
 #pragma unroll
       for (int off = 1; off < 32; off <<= 1) {
         const int t = __shfl_up_sync(0xFFFFFFFFu, incl, off);
         if ((int)lane >= off) incl += t;
       }
-      const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-      int k = n_hz + incl - h;
-      if (k + h <= FMAX + 8) {
-        for (int e = 0; e < 3; ++e)
-          if (hmask & (1u << e)) { P.hz_s[k] = (uint16_t)s; P.hz_e[k] = (uint8_t)e; ++k; }
-      }
-      n_hz += total;
+      int o = n_hz + incl - h;
+      for (int e = 0; e < 3; ++e)
+        if (hmask & (1u << e)) { P.hz_s[o] = (uint16_t)f; P.hz_e[o] = (uint8_t)e; ++o; }
+      n_hz += __shfl_sync(0xFFFFFFFFu, incl, 31);
     }
     const int new_live = live - n_rem + n_hz;
-    const int fresh = n_hz > n_free ? n_hz - n_free : 0;
-    if (n_hz < 3 || n_hz > FMAX + 8) return 2;
+    const int avail = fs_top + n_rem;
+    const int fresh = n_hz > avail ? n_hz - avail : 0;
+    if (n_hz < 3) return 2;
     if (new_live > max_faces || hw + fresh > FMAX) return 1;
+    // recycle the patch's slots (pushed above the older free slots)
+    for (int k = (int)lane; k < n_rem; k += 32) P.freestk[fs_top + k] = P.patch[k];
     __syncwarp();
-    // Phase A: read the horizon edges' endpoints and outside neighbours (the
-    // removed faces' slots are overwritten below).
-    uint32_t ha[(FMAX + 8 + 31) / 32], hb[(FMAX + 8 + 31) / 32], hg[(FMAX + 8 + 31) / 32];
+    // Phase A: endpoints and outside neighbours of the horizon edges (the
+    // patch slots are overwritten below); slots popped from the free stack.
+    constexpr int kPer = (3 * FMAX + 31) / 32;
+    uint32_t ha[kPer], hb[kPer], hg[kPer];
     int j = 0;
     for (int k = (int)lane; k < n_hz; k += 32, ++j) {
       const uint32_t s = P.hz_s[k], e = P.hz_e[k];
       ha[j] = fvert(P.fv[s], (int)e);
       hb[j] = fvert(P.fv[s], (int)((e + 1) % 3));
       hg[j] = P.fadj[s][e];
-      P.hz_slot[k] = (k < n_free) ? P.freelist[k] : (uint16_t)(hw + (k - n_free));
+      P.hz_slot[k] = (k < avail) ? P.freestk[avail - 1 - k] : (uint16_t)(hw + (k - avail));
     }
     __syncwarp();
-    for (int s = (int)lane; s < hw; s += 32)
-      if (P.fvis[s] == 2) P.falive[s] = 0;
+    for (int k = (int)lane; k < n_rem; k += 32) {
+      const uint32_t f = P.patch[k];
+      P.fn[f].w = INFINITY;
+      P.fkey[f] = INFINITY;
+    }
     j = 0;
     for (int k = (int)lane; k < n_hz; k += 32, ++j) {
       P.start_at[ha[j]] = kNoSlot;
@@ -414,10 +423,8 @@ struct EpaWarp {
     for (int k = (int)lane; k < n_hz; k += 32, ++j) {
       const uint32_t t = P.hz_slot[k];
       const uint32_t a = ha[j], b = hb[j], g = hg[j];
-      const float4 pl = face_plane(W(a), W(b), w);
-      P.fv[t] = a | (b << 8) | (vnew << 16) | (projects_inside(W(a), W(b), w, pl) << 24);
-      P.fn[t] = pl;
-      P.falive[t] = 1;
+      write_face(t, a, b, vnew);
+      P.fmark[t] = 0;
       P.fadj[t][0] = (uint16_t)g;
       const uint32_t gv = P.fv[g];
       int gj = -1;
@@ -441,6 +448,7 @@ struct EpaWarp {
     __syncwarp();
     if (__any_sync(0xFFFFFFFFu, err)) return 2;
     live = new_live;
+    fs_top = avail > n_hz ? avail - n_hz : 0;
     hw += fresh;
     return 0;
   }
@@ -455,6 +463,7 @@ struct EpaWarp {
     nv = 0;
     hw = 0;
     live = 0;
+    fs_top = 0;
     const float tol2 = tol * tol;
     for (int i = 0; i < rank; ++i) {
       if (sqn(spa[i] - spb[i]) <= tol2) { touching(spa[i], spb[i], r); return r; }
@@ -466,7 +475,7 @@ struct EpaWarp {
       const int faces[4][3] = {{0, 1, 2}, {0, 2, 3}, {0, 1, 3}, {1, 2, 3}};
       int tri = -1;
       for (int f = 0; f < 4 && tri < 0; ++f)
-        if (origin_to_plane(W(faces[f][0]), W(faces[f][1]), W(faces[f][2])) < tol) tri = f;
+        if (point_to_plane(mk3(0, 0, 0), W(faces[f][0]), W(faces[f][1]), W(faces[f][2])) < tol) tri = f;
       if (tri < 0) {
         ok = tetra();
       } else {
@@ -491,7 +500,7 @@ struct EpaWarp {
     if (done) return r;
     if (!ok) { r.status = kEpaFailed; return r; }
     __syncwarp();
-    for (int it = 0;; ) {
+    for (int it = 0;;) {
       int bs;
       float bd;
       nearest(bs, bd);
@@ -521,12 +530,15 @@ struct EpaWarp {
         return r;
       }
       if (ex == 2) {
-        // The new point's visible patch has no simple horizon at FP32
-        // resolution (near-coplanar faces, delta is already tiny): end with
-        // the current nearest face, whose plane is within delta of the
-        // support.
-        finalize(bfv, pa, pb, r);
-        r.status = kEpaOK;
+        // The visible patch has no simple horizon at FP32 resolution.  Near
+        // convergence (support within 10 tolerances of the face) the current
+        // nearest face is the answer; otherwise report failure.
+        if (delta <= 10.f * tol) {
+          finalize(bfv, pa, pb, r);
+          r.status = kEpaOK;
+        } else {
+          r.status = kEpaFailed;
+        }
         return r;
       }
       ++it;
