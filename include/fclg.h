@@ -133,8 +133,24 @@ int fclg_collide(fclg_context* ctx, const fclg_pair* pairs, uint32_t n_pairs, co
 int fclg_collide_device(fclg_context* ctx, const fclg_pair* d_pairs, uint32_t n_pairs, const fclg_request* req,
                         fclg_result* d_results, void* stream);
 
-/* Launch shape of the two query passes (lanes per pair of the GJK pass,
-   CTAs of the EPA pass); 0 keeps the built-in choice.  For tuning. */
+/* Launch shape of the query passes.  Pairs are first sorted on the device by
+   shape class (box / sphere / capsule / cylinder / convex hull, hulls split at
+   large_hull_vertices); pairs without a large hull run the GJK pass with
+   gjk_lanes_small lanes per pair, the rest with gjk_lanes_large.  Zero
+   fields keep the current value.  Defaults: bucketing on, 1 and 8 lanes,
+   128 vertices, 4 GJK and 5 EPA CTAs per SM (the EPA pass's first,
+   128-face layout). */
+typedef struct fclg_tuning {
+  int32_t bucketing;            /* 1 on, -1 off, 0 unchanged */
+  int32_t gjk_lanes_small;      /* 1, 2, 4, 8, 16 or 32 */
+  int32_t gjk_lanes_large;
+  int32_t large_hull_vertices;
+  int32_t gjk_ctas_per_sm;
+  int32_t epa_ctas_per_sm;
+} fclg_tuning;
+int fclg_set_tuning(fclg_context* ctx, const fclg_tuning* tuning);
+int fclg_get_tuning(const fclg_context* ctx, fclg_tuning* tuning);
+/* Shorthand: the same lane count for both GJK launches, and the EPA CTAs per SM. */
 int fclg_set_launch(fclg_context* ctx, int gjk_lanes, int epa_ctas_per_sm);
 
 /* Kernel launches issued by this context since creation (for accounting). */
@@ -146,6 +162,50 @@ uint64_t fclg_launch_count(const fclg_context* ctx);
    queries timed since the last reset (reset = 1 clears the sums). */
 int fclg_set_profiling(fclg_context* ctx, int enable);
 int fclg_pass_times(fclg_context* ctx, double* gjk_ms, double* epa_ms, uint64_t* queries, int reset);
+
+/* ---------------------------------------------------------------- meshes --
+   Triangle meshes with an OBB bounding-volume hierarchy built on the host
+   (replaces BVHModel<OBBRSS>::beginModel / addSubModel / endModel,
+   geometry/bvh/BVH_model-inl.h:136-303), and batched boolean mesh-mesh
+   collision (fcl::collide on two BVHModel<OBBRSS> with penetration off:
+   OrientedNodeBVHSolver::MeshIntersect, bvh_solver-inl.h:74-164). */
+typedef struct fclg_mesh fclg_mesh;
+
+typedef struct fclg_mesh_node { /* 64 bytes */
+  float axis[9];    /* row-major; the columns are the box axes */
+  float center[3];
+  float extent[3];  /* half sizes */
+  int32_t child;    /* >= 0: children child and child + 1; < 0: leaf of triangle -(child + 1) */
+} fclg_mesh_node;
+
+/* Builds the hierarchy on the host only (no device, no context): 2 x
+   n_triangles - 1 nodes, root first, and the triangle soup
+   (n_triangles x 3 x xyzw floats).  Returns FCLG_OK or FCLG_E_INVALID. */
+int fclg_bvh_build(const float* vertices_xyz, uint32_t n_vertices, const int32_t* triangles, uint32_t n_triangles,
+                   fclg_mesh_node* nodes, float* triangles_xyzw);
+
+/* Builds the hierarchy over triangles (3 vertex indices each) and uploads
+   it to the context's device. */
+int fclg_mesh_create(fclg_context* ctx, const float* vertices_xyz, uint32_t n_vertices, const int32_t* triangles,
+                     uint32_t n_triangles, fclg_mesh** mesh);
+void fclg_mesh_destroy(fclg_mesh* mesh);
+int fclg_mesh_info(const fclg_mesh* mesh, uint32_t* n_nodes, uint32_t* n_triangles);
+/* Copies the flattened hierarchy (n_nodes nodes) and the triangle soup
+   (n_triangles x 3 x xyzw floats) to host memory. */
+int fclg_mesh_export(const fclg_mesh* mesh, fclg_mesh_node* nodes, float* triangles_xyzw);
+
+/* Boolean collision of mesh b posed by poses[i] (rotation row-major, then
+   translation: 12 floats, b in a's frame) against mesh a.  A pose stops after
+   max_contacts colliding triangle pairs (CollisionRequest::num_max_contacts;
+   1 is first-contact mode).  Outputs per pose: flags (1 if colliding),
+   counts, pairs (max_contacts x 2 triangle ids of a and b) and, when not
+   NULL, status (bit 0: the traversal stack overflowed, the pair set may be
+   incomplete; bit 1: round limit). */
+int fclg_mesh_collide(fclg_context* ctx, const fclg_mesh* a, const fclg_mesh* b, const float* poses, uint32_t n_poses,
+                      uint32_t max_contacts, uint8_t* flags, uint32_t* counts, int32_t* pairs, uint32_t* status);
+int fclg_mesh_collide_device(fclg_context* ctx, const fclg_mesh* a, const fclg_mesh* b, const float* d_poses,
+                             uint32_t n_poses, uint32_t max_contacts, uint8_t* d_flags, uint32_t* d_counts,
+                             int32_t* d_pairs, uint32_t* d_status, void* stream);
 
 #ifdef __cplusplus
 }

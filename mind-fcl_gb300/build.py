@@ -22,7 +22,7 @@ FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxe
 
 
 def sources():
-    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
 
 
 def headers():
@@ -32,7 +32,7 @@ def headers():
 
 
 def _obj(src):
-    return os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+    return os.path.join(BUILD, os.path.splitext(os.path.basename(src))[0] + ".o")
 
 
 def _stale(target, deps):

@@ -8,6 +8,8 @@
 
 #include "fclg.h"
 #include "kernels.h"
+#include "mesh_build.h"
+#include "mesh_kernels.h"
 
 struct fclg_context {
   int device = 0;
@@ -22,17 +24,27 @@ struct fclg_context {
   uint32_t n_shapes = 0;
   uint64_t n_verts = 0;
   // scratch handed from the GJK pass to the EPA pass
-  uint32_t* epa_count = nullptr;
+  uint32_t* epa_count = nullptr;  // [2]: work list, overflow list
   uint32_t* epa_list = nullptr;
+  uint32_t* epa_ovf = nullptr;
   float4* epa_rec = nullptr;
   size_t epa_cap = 0;
   // device staging of the host-pointer entry points
   void* io_pairs = nullptr;
   void* io_results = nullptr;
   size_t io_cap = 0;
+  // bucketing scratch
+  uint8_t* bk_keys = nullptr;
+  uint32_t* bk_order = nullptr;
+  uint32_t* bk_small = nullptr;  // hist | cursor | ranges
+  size_t bk_cap = 0;
   // launch shape
+  bool bucketing = true;
   int gjk_lanes = 1;
-  int epa_ctas_per_sm = 3;
+  int gjk_lanes_large = 8;
+  int large_hull = 128;
+  int gjk_ctas_per_sm = 4;
+  int epa_ctas_per_sm = 5;
   uint64_t launches = 0;
   // optional per-pass timing
   bool profiling = false;
@@ -41,6 +53,17 @@ struct fclg_context {
   bool ev_epa = false;
   double gjk_ms = 0, epa_ms = 0;
   uint64_t timed = 0;
+  // device staging of the host-pointer mesh entry point
+  void* mesh_io = nullptr;
+  size_t mesh_io_bytes = 0;
+};
+
+struct fclg_mesh {
+  int device = 0;
+  void* nodes = nullptr;
+  void* tris = nullptr;
+  uint32_t n_nodes = 0;
+  uint32_t n_tris = 0;
 };
 
 namespace {
@@ -92,14 +115,35 @@ void release_shapes(fclg_context* c) {
 int ensure_epa(fclg_context* c, size_t n) {
   if (n <= c->epa_cap) return FCLG_OK;
   if (c->epa_list) cudaFree(c->epa_list);
+  if (c->epa_ovf) cudaFree(c->epa_ovf);
   if (c->epa_rec) cudaFree(c->epa_rec);
   c->epa_list = nullptr;
+  c->epa_ovf = nullptr;
   c->epa_rec = nullptr;
   c->epa_cap = 0;
   const size_t cap = std::max<size_t>(n, 1024);
   FCLG_CUDA(c, cudaMalloc(&c->epa_list, cap * sizeof(uint32_t)));
+  FCLG_CUDA(c, cudaMalloc(&c->epa_ovf, cap * sizeof(uint32_t)));
   FCLG_CUDA(c, cudaMalloc(&c->epa_rec, cap * fclg::kEpaRecordBytes));
   c->epa_cap = cap;
+  return FCLG_OK;
+}
+
+int ensure_bucket(fclg_context* c, size_t n) {
+  if (!c->bk_small) {
+    FCLG_CUDA(c, cudaMalloc(&c->bk_small, (2 * fclg::kBucketKeys + 4) * sizeof(uint32_t)));
+    FCLG_CUDA(c, cudaMemset(c->bk_small, 0, (2 * fclg::kBucketKeys + 4) * sizeof(uint32_t)));
+  }
+  if (n <= c->bk_cap) return FCLG_OK;
+  if (c->bk_keys) cudaFree(c->bk_keys);
+  if (c->bk_order) cudaFree(c->bk_order);
+  c->bk_keys = nullptr;
+  c->bk_order = nullptr;
+  c->bk_cap = 0;
+  const size_t cap = std::max<size_t>(n, 1024);
+  FCLG_CUDA(c, cudaMalloc(&c->bk_keys, cap));
+  FCLG_CUDA(c, cudaMalloc(&c->bk_order, cap * sizeof(uint32_t)));
+  c->bk_cap = cap;
   return FCLG_OK;
 }
 
@@ -168,14 +212,29 @@ int run_query(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_
     const int rc = collect_times(c);
     if (rc) return rc;
   }
-  if (prm.want_epa) FCLG_CUDA(c, cudaMemsetAsync(c->epa_count, 0, sizeof(uint32_t), st));
+  if (prm.want_epa) FCLG_CUDA(c, cudaMemsetAsync(c->epa_count, 0, 2 * sizeof(uint32_t), st));
+  if (c->bucketing) {
+    const int rc = ensure_bucket(c, n);
+    if (rc) return rc;
+  }
   if (c->profiling) FCLG_CUDA(c, cudaEventRecord(c->ev[0], st));
-  FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes, st));
-  c->launches += 1;
+  if (c->bucketing) {
+    fclg::BucketScratch bs{c->bk_keys, c->bk_order, c->bk_small, c->bk_small + fclg::kBucketKeys,
+                           c->bk_small + 2 * fclg::kBucketKeys};
+    FCLG_CUDA(c, fclg::launch_bucketing(b, bs, (uint32_t)c->large_hull, st));
+    const int blocks = c->num_sms * c->gjk_ctas_per_sm;
+    FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes, bs.order, bs.ranges, blocks, st));
+    FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes_large, bs.order, bs.ranges + 2, blocks, st));
+    c->launches += 5;
+  } else {
+    FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes, nullptr, nullptr, 0, st));
+    c->launches += 1;
+  }
   if (c->profiling) FCLG_CUDA(c, cudaEventRecord(c->ev[1], st));
   if (prm.want_epa) {
-    FCLG_CUDA(c, fclg::launch_epa(b, prm, q, c->num_sms * c->epa_ctas_per_sm, st));
-    c->launches += 1;
+    fclg::EpaQueue ovf{c->epa_count + 1, c->epa_ovf, nullptr};
+    FCLG_CUDA(c, fclg::launch_epa(b, prm, q, ovf, c->num_sms, c->epa_ctas_per_sm, st));
+    c->launches += prm.epa_max_faces > 128 ? 2 : 1;
     if (c->profiling) FCLG_CUDA(c, cudaEventRecord(c->ev[2], st));
   }
   if (c->profiling) {
@@ -222,7 +281,7 @@ int fclg_create(fclg_context** out, int device) {
   c->device = device;
   c->num_sms = prop.multiProcessorCount;
   if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaMalloc(&c->epa_count, sizeof(uint32_t)) != cudaSuccess || fclg::prepare_epa() != cudaSuccess) {
+      cudaMalloc(&c->epa_count, 2 * sizeof(uint32_t)) != cudaSuccess || fclg::prepare_epa() != cudaSuccess) {
     fclg_destroy(c);
     return FCLG_E_CUDA;
   }
@@ -236,9 +295,14 @@ void fclg_destroy(fclg_context* c) {
   release_shapes(c);
   if (c->epa_count) cudaFree(c->epa_count);
   if (c->epa_list) cudaFree(c->epa_list);
+  if (c->epa_ovf) cudaFree(c->epa_ovf);
   if (c->epa_rec) cudaFree(c->epa_rec);
   if (c->io_pairs) cudaFree(c->io_pairs);
   if (c->io_results) cudaFree(c->io_results);
+  if (c->bk_keys) cudaFree(c->bk_keys);
+  if (c->bk_order) cudaFree(c->bk_order);
+  if (c->bk_small) cudaFree(c->bk_small);
+  if (c->mesh_io) cudaFree(c->mesh_io);
   if (c->stream) cudaStreamDestroy(c->stream);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -305,21 +369,172 @@ int fclg_collide_device(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, c
   return run_query(c, d_pairs, n, req, d_results, static_cast<cudaStream_t>(stream), false);
 }
 
-int fclg_set_launch(fclg_context* c, int gjk_lanes, int epa_ctas_per_sm) {
-  if (!c) return FCLG_E_INVALID;
-  if (gjk_lanes) {
-    if (gjk_lanes != 1 && gjk_lanes != 2 && gjk_lanes != 4 && gjk_lanes != 8 && gjk_lanes != 16 && gjk_lanes != 32)
-      return fail(c, FCLG_E_INVALID, "gjk_lanes must be 1, 2, 4, 8, 16 or 32");
-    c->gjk_lanes = gjk_lanes;
-  }
-  if (epa_ctas_per_sm) {
-    if (epa_ctas_per_sm < 1 || epa_ctas_per_sm > 32) return fail(c, FCLG_E_INVALID, "epa_ctas_per_sm out of range");
-    c->epa_ctas_per_sm = epa_ctas_per_sm;
-  }
+static bool valid_lanes(int l) { return l == 1 || l == 2 || l == 4 || l == 8 || l == 16 || l == 32; }
+
+int fclg_set_tuning(fclg_context* c, const fclg_tuning* t) {
+  if (!c || !t) return FCLG_E_INVALID;
+  if ((t->gjk_lanes_small && !valid_lanes(t->gjk_lanes_small)) ||
+      (t->gjk_lanes_large && !valid_lanes(t->gjk_lanes_large)))
+    return fail(c, FCLG_E_INVALID, "GJK lanes per pair must be 1, 2, 4, 8, 16 or 32");
+  if (t->gjk_ctas_per_sm < 0 || t->gjk_ctas_per_sm > 32 || t->epa_ctas_per_sm < 0 || t->epa_ctas_per_sm > 32)
+    return fail(c, FCLG_E_INVALID, "CTAs per SM out of range");
+  if (t->large_hull_vertices < 0) return fail(c, FCLG_E_INVALID, "negative hull size threshold");
+  if (t->bucketing) c->bucketing = t->bucketing > 0;
+  if (t->gjk_lanes_small) c->gjk_lanes = t->gjk_lanes_small;
+  if (t->gjk_lanes_large) c->gjk_lanes_large = t->gjk_lanes_large;
+  if (t->large_hull_vertices) c->large_hull = t->large_hull_vertices;
+  if (t->gjk_ctas_per_sm) c->gjk_ctas_per_sm = t->gjk_ctas_per_sm;
+  if (t->epa_ctas_per_sm) c->epa_ctas_per_sm = t->epa_ctas_per_sm;
   return FCLG_OK;
 }
 
+int fclg_get_tuning(const fclg_context* c, fclg_tuning* t) {
+  if (!c || !t) return FCLG_E_INVALID;
+  t->bucketing = c->bucketing ? 1 : -1;
+  t->gjk_lanes_small = c->gjk_lanes;
+  t->gjk_lanes_large = c->gjk_lanes_large;
+  t->large_hull_vertices = c->large_hull;
+  t->gjk_ctas_per_sm = c->gjk_ctas_per_sm;
+  t->epa_ctas_per_sm = c->epa_ctas_per_sm;
+  return FCLG_OK;
+}
+
+int fclg_set_launch(fclg_context* c, int gjk_lanes, int epa_ctas_per_sm) {
+  fclg_tuning t{};
+  t.gjk_lanes_small = gjk_lanes;
+  t.gjk_lanes_large = gjk_lanes;
+  t.epa_ctas_per_sm = epa_ctas_per_sm;
+  return fclg_set_tuning(c, &t);
+}
+
 uint64_t fclg_launch_count(const fclg_context* c) { return c ? c->launches : 0; }
+
+int fclg_bvh_build(const float* vertices, uint32_t nv, const int32_t* tris, uint32_t nt, fclg_mesh_node* nodes,
+                   float* tris_xyzw) {
+  if (!vertices || !tris || !nodes || !tris_xyzw || nv == 0 || nt == 0 || nt > (1u << 29)) return FCLG_E_INVALID;
+  std::vector<fclg::MeshNodeRec> nn;
+  std::vector<float> soup;
+  if (fclg::build_obb_bvh(vertices, nv, tris, nt, nn, soup) != 0) return FCLG_E_INVALID;
+  std::memcpy(nodes, nn.data(), nn.size() * sizeof(fclg::MeshNodeRec));
+  std::memcpy(tris_xyzw, soup.data(), soup.size() * sizeof(float));
+  return FCLG_OK;
+}
+
+int fclg_mesh_create(fclg_context* c, const float* vertices, uint32_t nv, const int32_t* tris, uint32_t nt,
+                     fclg_mesh** out) {
+  if (!c) return FCLG_E_INVALID;
+  if (!out || !vertices || !tris || nv == 0 || nt == 0) return fail(c, FCLG_E_INVALID, "empty mesh or null pointer");
+  *out = nullptr;
+  if (nt > (1u << 29)) return fail(c, FCLG_E_TOO_LARGE, "too many triangles");
+  std::vector<fclg::MeshNodeRec> nodes;
+  std::vector<float> soup;
+  const int rc = fclg::build_obb_bvh(vertices, nv, tris, nt, nodes, soup);
+  if (rc == -2) return fail(c, FCLG_E_INVALID, "triangle vertex index out of range");
+  if (rc) return fail(c, FCLG_E_INVALID, "empty mesh");
+  FCLG_CUDA(c, cudaSetDevice(c->device));
+  fclg_mesh* m = new fclg_mesh();
+  m->device = c->device;
+  m->n_nodes = (uint32_t)nodes.size();
+  m->n_tris = nt;
+  cudaError_t e = cudaMalloc(&m->nodes, nodes.size() * sizeof(fclg::MeshNodeRec));
+  if (e == cudaSuccess) e = cudaMalloc(&m->tris, soup.size() * sizeof(float));
+  if (e == cudaSuccess)
+    e = cudaMemcpy(m->nodes, nodes.data(), nodes.size() * sizeof(fclg::MeshNodeRec), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(m->tris, soup.data(), soup.size() * sizeof(float), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    fclg_mesh_destroy(m);
+    return cuda_fail(c, e, "mesh upload");
+  }
+  *out = m;
+  return FCLG_OK;
+}
+
+void fclg_mesh_destroy(fclg_mesh* m) {
+  if (!m) return;
+  cudaSetDevice(m->device);
+  if (m->nodes) cudaFree(m->nodes);
+  if (m->tris) cudaFree(m->tris);
+  delete m;
+}
+
+int fclg_mesh_info(const fclg_mesh* m, uint32_t* n_nodes, uint32_t* n_tris) {
+  if (!m) return FCLG_E_INVALID;
+  if (n_nodes) *n_nodes = m->n_nodes;
+  if (n_tris) *n_tris = m->n_tris;
+  return FCLG_OK;
+}
+
+int fclg_mesh_export(const fclg_mesh* m, fclg_mesh_node* nodes, float* tris) {
+  if (!m) return FCLG_E_INVALID;
+  if (cudaSetDevice(m->device) != cudaSuccess) return FCLG_E_CUDA;
+  if (nodes && cudaMemcpy(nodes, m->nodes, (size_t)m->n_nodes * 64, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return FCLG_E_CUDA;
+  if (tris && cudaMemcpy(tris, m->tris, (size_t)m->n_tris * 48, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return FCLG_E_CUDA;
+  return FCLG_OK;
+}
+
+int fclg_mesh_collide_device(fclg_context* c, const fclg_mesh* a, const fclg_mesh* b, const float* d_poses,
+                             uint32_t n, uint32_t max_contacts, uint8_t* d_flags, uint32_t* d_counts, int32_t* d_pairs,
+                             uint32_t* d_status, void* stream) {
+  if (!c) return FCLG_E_INVALID;
+  if (!a || !b) return fail(c, FCLG_E_INVALID, "null mesh");
+  if (n == 0) return FCLG_OK;
+  if (max_contacts == 0) return fail(c, FCLG_E_INVALID, "max_contacts must be >= 1");
+  if (!d_poses || !d_flags || !d_counts || !d_pairs) return fail(c, FCLG_E_INVALID, "null pointer");
+  if (a->device != c->device || b->device != c->device) return fail(c, FCLG_E_INVALID, "mesh on another device");
+  FCLG_CUDA(c, cudaSetDevice(c->device));
+  fclg::MeshArgs m;
+  m.a = fclg::MeshDev{static_cast<const float4*>(a->nodes), static_cast<const float4*>(a->tris), a->n_nodes, a->n_tris};
+  m.b = fclg::MeshDev{static_cast<const float4*>(b->nodes), static_cast<const float4*>(b->tris), b->n_nodes, b->n_tris};
+  m.poses = reinterpret_cast<const float4*>(d_poses);
+  m.n_poses = n;
+  m.max_contacts = max_contacts;
+  m.flags = d_flags;
+  m.counts = d_counts;
+  m.pairs = d_pairs;
+  m.status = d_status;
+  const int blocks = c->num_sms * 8;
+  FCLG_CUDA(c, fclg::launch_mesh_collide(m, blocks, static_cast<cudaStream_t>(stream)));
+  c->launches += 1;
+  return FCLG_OK;
+}
+
+int fclg_mesh_collide(fclg_context* c, const fclg_mesh* a, const fclg_mesh* b, const float* poses, uint32_t n,
+                      uint32_t max_contacts, uint8_t* flags, uint32_t* counts, int32_t* pairs, uint32_t* status) {
+  if (!c) return FCLG_E_INVALID;
+  if (n == 0) return FCLG_OK;
+  if (!poses || !flags || !counts || !pairs) return fail(c, FCLG_E_INVALID, "null pointer");
+  if (max_contacts == 0) return fail(c, FCLG_E_INVALID, "max_contacts must be >= 1");
+  auto up16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
+  const size_t b_poses = up16((size_t)n * 48), b_flags = up16(n), b_counts = up16((size_t)n * 4),
+               b_pairs = up16((size_t)n * max_contacts * 8), b_status = up16((size_t)n * 4);
+  const size_t need = b_poses + b_flags + b_counts + b_pairs + b_status;
+  if (need > c->mesh_io_bytes) {
+    if (c->mesh_io) cudaFree(c->mesh_io);
+    c->mesh_io = nullptr;
+    c->mesh_io_bytes = 0;
+    FCLG_CUDA(c, cudaSetDevice(c->device));
+    FCLG_CUDA(c, cudaMalloc(&c->mesh_io, need));
+    c->mesh_io_bytes = need;
+  }
+  char* base = static_cast<char*>(c->mesh_io);
+  float* d_poses = reinterpret_cast<float*>(base);
+  uint8_t* d_flags = reinterpret_cast<uint8_t*>(base + b_poses);
+  uint32_t* d_counts = reinterpret_cast<uint32_t*>(base + b_poses + b_flags);
+  int32_t* d_pairs = reinterpret_cast<int32_t*>(base + b_poses + b_flags + b_counts);
+  uint32_t* d_status = reinterpret_cast<uint32_t*>(base + b_poses + b_flags + b_counts + b_pairs);
+  FCLG_CUDA(c, cudaMemcpyAsync(d_poses, poses, (size_t)n * 48, cudaMemcpyHostToDevice, c->stream));
+  const int rc = fclg_mesh_collide_device(c, a, b, d_poses, n, max_contacts, d_flags, d_counts, d_pairs, d_status,
+                                          c->stream);
+  if (rc) return rc;
+  FCLG_CUDA(c, cudaMemcpyAsync(flags, d_flags, n, cudaMemcpyDeviceToHost, c->stream));
+  FCLG_CUDA(c, cudaMemcpyAsync(counts, d_counts, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+  FCLG_CUDA(c, cudaMemcpyAsync(pairs, d_pairs, (size_t)n * max_contacts * 8, cudaMemcpyDeviceToHost, c->stream));
+  if (status) FCLG_CUDA(c, cudaMemcpyAsync(status, d_status, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+  FCLG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return FCLG_OK;
+}
 
 int fclg_set_profiling(fclg_context* c, int enable) {
   if (!c) return FCLG_E_INVALID;

@@ -9,9 +9,10 @@
 // (epa_polytope_expand.hpp:120-180) — and fan new faces from the point to the
 // patch's horizon.  Capacity (live faces <= max_faces, the reference's
 // MallocFailed) and the iteration limit end the loop with the current nearest
-// face, as the reference does.  A face counts as seen when the point lies more
-// than the tolerance beyond its plane (the reference uses >= 0): coplanar
-// faces stay, which keeps the FP32 polytope convex where supports tie.
+// face, as the reference does.  A face counts as seen when the point lies
+// beyond its plane by more than a tenth of the tolerance (the reference uses
+// >= 0): faces coplanar at FP32 resolution stay, which keeps the polytope
+// convex where supports tie exactly.
 //
 // Faces are ranked by plane distance among those the origin projects into
 // (the reference's pointToTriangle witness_in_simplex, epa_polytope_utils.h:
@@ -43,11 +44,18 @@
 namespace fclg {
 
 constexpr uint32_t kNoSlot = 0xFFFFFFFFu;
+// EPA outcome internal to the two-layout scheme: the polytope outgrew the
+// small layout; the pair is rerun in the large one.
+constexpr int kEpaOverflow = 16;
+// A face counts as seen by a new point lying more than kVisEps * tolerance
+// beyond its plane: above FP32 rounding of the plane test, far below the
+// convergence tolerance.
+constexpr float kVisEps = 0.1f;
 
 template <int FMAX, int VMAX>
 struct EpaSmem {
   float4 fn[FMAX];         // outward unit normal xyz, plane distance (inf: dead or degenerate)
-  float fkey[FMAX];        // plane distance when the origin projects inside, else inf
+  float fkey[FMAX];        // selection key: plane distance, + tolerance when the origin projects outside
   uint32_t fv[FMAX];       // vertex indices v0 | v1 << 8 | v2 << 16, counter-clockwise seen from outside
   uint16_t fadj[FMAX][4];  // neighbour across edge k = (v_k, v_k+1)
   uint32_t fmark[FMAX];    // classification stamp of the current expansion
@@ -56,9 +64,9 @@ struct EpaSmem {
   uint32_t start_at[VMAX];
   uint16_t patch[FMAX];    // faces of the visible patch, in discovery order
   uint16_t freestk[FMAX];  // recycled face slots
-  uint16_t hz_s[3 * FMAX]; // horizon edge: patch face
-  uint8_t hz_e[3 * FMAX];  //              and its edge index
-  uint16_t hz_slot[3 * FMAX];
+  uint16_t hz_s[FMAX + 8];  // horizon edge: patch face (a simple horizon has at most
+  uint8_t hz_e[FMAX + 8];   // patch size + 2 edges) and its edge index
+  uint16_t hz_slot[FMAX + 8];
   uint32_t npatch;
 };
 
@@ -73,11 +81,10 @@ __device__ __forceinline__ float4 face_plane(f3 a, f3 b, f3 c) {
   return make_float4(u.x, u.y, u.z, dot(u, a));
 }
 
-// Selection key of a face: its plane distance when the origin's projection
-// onto the plane lies inside the triangle (barycentric coordinates >= -1e-4),
-// else infinity.
-__device__ __forceinline__ float face_key(f3 a, f3 b, f3 c, float4 plane) {
-  if (!(plane.w < INFINITY)) return INFINITY;
+// Whether the origin's projection onto a face's plane lies inside its
+// triangle (barycentric coordinates >= -1e-4).
+__device__ __forceinline__ bool projects_inside(f3 a, f3 b, f3 c, float4 plane) {
+  if (!(plane.w < INFINITY)) return false;
   const f3 u = ld3(plane);
   const f3 p = u * plane.w;
   const float e0 = dot(u, cross(b - a, p - a));
@@ -85,7 +92,7 @@ __device__ __forceinline__ float face_key(f3 a, f3 b, f3 c, float4 plane) {
   const float e2 = dot(u, cross(a - c, p - c));
   const float tot = e0 + e1 + e2;
   const float slack = -1e-4f * fabsf(tot);
-  return (tot > 0.f && e0 >= slack && e1 >= slack && e2 >= slack) ? plane.w : INFINITY;
+  return tot > 0.f && e0 >= slack && e1 >= slack && e2 >= slack;
 }
 
 struct EpaResult {
@@ -135,7 +142,13 @@ struct EpaWarp {
     const float4 pl = face_plane(A, B, C);
     P.fv[t] = a | (b << 8) | (c << 16);
     P.fn[t] = pl;
-    P.fkey[t] = face_key(A, B, C, pl);
+    // Selection key: the plane distance, biased by the tolerance when the
+    // origin's projection misses the triangle.  The argmin of the key is the
+    // nearest face, except that a face the origin projects into wins when it
+    // is within the tolerance of the nearest plane: among coplanar triangles
+    // it holds the nearest point, and a sliver whose plane is nearest but
+    // whose triangle misses the projection is the reference's edge feature.
+    P.fkey[t] = projects_inside(A, B, C, pl) ? pl.w : pl.w + tol;
   }
 
   // Initial polytope from faces (index triples into the vertices already
@@ -180,38 +193,54 @@ struct EpaWarp {
     return build_faces(tri, 4);
   }
 
-  // Final closest-face solve in FP64 (epa.hpp:425-498); falls back to the
-  // last support pair like assignPenetrationPair (epa.hpp:340-365).
+  // Final closest-face solve in FP64: the point of the face's triangle
+  // nearest the origin (Ericson, Real-Time Collision Detection, 5.1.5) and its
+  // barycentric weights, which interpolate the support points into the
+  // witness pair (epa.hpp:425-498; when the origin projects into the
+  // triangle this is the reference's face parameterisation, otherwise its
+  // edge / vertex feature).  Depth is that point's distance from the origin
+  // (the reference's min_distance_square).  A degenerate triangle falls back
+  // to the last support pair like assignPenetrationPair (epa.hpp:340-365).
   __device__ void finalize(uint32_t fvp, f3 cand_pa, f3 cand_pb, EpaResult& r) const {
     const uint32_t ia = fvert(fvp, 0), ib = fvert(fvp, 1), ic = fvert(fvp, 2);
     const d3 a = tod(W(ia)), b = tod(W(ib)), c = tod(W(ic));
-    const d3 n = cross(b - a, c - a);
-    const double n2 = dot(n, n);
-    if (n2 > 0.0) {
-      const d3 u = n * (1.0 / sqrt(n2));
-      const double dist = dot(u, a);
-      const d3 p = u * dist;
-      const double area = sqrt(n2);
-      const d3 dl0 = a - b, dl1 = b - c, dl2 = c - a;
-      const d3 q0 = cross(dl1, b - p), q1 = cross(dl2, c - p), q2 = cross(dl0, a - p);
-      const double w0 = sqrt(dot(q0, q0)) / area;
-      const double w1 = sqrt(dot(q1, q1)) / area;
-      const double chk = sqrt(dot(q2, q2)) / area;
-      const double w2 = 1.0 - w0 - w1;
-      if (!(fabs(chk - w2) > 0.01)) {
-        const d3 pa0 = tod(ld3(P.vpa[ia])), pa1 = tod(ld3(P.vpa[ib])), pa2 = tod(ld3(P.vpa[ic]));
-        const d3 pb0 = pa0 - a, pb1 = pa1 - b, pb2 = pa2 - c;
-        const d3 x0 = (pa0 * w0 + pa1 * w1) + pa2 * w2;
-        const d3 x1 = (pb0 * w0 + pb1 * w1) + pb2 * w2;
-        r.p0 = mk3((float)x0.x, (float)x0.y, (float)x0.z);
-        r.p1 = mk3((float)x1.x, (float)x1.y, (float)x1.z);
-        r.depth = (float)fabs(dist);
-        return;
-      }
+    const d3 ab = b - a, ac = c - a;
+    const d3 n = cross(ab, ac);
+    if (!(dot(n, n) > 0.0)) {
+      r.p0 = cand_pa;
+      r.p1 = cand_pb;
+      r.depth = nrm(cand_pa - cand_pb);
+      return;
     }
-    r.p0 = cand_pa;
-    r.p1 = cand_pb;
-    r.depth = nrm(cand_pa - cand_pb);
+    double u, v, w;
+    const d3 ap = a * -1.0, bp = b * -1.0, cp = c * -1.0;
+    const double d1 = dot(ab, ap), d2 = dot(ac, ap);
+    const double d3v = dot(ab, bp), d4 = dot(ac, bp);
+    const double d5 = dot(ab, cp), d6 = dot(ac, cp);
+    const double vc = d1 * d4 - d3v * d2, vb = d5 * d2 - d1 * d6, va = d3v * d6 - d5 * d4;
+    if (d1 <= 0.0 && d2 <= 0.0) { u = 1; v = 0; w = 0; }
+    else if (d3v >= 0.0 && d4 <= d3v) { u = 0; v = 1; w = 0; }
+    else if (vc <= 0.0 && d1 >= 0.0 && d3v <= 0.0) { v = d1 / (d1 - d3v); u = 1 - v; w = 0; }
+    else if (d6 >= 0.0 && d5 <= d6) { u = 0; v = 0; w = 1; }
+    else if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) { w = d2 / (d2 - d6); u = 1 - w; v = 0; }
+    else if (va <= 0.0 && (d4 - d3v) >= 0.0 && (d5 - d6) >= 0.0) {
+      w = (d4 - d3v) / ((d4 - d3v) + (d5 - d6));
+      u = 0;
+      v = 1 - w;
+    } else {
+      const double inv = 1.0 / (va + vb + vc);
+      v = vb * inv;
+      w = vc * inv;
+      u = 1.0 - v - w;
+    }
+    const d3 q = (a * u + b * v) + c * w;
+    const d3 pa0 = tod(ld3(P.vpa[ia])), pa1 = tod(ld3(P.vpa[ib])), pa2 = tod(ld3(P.vpa[ic]));
+    const d3 pb0 = pa0 - a, pb1 = pa1 - b, pb2 = pa2 - c;
+    const d3 x0 = (pa0 * u + pa1 * v) + pa2 * w;
+    const d3 x1 = (pb0 * u + pb1 * v) + pb2 * w;
+    r.p0 = mk3((float)x0.x, (float)x0.y, (float)x0.z);
+    r.p1 = mk3((float)x1.x, (float)x1.y, (float)x1.z);
+    r.depth = (float)sqrt(dot(q, q));
   }
 
   __device__ void touching(f3 pa, f3 pb, EpaResult& r) const {
@@ -293,40 +322,28 @@ struct EpaWarp {
     return build_faces(tri, 8);
   }
 
-  // Warp argmin of the selection key (ties: lowest slot); when no face
-  // qualifies, the argmin of the plane distance over live faces.
+  // Warp argmin of the selection key over live faces (ties: lowest slot);
+  // returns the slot and its plane distance.
   __device__ __forceinline__ void nearest(int& best_slot, float& best_d) const {
-    float bd = INFINITY;
+    float bk = INFINITY;
     int bs = 0x7FFFFFFF;
     for (int s = (int)lane; s < hw; s += 32) {
-      const float d = P.fkey[s];
-      if (d < bd) { bd = d; bs = s; }
+      const float k = P.fkey[s];
+      if (k < bk) { bk = k; bs = s; }
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
-      const float od = __shfl_xor_sync(0xFFFFFFFFu, bd, off);
+      const float ok = __shfl_xor_sync(0xFFFFFFFFu, bk, off);
       const int os = __shfl_xor_sync(0xFFFFFFFFu, bs, off);
-      if (od < bd || (od == bd && os < bs)) { bd = od; bs = os; }
-    }
-    if (!(bd < INFINITY)) {
-      bs = 0x7FFFFFFF;
-      for (int s = (int)lane; s < hw; s += 32) {
-        const float d = P.fn[s].w;
-        if (d < bd) { bd = d; bs = s; }
-      }
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        const float od = __shfl_xor_sync(0xFFFFFFFFu, bd, off);
-        const int os = __shfl_xor_sync(0xFFFFFFFFu, bs, off);
-        if (od < bd || (od == bd && os < bs)) { bd = od; bs = os; }
-      }
+      if (ok < bk || (ok == bk && os < bs)) { bk = ok; bs = os; }
     }
     best_slot = __shfl_sync(0xFFFFFFFFu, bs, 0);
-    best_d = __shfl_sync(0xFFFFFFFFu, bd, 0);
+    best_d = (best_slot != 0x7FFFFFFF) ? P.fn[best_slot].w : INFINITY;
   }
 
   // One expansion with the new vertex nv-1 from the visible face `start`;
-  // returns 0 ok, 1 capacity, 2 broken topology.
+  // returns 0 ok, 1 over max_faces live faces, 2 broken topology, 3 out of
+  // face slots in this layout.
   __device__ int expand(int start, int max_faces) {
     const uint32_t vnew = (uint32_t)(nv - 1);
     const f3 w = W(vnew);
@@ -349,7 +366,7 @@ struct EpaWarp {
           const uint32_t m = P.fmark[g];
           if (m == kVis || m == kHid) continue;
           const float4 q = P.fn[g];
-          const bool visible = dot(ld3(q), w - W(fvert(P.fv[g], 0))) > tol;
+          const bool visible = dot(ld3(q), w - W(fvert(P.fv[g], 0))) > kVisEps * tol;
           if (atomicCAS(&P.fmark[g], m, visible ? kVis : kHid) == m && visible) {
             const uint32_t slot = atomicAdd(&P.npatch, 1u);
             if (slot < FMAX) P.patch[slot] = (uint16_t)g;
@@ -382,20 +399,21 @@ struct EpaWarp {
       }
       int o = n_hz + incl - h;
       for (int e = 0; e < 3; ++e)
-        if (hmask & (1u << e)) { P.hz_s[o] = (uint16_t)f; P.hz_e[o] = (uint8_t)e; ++o; }
+        if ((hmask & (1u << e)) && o < FMAX + 8) { P.hz_s[o] = (uint16_t)f; P.hz_e[o] = (uint8_t)e; ++o; }
       n_hz += __shfl_sync(0xFFFFFFFFu, incl, 31);
     }
     const int new_live = live - n_rem + n_hz;
     const int avail = fs_top + n_rem;
     const int fresh = n_hz > avail ? n_hz - avail : 0;
-    if (n_hz < 3) return 2;
-    if (new_live > max_faces || hw + fresh > FMAX) return 1;
+    if (n_hz < 3 || n_hz > FMAX + 8) return 2;
+    if (new_live > max_faces) return 1;
+    if (hw + fresh > FMAX) return 3;
     // recycle the patch's slots (pushed above the older free slots)
     for (int k = (int)lane; k < n_rem; k += 32) P.freestk[fs_top + k] = P.patch[k];
     __syncwarp();
     // Phase A: endpoints and outside neighbours of the horizon edges (the
     // patch slots are overwritten below); slots popped from the free stack.
-    constexpr int kPer = (3 * FMAX + 31) / 32;
+    constexpr int kPer = (FMAX + 8 + 31) / 32;
     uint32_t ha[kPer], hb[kPer], hg[kPer];
     int j = 0;
     for (int k = (int)lane; k < n_hz; k += 32, ++j) {
@@ -453,8 +471,11 @@ struct EpaWarp {
     return 0;
   }
 
-  // Runs EPA from the GJK simplex (rank, pa[], pb[]).
-  __device__ EpaResult run(int rank, const f3* spa, const f3* spb, int max_iter, int max_faces) {
+  // Runs EPA from the GJK simplex (rank, pa[], pb[]).  When this layout runs
+  // out of face or vertex slots before max_faces, the result is kEpaOverflow
+  // (rerun in a larger layout) unless overflow_is_final.
+  __device__ EpaResult run(int rank, const f3* spa, const f3* spb, int max_iter, int max_faces,
+                           bool overflow_is_final) {
     EpaResult r;
     r.status = kEpaFailed;
     r.depth = 0.f;
@@ -518,15 +539,19 @@ struct EpaWarp {
       }
       if (nv >= VMAX) {
         finalize(bfv, pa, pb, r);
-        r.status = kEpaMallocFailed;
+        r.status = overflow_is_final ? kEpaMallocFailed : kEpaOverflow;
         return r;
       }
       push_vertex(pa, pb);
       __syncwarp();
       const int ex = expand(bs, max_faces);
-      if (ex == 1) {
+      if (ex == 1 || (ex == 3 && overflow_is_final)) {
         finalize(bfv, pa, pb, r);
         r.status = kEpaMallocFailed;
+        return r;
+      }
+      if (ex == 3) {
+        r.status = kEpaOverflow;
         return r;
       }
       if (ex == 2) {

@@ -27,10 +27,33 @@ struct EpaQueue {
 };
 constexpr size_t kEpaRecordBytes = 7 * sizeof(float4);
 
-cudaError_t launch_gjk(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q, int lanes, cudaStream_t st);
+// Scratch of the bucketing pass: pairs sorted by shape class (bucket.cu).
+constexpr int kShapeClasses = 6;  // box, sphere, capsule, cylinder, convex <= big_nv, convex > big_nv
+constexpr int kBucketSmallKeys = kShapeClasses * kShapeClasses;
+constexpr int kBucketKeys = 2 * kBucketSmallKeys;
+struct BucketScratch {
+  uint8_t* keys;      // [n] class key per pair
+  uint32_t* order;    // [n] pair indices sorted by key
+  uint32_t* hist;     // [kBucketKeys], zero between batches
+  uint32_t* cursor;   // [kBucketKeys]
+  uint32_t* ranges;   // [4]: [begin, end) of the small-pair launch, then of the large-pair launch
+};
+
+cudaError_t launch_bucketing(const BatchArgs& b, const BucketScratch& s, uint32_t big_nv, cudaStream_t st);
+
+// GJK pass over order[range[0] .. range[1]) (order / range may be null: all
+// pairs in index order) with `lanes` lanes per pair, as a persistent grid of
+// `blocks` CTAs (0: one CTA per 128 lanes of work, not persistent).
+cudaError_t launch_gjk(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q, int lanes,
+                       const uint32_t* order, const uint32_t* range, int blocks, cudaStream_t st);
 cudaError_t prepare_epa();
-cudaError_t launch_epa(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q, int blocks, cudaStream_t st);
+// EPA over q's list: the small-polytope pass, then (when max_faces exceeds it)
+// the large pass over the pairs ovf collected.  ovf.count must be zero and
+// ovf.list hold q's capacity; ovf.rec is unused.
+cudaError_t launch_epa(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q, const EpaQueue& ovf,
+                       int num_sms, int ctas_per_sm, cudaStream_t st);
 size_t epa_smem_bytes();
+size_t epa_smem_bytes_large();
 int epa_max_faces_supported();
 
 }  // namespace fclg

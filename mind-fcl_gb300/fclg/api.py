@@ -22,12 +22,24 @@ EXPORTS = [
     "fclg_create", "fclg_destroy", "fclg_last_error", "fclg_version", "fclg_built_arch",
     "fclg_set_shapes", "fclg_set_shapes_device",
     "fclg_distance", "fclg_distance_device", "fclg_collide", "fclg_collide_device",
-    "fclg_set_launch", "fclg_launch_count", "fclg_set_profiling", "fclg_pass_times",
+    "fclg_set_launch", "fclg_set_tuning", "fclg_get_tuning", "fclg_launch_count", "fclg_set_profiling",
+    "fclg_pass_times", "fclg_bvh_build", "fclg_mesh_create", "fclg_mesh_destroy", "fclg_mesh_info", "fclg_mesh_export",
+    "fclg_mesh_collide", "fclg_mesh_collide_device",
 ]
+
+MESH_NODE_DTYPE = np.dtype([("axis", "<f4", (9,)), ("center", "<f4", (3,)), ("extent", "<f4", (3,)),
+                            ("child", "<i4")])
+assert MESH_NODE_DTYPE.itemsize == 64
 
 
 class FclgError(RuntimeError):
     pass
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("bucketing", ctypes.c_int32), ("gjk_lanes_small", ctypes.c_int32),
+                ("gjk_lanes_large", ctypes.c_int32), ("large_hull_vertices", ctypes.c_int32),
+                ("gjk_ctas_per_sm", ctypes.c_int32), ("epa_ctas_per_sm", ctypes.c_int32)]
 
 
 class Request(ctypes.Structure):
@@ -69,6 +81,10 @@ def load_library(path=LIB_PATH):
         getattr(lib, name).restype = i32
     lib.fclg_set_launch.argtypes = [vp, i32, i32]
     lib.fclg_set_launch.restype = i32
+    lib.fclg_set_tuning.argtypes = [vp, ctypes.POINTER(Tuning)]
+    lib.fclg_set_tuning.restype = i32
+    lib.fclg_get_tuning.argtypes = [vp, ctypes.POINTER(Tuning)]
+    lib.fclg_get_tuning.restype = i32
     lib.fclg_launch_count.argtypes = [vp]
     lib.fclg_launch_count.restype = u64
     lib.fclg_set_profiling.argtypes = [vp, i32]
@@ -76,6 +92,20 @@ def load_library(path=LIB_PATH):
     lib.fclg_pass_times.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                                     ctypes.POINTER(u64), i32]
     lib.fclg_pass_times.restype = i32
+    lib.fclg_bvh_build.argtypes = [vp, u32, vp, u32, vp, vp]
+    lib.fclg_bvh_build.restype = i32
+    lib.fclg_mesh_create.argtypes = [vp, vp, u32, vp, u32, ctypes.POINTER(vp)]
+    lib.fclg_mesh_create.restype = i32
+    lib.fclg_mesh_destroy.argtypes = [vp]
+    lib.fclg_mesh_destroy.restype = None
+    lib.fclg_mesh_info.argtypes = [vp, ctypes.POINTER(u32), ctypes.POINTER(u32)]
+    lib.fclg_mesh_info.restype = i32
+    lib.fclg_mesh_export.argtypes = [vp, vp, vp]
+    lib.fclg_mesh_export.restype = i32
+    lib.fclg_mesh_collide.argtypes = [vp, vp, vp, vp, u32, u32, vp, vp, vp, vp]
+    lib.fclg_mesh_collide.restype = i32
+    lib.fclg_mesh_collide_device.argtypes = [vp, vp, vp, vp, u32, u32, vp, vp, vp, vp, vp]
+    lib.fclg_mesh_collide_device.restype = i32
     _lib = lib
     return lib
 
@@ -170,6 +200,20 @@ class Context:
     def set_launch(self, gjk_lanes=0, epa_ctas_per_sm=0):
         self._check(self.lib.fclg_set_launch(self.h, gjk_lanes, epa_ctas_per_sm), "fclg_set_launch")
 
+    def set_tuning(self, **kw):
+        """Fields of fclg_tuning by name; unspecified ones keep their value."""
+        t = Tuning()
+        for k, v in kw.items():
+            if k == "bucketing":
+                v = 1 if v else -1
+            setattr(t, k, int(v))
+        self._check(self.lib.fclg_set_tuning(self.h, ctypes.byref(t)), "fclg_set_tuning")
+
+    def get_tuning(self):
+        t = Tuning()
+        self._check(self.lib.fclg_get_tuning(self.h, ctypes.byref(t)), "fclg_get_tuning")
+        return {name: getattr(t, name) for name, _ in Tuning._fields_}
+
     def set_profiling(self, enable=True):
         self._check(self.lib.fclg_set_profiling(self.h, int(enable)), "fclg_set_profiling")
 
@@ -183,3 +227,63 @@ class Context:
     @property
     def launch_count(self):
         return int(self.lib.fclg_launch_count(self.h))
+
+
+class GpuMesh:
+    """A triangle mesh with its OBB hierarchy on the context's device."""
+
+    def __init__(self, ctx, vertices, triangles):
+        self.ctx = ctx
+        v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+        t = np.ascontiguousarray(triangles, np.int32).reshape(-1, 3)
+        h = ctypes.c_void_p()
+        ctx._check(ctx.lib.fclg_mesh_create(ctx.h, _ptr(v), len(v), _ptr(t), len(t), ctypes.byref(h)),
+                   "fclg_mesh_create")
+        self.h = h
+        nn, nt = ctypes.c_uint32(), ctypes.c_uint32()
+        ctx.lib.fclg_mesh_info(h, ctypes.byref(nn), ctypes.byref(nt))
+        self.n_nodes, self.n_tris = nn.value, nt.value
+
+    def export(self):
+        """(nodes [n_nodes] MESH_NODE_DTYPE, triangles float32 [n_tris, 3, 4])."""
+        nodes = np.zeros(self.n_nodes, MESH_NODE_DTYPE)
+        tris = np.zeros((self.n_tris, 3, 4), np.float32)
+        assert self.ctx.lib.fclg_mesh_export(self.h, _ptr(nodes), _ptr(tris)) == 0
+        return nodes, tris
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.fclg_mesh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def mesh_collide(ctx, mesh_a, mesh_b, poses, max_contacts=1):
+    """Boolean mesh-mesh collision per pose (host arrays): (flags, counts, pairs, status)."""
+    p = np.ascontiguousarray(poses, np.float32).reshape(-1, 12)
+    n = len(p)
+    flags = np.zeros(n, np.uint8)
+    counts = np.zeros(n, np.uint32)
+    pairs = np.full((n, max_contacts, 2), -1, np.int32)
+    status = np.zeros(n, np.uint32)
+    ctx._check(ctx.lib.fclg_mesh_collide(ctx.h, mesh_a.h, mesh_b.h, _ptr(p), n, max_contacts, _ptr(flags),
+                                         _ptr(counts), _ptr(pairs), _ptr(status)), "fclg_mesh_collide")
+    return flags, counts, pairs, status
+
+
+def bvh_build(vertices, triangles):
+    """Host-only BVH build: (nodes [2 nt - 1] MESH_NODE_DTYPE, triangles float32 [nt, 3, 4])."""
+    lib = load_library()
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+    t = np.ascontiguousarray(triangles, np.int32).reshape(-1, 3)
+    nodes = np.zeros(2 * len(t) - 1, MESH_NODE_DTYPE)
+    soup = np.zeros((len(t), 3, 4), np.float32)
+    rc = lib.fclg_bvh_build(_ptr(v), len(v), _ptr(t), len(t), _ptr(nodes), _ptr(soup))
+    if rc != 0:
+        raise FclgError("fclg_bvh_build failed (%d)" % rc)
+    return nodes, soup

@@ -194,3 +194,65 @@ def pareto(n_pairs=4_000_000, seed=SEED_BASE + 4, g_max=PARETO_G_MAX):
     s, v, rho = _make_shapes(rng, types, 0.02, 0.4, lambda k: pareto_counts(rng, k))
     p = _pairs(rng, n_pairs, rho, g_max)
     return Batch("pareto", s, v, p, {"seed": seed, "g_max": g_max})
+
+
+# ------------------------------------------------------------------ meshes --
+_ICO_T = (1.0 + 5.0 ** 0.5) / 2.0
+_ICO_V = np.array([(-1, _ICO_T, 0), (1, _ICO_T, 0), (-1, -_ICO_T, 0), (1, -_ICO_T, 0), (0, -1, _ICO_T),
+                   (0, 1, _ICO_T), (0, -1, -_ICO_T), (0, 1, -_ICO_T), (_ICO_T, 0, -1), (_ICO_T, 0, 1),
+                   (-_ICO_T, 0, -1), (-_ICO_T, 0, 1)], np.float64)
+_ICO_F = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2), (10, 7, 6),
+          (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10),
+          (8, 6, 7), (9, 8, 1)]
+
+
+@dataclass
+class Mesh:
+    vertices: np.ndarray   # float32 [nv, 3]
+    triangles: np.ndarray  # int32 [nt, 3]
+
+
+def geodesic_sphere(freq, radius=1.0, noise=0.0, seed=SEED_BASE + 2):
+    """Class I geodesic sphere: every icosahedron face split into freq^2
+    triangles (20 freq^2 triangles, 10 freq^2 + 2 vertices), projected to the
+    sphere, each vertex then moved radially by N(0, noise) metres."""
+    keys = {}
+    verts = []
+    tris = []
+
+    def vid(face, i, j):
+        a, b, c = face
+        w = {a: freq - i - j, b: i, c: j}
+        key = tuple(sorted((k, v) for k, v in w.items() if v > 0))
+        if key not in keys:
+            keys[key] = len(verts)
+            p = (w[a] * _ICO_V[a] + w[b] * _ICO_V[b] + w[c] * _ICO_V[c]) / freq
+            verts.append(p / np.linalg.norm(p))
+        return keys[key]
+
+    for face in _ICO_F:
+        for i in range(freq):
+            for j in range(freq - i):
+                tris.append((vid(face, i, j), vid(face, i + 1, j), vid(face, i, j + 1)))
+                if i + j + 1 < freq:
+                    tris.append((vid(face, i + 1, j), vid(face, i + 1, j + 1), vid(face, i, j + 1)))
+    v = np.array(verts)
+    r = np.full(len(v), float(radius))
+    if noise:
+        r = r + noise * _normals(_rng(seed), (len(v),))
+    return Mesh((v * r[:, None]).astype(np.float32), np.array(tris, np.int32))
+
+
+def mesh_poses(n, max_dist=0.8, seed=SEED_BASE + 3):
+    """Random relative poses: translation uniform in a ball of radius max_dist,
+    uniform rotation; float32 [n, 12] (rotation row-major, translation)."""
+    rng = _rng(seed)
+    R = random_rotations(rng, n)
+    d = unit_vectors(rng, n)
+    t = d * (max_dist * rng.random(n) ** (1.0 / 3.0))[:, None]
+    return np.concatenate([R, t], axis=1).astype(np.float32)
+
+
+def mesh_pair(freq=50, radius=0.3, noise=0.05, seed=SEED_BASE + 2):
+    """The two bumpy 50k-triangle spheres of the mesh-mesh workload."""
+    return (geodesic_sphere(freq, radius, noise, seed), geodesic_sphere(freq, radius, noise, seed + 100))

@@ -55,8 +55,12 @@ def _load():
         lib.orc_collide.restype = i
         lib.orc_time_signed_distance.argtypes = [vp, i, vp, vp, i, vp, i]
         lib.orc_time_signed_distance.restype = d
-        if hasattr(lib, "orc_mesh_collide"):
-            lib.orc_mesh_collide.restype = i
+        lib.orc_mesh_collide.argtypes = [vp, vp, vp, vp, vp, i, i, i, vp, vp, vp, i]
+        lib.orc_mesh_collide.restype = i
+        lib.orc_mesh_allpairs.argtypes = [vp, i, vp, i, vp, vp, i]
+        lib.orc_mesh_allpairs.restype = i
+        lib.orc_tri_tri.argtypes = [vp, vp, vp]
+        lib.orc_tri_tri.restype = i
         _lib = lib
     return _lib
 
@@ -147,3 +151,43 @@ def ref_collide(batch, want_contact=False, threads=None):
     assert lib.ref_collide(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), int(want_contact), _ptr(out),
                            threads or default_threads()) == 0
     return out
+
+
+def mesh_collide(nodes_a, tris_a, nodes_b, tris_b, poses, max_contacts=1, pair_cap=None, threads=None):
+    """MeshIntersect per pose over the given flattened trees (restatement).
+
+    max_contacts = 0: every colliding pair (up to pair_cap stored per pose).
+    Returns (flags, counts, pairs[n, pair_cap, 2])."""
+    lib = _load()
+    poses = np.ascontiguousarray(poses, np.float32).reshape(-1, 12)
+    n = len(poses)
+    cap = pair_cap if pair_cap is not None else max(max_contacts, 1)
+    flags = np.zeros(n, np.uint8)
+    counts = np.zeros(n, np.uint32)
+    pairs = np.full((n, cap, 2), -1, np.int32)
+    na = np.ascontiguousarray(nodes_a)
+    nb = np.ascontiguousarray(nodes_b)
+    ta = np.ascontiguousarray(tris_a, np.float32)
+    tb = np.ascontiguousarray(tris_b, np.float32)
+    assert lib.orc_mesh_collide(_ptr(na), _ptr(ta), _ptr(nb), _ptr(tb), _ptr(poses), n, int(max_contacts), cap,
+                                _ptr(flags), _ptr(counts), _ptr(pairs), threads or default_threads()) == 0
+    return flags, counts, pairs
+
+
+def mesh_allpairs(tris_a, tris_b, pose, cap=1 << 20):
+    """Every colliding triangle pair of one pose by brute force."""
+    lib = _load()
+    ta = np.ascontiguousarray(tris_a, np.float32)
+    tb = np.ascontiguousarray(tris_b, np.float32)
+    p = np.ascontiguousarray(pose, np.float32).reshape(12)
+    out = np.zeros((cap, 2), np.int32)
+    n = lib.orc_mesh_allpairs(_ptr(ta), len(ta), _ptr(tb), len(tb), _ptr(p), _ptr(out), cap)
+    return out[:min(n, cap)]
+
+
+def tri_tri(p, q, pose):
+    lib = _load()
+    p = np.ascontiguousarray(p, np.float64).reshape(9)
+    q = np.ascontiguousarray(q, np.float64).reshape(9)
+    pose = np.ascontiguousarray(pose, np.float64).reshape(12)
+    return bool(lib.orc_tri_tri(_ptr(p), _ptr(q), _ptr(pose)))

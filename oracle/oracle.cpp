@@ -7,11 +7,13 @@
 // (include/fcl/narrowphase/collision_interface-inl.h:18 builds a solver per call).
 #include <chrono>
 #include <cstdint>
+#include <cstdint>
 #include <cstring>
 #include <thread>
 #include <vector>
 
 #include "orc_convex.hpp"
+#include "orc_mesh.hpp"
 
 namespace {
 
@@ -176,6 +178,63 @@ double orc_time_signed_distance(const void* shapes, int n_shapes, const float* v
   orc_signed_distance(shapes, n_shapes, verts, pairs, n_pairs, nullptr, out, n_threads, 0, 0, 0, 0, 0);
   const auto t1 = std::chrono::steady_clock::now();
   return std::chrono::duration<double>(t1 - t0).count();
+}
+
+// OrientedNodeBVHSolver::MeshIntersect with penetration off per pose
+// (bvh_solver-inl.h:74-164): b posed by poses[i] (12 floats, rotation
+// row-major then translation) in a's frame, traversing the given flattened
+// OBB trees; up to max_contacts (a, b) triangle pairs per pose in the
+// reference's traversal order.  max_contacts = 0 means no limit (every
+// colliding pair; pairs must then hold pair_cap entries per pose).
+int orc_mesh_collide(const void* nodes_a, const float* tris_a, const void* nodes_b, const float* tris_b,
+                     const float* poses, int n_poses, int max_contacts, int pair_cap, uint8_t* flags, uint32_t* counts,
+                     int32_t* pairs, int n_threads) {
+  const orc::MeshNode* na = (const orc::MeshNode*)nodes_a;
+  const orc::MeshNode* nb = (const orc::MeshNode*)nodes_b;
+  parallelFor(n_poses, n_threads, [&](int b, int e) {
+    std::vector<std::pair<int, int>> c;
+    for (int i = b; i < e; ++i) {
+      orc::Mat3 R;
+      for (int k = 0; k < 9; ++k) R.m[k] = poses[12 * (size_t)i + k];
+      const double T[3] = {poses[12 * (size_t)i + 9], poses[12 * (size_t)i + 10], poses[12 * (size_t)i + 11]};
+      orc::meshIntersect(na, tris_a, nb, tris_b, R, T, max_contacts > 0 ? (size_t)max_contacts : SIZE_MAX, c);
+      flags[i] = c.empty() ? 0 : 1;
+      counts[i] = (uint32_t)c.size();
+      const size_t cap = (size_t)pair_cap;
+      for (size_t k = 0; k < c.size() && k < cap; ++k) {
+        pairs[2 * (cap * i + k)] = c[k].first;
+        pairs[2 * (cap * i + k) + 1] = c[k].second;
+      }
+    }
+  });
+  return 0;
+}
+
+// Every colliding triangle pair of one pose by brute force (returns the count;
+// writes up to cap pairs).
+int orc_mesh_allpairs(const float* tris_a, int n_a, const float* tris_b, int n_b, const float* pose, int32_t* pairs,
+                      int cap) {
+  orc::Mat3 R;
+  for (int k = 0; k < 9; ++k) R.m[k] = pose[k];
+  const double T[3] = {pose[9], pose[10], pose[11]};
+  std::vector<std::pair<int, int>> c;
+  orc::allPairs(tris_a, n_a, tris_b, n_b, R, T, c);
+  for (size_t k = 0; k < c.size() && (int)k < cap; ++k) {
+    pairs[2 * k] = c[k].first;
+    pairs[2 * k + 1] = c[k].second;
+  }
+  return (int)c.size();
+}
+
+// One triangle-triangle verdict (intersect_Triangle, boolean).
+int orc_tri_tri(const double* p /* 9 */, const double* q /* 9 */, const double* pose /* 12 */) {
+  orc::Mat3 R;
+  for (int k = 0; k < 9; ++k) R.m[k] = pose[k];
+  const double T[3] = {pose[9], pose[10], pose[11]};
+  return orc::intersectTriangle({p[0], p[1], p[2]}, {p[3], p[4], p[5]}, {p[6], p[7], p[8]}, {q[0], q[1], q[2]},
+                                {q[3], q[4], q[5]}, {q[6], q[7], q[8]}, R, T)
+             ? 1
+             : 0;
 }
 
 }  // extern "C"
