@@ -25,9 +25,9 @@
 // stamp), horizon edges are gathered with a warp prefix sum, slots are
 // recycled through a free stack, and the fan is linked through a per-vertex
 // "edge starting here" table.  Only the nearest-face argmin touches every
-// slot: one shared-memory load per lane per 32 slots.  Faces carry FP32 unit
-// normals and plane distances; the final closest-face solve (normal, depth,
-// barycentric witness points) runs in FP64.
+// slot: one shared-memory load per lane per 32 slots.  Face planes are solved
+// in FP64 and stored as FP32 unit normals and distances; the final
+// closest-face solve (depth, barycentric witness points) runs in FP64.
 //
 // Initial polytope from the GJK simplex: epa_simplex2polytope.hpp:41-376
 // (touching detection, triangle blown up along +-normal, segment search over
@@ -73,12 +73,18 @@ struct EpaSmem {
 __device__ __forceinline__ uint32_t fvert(uint32_t packed, int k) { return (packed >> (8 * k)) & 0xFFu; }
 __device__ __forceinline__ f3 ld3(const float4& q) { return mk3(q.x, q.y, q.z); }
 
+// Face plane (outward unit normal, distance from the origin) solved in FP64:
+// differences of the FP32 vertices are exact in FP64, so the normal of a small
+// face far from the origin keeps its direction; an FP32 cross product there
+// errs by ~eps |a| / |edge| radians, enough to misjudge which faces a distant
+// support point sees and fold the polytope.
 __device__ __forceinline__ float4 face_plane(f3 a, f3 b, f3 c) {
-  const f3 n = cross(b - a, c - a);
-  const float n2 = sqn(n);
-  if (!(n2 > 0.f)) return make_float4(0.f, 0.f, 0.f, INFINITY);
-  const f3 u = n * rsqrtf(n2);
-  return make_float4(u.x, u.y, u.z, dot(u, a));
+  const d3 A = tod(a);
+  const d3 n = cross(tod(b) - A, tod(c) - A);
+  const double n2 = dot(n, n);
+  if (!(n2 > 0.0)) return make_float4(0.f, 0.f, 0.f, INFINITY);
+  const d3 u = n * (1.0 / sqrt(n2));
+  return make_float4((float)u.x, (float)u.y, (float)u.z, (float)dot(u, A));
 }
 
 // Whether the origin's projection onto a face's plane lies inside its
