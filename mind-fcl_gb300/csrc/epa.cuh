@@ -25,9 +25,10 @@
 // stamp), horizon edges are gathered with a warp prefix sum, slots are
 // recycled through a free stack, and the fan is linked through a per-vertex
 // "edge starting here" table.  Only the nearest-face argmin touches every
-// slot: one shared-memory load per lane per 32 slots.  Face planes are solved
-// in FP64 and stored as FP32 unit normals and distances; the final
-// closest-face solve (depth, barycentric witness points) runs in FP64.
+// slot: one shared-memory load per lane per 32 slots.  Face planes are FP32
+// unit normals and distances whose cross products are compensated (see
+// face_plane); the final closest-face solve (depth, barycentric witness
+// points) runs in FP64.
 //
 // Initial polytope from the GJK simplex: epa_simplex2polytope.hpp:41-376
 // (touching detection, triangle blown up along +-normal, segment search over
@@ -38,6 +39,13 @@
 #ifndef FCLG_EPA_TRACE
 #define FCLG_EPA_TRACE(...) \
   do {                      \
+  } while (0)
+#endif
+// Phase-timing hook (cycle counts per EPA phase when defined by a profiling
+// build; nothing by default).
+#ifndef FCLG_EPA_PHASE
+#define FCLG_EPA_PHASE(k) \
+  do {                    \
   } while (0)
 #endif
 
@@ -73,18 +81,30 @@ struct EpaSmem {
 __device__ __forceinline__ uint32_t fvert(uint32_t packed, int k) { return (packed >> (8 * k)) & 0xFFu; }
 __device__ __forceinline__ f3 ld3(const float4& q) { return mk3(q.x, q.y, q.z); }
 
-// Face plane (outward unit normal, distance from the origin) solved in FP64:
-// differences of the FP32 vertices are exact in FP64, so the normal of a small
-// face far from the origin keeps its direction; an FP32 cross product there
-// errs by ~eps |a| / |edge| radians, enough to misjudge which faces a distant
-// support point sees and fold the polytope.
+// a * b - c * d to within about one rounding of the exact value (Kahan's
+// difference of products with one FMA recovering the rounding of c * d).
+__device__ __forceinline__ float diff_of_products(float a, float b, float c, float d) {
+  const float w = c * d;
+  const float e = fmaf(-c, d, w);
+  const float f = fmaf(a, b, -w);
+  return f + e;
+}
+
+// Face plane (outward unit normal, distance from the origin).  The edge
+// vectors of a face are differences of nearby FP32 vertices, exact or nearly
+// so; a plain FP32 cross product of them still loses the digits that give a
+// thin face its direction (error ~ eps |e1||e2| / |e1 x e2| radians), enough to
+// misjudge which faces a distant support point sees and fold the polytope.
+// Each component is therefore formed as a compensated difference of products,
+// which keeps the normal accurate to a few FP32 roundings.
 __device__ __forceinline__ float4 face_plane(f3 a, f3 b, f3 c) {
-  const d3 A = tod(a);
-  const d3 n = cross(tod(b) - A, tod(c) - A);
-  const double n2 = dot(n, n);
-  if (!(n2 > 0.0)) return make_float4(0.f, 0.f, 0.f, INFINITY);
-  const d3 u = n * (1.0 / sqrt(n2));
-  return make_float4((float)u.x, (float)u.y, (float)u.z, (float)dot(u, A));
+  const f3 u = b - a, v = c - a;
+  const f3 n = mk3(diff_of_products(u.y, v.z, u.z, v.y), diff_of_products(u.z, v.x, u.x, v.z),
+                   diff_of_products(u.x, v.y, u.y, v.x));
+  const float n2 = sqn(n);
+  if (!(n2 > 0.f)) return make_float4(0.f, 0.f, 0.f, INFINITY);
+  const f3 nu = n * rsqrtf(n2);
+  return make_float4(nu.x, nu.y, nu.z, dot(nu, a));
 }
 
 // Whether the origin's projection onto a face's plane lies inside its
@@ -362,6 +382,7 @@ struct EpaWarp {
     }
     __syncwarp();
     // frontier rounds
+    FCLG_EPA_PHASE(3);
     int lo = 0, hi = 1;
     for (int round = 0; round < FMAX && lo < hi; ++round) {
       for (int k = lo + (int)lane; k < hi; k += 32) {
@@ -385,6 +406,7 @@ struct EpaWarp {
       __syncwarp();
     }
     const int n_rem = hi;
+    FCLG_EPA_PHASE(4);
     // horizon edges of the patch, gathered in patch order
     int n_hz = 0;
     for (int base = 0; base < n_rem; base += 32) {
@@ -441,6 +463,7 @@ struct EpaWarp {
       P.start_at[hb[j]] = kNoSlot;
     }
     __syncwarp();
+    FCLG_EPA_PHASE(5);
     // Phase B: write the fan (a, b, new) and re-point the outside neighbours.
     bool err = false;
     j = 0;
@@ -470,6 +493,7 @@ struct EpaWarp {
       P.fadj[u][2] = (uint16_t)t;
     }
     __syncwarp();
+    FCLG_EPA_PHASE(6);
     if (__any_sync(0xFFFFFFFFu, err)) return 2;
     live = new_live;
     fs_top = avail > n_hz ? avail - n_hz : 0;
@@ -530,12 +554,15 @@ struct EpaWarp {
     for (int it = 0;;) {
       int bs;
       float bd;
+      FCLG_EPA_PHASE(0);
       nearest(bs, bd);
+      FCLG_EPA_PHASE(1);
       if (bs == 0x7FFFFFFF || !(bd < INFINITY)) { r.status = kEpaFailed; return r; }
       const f3 n = ld3(P.fn[bs]);
       const uint32_t bfv = P.fv[bs];  // the slot may be reused by the expansion below
       f3 pa, pb;
       sup(n, pa, pb);
+      FCLG_EPA_PHASE(2);
       const float delta = dot(n, pa - pb) - bd;
       FCLG_EPA_TRACE(P, it, bs, bd, delta, live, hw, nv);
       if (delta <= tol) {
