@@ -133,6 +133,19 @@ int fclg_collide(fclg_context* ctx, const fclg_pair* pairs, uint32_t n_pairs, co
 int fclg_collide_device(fclg_context* ctx, const fclg_pair* d_pairs, uint32_t n_pairs, const fclg_request* req,
                         fclg_result* d_results, void* stream);
 
+/* Signed distance on device pointers without any allocation in the call (no
+   counterpart in the reference, whose per-pair solver keeps its polytope on
+   the stack).  Same results as fclg_distance_device; the overlapping pairs
+   handed from the GJK pass to the EPA pass are kept in a fixed device array of
+   the library instead of context buffers, so n_pairs is at most
+   FCLG_STATIC_MAX_PAIRS (larger batches return FCLG_E_TOO_LARGE; split them).
+   The first call on a device sets that array up (an address lookup): make it
+   before any stream capture.  Calls on one device share the array, so calls
+   that overlap in time on that device race; order them on one stream. */
+#define FCLG_STATIC_MAX_PAIRS 16384u
+int fclg_distance_device_static(fclg_context* ctx, const fclg_pair* d_pairs, uint32_t n_pairs,
+                                const fclg_request* req, fclg_result* d_results, void* stream);
+
 /* Launch shape of the query passes.  Pairs are first sorted on the device by
    shape class (box / sphere / capsule / cylinder / convex hull, hulls split at
    large_hull_vertices); pairs without a large hull run the GJK pass with

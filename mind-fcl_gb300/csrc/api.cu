@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -560,3 +561,103 @@ int fclg_pass_times(fclg_context* c, double* gjk_ms, double* epa_ms, uint64_t* q
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Scratch-free signed distance: fclg_distance_device_static.
+//
+// The same GJK + EPA passes as fclg_distance_device (unbucketed launch: every
+// pair with the context's small-pair GJK lane count), but the EPA queue lives
+// in the file-scope device array below instead of context buffers grown with
+// cudaMalloc, so a call allocates nothing.  Layout of the array:
+//   [0, 256)                         counts[2]: EPA work list, overflow list
+//   [256, +4 * kStaticMax)           work list (pair indices)
+//   [.., +4 * kStaticMax)            overflow list (work-list items)
+//   [.., +kEpaRecordBytes * kStaticMax)  final GJK simplex per work-list item
+// counts must be zero before the GJK pass; each call zeroes them with
+// cudaMemsetAsync on its stream (the lists and records are written before
+// they are read and need no clearing).
+//
+// Set-up: the first call on a device (with that device current) looks the
+// array up with cudaGetSymbolAddress and caches the address for the device;
+// later calls only read the cache.  Make the first call before any stream
+// capture.  Every call on a device shares the one array, so calls that
+// overlap in time on that device (other streams, other contexts, other host
+// threads) race on it: order them on one stream, or join them by events.
+// ---------------------------------------------------------------------------
+
+namespace {
+
+constexpr size_t kStaticMax = FCLG_STATIC_MAX_PAIRS;
+constexpr size_t kStaticHeadBytes = 256;
+constexpr size_t kStaticListOffset = kStaticHeadBytes;
+constexpr size_t kStaticOvfOffset = kStaticListOffset + kStaticMax * sizeof(uint32_t);
+constexpr size_t kStaticRecOffset = kStaticOvfOffset + kStaticMax * sizeof(uint32_t);
+constexpr size_t kStaticBytes = kStaticRecOffset + kStaticMax * fclg::kEpaRecordBytes;
+static_assert(kStaticRecOffset % 16 == 0, "simplex records hold float4");
+constexpr int kStaticMaxDevices = 64;
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
+
+namespace {
+
+std::mutex g_static_mutex;
+unsigned char* g_static_base[kStaticMaxDevices] = {};
+
+// Address of g_static_scratch on the current device (c->device), looked up on
+// the first call for that device.
+int static_scratch(fclg_context* c, unsigned char** out) {
+  if (c->device < 0 || c->device >= kStaticMaxDevices) return fail(c, FCLG_E_INVALID, "device ordinal above 63");
+  std::lock_guard<std::mutex> lock(g_static_mutex);
+  if (!g_static_base[c->device]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaGetSymbolAddress(g_static_scratch)");
+    g_static_base[c->device] = static_cast<unsigned char*>(p);
+  }
+  *out = g_static_base[c->device];
+  return FCLG_OK;
+}
+
+}  // namespace
+
+extern "C" int fclg_distance_device_static(fclg_context* c, const fclg_pair* d_pairs, uint32_t n,
+                                           const fclg_request* req, fclg_result* d_results, void* stream) {
+  if (!c) return FCLG_E_INVALID;
+  if (n > kStaticMax) {
+    char b[160];
+    snprintf(b, sizeof b, "fclg_distance_device_static: %u pairs exceed its fixed scratch of %u pairs per call", n,
+             (unsigned)kStaticMax);
+    return fail(c, FCLG_E_TOO_LARGE, b);
+  }
+  if (n == 0) return FCLG_OK;
+  if (!d_pairs || !d_results) return fail(c, FCLG_E_INVALID, "null pair or result pointer");
+  if (!c->shapes) return fail(c, FCLG_E_NO_SHAPES, "no shapes set");
+  FCLG_CUDA(c, cudaSetDevice(c->device));
+  unsigned char* base = nullptr;
+  const int rc = static_scratch(c, &base);
+  if (rc) return rc;
+  const cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const fclg::QueryParams prm = make_params(req, true);
+  fclg::BatchArgs b;
+  b.shapes = c->shapes;
+  b.verts = c->verts;
+  b.pairs = reinterpret_cast<const float4*>(d_pairs);
+  b.guess = nullptr;
+  b.results = reinterpret_cast<float4*>(d_results);
+  b.n_pairs = n;
+  b.n_shapes = c->n_shapes;
+  uint32_t* counts = reinterpret_cast<uint32_t*>(base);
+  fclg::EpaQueue q{counts, reinterpret_cast<uint32_t*>(base + kStaticListOffset),
+                   reinterpret_cast<float4*>(base + kStaticRecOffset)};
+  if (prm.want_epa) FCLG_CUDA(c, cudaMemsetAsync(counts, 0, 2 * sizeof(uint32_t), st));
+  FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes, nullptr, nullptr, 0, st));
+  c->launches += 1;
+  if (prm.want_epa) {
+    fclg::EpaQueue ovf{counts + 1, reinterpret_cast<uint32_t*>(base + kStaticOvfOffset), nullptr};
+    FCLG_CUDA(c, fclg::launch_epa(b, prm, q, ovf, c->num_sms, c->epa_ctas_per_sm, st));
+    c->launches += prm.epa_max_faces > 128 ? 2 : 1;
+  }
+  return FCLG_OK;
+}

@@ -21,11 +21,13 @@ FCLG_REQ_WARM_START = 4
 EXPORTS = [
     "fclg_create", "fclg_destroy", "fclg_last_error", "fclg_version", "fclg_built_arch",
     "fclg_set_shapes", "fclg_set_shapes_device",
-    "fclg_distance", "fclg_distance_device", "fclg_collide", "fclg_collide_device",
+    "fclg_distance", "fclg_distance_device", "fclg_distance_device_static", "fclg_collide", "fclg_collide_device",
     "fclg_set_launch", "fclg_set_tuning", "fclg_get_tuning", "fclg_launch_count", "fclg_set_profiling",
     "fclg_pass_times", "fclg_bvh_build", "fclg_mesh_create", "fclg_mesh_destroy", "fclg_mesh_info", "fclg_mesh_export",
     "fclg_mesh_collide", "fclg_mesh_collide_device",
 ]
+
+STATIC_MAX_PAIRS = 16384  # FCLG_STATIC_MAX_PAIRS
 
 MESH_NODE_DTYPE = np.dtype([("axis", "<f4", (9,)), ("center", "<f4", (3,)), ("extent", "<f4", (3,)),
                             ("child", "<i4")])
@@ -76,7 +78,7 @@ def load_library(path=LIB_PATH):
     for name in ("fclg_distance", "fclg_collide"):
         getattr(lib, name).argtypes = [vp, vp, u32, vp, vp]
         getattr(lib, name).restype = i32
-    for name in ("fclg_distance_device", "fclg_collide_device"):
+    for name in ("fclg_distance_device", "fclg_distance_device_static", "fclg_collide_device"):
         getattr(lib, name).argtypes = [vp, vp, u32, vp, vp, vp]
         getattr(lib, name).restype = i32
     lib.fclg_set_launch.argtypes = [vp, i32, i32]
@@ -193,6 +195,10 @@ class Context:
     def distance_device(self, d_pairs, n, d_results, request=None, stream=0):
         """Asynchronous signed distance on device pointers (ints) on a CUDA stream handle."""
         self._dev_query(self.lib.fclg_distance_device, d_pairs, n, d_results, request, stream)
+
+    def distance_device_static(self, d_pairs, n, d_results, request=None, stream=0):
+        """distance_device without allocation in the call (at most STATIC_MAX_PAIRS pairs)."""
+        self._dev_query(self.lib.fclg_distance_device_static, d_pairs, n, d_results, request, stream)
 
     def collide_device(self, d_pairs, n, d_results, request=None, stream=0):
         self._dev_query(self.lib.fclg_collide_device, d_pairs, n, d_results, request, stream)

@@ -1,0 +1,84 @@
+"""fclg_distance_device_static (signed distance with its EPA scratch in a fixed
+device array, no allocation in the call) against fclg_distance_device.
+
+Tolerance: with the same launch shape (bucketing off, so both run the GJK pass
+with one lane per pair) the two entry points run the same kernels on the same
+pairs, so statuses and collision flags must be identical and distances may
+differ by at most 1e-6 m.  Against the default bucketed launch the bar is the
+convex parity bar's: >= 99.9 % of pairs within 1e-5 m, none beyond 1e-3 m.
+
+This file is collected last so that it also runs after every other GPU test
+has used the device.
+"""
+import numpy as np
+import pytest
+
+from fclg import workloads
+from fclg.layout import RESULT_DTYPE
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(fn, d_pairs, n, torch):
+    d_res = torch.zeros(n * RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    fn(d_pairs.data_ptr(), n, d_res.data_ptr())
+    torch.cuda.synchronize()
+    return d_res.cpu().numpy().view(RESULT_DTYPE).copy()
+
+
+def _assert_same(a, b, tol):
+    assert np.array_equal(a["ok"], b["ok"])
+    assert np.array_equal(a["collide"], b["collide"])
+    assert np.array_equal(a["status"], b["status"])
+    d = np.abs(a["distance"].astype(np.float64) - b["distance"].astype(np.float64))
+    assert d.max() <= tol, "max |distance diff| %.3g" % d.max()
+
+
+def test_static_matches_device_entry_twice():
+    torch = pytest.importorskip("torch")
+    from fclg.api import STATIC_MAX_PAIRS, Context
+    b = workloads.mixed(STATIC_MAX_PAIRS, seed=workloads.SEED_BASE + 41)
+    ctx = Context(0)
+    try:
+        ctx.set_batch(b)
+        d_pairs = torch.from_numpy(b.pairs.view(np.uint8).copy()).cuda()
+        n = b.n_pairs
+        first = _run(ctx.distance_device_static, d_pairs, n, torch)
+        free_before = torch.cuda.mem_get_info()[0]
+        second = _run(ctx.distance_device_static, d_pairs, n, torch)
+        assert torch.cuda.mem_get_info()[0] == free_before
+        # the two calls in a row agree bit for bit
+        assert first.tobytes() == second.tobytes()
+        assert (first["distance"] < 0).mean() > 0.3  # the EPA pass ran on a real share of the batch
+
+        ctx.set_tuning(bucketing=False)
+        same_shape = _run(ctx.distance_device, d_pairs, n, torch)
+        for got in (first, second):
+            _assert_same(got, same_shape, 1e-6)
+
+        ctx.set_tuning(bucketing=True)
+        bucketed = _run(ctx.distance_device, d_pairs, n, torch)
+        assert np.array_equal(first["collide"], bucketed["collide"])
+        err = np.abs(first["distance"].astype(np.float64) - bucketed["distance"].astype(np.float64))
+        assert np.mean(err <= 1e-5) >= 0.999 and err.max() <= 1e-3
+    finally:
+        ctx.close()
+
+
+def test_static_rejects_oversized_batch():
+    torch = pytest.importorskip("torch")
+    from fclg.api import STATIC_MAX_PAIRS, Context, FclgError
+    b = workloads.mixed(STATIC_MAX_PAIRS + 1, seed=workloads.SEED_BASE + 42)
+    ctx = Context(0)
+    try:
+        ctx.set_batch(b)
+        d_pairs = torch.from_numpy(b.pairs.view(np.uint8).copy()).cuda()
+        d_res = torch.zeros(b.n_pairs * RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+        with pytest.raises(FclgError, match="exceed"):
+            ctx.distance_device_static(d_pairs.data_ptr(), b.n_pairs, d_res.data_ptr())
+        torch.cuda.synchronize()
+        assert int(d_res.count_nonzero()) == 0
+        # an empty batch is a no-op
+        ctx.distance_device_static(d_pairs.data_ptr(), 0, d_res.data_ptr())
+    finally:
+        ctx.close()
