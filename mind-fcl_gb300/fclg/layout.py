@@ -19,7 +19,7 @@ SHAPE_DTYPE = np.dtype(
 )
 PAIR_DTYPE = np.dtype(
     [("shape_a", "<u4"), ("shape_b", "<u4"), ("rot", "<f4", (9,)), ("trans", "<f4", (3,)),
-     ("flags", "<u4"), ("reserved", "<u4")],
+     ("flags", "<u4"), ("pair_class", "<u4")],
     align=False,
 )
 # fclg_result: what the GPU writes per pair (48 bytes).

@@ -15,6 +15,14 @@ Workloads (sizes as the project's benchmark configurations state them):
   about 40 % of the pairs overlap.
 * ``pareto``        convex pairs with V ~ Pareto(alpha = 1.5, x_m = 4) clipped
   to [4, 1024]; about 30 % overlap.
+* ``arm``           a 7-link serial arm (each link the hull of 64..256 points on
+  an ellipsoid around the link) against 32 obstacle hulls of 64 points, every
+  link-obstacle pair of each random joint configuration (224 pairs per
+  configuration).
+
+Every pair carries a shape-pair class for the warm-start model's embedding:
+the type pair (5 x 5 classes) for ``mixed``, the pair of log2 vertex-count
+buckets (9 x 9) for ``pareto``, link x 32 + obstacle (224) for ``arm``.
 
 Overlap control: the translation of shape b is a uniform direction times
 g * (rho_a + rho_b), rho the bounding-sphere radius and g ~ U[0, g_max]; g_max
@@ -28,6 +36,10 @@ import numpy as np
 from .layout import BOX, CAPSULE, CONVEX, CYLINDER, PAIR_DTYPE, SHAPE_DTYPE, SPHERE
 
 SEED_BASE = 20240611
+MIXED_CLASSES = 25
+PARETO_CLASSES = 81
+ARM_LINKS, ARM_OBSTACLES = 7, 32
+ARM_CLASSES = ARM_LINKS * ARM_OBSTACLES
 MIXED_G_MAX = 1.92   # calibrated: 40 % overlap on the mixed workload
 PARETO_G_MAX = 1.66  # calibrated: 30 % overlap on the pareto workload
 
@@ -185,6 +197,9 @@ def mixed(n_pairs=1_000_000, seed=SEED_BASE + 1, g_max=MIXED_G_MAX):
     types = choice[np.minimum((rng.random(2 * n_pairs) * 5).astype(np.int64), 4)]
     s, v, rho = _make_shapes(rng, types, 0.02, 0.4, lambda k: log_uniform_counts(rng, k, 8, 256))
     p = _pairs(rng, n_pairs, rho, g_max)
+    cls = np.zeros(CONVEX + 1, np.uint32)
+    cls[[BOX, SPHERE, CAPSULE, CYLINDER, CONVEX]] = np.arange(5)
+    p["pair_class"] = 5 * cls[s["type"][p["shape_a"]]] + cls[s["type"][p["shape_b"]]]
     return Batch("mixed", s, v, p, {"seed": seed, "g_max": g_max})
 
 
@@ -193,7 +208,89 @@ def pareto(n_pairs=4_000_000, seed=SEED_BASE + 4, g_max=PARETO_G_MAX):
     types = np.full(2 * n_pairs, CONVEX, np.int32)
     s, v, rho = _make_shapes(rng, types, 0.02, 0.4, lambda k: pareto_counts(rng, k))
     p = _pairs(rng, n_pairs, rho, g_max)
+    bucket = np.clip(np.floor(np.log2(np.maximum(s["vert_count"], 1))).astype(np.int64) - 2, 0, 8)
+    p["pair_class"] = 9 * bucket[p["shape_a"]] + bucket[p["shape_b"]]
     return Batch("pareto", s, v, p, {"seed": seed, "g_max": g_max})
+
+
+def _rot(axis, ang):
+    """Batched rotation matrices [n, 3, 3] about a coordinate axis."""
+    c, s_ = np.cos(ang), np.sin(ang)
+    R = np.zeros((len(ang), 3, 3))
+    i, j = {"x": (1, 2), "z": (0, 1)}[axis]
+    k = 3 - i - j
+    R[:, k, k] = 1.0
+    R[:, i, i] = c
+    R[:, j, j] = c
+    R[:, i, j] = -s_
+    R[:, j, i] = s_
+    return R
+
+
+def arm(n_configs=100_000, seed=SEED_BASE + 3, chunk=8192):
+    """7-link arm against 32 obstacles: every link-obstacle pair of n_configs
+    random joint configurations (pair index (config * 7 + link) * 32 + obstacle;
+    shape a the link, shape b the obstacle, posed in the link's frame)."""
+    rng = _rng(seed)
+    L, O = ARM_LINKS, ARM_OBSTACLES
+    length = 0.20 + 0.15 * rng.random(L)        # joint-to-joint distance along the link's x axis
+    radius = 0.04 + 0.03 * rng.random(L)
+    link_nv = (64 + np.floor(rng.random(L) * 193)).astype(np.int64)  # 64..256
+    d_off = 0.10 * rng.random(L)                # DH offsets along z
+    twist = np.where(np.arange(L) % 2 == 0, np.pi / 2, -np.pi / 2)
+    obs_r = 0.06 + 0.12 * rng.random(O)
+    obs_dir = unit_vectors(rng, O)
+    obs_dist = 0.3 + 0.6 * rng.random(O)
+    obs_pos = obs_dir * obs_dist[:, None] + np.array([0.0, 0.0, 0.3])
+    obs_rot = random_rotations(rng, O).reshape(O, 3, 3)
+    # shapes: links are hulls of points on an ellipsoid spanning the link, obstacles of points on a sphere
+    counts = np.concatenate([link_nv, np.full(O, 64, np.int64)])
+    s = np.zeros(L + O, SHAPE_DTYPE)
+    s["type"] = CONVEX
+    s["vert_count"] = counts
+    s["vert_offset"] = np.concatenate([[0], np.cumsum(counts)[:-1]])
+    verts = np.zeros((int(counts.sum()), 4), np.float32)
+    u = unit_vectors(rng, int(counts.sum()))
+    for i in range(L + O):
+        a, c = int(s["vert_offset"][i]), int(counts[i])
+        if i < L:
+            semi = np.array([0.5 * length[i] + 0.5 * radius[i], radius[i], radius[i]])
+            pts = u[a:a + c] * semi + np.array([0.5 * length[i], 0.0, 0.0])
+        else:
+            pts = u[a:a + c] * obs_r[i - L]
+        verts[a:a + c, :3] = pts
+        s["param"][i, :3] = pts.mean(axis=0)
+        s["param"][i, 3] = np.linalg.norm(pts, axis=1).max()
+    # joint configurations and link frames
+    q = (rng.random((n_configs, L)) * 2.0 - 1.0) * np.pi
+    pairs = np.zeros(n_configs * L * O, PAIR_DTYPE)
+    obs_R = obs_rot[None]                                       # [1, O, 3, 3]
+    for c0 in range(0, n_configs, chunk):
+        qc = q[c0:c0 + chunk]
+        m = len(qc)
+        R = np.broadcast_to(np.eye(3), (m, 3, 3)).copy()
+        t = np.zeros((m, 3))
+        link_R = np.empty((m, L, 3, 3))
+        link_t = np.empty((m, L, 3))
+        for j in range(L):
+            R = R @ _rot("z", qc[:, j])
+            t = t + R[:, :, 2] * d_off[j]
+            link_R[:, j] = R
+            link_t[:, j] = t
+            t = t + R[:, :, 0] * length[j]
+            R = R @ _rot("x", np.full(m, twist[j]))
+        RT = np.swapaxes(link_R, -1, -2)                        # [m, L, 3, 3]
+        rel_R = np.einsum("mlij,ojk->mloik", RT, obs_R[0])       # [m, L, O, 3, 3]
+        rel_t = np.einsum("mlij,mloj->mloi", RT, obs_pos[None, None] - link_t[:, :, None, :])
+        blk = pairs[c0 * L * O:(c0 + m) * L * O]
+        blk["shape_a"] = np.broadcast_to(np.arange(L)[None, :, None], (m, L, O)).ravel()
+        blk["shape_b"] = np.broadcast_to(L + np.arange(O)[None, None, :], (m, L, O)).ravel()
+        blk["rot"] = rel_R.reshape(-1, 9)
+        blk["trans"] = rel_t.reshape(-1, 3)
+        blk["pair_class"] = np.broadcast_to(np.arange(L)[None, :, None] * O + np.arange(O)[None, None, :],
+                                            (m, L, O)).ravel()
+    return Batch("arm", s, verts, pairs, {"seed": seed, "configs": n_configs, "links": L, "obstacles": O,
+                                          "link_vertices": link_nv.tolist()})
 
 
 # ------------------------------------------------------------------ meshes --

@@ -1,0 +1,164 @@
+"""Learned GJK warm start on the GPU (fclg_warmstart_*).
+
+* Forward: the fused inference kernel and the training kernels against the
+  CPU oracle (oracle/mlp.py, BF16 rounding points): per pair
+  |y - y_oracle| <= 2e-2 (|y_oracle| + 1e-2), median relative error <= 2e-3.
+  The two sides round the same FP32 pre-activations to BF16 but sum in a
+  different order, so a pre-activation within ~1e-6 of a rounding boundary
+  may round the other way; the bound covers those.
+* Gradient: the GPU backward pass against the oracle's on the same batch:
+  per parameter block ||g - g_oracle|| <= 2e-2 ||g_oracle||, loss within 1e-4.
+* Training and the gain: a model trained on the GPU on plain-GJK directions
+  of held-out arm configurations lowers the mean GJK iteration count of
+  unseen configurations by >= 25 % against plain initialisation.
+* Answers: warm-started GPU results against the FP64 oracle started from the
+  same directions meet the convex parity bar (flags exact outside the 1e-6 m
+  band, separation within 1e-5 m for >= 99.5 % of pairs and 1e-3 m for all).
+  Against plain initialisation: collision flags identical outside the band,
+  overlapping pairs bit-identical (they rerun from the plain direction),
+  separation within 1e-5 m for >= 99.5 % of pairs and within 5e-3 m for all.
+  The last bound is the reference algorithm's own dependence on the start
+  direction: its distance loop stops when one iteration improves the bound
+  by less than the tolerance (gjk_distance.hpp:78-90), which on curved or
+  near-parallel features can happen up to ~2e-3 m from the optimum, for
+  either start (measured on 10^6 mixed pairs: max 1.9e-3 m, neither start
+  closer to a tight solve more often).
+"""
+import numpy as np
+import pytest
+
+from fclg import workloads
+from fclg.layout import RESULT_DTYPE
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    return pytest.importorskip("torch")
+
+
+def _dev(torch, arr):
+    return torch.from_numpy(np.ascontiguousarray(arr).view(np.uint8).copy()).cuda()
+
+
+def test_forward_matches_oracle(torch):
+    from fclg.api import WarmStart
+    from oracle import mlp
+    b = workloads.arm(8, seed=workloads.SEED_BASE + 301)  # 1792 pairs
+    n = b.n_pairs
+    ws = WarmStart(workloads.ARM_CLASSES, seed=5)
+    params = ws.get_params()
+    d_pairs = _dev(torch, b.pairs)
+    ref, _ = mlp.forward(params, b.pairs, workloads.ARM_CLASSES, on=True)
+    for fused in (True, False):
+        d_y = torch.zeros(n * 3, dtype=torch.float32, device="cuda")
+        if fused:
+            ws.predict(d_pairs.data_ptr(), n, d_y.data_ptr(), normalize=False)
+        else:
+            ws.forward(d_pairs.data_ptr(), n, d_y.data_ptr())
+        torch.cuda.synchronize()
+        y = d_y.cpu().numpy().reshape(n, 3)
+        scale = np.linalg.norm(ref, axis=1) + 1e-2
+        rel = np.linalg.norm(y - ref, axis=1) / scale
+        assert rel.max() <= 2e-2 and np.median(rel) <= 2e-3, (fused, rel.max(), np.median(rel))
+    # normalised output is the unit direction of the raw one
+    d_u = torch.zeros(n * 3, dtype=torch.float32, device="cuda")
+    ws.predict(d_pairs.data_ptr(), n, d_u.data_ptr(), normalize=True)
+    torch.cuda.synchronize()
+    u = d_u.cpu().numpy().reshape(n, 3)
+    assert np.allclose(np.linalg.norm(u, axis=1), 1.0, atol=1e-5)
+    ws.close()
+
+
+def test_gradient_matches_oracle(torch):
+    from fclg.api import WarmStart
+    from oracle import mlp
+    b = workloads.arm(3, seed=workloads.SEED_BASE + 302)  # 672 pairs: ten 64-row tiles plus a ragged one
+    n = b.n_pairs
+    rng = np.random.default_rng(7)
+    u = rng.normal(size=(n, 3))
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    ws = WarmStart(workloads.ARM_CLASSES, seed=6)
+    params = ws.get_params()
+    d_pairs = _dev(torch, b.pairs)
+    d_lab = torch.from_numpy(u.astype(np.float32)).cuda()
+    loss, g = ws.gradient(d_pairs.data_ptr(), d_lab.data_ptr(), n)
+    ref_loss, ref_g = mlp.gradient(params, b.pairs, u, workloads.ARM_CLASSES, on=True)
+    assert abs(loss - ref_loss) <= 1e-4
+    o = mlp.offsets(workloads.ARM_CLASSES)
+    for name in ("W1", "b1", "W2", "b2", "W3", "b3", "W4", "b4", "E"):
+        s, k = o[name]
+        a, r = g[s:s + k].astype(np.float64), ref_g[s:s + k]
+        assert np.linalg.norm(a - r) <= 2e-2 * np.linalg.norm(r) + 1e-9, name
+    ws.close()
+
+
+def _query(torch, ctx, d_pairs, n, flags):
+    from fclg.api import make_request
+    d_res = torch.zeros(n * RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    ctx.distance_device(d_pairs.data_ptr(), n, d_res.data_ptr(), make_request(flags=flags))
+    torch.cuda.synchronize()
+    return d_res.cpu().numpy().view(RESULT_DTYPE).copy()
+
+
+def test_trained_model_cuts_iterations_and_keeps_answers(torch):
+    from fclg.api import Context, FclgError, WarmStart, direction_labels
+    WARM = 4  # FCLG_REQ_WARM_START
+    ctx = Context(0)
+    try:
+        # training set: plain-GJK directions of held-out configurations
+        train = workloads.arm(1200, seed=workloads.SEED_BASE + 303)  # 268,800 pairs
+        ctx.set_batch(train)
+        d_tr = _dev(torch, train.pairs)
+        res = _query(torch, ctx, d_tr, train.n_pairs, 0)
+        lab, ok = direction_labels(res)
+        keep = np.nonzero(ok)[0]
+        d_tr = _dev(torch, train.pairs[keep])
+        d_lab = torch.from_numpy(lab[keep]).cuda()
+        ws = WarmStart(workloads.ARM_CLASSES, seed=1)
+        losses = ws.train(d_tr.data_ptr(), d_lab.data_ptr(), len(keep), epochs=6, batch=4096, lr=2e-3)
+        assert losses[-1] < 0.5 * losses[0], losses
+
+        # unseen configurations
+        test = workloads.arm(400, seed=workloads.SEED_BASE + 304)
+        ctx.set_batch(test)
+        d_te = _dev(torch, test.pairs)
+        with pytest.raises(FclgError):
+            _query(torch, ctx, d_te, test.n_pairs, WARM)  # no model set
+        ctx.set_warmstart(ws)
+        plain = _query(torch, ctx, d_te, test.n_pairs, 0)
+        warm = _query(torch, ctx, d_te, test.n_pairs, WARM)
+
+        assert np.array_equal(plain["ok"], warm["ok"])
+        dp, dw = plain["distance"].astype(np.float64), warm["distance"].astype(np.float64)
+        outside = np.abs(dp) > 1e-6
+        assert np.array_equal((dp < 0)[outside], (dw < 0)[outside])
+        ov = dp < 0
+        # overlapping pairs rerun from the plain direction: same EPA answer
+        assert np.array_equal(dp[ov], dw[ov])
+        sep = ~ov & (plain["ok"] == 1)
+        err = np.abs(dp - dw)[sep]
+        assert np.mean(err <= 1e-5) >= 0.995 and err.max() <= 5e-3
+        # the warm answers are the reference algorithm's answers from the same start
+        import oracle
+        d_g = torch.zeros(test.n_pairs * 3, dtype=torch.float32, device="cuda")
+        ws.predict(d_te.data_ptr(), test.n_pairs, d_g.data_ptr())
+        torch.cuda.synchronize()
+        guess = d_g.cpu().numpy().reshape(-1, 3)
+        sub = np.arange(0, test.n_pairs, 4)
+        ref = oracle.signed_distance(test.subset(sub), guess=guess[sub])
+        both = (ref["ok"] == 1) & (warm["ok"][sub] == 1)
+        assert both.mean() >= 0.999
+        rd, gd = ref["distance"], warm["distance"][sub].astype(np.float64)
+        out = np.abs(rd) > 1e-6
+        assert np.array_equal((rd < 0)[out & both], (gd < 0)[out & both])
+        e = np.abs(rd - gd)[both & (rd > 0)]
+        assert np.mean(e <= 1e-5) >= 0.995 and e.max() <= 1e-3
+        it_p = plain["iterations"][sep].astype(np.float64).mean()
+        it_w = warm["iterations"][sep].astype(np.float64).mean()
+        assert it_w <= 0.75 * it_p, (it_p, it_w)
+        ctx.set_warmstart(None)
+        ws.close()
+    finally:
+        ctx.close()
