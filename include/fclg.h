@@ -176,10 +176,16 @@ const char* fclg_warmstart_last_error(const fclg_warmstart* model);
 uint64_t fclg_warmstart_param_count(const fclg_warmstart* model);
 int fclg_warmstart_get_params(const fclg_warmstart* model, float* params, uint64_t n_params);
 int fclg_warmstart_set_params(fclg_warmstart* model, const float* params, uint64_t n_params);
-/* Inference (the fused kernel the queries use): d_out float[n][3], the unit
-   direction (normalize != 0) or the raw output y. */
+/* Inference: d_out float[n][3], the unit direction (FCLG_WS_NORMALIZE) or the
+   raw output y.  The queries use the tcgen05 kernel (TMEM accumulators,
+   weights streamed by bulk async copies); FCLG_WS_MMA_SYNC selects the
+   mma.sync kernel instead (the same model, for comparison). */
+enum { FCLG_WS_NORMALIZE = 1u << 0, FCLG_WS_MMA_SYNC = 1u << 1 };
 int fclg_warmstart_predict(fclg_warmstart* model, const fclg_pair* d_pairs, uint32_t n_pairs, float* d_out,
-                           int normalize, void* stream);
+                           uint32_t flags, void* stream);
+/* Synchronises the device; FCLG_E_CUDA if an inference launch since the last
+   call gave up one of its bounded waits (the directions it owed are unset). */
+int fclg_warmstart_status(fclg_warmstart* model);
 /* The raw output y (float[n][3]) through the training kernels. */
 int fclg_warmstart_forward(fclg_warmstart* model, const fclg_pair* d_pairs, uint32_t n_pairs, float* d_y,
                            void* stream);

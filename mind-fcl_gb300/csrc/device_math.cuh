@@ -38,6 +38,32 @@ __device__ __forceinline__ d3 cross(d3 a, d3 b) {
   return d3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
 
+// Barycentric weights (u, v, w) of the point of triangle (a, b, c) nearest the
+// origin (Ericson, Real-Time Collision Detection, 5.1.5), in FP64.
+__device__ __forceinline__ void closest_bary_origin(d3 a, d3 b, d3 c, double& u, double& v, double& w) {
+  const d3 ab = b - a, ac = c - a;
+  const d3 ap = a * -1.0, bp = b * -1.0, cp = c * -1.0;
+  const double d1 = dot(ab, ap), d2 = dot(ac, ap);
+  const double d3v = dot(ab, bp), d4 = dot(ac, bp);
+  const double d5 = dot(ab, cp), d6 = dot(ac, cp);
+  const double vc = d1 * d4 - d3v * d2, vb = d5 * d2 - d1 * d6, va = d3v * d6 - d5 * d4;
+  if (d1 <= 0.0 && d2 <= 0.0) { u = 1; v = 0; w = 0; }
+  else if (d3v >= 0.0 && d4 <= d3v) { u = 0; v = 1; w = 0; }
+  else if (vc <= 0.0 && d1 >= 0.0 && d3v <= 0.0) { v = d1 / (d1 - d3v); u = 1 - v; w = 0; }
+  else if (d6 >= 0.0 && d5 <= d6) { u = 0; v = 0; w = 1; }
+  else if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) { w = d2 / (d2 - d6); u = 1 - w; v = 0; }
+  else if (va <= 0.0 && (d4 - d3v) >= 0.0 && (d5 - d6) >= 0.0) {
+    w = (d4 - d3v) / ((d4 - d3v) + (d5 - d6));
+    u = 0;
+    v = 1 - w;
+  } else {
+    const double inv = 1.0 / (va + vb + vc);
+    v = vb * inv;
+    w = vc * inv;
+    u = 1.0 - v - w;
+  }
+}
+
 // Shape types: the reference's GJKShapeType values (gjk_shape.h:9-28).
 enum : int32_t { kBox = 0, kSphere = 1, kCapsule = 3, kCylinder = 5, kConvex = 100 };
 

@@ -239,26 +239,7 @@ struct EpaWarp {
       return;
     }
     double u, v, w;
-    const d3 ap = a * -1.0, bp = b * -1.0, cp = c * -1.0;
-    const double d1 = dot(ab, ap), d2 = dot(ac, ap);
-    const double d3v = dot(ab, bp), d4 = dot(ac, bp);
-    const double d5 = dot(ab, cp), d6 = dot(ac, cp);
-    const double vc = d1 * d4 - d3v * d2, vb = d5 * d2 - d1 * d6, va = d3v * d6 - d5 * d4;
-    if (d1 <= 0.0 && d2 <= 0.0) { u = 1; v = 0; w = 0; }
-    else if (d3v >= 0.0 && d4 <= d3v) { u = 0; v = 1; w = 0; }
-    else if (vc <= 0.0 && d1 >= 0.0 && d3v <= 0.0) { v = d1 / (d1 - d3v); u = 1 - v; w = 0; }
-    else if (d6 >= 0.0 && d5 <= d6) { u = 0; v = 0; w = 1; }
-    else if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) { w = d2 / (d2 - d6); u = 1 - w; v = 0; }
-    else if (va <= 0.0 && (d4 - d3v) >= 0.0 && (d5 - d6) >= 0.0) {
-      w = (d4 - d3v) / ((d4 - d3v) + (d5 - d6));
-      u = 0;
-      v = 1 - w;
-    } else {
-      const double inv = 1.0 / (va + vb + vc);
-      v = vb * inv;
-      w = vc * inv;
-      u = 1.0 - v - w;
-    }
+    closest_bary_origin(a, b, c, u, v, w);
     const d3 q = (a * u + b * v) + c * w;
     const d3 pa0 = tod(ld3(P.vpa[ia])), pa1 = tod(ld3(P.vpa[ib])), pa2 = tod(ld3(P.vpa[ic]));
     const d3 pb0 = pa0 - a, pb1 = pa1 - b, pb2 = pa2 - c;

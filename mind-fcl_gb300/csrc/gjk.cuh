@@ -282,18 +282,52 @@ __device__ FCLG_GJK_COLD bool extract_no_sub(const Simplex& s, f3& p0, f3& p1) {
     p1 = s.b[0] * w1 + s.b[1] * w2;
     return true;
   }
-  const f3 s1_to_s2 = s.w[1] - s.w[0], s1_to_s3 = s.w[2] - s.w[0];
-  const f3 n = cross(s1_to_s2, s1_to_s3);
-  const float area2 = sqn(n);
-  if (area2 <= 0.f) return false;
-  const f3 proj = n * (dot(s.w[0], n) / area2);
-  const float area = sqrtf(area2);
-  const float w2 = nrm(cross(s1_to_s3, s.w[0] - proj)) / area;
-  const float w3 = nrm(cross(s1_to_s2, s.w[0] - proj)) / area;
-  const float w1 = 1.f - w2 - w3;
-  if (w1 < -kBaryTol || w2 < -kBaryTol || w3 < -kBaryTol) return false;
-  p0 = (s.a[0] * w1 + s.a[1] * w2) + s.a[2] * w3;
-  p1 = (s.b[0] * w1 + s.b[1] * w2) + s.b[2] * w3;
+  // Triangle.  FP32 when the triangle is well shaped (sin^2 of its angle at
+  // vertex 0 >= 1e-4) and the origin projects inside it; otherwise the
+  // barycentric solve reruns in FP64 on the FP32 support points: on a sliver
+  // (near-collinear support points, common on curved surfaces) FP32 area
+  // ratios lose every digit and the witness points can land centimetres
+  // from the simplex's closest point.
+  {
+    const f3 s1_to_s2 = s.w[1] - s.w[0], s1_to_s3 = s.w[2] - s.w[0];
+    const f3 n = cross(s1_to_s2, s1_to_s3);
+    const float area2 = sqn(n);
+    if (area2 > 1e-4f * sqn(s1_to_s2) * sqn(s1_to_s3)) {
+      const f3 proj = n * (dot(s.w[0], n) / area2);
+      const float area = sqrtf(area2);
+      const float w2 = nrm(cross(s1_to_s3, s.w[0] - proj)) / area;
+      const float w3 = nrm(cross(s1_to_s2, s.w[0] - proj)) / area;
+      const float w1 = 1.f - w2 - w3;
+      if (w1 >= -kBaryTol && w2 >= -kBaryTol && w3 >= -kBaryTol) {
+        p0 = (s.a[0] * w1 + s.a[1] * w2) + s.a[2] * w3;
+        p1 = (s.b[0] * w1 + s.b[1] * w2) + s.b[2] * w3;
+        return true;
+      }
+    }
+  }
+  const auto tof = [](d3 v) { return mk3((float)v.x, (float)v.y, (float)v.z); };
+  const d3 a0 = tod(s.a[0]), a1 = tod(s.a[1]), a2 = tod(s.a[2]);
+  const d3 b0 = tod(s.b[0]), b1 = tod(s.b[1]), b2 = tod(s.b[2]);
+  const d3 w0 = a0 - b0, w1v = a1 - b1, w2v = a2 - b2;
+  const d3 s1_to_s2 = w1v - w0, s1_to_s3 = w2v - w0;
+  const d3 n = cross(s1_to_s2, s1_to_s3);
+  const double area2 = dot(n, n);
+  if (area2 <= 0.0) return false;
+  const d3 proj = n * (dot(w0, n) / area2);
+  const double area = sqrt(area2);
+  const d3 c2 = cross(s1_to_s3, w0 - proj), c3 = cross(s1_to_s2, w0 - proj);
+  double u2 = sqrt(dot(c2, c2)) / area;
+  double u3 = sqrt(dot(c3, c3)) / area;
+  double u1 = 1.0 - u2 - u3;
+  if (u1 < -(double)kBaryTol || u2 < -(double)kBaryTol || u3 < -(double)kBaryTol) {
+    // The FP32 iterates converged on this triangle, but its exact closest
+    // point lies on an edge or vertex (a sliver's weights move by more than
+    // the tolerance under FP32 rounding of the support points): take that
+    // point, where the reference would report no witness.
+    closest_bary_origin(w0, w1v, w2v, u1, u2, u3);
+  }
+  p0 = tof((a0 * u1 + a1 * u2) + a2 * u3);
+  p1 = tof((b0 * u1 + b1 * u2) + b2 * u3);
   return true;
 }
 

@@ -109,6 +109,14 @@ __device__ __forceinline__ float feature(const float* q, const bf16* e, int c) {
   return 0.f;
 }
 
+}  // namespace wsm
+}  // namespace fclg
+
+#include "warmstart_tc.cuh"
+
+namespace fclg {
+namespace wsm {
+
 // ---------------------------------------------------------------- training --
 
 // X0[m][0..31] for the pairs order[m] (or m), m < M (rows past n are zero).
@@ -311,8 +319,8 @@ __global__ void colsum_kernel(const bf16* __restrict__ D, int M, int N, float* _
 }
 
 __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ mom,
-                            float* __restrict__ vel, bf16* __restrict__ pb, size_t n, float lr, float b1, float b2,
-                            float c1, float c2, float eps) {
+                            float* __restrict__ vel, bf16* __restrict__ pb, bf16* __restrict__ pt, size_t n, float lr,
+                            float b1, float b2, float c1, float c2, float eps) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const float gi = g[i];
     const float m = b1 * mom[i] + (1.f - b1) * gi;
@@ -323,13 +331,18 @@ __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, 
     p[i] = x;
     const long long q = bf16_slot(i);
     if (q >= 0) pb[q] = __float2bfloat16(x);
+    const long long t = tc_slot(i);
+    if (t >= 0) pt[t] = __float2bfloat16(x);
   }
 }
 
-__global__ void to_bf16_kernel(const float* __restrict__ p, bf16* __restrict__ pb, size_t n) {
+// BF16 copies of the weights: row-major (pb) and tensor-core operand layout (pt).
+__global__ void to_bf16_kernel(const float* __restrict__ p, bf16* __restrict__ pb, bf16* __restrict__ pt, size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     const long long q = bf16_slot(i);
     if (q >= 0) pb[q] = __float2bfloat16(p[i]);
+    const long long t = tc_slot(i);
+    if (t >= 0) pt[t] = __float2bfloat16(p[i]);
   }
 }
 
@@ -514,7 +527,9 @@ struct fclg_warmstart {
   size_t n_params = 0;
   std::string err;
   float* params = nullptr;  // FP32 master
-  bf16* wb = nullptr;       // BF16 weights + embedding
+  bf16* wb = nullptr;       // BF16 weights (row-major) + embedding
+  bf16* wt = nullptr;       // BF16 weights in the tensor-core operand layout
+  int* abort_flag = nullptr;  // set by an inference CTA whose bounded wait ran out
   float* grad = nullptr;
   float* mom = nullptr;
   float* vel = nullptr;
@@ -657,12 +672,26 @@ int load_features(fclg_warmstart* w, const float4* pairs, const uint32_t* order,
 
 namespace fclg {
 
-cudaError_t warmstart_predict(fclg_warmstart* w, const float4* pairs, uint32_t n, float* guess, cudaStream_t st) {
+namespace {
+
+cudaError_t launch_infer(fclg_warmstart* w, const float4* pairs, uint32_t n, float* out, int normalize, bool legacy,
+                         cudaStream_t st) {
   if (n == 0) return cudaSuccess;
   const uint32_t tiles = (n + kTile - 1) / kTile;
   const uint32_t blocks = std::min<uint32_t>(tiles, (uint32_t)w->num_sms);
-  infer_kernel<<<blocks, kInferWarps * 32, kInferSmem, st>>>(pairs, n, w->wb, w->params, w->n_classes, guess, 1);
+  if (legacy)
+    infer_kernel<<<blocks, kInferWarps * 32, kInferSmem, st>>>(pairs, n, w->wb, w->params, w->n_classes, out,
+                                                               normalize);
+  else
+    infer_tc_kernel<<<blocks, kTcThreads, kTcSmem, st>>>(pairs, n, w->wt, w->wb, w->params, w->n_classes, out,
+                                                         normalize, w->abort_flag);
   return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t warmstart_predict(fclg_warmstart* w, const float4* pairs, uint32_t n, float* guess, cudaStream_t st) {
+  return launch_infer(w, pairs, n, guess, 1, false, st);
 }
 
 int warmstart_device(const fclg_warmstart* w) { return w->device; }
@@ -708,7 +737,11 @@ int fclg_warmstart_create(int device, uint32_t n_classes, uint32_t seed, fclg_wa
   if (cudaSetDevice(device) != cudaSuccess || cudaMalloc(&w->params, w->n_params * 4) != cudaSuccess ||
       cudaMalloc(&w->wb, nb * sizeof(bf16)) != cudaSuccess || cudaMalloc(&w->grad, w->n_params * 4) != cudaSuccess ||
       cudaMalloc(&w->mom, w->n_params * 4) != cudaSuccess || cudaMalloc(&w->vel, w->n_params * 4) != cudaSuccess ||
+      cudaMalloc(&w->wt, tTotal * sizeof(bf16)) != cudaSuccess || cudaMalloc(&w->abort_flag, sizeof(int)) != cudaSuccess ||
+      cudaMemset(w->abort_flag, 0, sizeof(int)) != cudaSuccess ||
       cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem) !=
           cudaSuccess) {
     fclg_warmstart_destroy(w);
     return FCLG_E_CUDA;
@@ -725,7 +758,7 @@ void fclg_warmstart_destroy(fclg_warmstart* w) {
   if (!w) return;
   cudaSetDevice(w->device);
   free_train(w);
-  void* bufs[] = {w->params, w->wb, w->grad, w->mom, w->vel};
+  void* bufs[] = {w->params, w->wb, w->wt, w->abort_flag, w->grad, w->mom, w->vel};
   for (void* p : bufs)
     if (p) cudaFree(p);
   delete w;
@@ -750,7 +783,8 @@ int fclg_warmstart_set_params(fclg_warmstart* w, const float* params, uint64_t n
   WS_CUDA(w, cudaSetDevice(w->device));
   WS_CUDA(w, cudaMemcpy(w->params, params, n * 4, cudaMemcpyHostToDevice));
   WS_CUDA(w, cudaMemset(w->wb, 0, (qE + (size_t)kEmb * w->n_classes) * sizeof(bf16)));
-  to_bf16_kernel<<<256, 256>>>(w->params, w->wb, w->n_params);
+  WS_CUDA(w, cudaMemset(w->wt, 0, tTotal * sizeof(bf16)));
+  to_bf16_kernel<<<256, 256>>>(w->params, w->wb, w->wt, w->n_params);
   WS_CUDA(w, cudaGetLastError());
   WS_CUDA(w, cudaMemset(w->mom, 0, n * 4));
   WS_CUDA(w, cudaMemset(w->vel, 0, n * 4));
@@ -759,17 +793,28 @@ int fclg_warmstart_set_params(fclg_warmstart* w, const float* params, uint64_t n
   return FCLG_OK;
 }
 
-int fclg_warmstart_predict(fclg_warmstart* w, const fclg_pair* d_pairs, uint32_t n, float* d_out, int normalize,
+int fclg_warmstart_predict(fclg_warmstart* w, const fclg_pair* d_pairs, uint32_t n, float* d_out, uint32_t flags,
                            void* stream) {
   if (!w) return FCLG_E_INVALID;
   if (n == 0) return FCLG_OK;
   if (!d_pairs || !d_out) return ws_fail(w, FCLG_E_INVALID, "null pair or output pointer");
   WS_CUDA(w, cudaSetDevice(w->device));
-  const uint32_t tiles = (n + kTile - 1) / kTile;
-  const uint32_t blocks = std::min<uint32_t>(tiles, (uint32_t)w->num_sms);
-  infer_kernel<<<blocks, kInferWarps * 32, kInferSmem, static_cast<cudaStream_t>(stream)>>>(
-      reinterpret_cast<const float4*>(d_pairs), n, w->wb, w->params, w->n_classes, d_out, normalize ? 1 : 0);
-  WS_CUDA(w, cudaGetLastError());
+  WS_CUDA(w, fclg::launch_infer(w, reinterpret_cast<const float4*>(d_pairs), n, d_out,
+                          (flags & FCLG_WS_NORMALIZE) ? 1 : 0, (flags & FCLG_WS_MMA_SYNC) != 0,
+                          static_cast<cudaStream_t>(stream)));
+  return FCLG_OK;
+}
+
+int fclg_warmstart_status(fclg_warmstart* w) {
+  if (!w) return FCLG_E_INVALID;
+  WS_CUDA(w, cudaSetDevice(w->device));
+  WS_CUDA(w, cudaDeviceSynchronize());
+  int e = 0;
+  WS_CUDA(w, cudaMemcpy(&e, w->abort_flag, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) {
+    WS_CUDA(w, cudaMemset(w->abort_flag, 0, sizeof(int)));
+    return ws_fail(w, FCLG_E_CUDA, "a tensor-core inference CTA gave up a bounded wait; its directions are unset");
+  }
   return FCLG_OK;
 }
 
@@ -860,8 +905,8 @@ int fclg_warmstart_train(fclg_warmstart* w, const fclg_pair* d_pairs, const floa
       const float lr = (float)(lr1 + 0.5 * (lr0 - lr1) * (1.0 + std::cos(3.14159265358979 * f)));
       w->adam_t += 1;
       const float c1 = 1.f - std::pow(b1, (float)w->adam_t), c2 = 1.f - std::pow(b2, (float)w->adam_t);
-      adam_kernel<<<512, 256, 0, st>>>(w->params, w->grad, w->mom, w->vel, w->wb, w->n_params, lr, b1, b2, c1, c2,
-                                       eps);
+      adam_kernel<<<512, 256, 0, st>>>(w->params, w->grad, w->mom, w->vel, w->wb, w->wt, w->n_params, lr, b1, b2,
+                                       c1, c2, eps);
       ce = cudaGetLastError();
       if (ce != cudaSuccess) rc = ws_fail(w, FCLG_E_CUDA, cudaGetErrorString(ce));
     }

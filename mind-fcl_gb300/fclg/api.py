@@ -27,7 +27,7 @@ EXPORTS = [
     "fclg_mesh_collide", "fclg_mesh_collide_device",
     "fclg_warmstart_create", "fclg_warmstart_destroy", "fclg_warmstart_last_error", "fclg_warmstart_param_count",
     "fclg_warmstart_get_params", "fclg_warmstart_set_params", "fclg_warmstart_predict", "fclg_warmstart_forward",
-    "fclg_warmstart_gradient", "fclg_warmstart_train", "fclg_set_warmstart",
+    "fclg_warmstart_gradient", "fclg_warmstart_train", "fclg_set_warmstart", "fclg_warmstart_status",
 ]
 
 STATIC_MAX_PAIRS = 16384  # FCLG_STATIC_MAX_PAIRS
@@ -122,7 +122,9 @@ def load_library(path=LIB_PATH):
     for name in ("fclg_warmstart_get_params", "fclg_warmstart_set_params"):
         getattr(lib, name).argtypes = [vp, vp, u64]
         getattr(lib, name).restype = i32
-    lib.fclg_warmstart_predict.argtypes = [vp, vp, u32, vp, i32, vp]
+    lib.fclg_warmstart_predict.argtypes = [vp, vp, u32, vp, u32, vp]
+    lib.fclg_warmstart_status.argtypes = [vp]
+    lib.fclg_warmstart_status.restype = i32
     lib.fclg_warmstart_predict.restype = i32
     lib.fclg_warmstart_forward.argtypes = [vp, vp, u32, vp, vp]
     lib.fclg_warmstart_forward.restype = i32
@@ -299,10 +301,15 @@ class WarmStart:
         p = np.ascontiguousarray(params, np.float32)
         self._check(self.lib.fclg_warmstart_set_params(self.h, _ptr(p), len(p)), "fclg_warmstart_set_params")
 
-    def predict(self, d_pairs, n, d_out, normalize=True, stream=0):
+    def predict(self, d_pairs, n, d_out, normalize=True, mma_sync=False, stream=0):
+        """Directions (or raw outputs) by the tcgen05 kernel, or the mma.sync one."""
         st = ctypes.c_void_p(stream) if stream else None
+        flags = (1 if normalize else 0) | (2 if mma_sync else 0)
         self._check(self.lib.fclg_warmstart_predict(self.h, ctypes.c_void_p(d_pairs), n, ctypes.c_void_p(d_out),
-                                                    int(bool(normalize)), st), "fclg_warmstart_predict")
+                                                    flags, st), "fclg_warmstart_predict")
+
+    def status(self):
+        self._check(self.lib.fclg_warmstart_status(self.h), "fclg_warmstart_status")
 
     def forward(self, d_pairs, n, d_y, stream=0):
         st = ctypes.c_void_p(stream) if stream else None

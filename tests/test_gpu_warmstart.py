@@ -1,11 +1,15 @@
 """Learned GJK warm start on the GPU (fclg_warmstart_*).
 
-* Forward: the fused inference kernel and the training kernels against the
-  CPU oracle (oracle/mlp.py, BF16 rounding points): per pair
-  |y - y_oracle| <= 2e-2 (|y_oracle| + 1e-2), median relative error <= 2e-3.
-  The two sides round the same FP32 pre-activations to BF16 but sum in a
-  different order, so a pre-activation within ~1e-6 of a rounding boundary
-  may round the other way; the bound covers those.
+* Forward: the training kernels against the CPU oracle (oracle/mlp.py, BF16
+  rounding points): per pair |y - y_oracle| <= 2e-2 (|y_oracle| + 1e-2),
+  median relative error <= 2e-3.  The two sides round the same FP32
+  pre-activations to BF16 but sum in a different order, so a pre-activation
+  within ~1e-6 of a rounding boundary may round the other way; the bound
+  covers those.  The two inference kernels (tcgen05 and mma.sync) evaluate
+  GELU with the hardware tanh.approx (relative error ~2^-11, a tenth of a
+  BF16 step), which moves a few per cent of the activations by one BF16
+  step: against the oracle their bound is 5e-2 / median 5e-3, against each
+  other median 2e-3.
 * Gradient: the GPU backward pass against the oracle's on the same batch:
   per parameter block ||g - g_oracle|| <= 2e-2 ||g_oracle||, loss within 1e-4.
 * Training and the gain: a model trained on the GPU on plain-GJK directions
@@ -51,17 +55,22 @@ def test_forward_matches_oracle(torch):
     params = ws.get_params()
     d_pairs = _dev(torch, b.pairs)
     ref, _ = mlp.forward(params, b.pairs, workloads.ARM_CLASSES, on=True)
-    for fused in (True, False):
+    scale = np.linalg.norm(ref, axis=1) + 1e-2
+    outs = {}
+    for kind in ("tcgen05", "mma.sync", "training"):
         d_y = torch.zeros(n * 3, dtype=torch.float32, device="cuda")
-        if fused:
-            ws.predict(d_pairs.data_ptr(), n, d_y.data_ptr(), normalize=False)
-        else:
+        if kind == "training":
             ws.forward(d_pairs.data_ptr(), n, d_y.data_ptr())
-        torch.cuda.synchronize()
+        else:
+            ws.predict(d_pairs.data_ptr(), n, d_y.data_ptr(), normalize=False, mma_sync=kind == "mma.sync")
+        ws.status()
         y = d_y.cpu().numpy().reshape(n, 3)
-        scale = np.linalg.norm(ref, axis=1) + 1e-2
+        outs[kind] = y
         rel = np.linalg.norm(y - ref, axis=1) / scale
-        assert rel.max() <= 2e-2 and np.median(rel) <= 2e-3, (fused, rel.max(), np.median(rel))
+        bound, med = (2e-2, 2e-3) if kind == "training" else (5e-2, 5e-3)
+        assert rel.max() <= bound and np.median(rel) <= med, (kind, rel.max(), np.median(rel))
+    rel = np.linalg.norm(outs["tcgen05"] - outs["mma.sync"], axis=1) / scale
+    assert np.median(rel) <= 2e-3, np.median(rel)
     # normalised output is the unit direction of the raw one
     d_u = torch.zeros(n * 3, dtype=torch.float32, device="cuda")
     ws.predict(d_pairs.data_ptr(), n, d_u.data_ptr(), normalize=True)
