@@ -111,7 +111,7 @@ int fclg_built_arch(void);
 
 /* Shapes and hull vertices (float x, y, z, pad per vertex), copied to the
    device.  Replaces constructing fcl::Box / Sphere / Capsule / Cylinder /
-   Convex objects (geometry/shape/*.h). */
+   Convex objects (the geometry/shape headers). */
 int fclg_set_shapes(fclg_context* ctx, const fclg_shape* shapes, uint32_t n_shapes, const float* vertices_xyzw,
                     uint64_t n_vertices);
 /* Same, with the arrays already on the device; the context borrows them. */

@@ -1,0 +1,121 @@
+// Known answers through the fcl-style C++ API (include/fclg_fcl.hpp), from
+// the reference's own tests:
+//   sphere separation 0.2       test/cvx_collide/test_gjk2_distance.cpp:18-68
+//   sphere penetration 0.2      test/cvx_collide/test_epa2_with_gjk2.cpp:21-73
+//   box-box flags and depth     test/cvx_collide/test_gjk2.cpp:19-127
+// plus a rotated frame (witness points in the world frame), a convex cube,
+// the contact cap of fcl::collide and a mesh-mesh collide.
+#include <cmath>
+#include <cstdio>
+#include <memory>
+#include <vector>
+
+#include "fclg_fcl.hpp"
+
+using namespace fclg::fcl;
+using S = double;
+
+static int failures = 0;
+#define CHECK(cond, ...)                        \
+  do {                                          \
+    if (!(cond)) {                              \
+      std::printf("FAIL %s:%d: ", __FILE__, __LINE__); \
+      std::printf(__VA_ARGS__);                 \
+      std::printf("\n");                        \
+      ++failures;                               \
+    }                                           \
+  } while (0)
+
+static Transform3<S> at(S x, S y, S z) {
+  Transform3<S> t;
+  t.translation() = Vector3<S>(x, y, z);
+  return t;
+}
+
+static Transform3<S> rot_z(S ang, S x, S y, S z) {
+  Transform3<S> t = at(x, y, z);
+  t.linear()(0, 0) = std::cos(ang);
+  t.linear()(0, 1) = -std::sin(ang);
+  t.linear()(1, 0) = std::sin(ang);
+  t.linear()(1, 1) = std::cos(ang);
+  return t;
+}
+
+int main() {
+  GJKSolver<S> solver;
+  // spheres of radius 0.5: separated by 0.2, then penetrating by 0.2
+  Sphere<S> s1(0.5), s2(0.5);
+  S d = 0;
+  Vector3<S> p1, p2;
+  CHECK(solver.shapeSignedDistance(s1, at(0, 0, 0), s2, at(1.2, 0, 0), &d, &p1, &p2), "sphere distance ok");
+  CHECK(std::fabs(d - 0.2) < 1e-4, "sphere separation %.7f", d);
+  CHECK(std::fabs(p1[0] - 0.5) < 1e-3 && std::fabs(p2[0] - 0.7) < 1e-3, "witness %.5f %.5f", p1[0], p2[0]);
+  CHECK(solver.shapeSignedDistance(s1, at(0, 0, 0), s2, at(0.8, 0, 0), &d), "sphere depth ok");
+  CHECK(std::fabs(d + 0.2) < 1e-3, "sphere depth %.7f", d);
+
+  // the same separation in a rotated, translated frame: world-frame witness points
+  CHECK(solver.shapeSignedDistance(s1, rot_z(0.7, 1, 2, 3), s2, rot_z(-0.3, 1, 3.2, 3), &d, &p1, &p2), "rot ok");
+  CHECK(std::fabs(d - 0.2) < 1e-4, "rotated separation %.7f", d);
+  CHECK(std::fabs(p1[1] - 2.5) < 1e-3 && std::fabs(p2[1] - 2.7) < 1e-3, "rotated witness %.5f %.5f", p1[1], p2[1]);
+
+  // unit boxes overlapping by 0.1 along x: boolean, then depth and normal (escape of o2: +x)
+  Box<S> b1(1, 1, 1), b2(1, 1, 1);
+  CollisionRequest<S> boolean_req;
+  CollisionResult<S> res;
+  CHECK(collide(&b1, at(0, 0, 0), &b2, at(0.9, 0, 0), boolean_req, res) == 1, "box collide");
+  res.clear();
+  CHECK(collide(&b1, at(0, 0, 0), &b2, at(1.1, 0, 0), boolean_req, res) == 0, "box separated");
+  CollisionRequest<S> pen_req;
+  pen_req.useDefaultPenetration();
+  res.clear();
+  collide(&b1, at(0, 0, 0), &b2, at(0.9, 0.05, 0), pen_req, res);
+  CHECK(res.isCollision(), "box contact");
+  if (res.isCollision()) {
+    const auto& c = res.getContact(0);
+    CHECK(std::fabs(c.penetration_depth - 0.1) < 1e-4, "box depth %.7f", c.penetration_depth);
+    CHECK(c.normal[0] > 0.999, "box normal %.4f %.4f %.4f", c.normal[0], c.normal[1], c.normal[2]);
+    CHECK(c.o1 == &b1 && c.o2 == &b2, "contact objects");
+  }
+  CollisionRequest<S> zero_req(0);
+  res.clear();
+  CHECK(collide(&b1, at(0, 0, 0), &b2, at(0.5, 0, 0), zero_req, res) == 0, "no contacts requested");
+
+  // convex cube (8 vertices) against a sphere: distance 0.3
+  auto verts = std::make_shared<std::vector<Vector3<S>>>();
+  for (int i = 0; i < 8; ++i) verts->push_back(Vector3<S>((i & 1) ? 0.5 : -0.5, (i & 2) ? 0.5 : -0.5, (i & 4) ? 0.5 : -0.5));
+  auto faces = std::make_shared<std::vector<int>>();
+  Convex<S> cube(verts, 6, faces);
+  CHECK(solver.shapeSignedDistance(cube, at(0, 0, 0), s2, at(0, 0, 1.3), &d), "convex ok");
+  CHECK(std::fabs(d - 0.3) < 1e-4, "convex-sphere %.7f", d);
+
+  // batch: 1000 sphere pairs at growing distance, one call
+  BatchQuery<S> batch;
+  for (int i = 0; i < 1000; ++i) batch.add(&s1, at(0, 0, 0), &s2, at(0.5 + 0.001 * i, 0, 0));
+  const auto out = batch.signedDistance();
+  int bad = 0;
+  for (int i = 0; i < 1000; ++i) {
+    const S want = 0.5 + 0.001 * i - 1.0;
+    if (!out[i].ok || std::fabs(out[i].distance - want) > 2e-3) ++bad;
+  }
+  CHECK(bad == 0, "batch sphere pairs off: %d", bad);
+
+  // meshes: two octahedra, overlapping and apart
+  std::vector<Vector3<S>> pts = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+  std::vector<Triangle> tris = {{0, 2, 4}, {2, 1, 4}, {1, 3, 4}, {3, 0, 4}, {2, 0, 5}, {1, 2, 5}, {3, 1, 5}, {0, 3, 5}};
+  BVHModel<OBBRSS<S>> m1, m2;
+  m1.beginModel();
+  m1.addSubModel(pts, tris);
+  m1.endModel();
+  m2.beginModel();
+  m2.addSubModel(pts, tris);
+  m2.endModel();
+  CollisionRequest<S> mesh_req(4);
+  res.clear();
+  CHECK(collide(&m1, at(0, 0, 0), &m2, at(1.5, 0, 0), mesh_req, res) > 0, "mesh overlap");
+  for (const auto& c : res.getContacts()) CHECK(c.b1 >= 0 && c.b1 < 8 && c.b2 >= 0 && c.b2 < 8, "triangle ids");
+  res.clear();
+  CHECK(collide(&m1, at(0, 0, 0), &m2, at(2.5, 0, 0), mesh_req, res) == 0, "mesh apart");
+
+  if (failures == 0) std::printf("fcl_compat_test: all passed\n");
+  return failures == 0 ? 0 : 1;
+}
