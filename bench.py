@@ -14,6 +14,13 @@ beforehand as a caller constructs its geometry objects once.  The inputs
 (~0.6 GB of pairs, shapes and hull vertices) exceed the 129 MB L2, so no L2
 flush is needed between steps.
 
+The default line also carries ``config.warm_start``: the learned warm start
+trained on the GPU on plain-GJK directions of held-out seeds (mixed and arm
+workloads), then plain vs warm queries/s on the same pairs, GJK iterations,
+answer differences and the tcgen05 inference kernel's TFLOP/s.
+``--workload pareto | plain_small | arm`` print the same line for the other
+convex configurations; ``--workload mesh`` the BVH line.
+
 ``--impl reference`` times the reference's CPU implementation of the same
 query (its GJKSolver::shapeSignedDistance path) on the host cores: the
 FP64 restatement in oracle/, which is bit-identical to the reference's own
@@ -54,8 +61,13 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="fclg", choices=["fclg", "reference"])
     ap.add_argument("--pairs", type=int, default=N_PAIRS)
-    ap.add_argument("--workload", default="mixed", choices=["mixed", "mesh"],
-                    help="mixed: the headline convex-pair batch; mesh: the 50k x 50k-triangle BVH workload")
+    ap.add_argument("--workload", default="mixed",
+                    choices=["mixed", "mesh", "pareto", "plain_small", "arm", "warmstart"],
+                    help="mixed: the headline convex-pair batch (with the warm-start comparison); mesh: the "
+                         "50k x 50k-triangle BVH workload; pareto: 4M heavy-tailed hull pairs; plain_small: 4096 "
+                         "hull pairs; arm: 7-link arm x 32 obstacles, 100k configurations; warmstart: the "
+                         "warm-start inference kernel alone on 2.24M arm pairs")
+    ap.add_argument("--no-warm", action="store_true", help="skip the warm-start comparison")
     ap.add_argument("--poses", type=int, default=65536)
     return ap.parse_args()
 
@@ -130,6 +142,131 @@ def peaks():
             d = json.load(f)
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def bf16_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["bf16_tflops"]), "measured"
+    return 1900.0, "fallback"
+
+
+# other convex workloads: (generator, compulsory bytes per query, description)
+CONVEX_WORKLOADS = {
+    "mixed": (None, ALGO_BYTES_PER_QUERY, WORKLOAD),
+    "pareto": ("pareto", 398.0, "large uneven batch: 4M convex pairs, hull vertex counts Pareto(alpha 1.5, x_m 4) "
+                                "clipped to [4, 1024], ~30% overlap; GJK distance + EPA"),
+    "plain_small": ("plain_small", 896.0, "plain method, small: 4096 pairs of 32-vertex hulls (radius "
+                                          "U[0.05,0.5] m), translation in a 1 m cube; GJK distance + EPA"),
+    "arm": ("arm", 128.0, "learned warm start workload: 7-link arm (hulls of 64-256 vertices) x 32 obstacle hulls "
+                          "(64 vertices), 100k joint configurations = 22.4M link-obstacle pairs; GJK distance + EPA"),
+}
+MLP_FLOP_PER_PAIR = 2.0 * (28 * 256 + 2 * 256 * 256 + 256 * 3)
+# DRAM bytes (read + write) of the two EPA launches of one mixed-workload query
+# at 10^6 pairs, from one ncu capture (profiles/epa_pass_mixed_1M.md)
+EPA_TRAFFIC_MIXED_1M = (369.110272 + 29.940224 + 16.344064 + 0.022016) * 1e6
+
+
+def _to_dev(torch, arr, dev):
+    return torch.from_numpy(np.ascontiguousarray(arr).view(np.uint8).copy()).to(dev)
+
+
+def _time_queries(torch, ctx, d_pairs, n, flags, steps, warmup, stream, dev):
+    """Device time per signed-distance query over n resident pairs, and the last results."""
+    from fclg.api import make_request
+    from fclg.layout import RESULT_DTYPE
+    req = make_request(flags=flags) if flags else None
+    d_res = torch.empty(n * 48, dtype=torch.uint8, device=dev)
+
+    def step():
+        ctx.distance_device(d_pairs.data_ptr(), n, d_res.data_ptr(), req, stream.cuda_stream)
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    return e0.elapsed_time(e1) / max(steps, 1), d_res.cpu().numpy().view(RESULT_DTYPE).copy()
+
+
+def warm_start_block(args, torch, dev, stream, local):
+    """Learned warm start against plain initialisation: the model is trained on
+    the GPU on plain-GJK directions of held-out seeds, then both runs are timed
+    on the test batch (same pairs, same device entry point)."""
+    from fclg import workloads
+    from fclg.api import Context, WarmStart, direction_labels
+    peak, peak_kind = bf16_peak()
+    cases = [
+        ("mixed", lambda: workloads.mixed(2_000_000, seed=workloads.SEED_BASE + 1001),
+         lambda: workloads.mixed(args.pairs), workloads.MIXED_CLASSES),
+        ("arm", lambda: workloads.arm(9000, seed=workloads.SEED_BASE + 1003),
+         lambda: workloads.arm(10000), workloads.ARM_CLASSES),
+    ]
+    out = {}
+    for name, make_train, make_test, n_classes in cases:
+        ctx = Context(local)
+        train = make_train()
+        ctx.set_batch(train)
+        d_tr = _to_dev(torch, train.pairs, dev)
+        _, res = _time_queries(torch, ctx, d_tr, train.n_pairs, 0, 1, 0, stream, dev)
+        labels, ok = direction_labels(res)
+        keep = np.nonzero(ok)[0]
+        d_tr = _to_dev(torch, train.pairs[keep], dev)
+        d_lab = torch.from_numpy(labels[keep]).to(dev)
+        ws = WarmStart(n_classes, seed=1, device=local)
+        t0 = time.perf_counter()
+        losses = ws.train(d_tr.data_ptr(), d_lab.data_ptr(), len(keep), epochs=8, batch=4096, lr=2e-3)
+        train_s = time.perf_counter() - t0
+        del d_tr, d_lab
+        test = make_test()
+        ctx.set_batch(test)
+        ctx.set_warmstart(ws)
+        n = test.n_pairs
+        d_te = _to_dev(torch, test.pairs, dev)
+        ms_p, rp = _time_queries(torch, ctx, d_te, n, 0, args.steps, args.warmup, stream, dev)
+        ms_w, rw = _time_queries(torch, ctx, d_te, n, 4, args.steps, args.warmup, stream, dev)
+        # the tcgen05 inference kernel alone
+        d_g = torch.empty(n * 3, dtype=torch.float32, device=dev)
+        for _ in range(2):
+            ws.predict(d_te.data_ptr(), n, d_g.data_ptr(), stream=stream.cuda_stream)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            ws.predict(d_te.data_ptr(), n, d_g.data_ptr(), stream=stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ws.status()
+        ms_mlp = e0.elapsed_time(e1) / args.steps
+        guess = d_g.cpu().numpy().reshape(-1, 3)
+        lt, okt = direction_labels(rp)
+        ang = np.degrees(np.arccos(np.clip(np.sum(guess * lt, axis=1), -1.0, 1.0)))[okt]
+        dp, dw = rp["distance"].astype(np.float64), rw["distance"].astype(np.float64)
+        sep = (dp > 0) & (rp["ok"] == 1)
+        err = np.abs(dp - dw)[sep]
+        band = np.abs(dp) > 1e-6
+        tflops = MLP_FLOP_PER_PAIR * n / (ms_mlp * 1e-3) / 1e12
+        out[name] = {
+            "pairs": n, "train_samples": int(len(keep)), "train_epochs": 8, "train_s": round(train_s, 3),
+            "train_loss": [round(float(x), 5) for x in (losses[0], losses[-1])],
+            "plain": n / (ms_p * 1e-3), "warm": n / (ms_w * 1e-3), "speedup": ms_p / ms_w,
+            "plain_ms": ms_p, "warm_ms": ms_w,
+            "gjk_iters_separated": [float(rp["iterations"][sep].mean()), float(rw["iterations"][sep].mean())],
+            "direction_error_deg_median": float(np.median(ang)),
+            "flag_mismatches_outside_band": int(np.sum(((dp < 0) != (dw < 0)) & band)),
+            "separation_diff_p99_5": float(np.percentile(err, 99.5)) if len(err) else 0.0,
+            "separation_diff_max": float(err.max()) if len(err) else 0.0,
+            "mlp_kernel": "tcgen05 (TMEM accumulators, bulk-async weight staging)", "mlp_ms": ms_mlp,
+            "mlp_tflops": tflops, "mlp_frac": tflops / peak, "mlp_peak_source": peak_kind,
+        }
+        ctx.close()
+        ws.close()
+    return out
 
 
 def cpu_baseline(batch, threads):
@@ -259,12 +396,57 @@ def run_mesh(args):
     return 0
 
 
+def run_warmstart_kernel(args):
+    """The warm-start inference kernels alone (tcgen05 and mma.sync) on the arm
+    workload's 2.24M pairs, untrained weights (the cost does not depend on them)."""
+    import torch
+    from fclg import workloads
+    from fclg.api import WarmStart
+    rank, world, local = dist_env()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream(dev)
+    b = workloads.arm(10000)
+    n = b.n_pairs
+    ws = WarmStart(workloads.ARM_CLASSES, seed=1, device=local)
+    d_pairs = _to_dev(torch, b.pairs, dev)
+    d_out = torch.empty(n * 3, dtype=torch.float32, device=dev)
+    peak, peak_kind = bf16_peak()
+    res = {}
+    for kind in ("tcgen05", "mma.sync"):
+        for _ in range(args.warmup):
+            ws.predict(d_pairs.data_ptr(), n, d_out.data_ptr(), mma_sync=kind == "mma.sync", stream=stream.cuda_stream)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            ws.predict(d_pairs.data_ptr(), n, d_out.data_ptr(), mma_sync=kind == "mma.sync", stream=stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ws.status()
+        ms = e0.elapsed_time(e1) / args.steps
+        res[kind] = {"ms": ms, "tflops": MLP_FLOP_PER_PAIR * n / (ms * 1e-3) / 1e12}
+    t = res["tcgen05"]["tflops"]
+    line = {"metric": "warm-start MLP inference (28-256-256-256-3, BF16, FP32 accumulate)",
+            "value": n / (res["tcgen05"]["ms"] * 1e-3), "unit": "pair directions/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["tcgen05"]["ms"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": "arm pairs (22.4M / 10)", "pairs": n, "kernels": res},
+            "roofline": {"bound": "tensor", "achieved": t, "peak": peak, "unit": "TFLOP/s", "frac": t / peak,
+                         "traffic": None, "kernel": "infer_tc_kernel", "peak_source": peak_kind}}
+    print(json.dumps(line))
+    ws.close()
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "mesh":
         return run_mesh(args)
+    if args.workload == "warmstart":
+        return run_warmstart_kernel(args)
     import torch
     rank, world, local = dist_env()
     if world > 1:
@@ -276,7 +458,15 @@ def main():
 
     from fclg import workloads
     from fclg.api import Context
-    batch = workloads.mixed(args.pairs, seed=workloads.SEED_BASE + 1 + rank)  # weak scaling: own batch per rank
+    gen, algo_bytes, workload_text = CONVEX_WORKLOADS[args.workload]
+    if gen is None:
+        batch = workloads.mixed(args.pairs, seed=workloads.SEED_BASE + 1 + rank)  # weak scaling: own batch per rank
+    elif gen == "arm":
+        batch = workloads.arm(100_000, seed=workloads.SEED_BASE + 3 + 100 * rank)
+    elif gen == "pareto":
+        batch = workloads.pareto(seed=workloads.SEED_BASE + 4 + 100 * rank)
+    else:
+        batch = workloads.plain_small(seed=workloads.SEED_BASE + 0 + 100 * rank)
     n = batch.n_pairs
     ctx = Context(local)
     ctx.set_batch(batch)
@@ -294,18 +484,38 @@ def main():
         torch.cuda.synchronize(dev)
 
     # ---- device-resident throughput (value)
+    in_bytes = batch.pairs.nbytes + batch.shapes.nbytes + batch.vertices.nbytes + n * 48
+    flush = None
+    if in_bytes < 256 << 20:
+        # inputs within twice the 129 MB L2: flush it before every timed step
+        flush = torch.empty(512 << 20, dtype=torch.uint8, device=dev)
+        l2_note = "L2 flushed (512 MB write) before each timed step, outside the step's events"
+    else:
+        l2_note = "inputs larger than L2 (no flush)"
     for _ in range(args.warmup):
         step()
     barrier()
     launches0 = ctx.launch_count
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
-        e0.record(stream)
-        for _ in range(args.steps):
-            step()
-        e1.record(stream)
-        barrier()
-    ms = e0.elapsed_time(e1) / args.steps
+        if flush is None:
+            e0.record(stream)
+            for _ in range(args.steps):
+                step()
+            e1.record(stream)
+            barrier()
+            ms = e0.elapsed_time(e1) / args.steps
+        else:
+            total = 0.0
+            for _ in range(args.steps):
+                flush.zero_()
+                e0.record(stream)
+                step()
+                e1.record(stream)
+                e1.synchronize()
+                total += e0.elapsed_time(e1)
+            barrier()
+            ms = total / args.steps
     launches = ctx.launch_count - launches0
     if world > 1:
         t = torch.tensor([ms], device=dev)
@@ -355,7 +565,7 @@ def main():
         peak, peak_kind = peaks()
         dominant = "epa_pass" if epa_ms >= gjk_ms else "gjk_pass"
         # algorithmic bytes of the whole query per step over the dominant pass time and over the step
-        achieved = ALGO_BYTES_PER_QUERY * n / (max(gjk_ms, epa_ms) * 1e-3) / 1e9
+        achieved = algo_bytes * n / (max(gjk_ms, epa_ms) * 1e-3) / 1e9
         threads = os.cpu_count() or 1
         cpu_v, cpu_n, cpu_s = cpu_baseline(batch, threads)
         line = {
@@ -363,20 +573,27 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (FP64 EPA closest-face solve and GJK tetrahedron tests)",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "pairs_per_gpu": n, "overlap_fraction": overlap,
-                       "seed": batch.meta["seed"], "l2": "inputs larger than L2 (no flush)",
+            "config": {"workload": workload_text, "pairs_per_gpu": n, "overlap_fraction": overlap,
+                       "seed": batch.meta["seed"], "l2": l2_note,
                        "gjk_pass_ms": gjk_ms, "epa_pass_ms": epa_ms},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "kernel": dominant,
+                         "frac": achieved / peak,
+                         "traffic": (EPA_TRAFFIC_MIXED_1M if args.workload == "mixed" and n == 1_000_000
+                                     and dominant == "epa_pass" else None),
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of both EPA "
+                                           "launches, profiles/epa_pass_mixed_1M.md",
+                         "kernel": dominant + " (all launches of the pass)",
                          "peak_source": peak_kind,
-                         "algorithmic_bytes": "498 B/query x %d queries per launch" % n},
+                         "algorithmic_bytes": "%d B/query x %d queries per launch" % (algo_bytes, n)},
             "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": "first %d pairs of the batch, repeated to %d queries, FP64 restatement (%.1f s)"
                                        % (min(CPU_SAMPLE_PAIRS, n), cpu_n, cpu_s)},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 64, "d2h_bytes_per_step": n * 48},
             "clocks": clk.summary(),
         }
+        if args.workload == "mixed" and not args.no_warm:
+            line["config"]["warm_start"] = warm_start_block(args, torch, dev, stream, local)
         print(json.dumps(line))
     ctx.close()
     if world > 1:
