@@ -277,7 +277,7 @@ def cpu_baseline(batch, threads):
     oracle.signed_distance(sample.subset(np.arange(2000)), threads=threads)  # warm the code path
     # repeat the sample until about CPU_SAMPLE_SECONDS of CPU work are timed
     done, secs = 0, 0.0
-    while secs < CPU_SAMPLE_SECONDS and done < 200 * sample.n_pairs:
+    while secs < CPU_SAMPLE_SECONDS and done < 100_000_000:
         s, _ = oracle.time_signed_distance(sample, threads=threads)
         secs += s
         done += sample.n_pairs
@@ -477,6 +477,9 @@ def main():
     def step():
         ctx.distance_device(d_pairs.data_ptr(), n, d_res.data_ptr(), None, stream.cuda_stream)
 
+    # launch shape chosen by the library's autotuner on this batch (untimed)
+    tuning, tune_ms = ctx.autotune(d_pairs.data_ptr(), n, d_res.data_ptr())
+
     def barrier():
         torch.cuda.synchronize(dev)
         if world > 1:
@@ -517,6 +520,23 @@ def main():
             barrier()
             ms = total / args.steps
     launches = ctx.launch_count - launches0
+    graph_ms = None
+    if n <= 65536 and world == 1:
+        # small batches are launch-bound: the same query replayed as one CUDA graph
+        g = ctx.graph(d_pairs.data_ptr(), n, d_res.data_ptr())
+        g.launch(stream.cuda_stream)
+        torch.cuda.synchronize(dev)
+        total = 0.0
+        for _ in range(args.steps):
+            if flush is not None:
+                flush.zero_()
+            e0.record(stream)
+            g.launch(stream.cuda_stream)
+            e1.record(stream)
+            e1.synchronize()
+            total += e0.elapsed_time(e1)
+        graph_ms = total / args.steps
+        g.close()
     if world > 1:
         t = torch.tensor([ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -575,7 +595,10 @@ def main():
             "data": "synthetic",
             "config": {"workload": workload_text, "pairs_per_gpu": n, "overlap_fraction": overlap,
                        "seed": batch.meta["seed"], "l2": l2_note,
-                       "gjk_pass_ms": gjk_ms, "epa_pass_ms": epa_ms},
+                       "gjk_pass_ms": gjk_ms, "epa_pass_ms": epa_ms,
+                       "tuning": dict(tuning, autotune_ms=tune_ms),
+                       "cuda_graph": (None if graph_ms is None else
+                                      {"ms_per_step": graph_ms, "value": n / (graph_ms * 1e-3)})},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak,

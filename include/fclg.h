@@ -76,7 +76,8 @@ typedef struct fclg_result { /* 48 bytes */
   float p_a[3];          /* witness point on a */
   float p_b[3];          /* witness point on b */
   int32_t status;        /* bits 0-7 GJK_Status (cvx_collide/gjk.h:13-28); bits 8-15 EPA_Status+1
-                            (cvx_collide/epa.h:14), 0 when EPA did not run */
+                            (cvx_collide/epa.h:14), 0 when EPA did not run; bit 16
+                            (FCLG_STATUS_MPR): a boolean decided by MPR */
   uint16_t iterations;   /* GJK (+distance) iterations, plus EPA expansions */
   uint8_t collide;       /* boolean collide flag */
   uint8_t ok;            /* the query produced a valid distance (shapeSignedDistance's return) */
@@ -95,8 +96,12 @@ typedef struct fclg_request {
 enum {
   FCLG_REQ_BOOLEAN_ONLY = 1u << 0,  /* collide flag only: no distance, no EPA */
   FCLG_REQ_NO_EPA = 1u << 1,        /* separation distance only; overlapping pairs get distance 0 */
-  FCLG_REQ_WARM_START = 1u << 2     /* seed GJK with the learned direction model (fclg_warmstart_*) */
+  FCLG_REQ_WARM_START = 1u << 2,    /* seed GJK with the learned direction model (fclg_warmstart_*) */
+  FCLG_REQ_GJK_BOOLEAN = 1u << 3    /* boolean collide by GJK instead of MPR (the reference's boolean
+                                       fcl::collide runs MPR, falling back to GJK when MPR fails) */
 };
+/* fclg_result.status bit 16: the boolean was decided by MPR. */
+#define FCLG_STATUS_MPR (1 << 16)
 
 typedef struct fclg_context fclg_context;
 
@@ -220,6 +225,26 @@ int fclg_set_tuning(fclg_context* ctx, const fclg_tuning* tuning);
 int fclg_get_tuning(const fclg_context* ctx, fclg_tuning* tuning);
 /* Shorthand: the same lane count for both GJK launches, and the EPA CTAs per SM. */
 int fclg_set_launch(fclg_context* ctx, int gjk_lanes, int epa_ctas_per_sm);
+
+/* Autotuner: times the query on (d_pairs, n) under each candidate launch shape
+   (GJK lanes for small / large hulls: 1-8 / 4-16, hull split 64 / 128 / 256
+   vertices, bucketing on / off; three queries each), keeps the fastest on the
+   context and returns it with its time per query.  d_results is overwritten.
+   No counterpart in the reference. */
+int fclg_autotune(fclg_context* ctx, const fclg_pair* d_pairs, uint32_t n_pairs, const fclg_request* req,
+                  fclg_result* d_results, int distance_query, fclg_tuning* best, float* best_ms);
+
+/* CUDA graph of one whole query (bucketing, both GJK launches, EPA, and the
+   warm-start inference when requested) on fixed device buffers: capture once,
+   then replay with fclg_graph_launch after refilling d_pairs.  The capture
+   allocates the query's scratch first; a graph goes stale (launch returns
+   FCLG_E_INVALID) when the context later reallocates that scratch for a
+   larger batch.  No counterpart in the reference. */
+typedef struct fclg_graph fclg_graph;
+int fclg_graph_create(fclg_context* ctx, const fclg_pair* d_pairs, uint32_t n_pairs, const fclg_request* req,
+                      fclg_result* d_results, int distance_query, fclg_graph** graph);
+int fclg_graph_launch(fclg_context* ctx, fclg_graph* graph, void* stream);
+void fclg_graph_destroy(fclg_graph* graph);
 
 /* Kernel launches issued by this context since creation (for accounting). */
 uint64_t fclg_launch_count(const fclg_context* ctx);

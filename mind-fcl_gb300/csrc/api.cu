@@ -62,6 +62,8 @@ struct fclg_context {
   fclg_warmstart* ws = nullptr;
   float* guess = nullptr;
   size_t guess_cap = 0;
+  // bumped whenever query scratch is reallocated (invalidates captured graphs)
+  uint64_t scratch_epoch = 0;
 };
 
 struct fclg_mesh {
@@ -132,6 +134,7 @@ int ensure_epa(fclg_context* c, size_t n) {
   FCLG_CUDA(c, cudaMalloc(&c->epa_ovf, cap * sizeof(uint32_t)));
   FCLG_CUDA(c, cudaMalloc(&c->epa_rec, cap * fclg::kEpaRecordBytes));
   c->epa_cap = cap;
+  c->scratch_epoch += 1;
   return FCLG_OK;
 }
 
@@ -150,6 +153,7 @@ int ensure_bucket(fclg_context* c, size_t n) {
   FCLG_CUDA(c, cudaMalloc(&c->bk_keys, cap));
   FCLG_CUDA(c, cudaMalloc(&c->bk_order, cap * sizeof(uint32_t)));
   c->bk_cap = cap;
+  c->scratch_epoch += 1;
   return FCLG_OK;
 }
 
@@ -174,6 +178,7 @@ int ensure_guess(fclg_context* c, size_t n) {
   const size_t cap = std::max<size_t>(n, 1024);
   FCLG_CUDA(c, cudaMalloc(&c->guess, cap * 3 * sizeof(float)));
   c->guess_cap = cap;
+  c->scratch_epoch += 1;
   return FCLG_OK;
 }
 
@@ -188,6 +193,9 @@ fclg::QueryParams make_params(const fclg_request* req, bool distance_query) {
   const bool boolean_only = (fl & FCLG_REQ_BOOLEAN_ONLY) != 0;
   p.want_distance = (distance_query || !boolean_only) ? 1 : 0;
   p.want_epa = (!boolean_only && !(fl & FCLG_REQ_NO_EPA)) ? 1 : 0;
+  // fcl::collide without contact runs MPR (gjk_solver-inl.h:86-97); a learned
+  // warm start applies to GJK only, so it keeps the GJK boolean
+  p.use_mpr = (!distance_query && boolean_only && !(fl & FCLG_REQ_WARM_START) && !(fl & FCLG_REQ_GJK_BOOLEAN)) ? 1 : 0;
   return p;
 }
 
@@ -696,5 +704,160 @@ extern "C" int fclg_distance_device_static(fclg_context* c, const fclg_pair* d_p
     FCLG_CUDA(c, fclg::launch_epa(b, prm, q, ovf, c->num_sms, c->epa_ctas_per_sm, st));
     c->launches += prm.epa_max_faces > 128 ? 2 : 1;
   }
+  return FCLG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// CUDA graphs of a whole query, and the launch-shape autotuner.
+// ---------------------------------------------------------------------------
+
+struct fclg_graph {
+  int device = 0;
+  const fclg_context* ctx = nullptr;
+  uint64_t epoch = 0;
+  uint64_t launches = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+// Allocates every scratch buffer a query of n pairs needs, so that a capture
+// or a timed loop allocates nothing.
+int reserve_query(fclg_context* c, uint32_t n, const fclg_request* req, bool distance_query) {
+  const fclg::QueryParams prm = make_params(req, distance_query);
+  int rc = FCLG_OK;
+  if (prm.want_epa) rc = ensure_epa(c, n);
+  if (!rc && c->bucketing) rc = ensure_bucket(c, n);
+  if (!rc && req && (req->flags & FCLG_REQ_WARM_START)) rc = ensure_guess(c, n);
+  return rc;
+}
+
+}  // namespace
+
+extern "C" int fclg_graph_create(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_request* req,
+                                 fclg_result* d_results, int distance_query, fclg_graph** out) {
+  if (!c || !out) return FCLG_E_INVALID;
+  *out = nullptr;
+  if (n == 0 || !d_pairs || !d_results) return fail(c, FCLG_E_INVALID, "graph of an empty or null batch");
+  if (!c->shapes) return fail(c, FCLG_E_NO_SHAPES, "no shapes set");
+  FCLG_CUDA(c, cudaSetDevice(c->device));
+  int rc = reserve_query(c, n, req, distance_query != 0);
+  if (rc) return rc;
+  cudaStream_t cs = nullptr;
+  FCLG_CUDA(c, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  const bool prof = c->profiling;
+  c->profiling = false;
+  const uint64_t l0 = c->launches;
+  cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  cudaGraph_t g = nullptr;
+  if (e == cudaSuccess) {
+    rc = run_query(c, d_pairs, n, req, d_results, cs, distance_query != 0);
+    e = cudaStreamEndCapture(cs, &g);
+  }
+  c->profiling = prof;
+  const uint64_t launches = c->launches - l0;
+  c->launches = l0;
+  cudaStreamDestroy(cs);
+  if (rc || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return rc ? rc : cuda_fail(c, e, "stream capture of a query");
+  }
+  cudaGraphExec_t ex = nullptr;
+  e = cudaGraphInstantiate(&ex, g, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return cuda_fail(c, e, "cudaGraphInstantiate");
+  }
+  fclg_graph* G = new fclg_graph();
+  G->device = c->device;
+  G->ctx = c;
+  G->epoch = c->scratch_epoch;
+  G->launches = launches;
+  G->graph = g;
+  G->exec = ex;
+  *out = G;
+  return FCLG_OK;
+}
+
+extern "C" int fclg_graph_launch(fclg_context* c, fclg_graph* g, void* stream) {
+  if (!c || !g || g->ctx != c) return fail(c, FCLG_E_INVALID, "graph of another context");
+  if (g->epoch != c->scratch_epoch)
+    return fail(c, FCLG_E_INVALID, "graph is stale: the context reallocated its query scratch since the capture");
+  FCLG_CUDA(c, cudaSetDevice(c->device));
+  FCLG_CUDA(c, cudaGraphLaunch(g->exec, static_cast<cudaStream_t>(stream)));
+  c->launches += g->launches;
+  return FCLG_OK;
+}
+
+extern "C" void fclg_graph_destroy(fclg_graph* g) {
+  if (!g) return;
+  cudaSetDevice(g->device);
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  delete g;
+}
+
+extern "C" int fclg_autotune(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_request* req,
+                             fclg_result* d_results, int distance_query, fclg_tuning* best, float* best_ms) {
+  if (!c) return FCLG_E_INVALID;
+  if (n == 0 || !d_pairs || !d_results) return fail(c, FCLG_E_INVALID, "autotune on an empty or null batch");
+  if (!c->shapes) return fail(c, FCLG_E_NO_SHAPES, "no shapes set");
+  FCLG_CUDA(c, cudaSetDevice(c->device));
+  fclg_tuning keep{};
+  fclg_get_tuning(c, &keep);
+  const bool prof = c->profiling;
+  c->profiling = false;
+  // candidates: GJK lanes for small / large hulls, the hull split, bucketing
+  std::vector<fclg_tuning> cand;
+  for (int ls : {1, 2, 4, 8})
+    for (int ll : {4, 8, 16})
+      for (int lh : {64, 128, 256}) {
+        fclg_tuning t = keep;
+        t.bucketing = 1;
+        t.gjk_lanes_small = ls;
+        t.gjk_lanes_large = ll;
+        t.large_hull_vertices = lh;
+        cand.push_back(t);
+      }
+  {
+    fclg_tuning t = keep;
+    t.bucketing = -1;
+    t.gjk_lanes_small = 1;
+    cand.push_back(t);
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = FCLG_OK;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+    rc = fail(c, FCLG_E_CUDA, "cudaEventCreate");
+  float best_t = 0.f;
+  fclg_tuning best_c = keep;
+  for (size_t i = 0; i < cand.size() && rc == FCLG_OK; ++i) {
+    rc = fclg_set_tuning(c, &cand[i]);
+    if (!rc) rc = reserve_query(c, n, req, distance_query != 0);
+    if (!rc) rc = run_query(c, d_pairs, n, req, d_results, c->stream, distance_query != 0);  // warm-up
+    if (rc) break;
+    cudaEventRecord(e0, c->stream);
+    for (int r = 0; r < 2 && !rc; ++r) rc = run_query(c, d_pairs, n, req, d_results, c->stream, distance_query != 0);
+    cudaEventRecord(e1, c->stream);
+    if (rc) break;
+    float ms = 0.f;
+    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+      rc = fail(c, FCLG_E_CUDA, "autotune timing");
+      break;
+    }
+    ms *= 0.5f;
+    if (i == 0 || ms < best_t) {
+      best_t = ms;
+      best_c = cand[i];
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  c->profiling = prof;
+  fclg_set_tuning(c, rc ? &keep : &best_c);
+  if (rc) return rc;
+  if (best) fclg_get_tuning(c, best);
+  if (best_ms) *best_ms = best_t;
   return FCLG_OK;
 }

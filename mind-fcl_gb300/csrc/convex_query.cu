@@ -12,6 +12,7 @@
 #include "epa.cuh"
 #include "gjk.cuh"
 #include "kernels.h"
+#include "mpr.cuh"
 
 namespace fclg {
 
@@ -82,6 +83,23 @@ __global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_pass(BatchArgs b, Quer
     sup.g = g;
     // GJKSolver's default guess (1, 0, 0), gjk_solver-inl.h:1129
     const f3 plain = mk3(1.f, 0.f, 0.f);
+    int mpr_iters = 0;
+    if (prm.use_mpr) {
+      // fcl::collide without contact: MPR decides, GJK only when MPR fails
+      // (ShapeIntersectIndepImpl::run, gjk_solver-inl.h:86-97)
+      Mpr<MinkowskiSupport<LANES>> mpr{sup, prm.gjk_max_iter, prm.gjk_tol};
+      const f3 v0 = load_interior(b.shapes, pr.a, sup.A.type) - pr.pose.apply(load_interior(b.shapes, pr.b, sup.B.type));
+      const MprStatus ms = mpr.intersect(v0);
+      mpr_iters = mpr.iterations;
+      if (ms != MprStatus::Failed) {
+        if (g.lane == 0) {
+          const bool hit = ms == MprStatus::Intersect;
+          store_result(b.results, pid, 0.f, mk3(0, 0, 1), mk3(0, 0, 0), mk3(0, 0, 0),
+                       (hit ? kGjkIntersect : kGjkSeparated) | kStatusMpr, (uint32_t)mpr_iters, hit, hit);
+        }
+        continue;
+      }
+    }
     Simplex s;
     GjkOut o;
     if (b.guess) {

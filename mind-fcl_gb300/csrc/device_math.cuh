@@ -126,6 +126,8 @@ __device__ __forceinline__ PairDev load_pair(const float4* __restrict__ pairs, u
 
 // Status word of a result: bits 0-7 GJK_Status, bits 8-15 EPA_Status + 1.
 enum : int32_t { kGjkIntersect = 0, kGjkSeparated = 1, kGjkNoProgress = 2, kGjkIterLimit = 3, kGjkFailed = 4 };
+// Result status bit: the boolean came from MPR (bits 0-7 then hold Intersect / Separated).
+constexpr int32_t kStatusMpr = 1 << 16;
 enum : int32_t { kEpaFailed = 0, kEpaOK = 1, kEpaTouching = 2, kEpaIterLimit = 3, kEpaMallocFailed = 4 };
 
 // 48-byte fclg_result written as three float4 stores.
@@ -145,6 +147,7 @@ struct QueryParams {
   int epa_max_iter;
   int epa_max_faces;
   int want_distance;  // 1: signed distance (GJK distance / EPA); 0: boolean only
+  int use_mpr;        // boolean collide: MPR first, GJK when MPR fails
   int want_epa;       // run EPA on overlapping pairs
 };
 

@@ -1,0 +1,137 @@
+// MPR boolean intersection (Minkowski portal refinement), the test
+// fcl::collide runs for a shape pair when no contact is requested
+// (ShapeIntersectIndepImpl::run, gjk_solver-inl.h:70-137, which falls back to
+// GJK when MPR reports failure).  Restates MPR::RunIntersect and its helpers
+// (cvx_collide/mpr.hpp:10-15, 33-185, 187-328, 434-493) in FP32, one thread
+// (or lane group) per pair.
+#pragma once
+#include "support.cuh"
+
+namespace fclg {
+
+enum class MprStatus : int { Intersect = 0, Separated = 1, Failed = 2 };
+
+// Interior point of a shape in its own frame: the vertex mean of a hull
+// (convex-inl.h:58-63, stored in fclg_shape.param[0:3]), the origin otherwise.
+__device__ __forceinline__ f3 load_interior(const int4* __restrict__ shapes, uint32_t i, int type) {
+  if (type != kConvex) return mk3(0.f, 0.f, 0.f);
+  const float4 p = __ldg(reinterpret_cast<const float4*>(shapes) + 2 * (size_t)i + 1);
+  return mk3(p.x, p.y, p.z);
+}
+
+// mpr.hpp:18-20: the tolerance tests use the L1 norm.
+__device__ __forceinline__ float absnorm(f3 v) { return fabsf(v.x) + fabsf(v.y) + fabsf(v.z); }
+
+template <class Sup>
+struct Mpr {
+  const Sup& sup;
+  int max_iter;
+  float tol;
+  int iterations = 0;
+
+  // mpr.hpp:10-15: the direction is normalised in place, then supported.
+  __device__ __forceinline__ f3 support(f3& d) const {
+    d = normalized(d);
+    f3 pa, pb;
+    sup(d, pa, pb);
+    return pa - pb;
+  }
+
+  // mpr.hpp:187-328: 0 iteration limit, 1 separated, 2 portal found.
+  __device__ int find_portal(f3 v0, f3& v1, f3& v2, f3& v3, f3& d1, f3& d2, f3& d3) {
+    constexpr float kEps = 1.1920929e-07f;  // dot_eps_ratio = epsilon<T>() (mpr.h:103), T = float
+    const float v0n = absnorm(v0);
+    for (int it = 0;; ++it) {
+      if (it >= max_iter) return 0;
+      ++iterations;
+      f3 a1 = v1 - v0, a2 = v2 - v0, a3 = v3 - v0;
+      f3 n031 = cross(a3, a1);
+      f3 n012 = cross(a1, a2);
+      if (dot(a2, n031) < 0.f) {
+        f3 t = v2; v2 = v3; v3 = t;
+        t = d2; d2 = d3; d3 = t;
+        t = a2; a2 = a3; a3 = t;
+        t = n012; n012 = n031; n031 = t;
+        n031 = -n031;
+        n012 = -n012;
+      }
+      if (dot(v0, n031) > kEps * v0n * absnorm(n031)) {
+        f3 sd = -n031;
+        v2 = support(sd);
+        d2 = sd;
+        if (dot(v2, sd) < 0.f) return 1;
+        continue;
+      }
+      if (dot(v0, n012) > kEps * v0n * absnorm(n012)) {
+        f3 sd = -n012;
+        v3 = support(sd);
+        d3 = sd;
+        if (dot(v3, sd) < 0.f) return 1;
+        continue;
+      }
+      const f3 n023 = cross(a2, a3);
+      if (dot(v0, n023) > kEps * v0n * absnorm(n023)) {
+        f3 sd = -n023;
+        v1 = support(sd);
+        d1 = sd;
+        if (dot(v1, sd) < 0.f) return 1;
+        continue;
+      }
+      return 2;
+    }
+  }
+
+  // mpr.hpp:434-493
+  __device__ __forceinline__ static void update_portal(f3 v0, f3 v4, f3 n, f3& v1, f3& v2, f3& v3, f3& d1, f3& d2,
+                                                       f3& d3) {
+    const f3 pn = cross(v4, v0);
+    if (dot(v1, pn) > 0.f) {
+      if (dot(v2, pn) > 0.f) { v1 = v4; d1 = n; }
+      else { v3 = v4; d3 = n; }
+    } else {
+      if (dot(v3, pn) > 0.f) { v2 = v4; d2 = n; }
+      else { v1 = v4; d1 = n; }
+    }
+  }
+
+  // mpr.hpp:33-185.  v0 is the interior point of the Minkowski difference.
+  __device__ MprStatus intersect(f3 v0) {
+    iterations = 0;
+    if (sqn(v0) <= tol * tol) return MprStatus::Intersect;
+    f3 d1 = -v0;
+    f3 v1 = support(d1);
+    if (dot(d1, v1) < 0.f) return MprStatus::Separated;
+    f3 d2 = cross(v0, v1);
+    if (absnorm(d2) <= absnorm(v0) * absnorm(v1) * tol) return MprStatus::Intersect;
+    f3 v2 = support(d2);
+    if (dot(d2, v2) < 0.f) return MprStatus::Separated;
+    f3 d3 = cross(v1 - v0, v2 - v0);
+    if (dot(d3, v0) > 0.f) {
+      f3 t = v1; v1 = v2; v2 = t;
+      t = d1; d1 = d2; d2 = t;
+      d3 = -d3;
+    }
+    f3 v3 = support(d3);
+    if (dot(d3, v3) < 0.f) return MprStatus::Separated;
+    const int fp = find_portal(v0, v1, v2, v3, d1, d2, d3);
+    if (fp == 0) return MprStatus::Failed;
+    if (fp == 1) return MprStatus::Separated;
+    for (int it = 0; it < max_iter; ++it) {
+      ++iterations;
+      f3 n = cross(v2 - v1, v3 - v1);
+      if (dot(n, v0) > 0.f) {
+        f3 t = v2; v2 = v3; v3 = t;
+        t = d2; d2 = d3; d3 = t;
+        n = -n;
+      }
+      if (!(dot(v1, n) < 0.f)) return MprStatus::Intersect;
+      const f3 v4 = support(n);
+      if (dot(v4, n) < 0.f) return MprStatus::Separated;
+      if (fabsf(dot(v4 - v1, n)) < tol * absnorm(n)) return MprStatus::Separated;
+      update_portal(v0, v4, n, v1, v2, v3, d1, d2, d3);
+    }
+    return MprStatus::Failed;
+  }
+};
+
+}  // namespace fclg

@@ -28,6 +28,7 @@ EXPORTS = [
     "fclg_warmstart_create", "fclg_warmstart_destroy", "fclg_warmstart_last_error", "fclg_warmstart_param_count",
     "fclg_warmstart_get_params", "fclg_warmstart_set_params", "fclg_warmstart_predict", "fclg_warmstart_forward",
     "fclg_warmstart_gradient", "fclg_warmstart_train", "fclg_set_warmstart", "fclg_warmstart_status",
+    "fclg_autotune", "fclg_graph_create", "fclg_graph_launch", "fclg_graph_destroy",
 ]
 
 STATIC_MAX_PAIRS = 16384  # FCLG_STATIC_MAX_PAIRS
@@ -134,6 +135,14 @@ def load_library(path=LIB_PATH):
     lib.fclg_warmstart_train.restype = i32
     lib.fclg_set_warmstart.argtypes = [vp, vp]
     lib.fclg_set_warmstart.restype = i32
+    lib.fclg_autotune.argtypes = [vp, vp, u32, vp, vp, i32, ctypes.POINTER(Tuning), ctypes.POINTER(ctypes.c_float)]
+    lib.fclg_autotune.restype = i32
+    lib.fclg_graph_create.argtypes = [vp, vp, u32, vp, vp, i32, ctypes.POINTER(vp)]
+    lib.fclg_graph_create.restype = i32
+    lib.fclg_graph_launch.argtypes = [vp, vp, vp]
+    lib.fclg_graph_launch.restype = i32
+    lib.fclg_graph_destroy.argtypes = [vp]
+    lib.fclg_graph_destroy.restype = None
     _lib = lib
     return lib
 
@@ -265,11 +274,51 @@ class Context:
     def launch_count(self):
         return int(self.lib.fclg_launch_count(self.h))
 
+    def autotune(self, d_pairs, n, d_results, request=None, distance=True):
+        """Times candidate launch shapes on the batch, keeps the fastest; returns (tuning dict, ms)."""
+        t = Tuning()
+        ms = ctypes.c_float()
+        req = ctypes.byref(request) if request is not None else None
+        self._check(self.lib.fclg_autotune(self.h, ctypes.c_void_p(d_pairs), n, req, ctypes.c_void_p(d_results),
+                                           int(distance), ctypes.byref(t), ctypes.byref(ms)), "fclg_autotune")
+        return {name: getattr(t, name) for name, _ in Tuning._fields_}, ms.value
+
+    def graph(self, d_pairs, n, d_results, request=None, distance=True):
+        """A CUDA graph of one query on these device buffers (QueryGraph)."""
+        return QueryGraph(self, d_pairs, n, d_results, request, distance)
+
     def set_warmstart(self, model):
         """Model for queries with FCLG_REQ_WARM_START (None: none)."""
         self._check(self.lib.fclg_set_warmstart(self.h, model.h if model is not None else None),
                     "fclg_set_warmstart")
         self._warmstart = model
+
+
+class QueryGraph:
+    """fclg_graph_*: one captured query, replayed with launch()."""
+
+    def __init__(self, ctx, d_pairs, n, d_results, request=None, distance=True):
+        self.ctx = ctx
+        h = ctypes.c_void_p()
+        req = ctypes.byref(request) if request is not None else None
+        ctx._check(ctx.lib.fclg_graph_create(ctx.h, ctypes.c_void_p(d_pairs), n, req, ctypes.c_void_p(d_results),
+                                             int(distance), ctypes.byref(h)), "fclg_graph_create")
+        self.h = h
+
+    def launch(self, stream=0):
+        st = ctypes.c_void_p(stream) if stream else None
+        self.ctx._check(self.ctx.lib.fclg_graph_launch(self.ctx.h, self.h, st), "fclg_graph_launch")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.fclg_graph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class WarmStart:

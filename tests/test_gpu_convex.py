@@ -112,6 +112,26 @@ def test_collide_vs_reference_golden(gpu_ctx, name):
     assert np.mean(err <= 1e-5) >= 0.99
 
 
+@pytest.mark.parametrize("workload,n", [("mixed", 60000), ("pareto", 60000)])
+def test_boolean_collide_mpr_vs_oracle(gpu_ctx, oracle_lib, workload, n):
+    """Boolean fcl::collide: MPR on the GPU (GJK where MPR fails) against the
+    restated reference's MPR, and against the GJK boolean; flags identical
+    outside the 1e-6 m band around contact."""
+    from fclg.api import make_request
+    BOOLEAN, GJK_BOOLEAN, MPR_BIT = 1, 8, 1 << 16
+    b = getattr(workloads, workload)(n)
+    gpu_ctx.set_batch(b)
+    got = gpu_ctx.collide(b.pairs, make_request(flags=BOOLEAN))
+    gjk = gpu_ctx.collide(b.pairs, make_request(flags=BOOLEAN | GJK_BOOLEAN))
+    ref = oracle_lib.collide(b)
+    sd = oracle_lib.signed_distance(b)
+    outside = np.abs(sd["distance"]) > BAND
+    assert np.sum((got["collide"] != ref["ok"]) & outside) == 0
+    assert np.sum((got["collide"] != gjk["collide"]) & outside) == 0
+    assert np.mean((got["status"] & MPR_BIT) != 0) > 0.99   # MPR decided (almost) every pair
+    assert np.all((gjk["status"] & MPR_BIT) == 0)
+
+
 @pytest.mark.parametrize("workload,n", [("plain_small", 4096), ("mixed", 60000), ("pareto", 60000)])
 def test_distance_vs_oracle(gpu_ctx, oracle_lib, workload, n):
     b = getattr(workloads, workload)(n)
