@@ -22,9 +22,9 @@
 // GPU layout: per iteration the work is proportional to the visible patch,
 // not to the polytope: the patch grows in frontier rounds (a lane per frontier
 // face, classification claimed with a compare-and-swap on a per-iteration
-// stamp), horizon edges are gathered with a warp prefix sum, slots are
-// recycled through a free stack, and the fan is linked through a per-vertex
-// "edge starting here" table.  Only the nearest-face argmin touches every
+// stamp), horizon edges are recorded by the same rounds (a patch face's edge
+// whose neighbour ends hidden), slots are recycled through a free stack, and
+// the fan is linked through a per-vertex "edge starting here" table.  Only the nearest-face argmin touches every
 // slot: one shared-memory load per lane per 32 slots.  Face planes are FP32
 // unit normals and distances whose cross products are compensated (see
 // face_plane); the final closest-face solve (depth, barycentric witness
@@ -76,6 +76,7 @@ struct EpaSmem {
   uint8_t hz_e[FMAX + 8];   // patch size + 2 edges) and its edge index
   uint16_t hz_slot[FMAX + 8];
   uint32_t npatch;
+  uint32_t nhz;             // horizon edges found by the flood fill
 };
 
 __device__ __forceinline__ uint32_t fvert(uint32_t packed, int k) { return (packed >> (8 * k)) & 0xFFu; }
@@ -360,9 +361,13 @@ struct EpaWarp {
       P.fmark[start] = kVis;
       P.patch[0] = (uint16_t)start;
       P.npatch = 1;
+      P.nhz = 0;
     }
     __syncwarp();
-    // frontier rounds
+    // Frontier rounds over the visible patch.  Each patch face looks across
+    // its three edges; the neighbour's mark is final once read as visible /
+    // hidden or once a CAS settled it (ours or another lane's), so an edge
+    // whose neighbour ends hidden is a horizon edge and is recorded here.
     FCLG_EPA_PHASE(3);
     int lo = 0, hi = 1;
     for (int round = 0; round < FMAX && lo < hi; ++round) {
@@ -371,13 +376,28 @@ struct EpaWarp {
 #pragma unroll
         for (int e = 0; e < 3; ++e) {
           const uint32_t g = P.fadj[f][e];
-          const uint32_t m = P.fmark[g];
-          if (m == kVis || m == kHid) continue;
-          const float4 q = P.fn[g];
-          const bool visible = dot(ld3(q), w - W(fvert(P.fv[g], 0))) > kVisEps * tol;
-          if (atomicCAS(&P.fmark[g], m, visible ? kVis : kHid) == m && visible) {
-            const uint32_t slot = atomicAdd(&P.npatch, 1u);
-            if (slot < FMAX) P.patch[slot] = (uint16_t)g;
+          uint32_t m = P.fmark[g];
+          if (m != kVis && m != kHid) {
+            const float4 q = P.fn[g];
+            const bool visible = dot(ld3(q), w - W(fvert(P.fv[g], 0))) > kVisEps * tol;
+            const uint32_t want = visible ? kVis : kHid;
+            const uint32_t old = atomicCAS(&P.fmark[g], m, want);
+            if (old == m) {
+              m = want;
+              if (visible) {
+                const uint32_t slot = atomicAdd(&P.npatch, 1u);
+                if (slot < FMAX) P.patch[slot] = (uint16_t)g;
+              }
+            } else {
+              m = old;  // settled by another lane this expansion
+            }
+          }
+          if (m == kHid) {
+            const uint32_t o = atomicAdd(&P.nhz, 1u);
+            if (o < FMAX + 8) {
+              P.hz_s[o] = (uint16_t)f;
+              P.hz_e[o] = (uint8_t)e;
+            }
           }
         }
       }
@@ -387,30 +407,9 @@ struct EpaWarp {
       __syncwarp();
     }
     const int n_rem = hi;
+    const int n_hz = (int)P.nhz;
     FCLG_EPA_PHASE(4);
-    // horizon edges of the patch, gathered in patch order
-    int n_hz = 0;
-    for (int base = 0; base < n_rem; base += 32) {
-      const int k = base + (int)lane;
-      int h = 0;
-      uint32_t hmask = 0, f = 0;
-      if (k < n_rem) {
-        f = P.patch[k];
-#pragma unroll
-        for (int e = 0; e < 3; ++e)
-          if (P.fmark[P.fadj[f][e]] != kVis) { hmask |= 1u << e; ++h; }
-      }
-      int incl = h;
-#pragma unroll
-      for (int off = 1; off < 32; off <<= 1) {
-        const int t = __shfl_up_sync(0xFFFFFFFFu, incl, off);
-        if ((int)lane >= off) incl += t;
-      }
-      int o = n_hz + incl - h;
-      for (int e = 0; e < 3; ++e)
-        if ((hmask & (1u << e)) && o < FMAX + 8) { P.hz_s[o] = (uint16_t)f; P.hz_e[o] = (uint8_t)e; ++o; }
-      n_hz += __shfl_sync(0xFFFFFFFFu, incl, 31);
-    }
+    if (P.npatch > (uint32_t)FMAX) return 2;
     const int new_live = live - n_rem + n_hz;
     const int avail = fs_top + n_rem;
     const int fresh = n_hz > avail ? n_hz - avail : 0;
