@@ -194,21 +194,29 @@ def _time_queries(torch, ctx, d_pairs, n, flags, steps, warmup, stream, dev):
     return e0.elapsed_time(e1) / max(steps, 1), d_res.cpu().numpy().view(RESULT_DTYPE).copy()
 
 
-def warm_start_block(args, torch, dev, stream, local):
+WARM_CASES = {
+    # name: (training batch on held-out seeds, test batch, embedding classes)
+    "mixed": (lambda w: w.mixed(2_000_000, seed=w.SEED_BASE + 1001), lambda w, a: w.mixed(a.pairs),
+              lambda w: w.MIXED_CLASSES),
+    "arm": (lambda w: w.arm(9000, seed=w.SEED_BASE + 1003), lambda w, a: w.arm(10000), lambda w: w.ARM_CLASSES),
+    "pareto": (lambda w: w.pareto(2_000_000, seed=w.SEED_BASE + 1004), lambda w, a: w.pareto(),
+               lambda w: w.PARETO_CLASSES),
+}
+
+
+def warm_start_block(args, torch, dev, stream, local, names):
     """Learned warm start against plain initialisation: the model is trained on
     the GPU on plain-GJK directions of held-out seeds, then both runs are timed
-    on the test batch (same pairs, same device entry point)."""
+    on the test batch (same pairs, same device entry point, autotuned launch)."""
     from fclg import workloads
     from fclg.api import Context, WarmStart, direction_labels
     peak, peak_kind = bf16_peak()
-    cases = [
-        ("mixed", lambda: workloads.mixed(2_000_000, seed=workloads.SEED_BASE + 1001),
-         lambda: workloads.mixed(args.pairs), workloads.MIXED_CLASSES),
-        ("arm", lambda: workloads.arm(9000, seed=workloads.SEED_BASE + 1003),
-         lambda: workloads.arm(10000), workloads.ARM_CLASSES),
-    ]
     out = {}
-    for name, make_train, make_test, n_classes in cases:
+    for name in names:
+        mk_train, mk_test, mk_classes = WARM_CASES[name]
+        make_train = lambda: mk_train(workloads)
+        make_test = lambda: mk_test(workloads, args)
+        n_classes = mk_classes(workloads)
         ctx = Context(local)
         train = make_train()
         ctx.set_batch(train)
@@ -228,6 +236,9 @@ def warm_start_block(args, torch, dev, stream, local):
         ctx.set_warmstart(ws)
         n = test.n_pairs
         d_te = _to_dev(torch, test.pairs, dev)
+        d_tmp = torch.empty(n * 48, dtype=torch.uint8, device=dev)
+        tuning, _ = ctx.autotune(d_te.data_ptr(), n, d_tmp.data_ptr())
+        del d_tmp
         ms_p, rp = _time_queries(torch, ctx, d_te, n, 0, args.steps, args.warmup, stream, dev)
         ms_w, rw = _time_queries(torch, ctx, d_te, n, 4, args.steps, args.warmup, stream, dev)
         # the tcgen05 inference kernel alone
@@ -263,6 +274,7 @@ def warm_start_block(args, torch, dev, stream, local):
             "separation_diff_max": float(err.max()) if len(err) else 0.0,
             "mlp_kernel": "tcgen05 (TMEM accumulators, bulk-async weight staging)", "mlp_ms": ms_mlp,
             "mlp_tflops": tflops, "mlp_frac": tflops / peak, "mlp_peak_source": peak_kind,
+            "tuning": tuning,
         }
         ctx.close()
         ws.close()
@@ -439,6 +451,32 @@ def run_warmstart_kernel(args):
     return 0
 
 
+def rank_batch(workloads, workload, rank, pairs=N_PAIRS):
+    """This rank's batch: every rank draws its own seeded batch of the same
+    shape (weak scaling; pairs are independent, nothing is exchanged)."""
+    if workload == "mixed":
+        return workloads.mixed(pairs, seed=workloads.SEED_BASE + 1 + rank)
+    if workload == "arm":
+        return workloads.arm(100_000, seed=workloads.SEED_BASE + 3 + 100 * rank)
+    if workload == "pareto":
+        return workloads.pareto(seed=workloads.SEED_BASE + 4 + 100 * rank)
+    return workloads.plain_small(seed=workloads.SEED_BASE + 0 + 100 * rank)
+
+
+def max_over_ranks(torch, ms, dev, world):
+    """The slowest rank's time (every rank returns the same value)."""
+    if world <= 1:
+        return ms
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(n_per_rank, world, ms):
+    """Whole-job throughput: the units all ranks processed over the slowest rank's time."""
+    return n_per_rank * world / (ms * 1e-3)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -459,14 +497,7 @@ def main():
     from fclg import workloads
     from fclg.api import Context
     gen, algo_bytes, workload_text = CONVEX_WORKLOADS[args.workload]
-    if gen is None:
-        batch = workloads.mixed(args.pairs, seed=workloads.SEED_BASE + 1 + rank)  # weak scaling: own batch per rank
-    elif gen == "arm":
-        batch = workloads.arm(100_000, seed=workloads.SEED_BASE + 3 + 100 * rank)
-    elif gen == "pareto":
-        batch = workloads.pareto(seed=workloads.SEED_BASE + 4 + 100 * rank)
-    else:
-        batch = workloads.plain_small(seed=workloads.SEED_BASE + 0 + 100 * rank)
+    batch = rank_batch(workloads, args.workload, rank, args.pairs)
     n = batch.n_pairs
     ctx = Context(local)
     ctx.set_batch(batch)
@@ -520,6 +551,8 @@ def main():
             barrier()
             ms = total / args.steps
     launches = ctx.launch_count - launches0
+    ms = max_over_ranks(torch, ms, dev, world)
+    value = job_value(n, world, ms)
     graph_ms = None
     if n <= 65536 and world == 1:
         # small batches are launch-bound: the same query replayed as one CUDA graph
@@ -537,11 +570,6 @@ def main():
             total += e0.elapsed_time(e1)
         graph_ms = total / args.steps
         g.close()
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = n * world / (ms * 1e-3)
 
     # ---- per-pass kernel times for the roofline (same steps, events on the launch stream)
     ctx.set_profiling(True)
@@ -575,11 +603,8 @@ def main():
         e2e_step()
     barrier()
     e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = n * world / (e2e_ms * 1e-3)
+    e2e_ms = max_over_ranks(torch, e2e_ms, dev, world)
+    e2e_value = job_value(n, world, e2e_ms)
 
     if rank == 0:
         peak, peak_kind = peaks()
@@ -615,8 +640,9 @@ def main():
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 64, "d2h_bytes_per_step": n * 48},
             "clocks": clk.summary(),
         }
-        if args.workload == "mixed" and not args.no_warm:
-            line["config"]["warm_start"] = warm_start_block(args, torch, dev, stream, local)
+        if not args.no_warm and args.workload in ("mixed", "arm", "pareto"):
+            names = ["mixed", "arm"] if args.workload == "mixed" else [args.workload]
+            line["config"]["warm_start"] = warm_start_block(args, torch, dev, stream, local, names)
         print(json.dumps(line))
     ctx.close()
     if world > 1:

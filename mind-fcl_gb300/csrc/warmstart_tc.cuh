@@ -1,13 +1,14 @@
 // Warm-start inference on the 5th-generation tensor cores (tcgen05), included
 // by warmstart.cu after the model constants.
 //
-// One persistent CTA of four warps per SM; each tile is 128 pairs (the MMA's
-// M).  Per tile:
+// One persistent CTA of sixteen warps per SM; each tile is 128 pairs (the
+// MMA's M).  Per tile:
 //   features -> act (shared, BF16)                        all threads
 //   per layer: D (TMEM, FP32, 128 lanes x N columns) = act x W^T
 //              by tcgen05.mma kind::f16 issued by one thread, operands read
 //              from shared memory through matrix descriptors
-//   epilogue:  tcgen05.ld of the thread's row, + bias, GELU, BF16 -> act
+//   epilogue:  tcgen05.ld of 64 columns of the thread's row (four warps per
+//              TMEM lane quarter), + bias, GELU, BF16 -> act
 // Weights stream from global memory (already in the MMA's K-major
 // core-matrix layout, see tc_slot) into two 64 KB buffers with cp.async.bulk
 // on mbarrier transaction counts: W1 | W2 (two N halves) | W3 (two halves) |
@@ -26,7 +27,7 @@
 namespace fclg {
 namespace wsm {
 
-constexpr int kTcThreads = 128;
+constexpr int kTcThreads = 512;  // 16 warps: warp w reads TMEM lane quarter w % 4, columns 64 (w / 4) ..
 constexpr uint32_t kTcCols = 256;                      // TMEM columns: one 128 x 256 FP32 accumulator
 constexpr uint32_t kActBytes = 128u * kH * 2u;         // 64 KB
 constexpr uint32_t kBufBytes = 65536u;
@@ -135,13 +136,13 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   return *reinterpret_cast<const uint32_t*>(&h);
 }
 
-// Row r of a 128 x 256 FP32 accumulator (TMEM row address trow) -> + bias,
-// GELU, BF16 -> act in the operand layout.
+// Columns [cbeg, cbeg + 64) of row r of a 128 x 256 FP32 accumulator (TMEM
+// row address trow) -> + bias, GELU, BF16 -> act in the operand layout.
 __device__ __forceinline__ void tc_epilogue_hidden(uint32_t trow, const float* __restrict__ bias, unsigned char* act,
-                                                   int r) {
+                                                   int r, int cbeg) {
   unsigned char* row = act + (size_t)(r >> 3) * kGroupStride + (size_t)(r & 7) * 16;
 #pragma unroll 1
-  for (int c0 = 0; c0 < kH; c0 += 32) {
+  for (int c0 = cbeg; c0 < cbeg + 64; c0 += 32) {
     uint32_t v0[16], v1[16];
     tmem_ld16(trow + (uint32_t)c0, v0);
     tmem_ld16(trow + (uint32_t)c0 + 16u, v1);
@@ -174,6 +175,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   volatile int* s_abort = reinterpret_cast<volatile int*>(bars + 6);
   const int tid = threadIdx.x, warp = tid >> 5;
   const bool leader = tid == 0;
+  const int row = (warp & 3) * 32 + (tid & 31);  // TMEM lane (tile row) this thread reads
+  const int cbeg = (warp >> 2) * 64;              // its 64 accumulator columns
   const uint32_t bar_full[2] = {smem_u32(&bars[0]), smem_u32(&bars[1])};
   const uint32_t bar_mma = smem_u32(&bars[2]), bar_half = smem_u32(&bars[3]), bar_drain = smem_u32(&bars[4]);
   const uint32_t a_act = smem_u32(act);
@@ -193,7 +196,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t taddr = *s_taddr;
-  const uint32_t trow = taddr + ((uint32_t)(warp * 32) << 16);  // this warp's TMEM lane quarter
+  const uint32_t trow = taddr + ((uint32_t)((warp & 3) * 32) << 16);  // this warp's TMEM lane quarter
 
   const char* src = reinterpret_cast<const char*>(wt);
   const char* srcW1 = src + tW1 * 2;
@@ -237,9 +240,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const uint32_t n_tiles = (n + 127) / 128;
   if (leader && blockIdx.x < n_tiles) load(0, srcW1, (uint32_t)(kH * kIn * 2));
   for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-    // features of row tid
+    // features: four threads per row, one 8-column chunk each
     {
-      const uint32_t pid = tile * 128 + (uint32_t)tid;
+      const int fr = tid >> 2, chunk = tid & 3;
+      const uint32_t pid = tile * 128 + (uint32_t)fr;
       float q[16];
       uint32_t cls = 0;
       if (pid < n) {
@@ -255,14 +259,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         if (cls >= n_classes) cls = 0;
       }
       const bf16* e = wb + qE + (size_t)cls * kEmb;
-      uint32_t p[16];
+      uint32_t p[4];
 #pragma unroll
-      for (int j = 0; j < 16; ++j)
-        p[j] = pid < n ? pack_bf16(feature(q, e, 2 * j), feature(q, e, 2 * j + 1)) : 0u;
-      unsigned char* row = act + (size_t)(tid >> 3) * kGroupStride + (size_t)(tid & 7) * 16;
-#pragma unroll
-      for (int c = 0; c < 4; ++c)
-        *reinterpret_cast<uint4*>(row + (size_t)c * 128) = make_uint4(p[4 * c], p[4 * c + 1], p[4 * c + 2], p[4 * c + 3]);
+      for (int j = 0; j < 4; ++j) {
+        const int c = 8 * chunk + 2 * j;
+        p[j] = pid < n ? pack_bf16(feature(q, e, c), feature(q, e, c + 1)) : 0u;
+      }
+      unsigned char* dst = act + (size_t)(fr >> 3) * kGroupStride + (size_t)chunk * 128 + (size_t)(fr & 7) * 16;
+      *reinterpret_cast<uint4*>(dst) = make_uint4(p[0], p[1], p[2], p[3]);
     }
     end_stage();
     if (*s_abort) break;
@@ -276,7 +280,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         umma_commit(bar_mma);
       }
     }
-    if (all_wait_mma()) tc_epilogue_hidden(trow, params + oB1, act, tid);
+    if (all_wait_mma()) tc_epilogue_hidden(trow, params + oB1, act, row, cbeg);
     end_stage();
     if (*s_abort) break;
 
@@ -300,7 +304,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           else load(1, srcW4, (uint32_t)(16 * kH * 2));
         }
       }
-      if (all_wait_mma()) tc_epilogue_hidden(trow, params + (layer == 2 ? oB2 : oB3), act, tid);
+      if (all_wait_mma()) tc_epilogue_hidden(trow, params + (layer == 2 ? oB2 : oB3), act, row, cbeg);
       end_stage();
       if (*s_abort) break;
     }
@@ -314,11 +318,11 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         umma_commit(bar_mma);
       }
     }
-    if (all_wait_mma()) {
+    if (all_wait_mma() && warp < 4) {
       uint32_t v[16];
       tmem_ld16(trow, v);
       tmem_wait_ld();
-      const uint32_t pid = tile * 128 + (uint32_t)tid;
+      const uint32_t pid = tile * 128 + (uint32_t)row;
       if (pid < n) {
         float y0 = __uint_as_float(v[0]) + __ldg(params + oB4);
         float y1 = __uint_as_float(v[1]) + __ldg(params + oB4 + 1);
