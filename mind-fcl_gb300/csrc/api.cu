@@ -1,5 +1,5 @@
 // The C ABI of include/fclg.h: contexts, shape upload, and the batched
-// collide / distance queries over the two kernel passes of convex_query.cu.
+// collide / distance queries over the GJK and EPA passes (gjk_pass*.cu, epa_pass.cu).
 #include <algorithm>
 #include <cstdio>
 #include <cstring>

@@ -1,0 +1,161 @@
+// GJK pass of a convex query batch (kernel template; instantiated two lane
+// counts per translation unit, gjk_pass_l*.cu, so the units compile in
+// parallel): one group of LANES lanes per pair, GJK
+// boolean (or MPR for a boolean fcl::collide) and, for separated pairs, the GJK
+// separation distance; overlapping pairs are appended (warp-aggregated
+// atomics) to a compact work list with their final simplex for the EPA pass
+// (epa_pass.cu).  The two passes are stream-ordered with no host round trip
+// between them: the EPA grid reads the list length from device memory, so a
+// query can be captured into a CUDA graph.
+#pragma once
+#include "gjk.cuh"
+#include "kernels.h"
+#include "mpr.cuh"
+
+namespace fclg {
+
+namespace {
+
+__device__ __forceinline__ void write_simplex(float4* __restrict__ rec, uint32_t slot, const Simplex& s, int iters) {
+  float f[28];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    f[1 + 6 * i + 0] = s.a[i].x;
+    f[1 + 6 * i + 1] = s.a[i].y;
+    f[1 + 6 * i + 2] = s.a[i].z;
+    f[1 + 6 * i + 3] = s.b[i].x;
+    f[1 + 6 * i + 4] = s.b[i].y;
+    f[1 + 6 * i + 5] = s.b[i].z;
+  }
+  f[0] = __int_as_float(s.rank);
+  f[25] = __int_as_float(iters);
+  f[26] = 0.f;
+  f[27] = 0.f;
+  float4* r = rec + 7 * (size_t)slot;
+#pragma unroll
+  for (int k = 0; k < 7; ++k) r[k] = make_float4(f[4 * k], f[4 * k + 1], f[4 * k + 2], f[4 * k + 3]);
+}
+
+__device__ __forceinline__ uint32_t aggregated_slot(uint32_t* counter) {
+  const unsigned m = __activemask();
+  const unsigned lane = threadIdx.x & 31u;
+  const int leader = __ffs(m) - 1;
+  uint32_t base = 0;
+  if ((int)lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
+  base = __shfl_sync(m, base, leader);
+  return base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ void store_invalid(float4* out, uint32_t pid) {
+  store_result(out, pid, -1.f, mk3(0, 0, 1), mk3(0, 0, 0), mk3(0, 0, 0), kGjkFailed, 0, false, false);
+}
+
+}  // namespace
+
+#ifndef FCLG_GJK_MINB
+#define FCLG_GJK_MINB 4
+#endif
+template <int LANES>
+__global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_pass(BatchArgs b, QueryParams prm, EpaQueue q,
+                                                   const uint32_t* __restrict__ order,
+                                                   const uint32_t* __restrict__ range) {
+  uint32_t begin = 0, end = b.n_pairs;
+  if (range) {
+    begin = range[0];
+    end = range[1];
+  }
+  const Group<LANES> g = Group<LANES>::make();
+  const uint32_t stride = gridDim.x * (blockDim.x / LANES);
+  for (uint32_t item = begin + (blockIdx.x * blockDim.x + threadIdx.x) / LANES; item < end; item += stride) {
+    const uint32_t pid = order ? order[item] : item;
+    const PairDev pr = load_pair(b.pairs, pid);
+    if (pr.a >= b.n_shapes || pr.b >= b.n_shapes) {
+      if (g.lane == 0) store_invalid(b.results, pid);
+      continue;
+    }
+    MinkowskiSupport<LANES> sup;
+    sup.A = load_shape(b.shapes, pr.a);
+    sup.B = load_shape(b.shapes, pr.b);
+    sup.pose = pr.pose;
+    sup.verts = b.verts;
+    sup.g = g;
+    // GJKSolver's default guess (1, 0, 0), gjk_solver-inl.h:1129
+    const f3 plain = mk3(1.f, 0.f, 0.f);
+    int mpr_iters = 0;
+    if (prm.use_mpr) {
+      // fcl::collide without contact: MPR decides, GJK only when MPR fails
+      // (ShapeIntersectIndepImpl::run, gjk_solver-inl.h:86-97)
+      Mpr<MinkowskiSupport<LANES>> mpr{sup, prm.gjk_max_iter, prm.gjk_tol};
+      const f3 v0 = load_interior(b.shapes, pr.a, sup.A.type) - pr.pose.apply(load_interior(b.shapes, pr.b, sup.B.type));
+      const MprStatus ms = mpr.intersect(v0);
+      mpr_iters = mpr.iterations;
+      if (ms != MprStatus::Failed) {
+        if (g.lane == 0) {
+          const bool hit = ms == MprStatus::Intersect;
+          store_result(b.results, pid, 0.f, mk3(0, 0, 1), mk3(0, 0, 0), mk3(0, 0, 0),
+                       (hit ? kGjkIntersect : kGjkSeparated) | kStatusMpr, (uint32_t)mpr_iters, hit, hit);
+        }
+        continue;
+      }
+    }
+    Simplex s;
+    GjkOut o;
+    if (b.guess) {
+      // Learned direction first.  Overlapping pairs (their EPA must start
+      // from the plain simplex) and pairs without a separation certificate
+      // are rerun from the plain direction; both runs count as iterations.
+      const f3 guess = mk3(__ldg(b.guess + 3 * (size_t)pid), __ldg(b.guess + 3 * (size_t)pid + 1),
+                           __ldg(b.guess + 3 * (size_t)pid + 2));
+      o = gjk_evaluate(sup, -guess, prm.gjk_tol, prm.gjk_max_iter, prm.want_distance != 0, s);
+      const bool keep = (o.status == kGjkSeparated && (o.point_valid || !prm.want_distance)) ||
+                        (o.status == kGjkIntersect && !prm.want_epa);
+      if (!keep) {
+        const int warm_iters = o.iterations;
+        o = gjk_evaluate(sup, -plain, prm.gjk_tol, prm.gjk_max_iter, prm.want_distance != 0, s);
+        o.iterations += warm_iters;
+      }
+    } else {
+      o = gjk_evaluate(sup, -plain, prm.gjk_tol, prm.gjk_max_iter, prm.want_distance != 0, s);
+    }
+    if (g.lane != 0) continue;
+    if (o.status == kGjkIntersect) {
+      if (prm.want_epa) {
+        const uint32_t slot = aggregated_slot(q.count);
+        q.list[slot] = pid;
+        write_simplex(q.rec, slot, s, o.iterations);
+        continue;
+      }
+      store_result(b.results, pid, 0.f, mk3(0, 0, 1), mk3(0, 0, 0), mk3(0, 0, 0), kGjkIntersect,
+                   (uint32_t)o.iterations, true, true);
+      continue;
+    }
+    if (!prm.want_distance) {
+      store_result(b.results, pid, 0.f, mk3(0, 0, 1), mk3(0, 0, 0), mk3(0, 0, 0), o.status, (uint32_t)o.iterations,
+                   false, o.status == kGjkSeparated);
+      continue;
+    }
+    // shapeSignedDistance: valid only for a separation certificate with valid points
+    const bool ok = (o.status == kGjkSeparated) && o.point_valid;
+    const f3 dv = o.p1 - o.p0;
+    const float dist = ok ? nrm(dv) : -1.f;
+    f3 nrmv = normalized(dv);
+    if (!(sqn(nrmv) > 0.f)) nrmv = mk3(0, 0, 1);
+    store_result(b.results, pid, dist, nrmv, o.p0, o.p1, o.status, (uint32_t)o.iterations, false, ok);
+  }
+}
+
+
+// Launches gjk_pass<LANES> (defined in the translation unit that instantiates LANES).
+template <int LANES>
+cudaError_t launch_gjk_lanes(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q, const uint32_t* order,
+                             const uint32_t* range, int blocks, cudaStream_t st);
+
+#define FCLG_GJK_INSTANTIATE(L)                                                                              \
+  template <>                                                                                                \
+  cudaError_t launch_gjk_lanes<L>(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q,             \
+                                  const uint32_t* order, const uint32_t* range, int blocks, cudaStream_t st) { \
+    gjk_pass<L><<<blocks, 128, 0, st>>>(b, prm, q, order, range);                                            \
+    return cudaGetLastError();                                                                               \
+  }
+
+}  // namespace fclg
