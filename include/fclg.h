@@ -97,11 +97,18 @@ enum {
   FCLG_REQ_BOOLEAN_ONLY = 1u << 0,  /* collide flag only: no distance, no EPA */
   FCLG_REQ_NO_EPA = 1u << 1,        /* separation distance only; overlapping pairs get distance 0 */
   FCLG_REQ_WARM_START = 1u << 2,    /* seed GJK with the learned direction model (fclg_warmstart_*) */
-  FCLG_REQ_GJK_BOOLEAN = 1u << 3    /* boolean collide by GJK instead of MPR (the reference's boolean
+  FCLG_REQ_GJK_BOOLEAN = 1u << 3,   /* boolean collide by GJK instead of MPR (the reference's boolean
                                        fcl::collide runs MPR, falling back to GJK when MPR fails) */
+  FCLG_REQ_NO_ANALYTIC = 1u << 4    /* collide: sphere pairs by MPR / GJK+EPA instead of the closed-form
+                                       solvers fcl::collide dispatches to (sphere-sphere, -capsule,
+                                       -box, -cylinder; gjk_solver-inl.h:209-218) */
 };
-/* fclg_result.status bit 16: the boolean was decided by MPR. */
+/* fclg_result.status bit 16: the boolean was decided by MPR.  Bit 17: the
+   result came from a closed-form sphere-pair solver (contact normal, the
+   contact position +- depth / 2 along it as p_a / p_b; when apart, the
+   centre-based separation with p_a = p_b = 0). */
 #define FCLG_STATUS_MPR (1 << 16)
+#define FCLG_STATUS_ANALYTIC (1 << 17)
 
 typedef struct fclg_context fclg_context;
 

@@ -46,7 +46,7 @@ struct fclg_context {
   int gjk_lanes_large = 4;
   int large_hull = 128;
   int gjk_ctas_per_sm = 4;
-  int epa_ctas_per_sm = 5;
+  int epa_ctas_per_sm = 6;
   uint64_t launches = 0;
   // optional per-pass timing
   bool profiling = false;
@@ -196,6 +196,9 @@ fclg::QueryParams make_params(const fclg_request* req, bool distance_query) {
   // fcl::collide without contact runs MPR (gjk_solver-inl.h:86-97); a learned
   // warm start applies to GJK only, so it keeps the GJK boolean
   p.use_mpr = (!distance_query && boolean_only && !(fl & FCLG_REQ_WARM_START) && !(fl & FCLG_REQ_GJK_BOOLEAN)) ? 1 : 0;
+  // fcl::collide answers sphere pairs in closed form (gjk_solver-inl.h:209-218);
+  // shapeSignedDistance (the distance entry points) has no such path
+  p.analytic = (!distance_query && !(fl & FCLG_REQ_NO_ANALYTIC)) ? 1 : 0;
   return p;
 }
 

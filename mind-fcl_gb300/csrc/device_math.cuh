@@ -128,6 +128,8 @@ __device__ __forceinline__ PairDev load_pair(const float4* __restrict__ pairs, u
 enum : int32_t { kGjkIntersect = 0, kGjkSeparated = 1, kGjkNoProgress = 2, kGjkIterLimit = 3, kGjkFailed = 4 };
 // Result status bit: the boolean came from MPR (bits 0-7 then hold Intersect / Separated).
 constexpr int32_t kStatusMpr = 1 << 16;
+// Result status bit: the answer came from a closed-form sphere-pair solver.
+constexpr int32_t kStatusAnalytic = 1 << 17;
 enum : int32_t { kEpaFailed = 0, kEpaOK = 1, kEpaTouching = 2, kEpaIterLimit = 3, kEpaMallocFailed = 4 };
 
 // 48-byte fclg_result written as three float4 stores.
@@ -148,6 +150,7 @@ struct QueryParams {
   int epa_max_faces;
   int want_distance;  // 1: signed distance (GJK distance / EPA); 0: boolean only
   int use_mpr;        // boolean collide: MPR first, GJK when MPR fails
+  int analytic;       // collide: closed-form solvers for sphere pairs
   int want_epa;       // run EPA on overlapping pairs
 };
 

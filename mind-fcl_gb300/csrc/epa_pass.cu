@@ -72,10 +72,17 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) epa_pass(BatchArgs b, QueryP
   }
 }
 
-// Small layout: 128 faces / 128 vertices (~10 KB of shared memory per warp,
-// five 4-warp CTAs per SM); large layout: the reference's 256 faces (~18 KB per
-// warp, three 4-warp CTAs per SM).
-constexpr int kSmallF = 128, kSmallV = 128, kSmallWarps = 4, kSmallMinB = 5;
+// Small layout: 128 faces / 72 vertices (~8.4 KB of shared memory per warp,
+// six 4-warp CTAs per SM; a polytope of 128 faces has about 66 vertices);
+// large layout: the reference's 256 faces (~18 KB per warp, three 4-warp CTAs
+// per SM).
+#ifndef FCLG_EPA_SMALL_V
+#define FCLG_EPA_SMALL_V 72
+#endif
+#ifndef FCLG_EPA_SMALL_MINB
+#define FCLG_EPA_SMALL_MINB 6
+#endif
+constexpr int kSmallF = 128, kSmallV = FCLG_EPA_SMALL_V, kSmallWarps = 4, kSmallMinB = FCLG_EPA_SMALL_MINB;
 #ifndef FCLG_EPA_LARGE_MINB
 #define FCLG_EPA_LARGE_MINB 3
 #endif

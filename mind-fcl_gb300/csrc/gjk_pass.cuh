@@ -8,6 +8,7 @@
 // between them: the EPA grid reads the list length from device memory, so a
 // query can be captured into a CUDA graph.
 #pragma once
+#include "analytic.cuh"
 #include "gjk.cuh"
 #include "kernels.h"
 #include "mpr.cuh"
@@ -81,6 +82,23 @@ __global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_pass(BatchArgs b, Quer
     sup.g = g;
     // GJKSolver's default guess (1, 0, 0), gjk_solver-inl.h:1129
     const f3 plain = mk3(1.f, 0.f, 0.f);
+    if (prm.analytic) {
+      // fcl::collide: closed-form solvers for sphere pairs (gjk_solver-inl.h:209-218)
+      AnalyticContact ac;
+      if (analytic_contact(sup.A, sup.B, pr.pose, ac)) {
+        if (g.lane == 0) {
+          const int32_t st = (ac.hit ? kGjkIntersect : kGjkSeparated) | kStatusAnalytic;
+          if (ac.hit) {
+            const f3 half = ac.normal * (0.5f * ac.depth);
+            store_result(b.results, pid, -ac.depth, ac.normal, ac.pos + half, ac.pos - half, st, 0u, true, true);
+          } else {
+            store_result(b.results, pid, ac.separation, ac.normal, mk3(0, 0, 0), mk3(0, 0, 0), st, 0u, false,
+                         prm.want_distance != 0);
+          }
+        }
+        continue;
+      }
+    }
     int mpr_iters = 0;
     if (prm.use_mpr) {
       // fcl::collide without contact: MPR decides, GJK only when MPR fails

@@ -51,7 +51,7 @@ def _load():
         vp, i, d = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
         lib.orc_signed_distance.argtypes = [vp, i, vp, vp, i, vp, vp, i, i, d, i, i, d]
         lib.orc_signed_distance.restype = i
-        lib.orc_collide.argtypes = [vp, i, vp, vp, i, i, vp, i]
+        lib.orc_collide.argtypes = [vp, i, vp, vp, i, i, i, vp, i]
         lib.orc_collide.restype = i
         lib.orc_time_signed_distance.argtypes = [vp, i, vp, vp, i, vp, i]
         lib.orc_time_signed_distance.restype = d
@@ -113,12 +113,14 @@ def signed_distance(batch, guess=None, threads=None, gjk_max_iter=0, gjk_tol=0.0
     return out
 
 
-def collide(batch, want_contact=False, threads=None):
-    """fcl::collide on convex pairs (restatement): MPR boolean, or GJK+EPA contact."""
+def collide(batch, want_contact=False, threads=None, analytic=True):
+    """fcl::collide on shape pairs (restatement): the closed-form sphere-pair
+    solvers (analytic=True, as fcl::collide dispatches), else MPR boolean or
+    GJK+EPA contact."""
     lib = _load()
     s, v, p = _prep(batch)
     out = np.zeros(len(p), RESULT_DTYPE)
-    rc = lib.orc_collide(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), int(want_contact), _ptr(out),
+    rc = lib.orc_collide(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), int(want_contact), int(analytic), _ptr(out),
                          threads or default_threads())
     assert rc == 0
     return out

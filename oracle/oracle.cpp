@@ -12,6 +12,7 @@
 #include <thread>
 #include <vector>
 
+#include "orc_analytic.hpp"
 #include "orc_convex.hpp"
 #include "orc_mesh.hpp"
 
@@ -155,8 +156,12 @@ int orc_signed_distance(const void* shapes, int n_shapes, const float* verts, co
 
 // fcl::collide on a convex pair (gjk_solver-inl.h:70-137): want_contact = 0 is
 // the boolean request (MPR, GJK fallback); 1 is useDefaultPenetration (GJK+EPA).
+// fcl::collide on a shape pair (ShapeIntersectIndepImpl::run): the closed-form
+// solvers for sphere pairs when use_analytic (gjk_solver-inl.h:209-218),
+// otherwise MPR (boolean) or GJK + EPA (contact).  Analytic results carry
+// gjk_status 20, the contact normal and pos +- depth / 2 along it as p0 / p1.
 int orc_collide(const void* shapes, int n_shapes, const float* verts, const void* pairs, int n_pairs,
-                int want_contact, OrcResult* out, int n_threads) {
+                int want_contact, int use_analytic, OrcResult* out, int n_threads) {
   if (n_pairs < 0 || n_shapes < 0) return -1;
   const auto sh = makeShapes((const ShapeRec*)shapes, n_shapes, verts);
   const PairRec* pr = (const PairRec*)pairs;
@@ -164,6 +169,19 @@ int orc_collide(const void* shapes, int n_shapes, const float* verts, const void
   parallelFor(n_pairs, n_threads, [&](int b, int e) {
     for (int i = b; i < e; ++i) {
       const orc::MinkDiff md = makeDiff(sh, pr[i]);
+      orc::AContact ac;
+      if (use_analytic && orc::analyticIntersect(*md.s0, *md.s1, md.to0, ac)) {
+        orc::QueryOut q;
+        q.ok = ac.hit;
+        q.gjk_status = 20;
+        q.distance = ac.hit ? -ac.depth : ac.separation;
+        q.p0 = ac.pos + ac.normal * (0.5 * ac.depth);
+        q.p1 = ac.pos - ac.normal * (0.5 * ac.depth);
+        fill(out[i], q, true);
+        if (ac.hit)
+          for (int k = 0; k < 3; ++k) out[i].normal[k] = ac.normal[k];
+        continue;
+      }
       fill(out[i], orc::intersect(md, sp, want_contact != 0, nullptr), true);
     }
   });

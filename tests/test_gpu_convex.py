@@ -104,12 +104,53 @@ def test_collide_vs_reference_golden(gpu_ctx, name):
     sd = g[name + "/signed_distance"]
     outside = np.abs(sd["distance"]) > BAND
     assert np.sum((got["collide"] != ref["ok"]) & outside) == 0
-    # with penetration: one contact per colliding pair
-    got_c = gpu_ctx.collide(b.pairs)
+    # with penetration: one contact per colliding pair, by GJK + EPA as the
+    # golden reference run computed it (the closed-form sphere solvers are
+    # checked against the oracle in test_collide_sphere_pairs_closed_form)
+    NO_ANALYTIC = 16
+    got_c = gpu_ctx.collide(b.pairs, make_request(flags=NO_ANALYTIC))
     ref_c = g[name + "/collide_contact"]
     hit = (ref_c["ok"] == 1) & (got_c["ok"] == 1) & (ref_c["distance"] < -1e-5)
     err = np.abs(got_c["distance"][hit] - ref_c["distance"][hit])
     assert np.mean(err <= 1e-5) >= 0.99
+
+
+def test_collide_sphere_pairs_closed_form(gpu_ctx, oracle_lib):
+    """fcl::collide's closed-form sphere solvers (sphere-sphere / capsule / box /
+    cylinder, either order): GPU FP32 against the FP64 restatement.  Flags equal
+    outside the 1e-6 m band; depth within 1e-5 m, contact position within
+    5e-5 m (the capsule and cylinder positions are formed as differences of
+    FP32 terms about 1 m long) and normal within 1e-3 rad, except
+    normals of nearly concentric spheres (|c2 - c1| < 1e-3 m), which are
+    ill-defined."""
+    ANALYTIC_BIT = 1 << 17
+    b = workloads.mixed(60000, seed=workloads.SEED_BASE + 77)
+    gpu_ctx.set_batch(b)
+    got = gpu_ctx.collide(b.pairs)
+    ref = oracle_lib.collide(b, want_contact=True)
+    an = ref["gjk_status"] == 20
+    assert an.mean() > 0.2
+    assert np.array_equal((got["status"] & ANALYTIC_BIT) != 0, an)
+    sd = oracle_lib.signed_distance(b)
+    outside = np.abs(sd["distance"]) > BAND
+    assert np.sum((got["collide"] != ref["ok"]) & an & outside) == 0
+    hit = an & (ref["ok"] == 1) & (got["collide"] == 1)
+    assert np.max(np.abs(got["distance"][hit] - ref["distance"][hit])) <= 1e-5
+    pos_g = 0.5 * (got["p_a"][hit] + got["p_b"][hit])
+    pos_r = 0.5 * (ref["p0"][hit] + ref["p1"][hit])
+    assert np.max(np.linalg.norm(pos_g - pos_r, axis=1)) <= 5e-5
+    cosang = np.clip(np.sum(got["normal"][hit] * ref["normal"][hit], axis=1), -1, 1)
+    centre = np.linalg.norm(b.pairs["trans"][hit], axis=1)
+    ok_normal = np.arccos(cosang) <= 1e-3
+    assert np.all(ok_normal | (centre < 1e-3))
+    # the analytic path gives the same flags as the MPR boolean
+    boolean = gpu_ctx.collide(b.pairs, make_request_flags(1))
+    assert np.sum((boolean["collide"] != got["collide"]) & outside) == 0
+
+
+def make_request_flags(flags):
+    from fclg.api import make_request
+    return make_request(flags=flags)
 
 
 @pytest.mark.parametrize("workload,n", [("mixed", 60000), ("pareto", 60000)])
@@ -118,12 +159,12 @@ def test_boolean_collide_mpr_vs_oracle(gpu_ctx, oracle_lib, workload, n):
     restated reference's MPR, and against the GJK boolean; flags identical
     outside the 1e-6 m band around contact."""
     from fclg.api import make_request
-    BOOLEAN, GJK_BOOLEAN, MPR_BIT = 1, 8, 1 << 16
+    BOOLEAN, GJK_BOOLEAN, NO_ANALYTIC, MPR_BIT = 1, 8, 16, 1 << 16
     b = getattr(workloads, workload)(n)
     gpu_ctx.set_batch(b)
-    got = gpu_ctx.collide(b.pairs, make_request(flags=BOOLEAN))
-    gjk = gpu_ctx.collide(b.pairs, make_request(flags=BOOLEAN | GJK_BOOLEAN))
-    ref = oracle_lib.collide(b)
+    got = gpu_ctx.collide(b.pairs, make_request(flags=BOOLEAN | NO_ANALYTIC))
+    gjk = gpu_ctx.collide(b.pairs, make_request(flags=BOOLEAN | GJK_BOOLEAN | NO_ANALYTIC))
+    ref = oracle_lib.collide(b, analytic=False)
     sd = oracle_lib.signed_distance(b)
     outside = np.abs(sd["distance"]) > BAND
     assert np.sum((got["collide"] != ref["ok"]) & outside) == 0

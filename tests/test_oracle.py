@@ -42,8 +42,9 @@ def _golden(name):
 def test_oracle_matches_reference_golden(oracle_lib, name):
     b, g = _golden(name)
     assert np.all(_same(oracle_lib.signed_distance(b, threads=2), g[name + "/signed_distance"]))
-    assert np.all(_same(oracle_lib.collide(b, False, threads=2), g[name + "/collide_bool"]))
-    assert np.all(_same(oracle_lib.collide(b, True, threads=2), g[name + "/collide_contact"]))
+    # the goldens ran the reference's cvx_collide path (MPR / GJK+EPA) for every pair
+    assert np.all(_same(oracle_lib.collide(b, False, threads=2, analytic=False), g[name + "/collide_bool"]))
+    assert np.all(_same(oracle_lib.collide(b, True, threads=2, analytic=False), g[name + "/collide_contact"]))
 
 
 def test_oracle_matches_reference_build(oracle_lib):
@@ -51,7 +52,7 @@ def test_oracle_matches_reference_build(oracle_lib):
         pytest.skip("oracle/_ref not built (reference sources absent)")
     for b in (workloads.mixed(3000, seed=7), workloads.pareto(3000, seed=8)):
         assert np.all(_same(oracle_lib.signed_distance(b), oracle_lib.ref_signed_distance(b)))
-        assert np.all(_same(oracle_lib.collide(b, True), oracle_lib.ref_collide(b, True)))
+        assert np.all(_same(oracle_lib.collide(b, True, analytic=False), oracle_lib.ref_collide(b, True)))
 
 
 def _rot_from_euler(rng, n):
@@ -285,3 +286,49 @@ def test_convex_support_known_answers(oracle_lib):
     o = oracle_lib.signed_distance(_batch(s, verts, p))
     expect = [4 - 0.1, 4 - 0.1, 4 - 0.1, 5 - 0.1, np.linalg.norm(dirs[4] - np.array([1, 1, 1]) / 3) - 0.1]
     assert np.allclose(o["distance"], expect, atol=1e-5)
+
+
+def test_analytic_sphere_solvers_known_answers(oracle_lib):
+    """The oracle's closed-form sphere solvers (oracle/orc_analytic.hpp, the
+    ones fcl::collide dispatches to) against hand-computed contacts:
+    sphere-sphere, sphere-box (face, edge, centre inside), sphere-capsule,
+    sphere-cylinder (cap, barrel, inside) and reversed orders."""
+    S, B, C, Y = SPHERE, BOX, CAPSULE, CYLINDER
+    shapes = np.zeros(8, SHAPE_DTYPE)
+    shapes["type"] = [S, S, B, C, Y, S, S, S]
+    shapes["param"][0, 0] = 0.5                    # sphere r 0.5
+    shapes["param"][1, 0] = 0.3                    # sphere r 0.3
+    shapes["param"][2, :3] = [2.0, 2.0, 2.0]       # box, half extent 1
+    shapes["param"][3, :2] = [0.2, 1.0]            # capsule r 0.2, lz 1
+    shapes["param"][4, :2] = [0.4, 1.0]            # cylinder r 0.4, lz 1
+    shapes["param"][5, 0] = 0.2
+    shapes["param"][6, 0] = 0.2
+    shapes["param"][7, 0] = 0.2
+    cases = [
+        # (a, b, trans of b, hit, depth, normal)
+        (0, 1, [0.7, 0, 0], True, 0.1, [1, 0, 0]),          # sphere-sphere
+        (0, 1, [0.81, 0, 0], False, None, None),
+        (0, 2, [1.3, 0, 0], True, 0.2, [1, 0, 0]),          # sphere outside the box's -x face
+        (0, 2, [0, 0, -1.3], True, 0.2, [0, 0, -1]),
+        (0, 2, [0.8, 0.0, 0.0], True, 0.7, [1, 0, 0]),      # centre inside, nearest face -x: n into box = +x
+        (2, 5, [1.1, 0, 0], True, 0.1, [1, 0, 0]),          # box-sphere (reversed), sphere beyond +x face
+        (0, 3, [0.6, 0, 0.3], True, 0.1, [1, 0, 0]),        # sphere-capsule, barrel side
+        (0, 3, [0, 0, 1.15], True, 0.05, [0, 0, 1]),        # sphere-capsule, end cap
+        (0, 4, [0.8, 0, 0], True, 0.1, [1, 0, 0]),          # sphere-cylinder barrel
+        (0, 4, [0, 0, 0.95], True, 0.05, [0, 0, 1]),        # sphere-cylinder cap
+        (4, 6, [0.3, 0, 0], True, 0.3, [1, 0, 0]),          # cylinder-sphere, centre inside, nearer the barrel
+    ]
+    p = np.zeros(len(cases), PAIR_DTYPE)
+    for i, (a, b, t, *_ ) in enumerate(cases):
+        p[i]["shape_a"], p[i]["shape_b"] = a, b
+        p[i]["rot"] = np.eye(3).ravel()
+        p[i]["trans"] = t
+    from fclg import workloads
+    batch = workloads.Batch("analytic", shapes, np.zeros((0, 4), np.float32), p)
+    r = oracle_lib.collide(batch, want_contact=True)
+    assert np.all(r["gjk_status"] == 20)
+    for i, (a, b, t, hit, depth, normal) in enumerate(cases):
+        assert bool(r["ok"][i]) == hit, i
+        if hit:
+            assert abs(-r["distance"][i] - depth) < 1e-6, (i, r["distance"][i])  # FP32 inputs
+            assert np.allclose(r["normal"][i], normal, atol=1e-6), (i, r["normal"][i])
