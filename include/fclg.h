@@ -213,6 +213,22 @@ int fclg_warmstart_train(fclg_warmstart* model, const fclg_pair* d_pairs, const 
    then fail).  The model must outlive its use by the context. */
 int fclg_set_warmstart(fclg_context* ctx, fclg_warmstart* model);
 
+/* fcl::collide with CollisionRequest::useDirectedPenetration
+   (collisionPenetrationMPR, collision_penetration-inl.h:106-250): the boolean
+   collide (closed form for sphere pairs, MPR with the GJK fallback otherwise),
+   then for colliding pairs MPR::RunDirectedPenetration (cvx_collide/mpr.hpp:
+   495-701) along dirs[i] (float[n][3], unit: shape b's escape direction in
+   shape a's frame).  Per pair: collide; distance = -(depth along the
+   direction) and ok = 1 when the directed run succeeded; normal = the
+   direction; p_a / p_b the directed witness points; status bit 18
+   (FCLG_STATUS_DIRECTED) with the directed status + 1 in bits 8-15 (0 OK,
+   1 Failed, 2 FailedNoIntersect, 3 iteration limit). */
+#define FCLG_STATUS_DIRECTED (1 << 18)
+int fclg_collide_directed(fclg_context* ctx, const fclg_pair* pairs, uint32_t n_pairs, const float* dirs,
+                          const fclg_request* req, fclg_result* results);
+int fclg_collide_directed_device(fclg_context* ctx, const fclg_pair* d_pairs, uint32_t n_pairs, const float* d_dirs,
+                                 const fclg_request* req, fclg_result* d_results, void* stream);
+
 /* Launch shape of the query passes.  Pairs are first sorted on the device by
    shape class (box / sphere / capsule / cylinder / convex hull, hulls split at
    large_hull_vertices); pairs without a large hull run the GJK pass with

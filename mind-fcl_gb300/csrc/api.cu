@@ -2,6 +2,7 @@
 // collide / distance queries over the GJK and EPA passes (gjk_pass*.cu, epa_pass.cu).
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -79,6 +80,17 @@ namespace {
 int fail(fclg_context* c, int code, const std::string& msg) {
   if (c) c->err = msg;
   return code;
+}
+
+// The CUDA runtime is shared with the rest of the process (PyTorch, the
+// caller): a non-sticky error some other caller left pending would otherwise
+// be reported by this library's first launch check.  Entry points that launch
+// clear it first; sticky errors (a faulted context) cannot be cleared and are
+// still reported by the calls that follow.
+inline void clear_pending_error() {
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess && getenv("FCLG_DEBUG_PENDING"))
+    fprintf(stderr, "fclg: cleared a pending CUDA error at entry: %s\n", cudaGetErrorString(e));
 }
 
 int cuda_fail(fclg_context* c, cudaError_t e, const char* what) {
@@ -199,6 +211,7 @@ fclg::QueryParams make_params(const fclg_request* req, bool distance_query) {
   // fcl::collide answers sphere pairs in closed form (gjk_solver-inl.h:209-218);
   // shapeSignedDistance (the distance entry points) has no such path
   p.analytic = (!distance_query && !(fl & FCLG_REQ_NO_ANALYTIC)) ? 1 : 0;
+  p.directed = 0;
   return p;
 }
 
@@ -222,6 +235,7 @@ int run_query(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_
   if (!d_pairs || !d_results) return fail(c, FCLG_E_INVALID, "null pair or result pointer");
   if (!c->shapes) return fail(c, FCLG_E_NO_SHAPES, "no shapes set");
   FCLG_CUDA(c, cudaSetDevice(c->device));
+  clear_pending_error();
   const fclg::QueryParams prm = make_params(req, distance_query);
   if (prm.want_epa) {
     const int rc = ensure_epa(c, n);
@@ -541,6 +555,7 @@ int fclg_mesh_collide_device(fclg_context* c, const fclg_mesh* a, const fclg_mes
   m.pairs = d_pairs;
   m.status = d_status;
   const int blocks = c->num_sms * 8;
+  clear_pending_error();
   FCLG_CUDA(c, fclg::launch_mesh_collide(m, blocks, static_cast<cudaStream_t>(stream)));
   c->launches += 1;
   return FCLG_OK;
@@ -683,6 +698,7 @@ extern "C" int fclg_distance_device_static(fclg_context* c, const fclg_pair* d_p
   if (req && (req->flags & FCLG_REQ_WARM_START))
     return fail(c, FCLG_E_INVALID, "fclg_distance_device_static: FCLG_REQ_WARM_START needs per-pair scratch");
   FCLG_CUDA(c, cudaSetDevice(c->device));
+  clear_pending_error();
   unsigned char* base = nullptr;
   const int rc = static_scratch(c, &base);
   if (rc) return rc;
@@ -707,6 +723,67 @@ extern "C" int fclg_distance_device_static(fclg_context* c, const fclg_pair* d_p
     FCLG_CUDA(c, fclg::launch_epa(b, prm, q, ovf, c->num_sms, c->epa_ctas_per_sm, st));
     c->launches += prm.epa_max_faces > 128 ? 2 : 1;
   }
+  return FCLG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// fcl::collide in the directed penetration mode (useDirectedPenetration).
+// ---------------------------------------------------------------------------
+
+namespace {
+
+int run_directed(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const float* d_dirs, const fclg_request* req,
+                 fclg_result* d_results, cudaStream_t st) {
+  if (!c) return FCLG_E_INVALID;
+  if (n == 0) return FCLG_OK;
+  if (!d_pairs || !d_dirs || !d_results) return fail(c, FCLG_E_INVALID, "null pair, direction or result pointer");
+  if (!c->shapes) return fail(c, FCLG_E_NO_SHAPES, "no shapes set");
+  if (req && (req->flags & FCLG_REQ_WARM_START))
+    return fail(c, FCLG_E_INVALID, "directed penetration takes no warm start");
+  FCLG_CUDA(c, cudaSetDevice(c->device));
+  clear_pending_error();
+  fclg::QueryParams prm = make_params(req, false);
+  prm.want_epa = 0;
+  prm.use_mpr = 0;
+  prm.analytic = 0;
+  prm.directed = 1;
+  fclg::BatchArgs b;
+  b.shapes = c->shapes;
+  b.verts = c->verts;
+  b.pairs = reinterpret_cast<const float4*>(d_pairs);
+  b.guess = d_dirs;
+  b.results = reinterpret_cast<float4*>(d_results);
+  b.n_pairs = n;
+  b.n_shapes = c->n_shapes;
+  FCLG_CUDA(c, fclg::launch_directed(b, prm, c->num_sms * c->gjk_ctas_per_sm, st));
+  c->launches += 1;
+  return FCLG_OK;
+}
+
+}  // namespace
+
+extern "C" int fclg_collide_directed_device(fclg_context* c, const fclg_pair* d_pairs, uint32_t n,
+                                            const float* d_dirs, const fclg_request* req, fclg_result* d_results,
+                                            void* stream) {
+  return run_directed(c, d_pairs, n, d_dirs, req, d_results, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int fclg_collide_directed(fclg_context* c, const fclg_pair* pairs, uint32_t n, const float* dirs,
+                                     const fclg_request* req, fclg_result* results) {
+  if (!c) return FCLG_E_INVALID;
+  if (n == 0) return FCLG_OK;
+  if (!pairs || !dirs || !results) return fail(c, FCLG_E_INVALID, "null pair, direction or result pointer");
+  int rc = ensure_io(c, n);
+  if (!rc) rc = ensure_guess(c, n);
+  if (rc) return rc;
+  FCLG_CUDA(c, cudaMemcpyAsync(c->io_pairs, pairs, (size_t)n * sizeof(fclg_pair), cudaMemcpyHostToDevice, c->stream));
+  FCLG_CUDA(c, cudaMemcpyAsync(c->guess, dirs, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  rc = run_directed(c, static_cast<const fclg_pair*>(c->io_pairs), n, c->guess, req,
+                    static_cast<fclg_result*>(c->io_results), c->stream);
+  if (rc) return rc;
+  FCLG_CUDA(c, cudaMemcpyAsync(results, c->io_results, (size_t)n * sizeof(fclg_result), cudaMemcpyDeviceToHost,
+                               c->stream));
+  FCLG_CUDA(c, cudaStreamSynchronize(c->stream));
   return FCLG_OK;
 }
 

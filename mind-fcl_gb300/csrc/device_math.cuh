@@ -130,6 +130,8 @@ enum : int32_t { kGjkIntersect = 0, kGjkSeparated = 1, kGjkNoProgress = 2, kGjkI
 constexpr int32_t kStatusMpr = 1 << 16;
 // Result status bit: the answer came from a closed-form sphere-pair solver.
 constexpr int32_t kStatusAnalytic = 1 << 17;
+// Result status bit: MPR directed penetration ran (bits 8-15 its status + 1).
+constexpr int32_t kStatusDirected = 1 << 18;
 enum : int32_t { kEpaFailed = 0, kEpaOK = 1, kEpaTouching = 2, kEpaIterLimit = 3, kEpaMallocFailed = 4 };
 
 // 48-byte fclg_result written as three float4 stores.
@@ -151,6 +153,7 @@ struct QueryParams {
   int want_distance;  // 1: signed distance (GJK distance / EPA); 0: boolean only
   int use_mpr;        // boolean collide: MPR first, GJK when MPR fails
   int analytic;       // collide: closed-form solvers for sphere pairs
+  int directed;       // collide with MPR directed penetration along BatchArgs::guess (directed_pass.cu)
   int want_epa;       // run EPA on overlapping pairs
 };
 

@@ -46,6 +46,8 @@ cudaError_t launch_bucketing(const BatchArgs& b, const BucketScratch& s, uint32_
 // `blocks` CTAs (0: one CTA per 128 lanes of work, not persistent).
 cudaError_t launch_gjk(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q, int lanes,
                        const uint32_t* order, const uint32_t* range, int blocks, cudaStream_t st);
+// fcl::collide with directed penetration along b.guess (directed_pass.cu).
+cudaError_t launch_directed(const BatchArgs& b, const QueryParams& prm, int blocks, cudaStream_t st);
 cudaError_t prepare_epa();
 // EPA over q's list: the small-polytope pass, then (when max_faces exceeds it)
 // the large pass over the pairs ovf collected.  ovf.count must be zero and

@@ -94,6 +94,80 @@ struct Mpr {
     }
   }
 
+  // Directed penetration, mpr.hpp:495-595 and :606-701: the depth of the
+  // Minkowski difference along the unit direction d (shape b's escape
+  // direction in a's frame) and witness points p0 / p1.  Returns 0 OK,
+  // 1 Failed, 2 FailedNoIntersect, 3 FailedRefinementIterationLimit.
+  __device__ int directed(f3 d, float& depth, f3& p0, f3& p1) {
+    iterations = 0;
+    const f3 v0 = -d;
+    f3 d1 = d;
+    f3 v1 = support(d1);
+    if (dot(d1, v1) < 0.f) return 2;
+    f3 d2 = cross(v0, v1);
+    if (absnorm(d2) <= absnorm(v1) * tol) {
+      depth = dot(v1, d);
+      sup(d1, p0, p1);
+      return 0;
+    }
+    f3 v2 = support(d2);
+    if (dot(d2, v2) < 0.f) return 2;
+    f3 d3 = cross(v1, v2);
+    if (dot(d3, v0) > 0.f) {
+      f3 t = v1; v1 = v2; v2 = t;
+      t = d1; d1 = d2; d2 = t;
+      d3 = -d3;
+    }
+    f3 v3 = support(d3);
+    if (dot(d3, v3) < 0.f) return 2;
+    const float m2 = fmaxf(sqn(v1), fmaxf(sqn(v2), sqn(v3)));
+    const f3 v0s = v0 * sqrtf(m2);
+    const int fp = find_portal(v0s, v1, v2, v3, d1, d2, d3);
+    if (fp == 0) return 1;
+    if (fp == 1) return 2;
+    for (int it = 0; it < max_iter; ++it) {
+      ++iterations;
+      f3 n = cross(v2 - v1, v3 - v1);
+      if (dot(n, d) < 0.f) {
+        f3 t = v2; v2 = v3; v3 = t;
+        t = d2; d2 = d3; d3 = t;
+        n = -n;
+      }
+      const f3 v4 = support(n);
+      if (dot(v4, n) < 0.f) return 2;
+      if (fabsf(dot(v4 - v1, n)) < tol * absnorm(n)) {
+        // finalizeDirectedPenetrationResult (mpr.hpp:606-701) with v4
+        const float ndd = dot(d, n);
+        if (!(fabsf(ndd) > 0.f)) {
+          const float a1 = dot(v1, d), a2 = dot(v2, d), a3 = dot(v3, d);
+          f3 db = d1;
+          depth = a1;
+          if (a2 > depth) { depth = a2; db = d2; }
+          if (a3 > depth) { depth = a3; db = d3; }
+          sup(db, p0, p1);
+          return 0;
+        }
+        const float dist_v123 = dot(v1, n) / ndd;
+        depth = dot(v4, n) / ndd;
+        const f3 o_proj = d * dist_v123;
+        const f3 a12 = v2 - v1, a13 = v3 - v1;
+        const float area = nrm(cross(a12, a13));
+        const float w2 = nrm(cross(a13, v1 - o_proj)) / area;
+        const float w3 = nrm(cross(a12, v1 - o_proj)) / area;
+        const float w1 = 1.f - w2 - w3;
+        f3 pa1, pb1, pa2, pb2, pa3, pb3;
+        sup(d1, pa1, pb1);
+        sup(d2, pa2, pb2);
+        sup(d3, pa3, pb3);
+        p0 = (pa1 * w1 + pa2 * w2) + pa3 * w3;
+        p1 = (pb1 * w1 + pb2 * w2) + pb3 * w3;
+        return 0;
+      }
+      update_portal(v0s, v4, n, v1, v2, v3, d1, d2, d3);
+    }
+    return 3;
+  }
+
   // mpr.hpp:33-185.  v0 is the interior point of the Minkowski difference.
   __device__ MprStatus intersect(f3 v0) {
     iterations = 0;

@@ -25,6 +25,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -677,6 +678,7 @@ namespace {
 cudaError_t launch_infer(fclg_warmstart* w, const float4* pairs, uint32_t n, float* out, int normalize, bool legacy,
                          cudaStream_t st) {
   if (n == 0) return cudaSuccess;
+  (void)cudaGetLastError();  // a non-sticky error another caller left pending is not ours
   const uint32_t tiles = (n + kTile - 1) / kTile;
   const uint32_t blocks = std::min<uint32_t>(tiles, (uint32_t)w->num_sms);
   if (legacy)
@@ -823,6 +825,7 @@ int fclg_warmstart_forward(fclg_warmstart* w, const fclg_pair* d_pairs, uint32_t
   if (n == 0) return FCLG_OK;
   if (!d_pairs || !d_y) return ws_fail(w, FCLG_E_INVALID, "null pair or output pointer");
   WS_CUDA(w, cudaSetDevice(w->device));
+  (void)cudaGetLastError();  // not ours: left pending by another caller
   int rc = ensure_train(w, n);
   if (rc) return rc;
   const cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -841,6 +844,7 @@ int fclg_warmstart_gradient(fclg_warmstart* w, const fclg_pair* d_pairs, const f
   if (!w) return FCLG_E_INVALID;
   if (!d_pairs || !d_labels || !grad || n == 0) return ws_fail(w, FCLG_E_INVALID, "bad gradient arguments");
   WS_CUDA(w, cudaSetDevice(w->device));
+  (void)cudaGetLastError();  // not ours: left pending by another caller
   int rc = ensure_train(w, n);
   if (rc) return rc;
   const uint32_t M = (n + 63) / 64 * 64;
@@ -868,6 +872,7 @@ int fclg_warmstart_train(fclg_warmstart* w, const fclg_pair* d_pairs, const floa
   const float lr1 = cfg->lr_final > 0.f ? cfg->lr_final : lr0 * 0.05f;
   if (batch % 64 != 0 || batch > (1u << 20)) return ws_fail(w, FCLG_E_INVALID, "batch must be a multiple of 64");
   WS_CUDA(w, cudaSetDevice(w->device));
+  (void)cudaGetLastError();  // not ours: left pending by another caller
   int rc = ensure_train(w, batch);
   if (rc) return rc;
   cudaStream_t st = nullptr;

@@ -29,6 +29,7 @@ EXPORTS = [
     "fclg_warmstart_get_params", "fclg_warmstart_set_params", "fclg_warmstart_predict", "fclg_warmstart_forward",
     "fclg_warmstart_gradient", "fclg_warmstart_train", "fclg_set_warmstart", "fclg_warmstart_status",
     "fclg_autotune", "fclg_graph_create", "fclg_graph_launch", "fclg_graph_destroy",
+    "fclg_collide_directed", "fclg_collide_directed_device",
 ]
 
 STATIC_MAX_PAIRS = 16384  # FCLG_STATIC_MAX_PAIRS
@@ -135,6 +136,10 @@ def load_library(path=LIB_PATH):
     lib.fclg_warmstart_train.restype = i32
     lib.fclg_set_warmstart.argtypes = [vp, vp]
     lib.fclg_set_warmstart.restype = i32
+    lib.fclg_collide_directed.argtypes = [vp, vp, u32, vp, vp, vp]
+    lib.fclg_collide_directed.restype = i32
+    lib.fclg_collide_directed_device.argtypes = [vp, vp, u32, vp, vp, vp, vp]
+    lib.fclg_collide_directed_device.restype = i32
     lib.fclg_autotune.argtypes = [vp, vp, u32, vp, vp, i32, ctypes.POINTER(Tuning), ctypes.POINTER(ctypes.c_float)]
     lib.fclg_autotune.restype = i32
     lib.fclg_graph_create.argtypes = [vp, vp, u32, vp, vp, i32, ctypes.POINTER(vp)]
@@ -273,6 +278,18 @@ class Context:
     @property
     def launch_count(self):
         return int(self.lib.fclg_launch_count(self.h))
+
+    def collide_directed(self, pairs, dirs, request=None):
+        """fcl::collide, directed penetration mode, host arrays: dirs float[n][3] (unit,
+        shape b's escape direction in shape a's frame)."""
+        p = np.ascontiguousarray(pairs, PAIR_DTYPE)
+        d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+        assert len(d) == len(p)
+        out = np.zeros(len(p), RESULT_DTYPE)
+        req = ctypes.byref(request) if request is not None else None
+        self._check(self.lib.fclg_collide_directed(self.h, _ptr(p), len(p), _ptr(d), req, _ptr(out)),
+                    "fclg_collide_directed")
+        return out
 
     def autotune(self, d_pairs, n, d_results, request=None, distance=True):
         """Times candidate launch shapes on the batch, keeps the fastest; returns (tuning dict, ms)."""

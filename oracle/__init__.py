@@ -52,6 +52,10 @@ def _load():
         lib.orc_signed_distance.argtypes = [vp, i, vp, vp, i, vp, vp, i, i, d, i, i, d]
         lib.orc_signed_distance.restype = i
         lib.orc_collide.argtypes = [vp, i, vp, vp, i, i, i, vp, i]
+        lib.orc_collide_directed.argtypes = [vp, i, vp, vp, i, vp, vp, i]
+        lib.orc_collide_directed.restype = i
+        lib.orc_directed_raw.argtypes = [vp, i, vp, vp, i, vp, vp, i]
+        lib.orc_directed_raw.restype = i
         lib.orc_collide.restype = i
         lib.orc_time_signed_distance.argtypes = [vp, i, vp, vp, i, vp, i]
         lib.orc_time_signed_distance.restype = d
@@ -77,6 +81,8 @@ def _load_ref():
         lib.ref_signed_distance.argtypes = [vp, i, vp, vp, i, vp, vp, i, i, ctypes.c_double]
         lib.ref_signed_distance.restype = i
         lib.ref_collide.argtypes = [vp, i, vp, vp, i, i, vp, i]
+        lib.ref_directed.argtypes = [vp, i, vp, vp, i, vp, vp, i]
+        lib.ref_directed.restype = i
         lib.ref_collide.restype = i
         _ref = lib
     return _ref
@@ -123,6 +129,42 @@ def collide(batch, want_contact=False, threads=None, analytic=True):
     rc = lib.orc_collide(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), int(want_contact), int(analytic), _ptr(out),
                          threads or default_threads())
     assert rc == 0
+    return out
+
+
+def collide_directed(batch, dirs, threads=None):
+    """fcl::collide with useDirectedPenetration: boolean collide, then
+    MPR::DirectedPenetration along dirs (unit, shape b's escape direction in
+    shape a's frame) for colliding pairs; epa_status = the directed status."""
+    lib = _load()
+    s, v, p = _prep(batch)
+    d = np.ascontiguousarray(dirs, np.float32)
+    out = np.zeros(len(p), RESULT_DTYPE)
+    rc = lib.orc_collide_directed(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), _ptr(d), _ptr(out),
+                                  threads or default_threads())
+    assert rc == 0
+    return out
+
+
+def directed_raw(batch, dirs, threads=None):
+    """Restated MPR::DirectedPenetration on every pair (status in epa_status)."""
+    lib = _load()
+    s, v, p = _prep(batch)
+    d = np.ascontiguousarray(dirs, np.float32)
+    out = np.zeros(len(p), RESULT_DTYPE)
+    assert lib.orc_directed_raw(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), _ptr(d), _ptr(out),
+                                threads or default_threads()) == 0
+    return out
+
+
+def ref_directed(batch, dirs, threads=None):
+    """The reference's MPR::RunDirectedPenetration on every pair."""
+    lib = _load_ref()
+    s, v, p = _prep(batch)
+    d = np.ascontiguousarray(dirs, np.float32)
+    out = np.zeros(len(p), RESULT_DTYPE)
+    assert lib.ref_directed(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), _ptr(d), _ptr(out),
+                            threads or default_threads()) == 0
     return out
 
 

@@ -188,6 +188,71 @@ int orc_collide(const void* shapes, int n_shapes, const float* verts, const void
   return 0;
 }
 
+// fcl::collide in the directed penetration mode (collisionPenetrationMPR,
+// collision_penetration-inl.h:106-250): the boolean collide (closed-form
+// sphere solvers, else MPR with the GJK fallback), then for colliding pairs
+// MPR::DirectedPenetration along dirs[i] (shape b's escape direction in a's
+// frame, unit).  Result: ok = collide; distance = -depth on direction (OK) or
+// -1; p0 / p1 the witness points; normal = the direction; epa_status = the
+// directed status (0 OK, 1 Failed, 2 FailedNoIntersect, 3 iteration limit).
+int orc_collide_directed(const void* shapes, int n_shapes, const float* verts, const void* pairs, int n_pairs,
+                         const float* dirs, OrcResult* out, int n_threads) {
+  if (n_pairs < 0 || n_shapes < 0 || !dirs) return -1;
+  const auto sh = makeShapes((const ShapeRec*)shapes, n_shapes, verts);
+  const PairRec* pr = (const PairRec*)pairs;
+  const orc::SolverParams sp;
+  parallelFor(n_pairs, n_threads, [&](int b, int e) {
+    for (int i = b; i < e; ++i) {
+      const orc::MinkDiff md = makeDiff(sh, pr[i]);
+      OrcResult& r = out[i];
+      r = OrcResult{};
+      orc::AContact ac;
+      bool hit;
+      if (orc::analyticIntersect(*md.s0, *md.s1, md.to0, ac)) hit = ac.hit;
+      else hit = orc::intersect(md, sp, false, nullptr).ok;
+      const orc::V3 d(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]);
+      for (int k = 0; k < 3; ++k) r.normal[k] = d[k];
+      r.ok = hit ? 1 : 0;
+      r.distance = -1;
+      r.epa_status = -1;
+      if (!hit) continue;
+      orc::MPR mpr(128, sp.epa_tol);
+      orc::MPR::Directed pd;
+      const int st = mpr.DirectedPenetration(md, d, pd);
+      r.epa_status = st;
+      if (st == 0) {
+        r.distance = -pd.distance;
+        for (int k = 0; k < 3; ++k) { r.p0[k] = pd.p0[k]; r.p1[k] = pd.p1[k]; }
+      }
+    }
+  });
+  return 0;
+}
+
+// The restated MPR::DirectedPenetration on every pair (no boolean gate), in
+// the layout of ref_directed, for the bit-for-bit pin.
+int orc_directed_raw(const void* shapes, int n_shapes, const float* verts, const void* pairs, int n_pairs,
+                     const float* dirs, OrcResult* out, int n_threads) {
+  if (n_pairs < 0 || n_shapes < 0 || !dirs) return -1;
+  const auto sh = makeShapes((const ShapeRec*)shapes, n_shapes, verts);
+  const PairRec* pr = (const PairRec*)pairs;
+  parallelFor(n_pairs, n_threads, [&](int b, int e) {
+    for (int i = b; i < e; ++i) {
+      const orc::MinkDiff md = makeDiff(sh, pr[i]);
+      OrcResult& r = out[i];
+      r = OrcResult{};
+      orc::MPR mpr(128, 1e-6);
+      orc::MPR::Directed pd;
+      const int st = mpr.DirectedPenetration(md, orc::V3(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]), pd);
+      r.epa_status = st;
+      r.distance = pd.distance;
+      for (int k = 0; k < 3; ++k) { r.p0[k] = pd.p0[k]; r.p1[k] = pd.p1[k]; }
+      r.ok = st == 0 ? 1 : 0;
+    }
+  });
+  return 0;
+}
+
 // Wall-clock seconds of orc_signed_distance over the pairs (for the CPU
 // baseline; excludes nothing but the call itself).
 double orc_time_signed_distance(const void* shapes, int n_shapes, const float* verts, const void* pairs, int n_pairs,

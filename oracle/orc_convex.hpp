@@ -1347,6 +1347,93 @@ class MPR {
       return 2;
     }
   }
+ public:
+  // ------------------------------------------------------------------
+  // Directed penetration, mpr.hpp:495-595 (RunDirectedPenetration) and
+  // :606-701 (finalizeDirectedPenetrationResult): the depth of the Minkowski
+  // difference along the unit direction d (shape 1's escape direction in
+  // shape 0's frame), with witness points p0 / p1 in shape 0's frame.
+  // Status: 0 OK, 1 Failed, 2 FailedNoIntersect, 3 FailedRefinementIterationLimit.
+  struct Directed {
+    V3 v1, v2, v3, d1, d2, d3, portal_normal, p0, p1;
+    double distance = 0;
+  };
+  int DirectedPenetration(const MinkDiff& shape, const V3& d, Directed& pd) const {
+    const V3 v0 = -d;
+    V3 &v1 = pd.v1, &v2 = pd.v2, &v3 = pd.v3, &d1 = pd.d1, &d2 = pd.d2, &d3 = pd.d3;
+    d1 = d;
+    v1 = sup(shape, d1);
+    if (dot(d1, v1) < 0) return 2;
+    d2 = cross(v0, v1);
+    if (absnorm(d2) <= absnorm(v1) * tol_) {
+      pd.distance = dot(v1, d);
+      pd.portal_normal = d1;
+      pd.p0 = shape.support0(d1);
+      pd.p1 = shape.support1(-d1);
+      return 0;
+    }
+    v2 = sup(shape, d2);
+    if (dot(d2, v2) < 0) return 2;
+    d3 = cross(v1, v2);
+    if (dot(d3, v0) > 0) {
+      std::swap(v1, v2);
+      std::swap(d1, d2);
+      d3 = -d3;
+    }
+    v3 = sup(shape, d3);
+    if (dot(d3, v3) < 0) return 2;
+    const double m2 = std::max(sqn(v1), std::max(sqn(v2), sqn(v3)));
+    const V3 v0s = v0 * std::sqrt(m2);
+    const int fp = findPortal(shape, v0s, v1, v2, v3, d1, d2, d3);
+    if (fp == 0) return 1;
+    if (fp == 1) return 2;
+    for (int it = 0; it < max_iter_; ++it) {
+      V3 n = cross(v2 - v1, v3 - v1);
+      if (dot(n, d) < 0) {
+        std::swap(v2, v3);
+        std::swap(d2, d3);
+        n = -n;
+      }
+      const V3 v4 = sup(shape, n);
+      if (dot(v4, n) < 0) return 2;
+      if (std::abs(dot(v4 - v1, n)) < tol_ * absnorm(n)) {
+        finalizeDirected(shape, d, n, pd, &v4);
+        return 0;
+      }
+      updatePortal(v0s, v4, n, v1, v2, v3, d1, d2, d3);
+    }
+    return 3;
+  }
+
+ private:
+  static void finalizeDirected(const MinkDiff& shape, const V3& d, const V3& n, Directed& pd, const V3* v4) {
+    pd.portal_normal = n;
+    const double ndd = dot(d, n);
+    if (std::abs(ndd) <= 0) {
+      const double dv[3] = {dot(pd.v1, d), dot(pd.v2, d), dot(pd.v3, d)};
+      const V3* dirs[3] = {&pd.d1, &pd.d2, &pd.d3};
+      double best = -std::numeric_limits<double>::infinity();
+      int bi = 0;
+      for (int i = 0; i < 3; ++i)
+        if (dv[i] > best) { best = dv[i]; bi = i; }
+      pd.distance = best;
+      pd.p0 = shape.support0(*dirs[bi]);
+      pd.p1 = shape.support1(-*dirs[bi]);
+      return;
+    }
+    const double dist_to_v123 = dot(pd.v1, n) / ndd;
+    pd.distance = v4 ? dot(*v4, n) / ndd : dist_to_v123;
+    const V3 o_projected = d * dist_to_v123;
+    const V3 a12 = pd.v2 - pd.v1, a13 = pd.v3 - pd.v1;
+    const double area = norm(cross(a12, a13));
+    const double w2 = norm(cross(a13, pd.v1 - o_projected)) / area;
+    const double w3 = norm(cross(a12, pd.v1 - o_projected)) / area;
+    const double w1 = 1.0 - w2 - w3;
+    pd.p0 = (shape.support0(pd.d1) * w1 + shape.support0(pd.d2) * w2) + shape.support0(pd.d3) * w3;
+    pd.p1 = (shape.support1(-pd.d1) * w1 + shape.support1(-pd.d2) * w2) + shape.support1(-pd.d3) * w3;
+  }
+
+ public:
   // mpr.hpp:434-493
   static void updatePortal(const V3& v0, const V3& v4, const V3& n, V3& v1, V3& v2, V3& v3, V3& d1, V3& d2, V3& d3) {
     const V3 pn = cross(v4, v0);

@@ -223,4 +223,28 @@ int ref_collide(const void* shapes, int n_shapes, const float* verts, const void
   return 0;
 }
 
+// The reference's MPR::RunDirectedPenetration (mpr.hpp:495-595) on every pair
+// along dirs[i], 128 iterations, tolerance 1e-6: epa_status = its status,
+// distance = distance_on_direction, p0 / p1 its witness points.
+int ref_directed(const void* shapes, int n_shapes, const float* verts, const void* pairs, int n_pairs,
+                 const float* dirs, RefResult* out, int n_threads) {
+  const Prepared p = prepare((const ShapeRec*)shapes, n_shapes, verts);
+  const PairRec* pr = (const PairRec*)pairs;
+  parallelFor(n_pairs, n_threads, [&](int b, int e) {
+    for (int i = b; i < e; ++i) {
+      RefResult& r = out[i];
+      r = RefResult{};
+      const MinkowskiDiff<double> md = makeDiff(p, pr[i]);
+      const Vec d(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]);
+      typename MPR<double>::DirectedPenetrationData data;
+      const auto st = MPR<double>::RunDirectedPenetration(md, d, data, 128, 1e-6);
+      r.epa_status = (int)st;
+      r.distance = data.distance_on_direction;
+      for (int k = 0; k < 3; ++k) { r.p0[k] = data.p0_in_shape0_frame[k]; r.p1[k] = data.p1_in_shape0_frame[k]; }
+      r.ok = st == MPR<double>::DirectedPenetrationStatus::OK ? 1 : 0;
+    }
+  });
+  return 0;
+}
+
 }  // extern "C"

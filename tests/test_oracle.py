@@ -332,3 +332,45 @@ def test_analytic_sphere_solvers_known_answers(oracle_lib):
         if hit:
             assert abs(-r["distance"][i] - depth) < 1e-6, (i, r["distance"][i])  # FP32 inputs
             assert np.allclose(r["normal"][i], normal, atol=1e-6), (i, r["normal"][i])
+
+
+def test_directed_penetration_pinned_to_reference(oracle_lib):
+    """The restated MPR::DirectedPenetration against the reference's own
+    RunDirectedPenetration (mpr.hpp:495-701) on random unit directions: the
+    same status everywhere, bit-identical depth and witness points wherever it
+    succeeds."""
+    if not oracle_lib.ref_available():
+        pytest.skip("reference build unavailable")
+    from fclg import workloads
+    for b in (workloads.mixed(6000, seed=31), workloads.pareto(4000, seed=32)):
+        rng = np.random.default_rng(3)
+        u = rng.normal(size=(b.n_pairs, 3))
+        u = (u / np.linalg.norm(u, axis=1, keepdims=True)).astype(np.float32)
+        o = oracle_lib.directed_raw(b, u, threads=2)
+        r = oracle_lib.ref_directed(b, u, threads=2)
+        assert np.array_equal(o["epa_status"], r["epa_status"])
+        ok = o["epa_status"] == 0
+        assert ok.mean() > 0.3
+        assert np.array_equal(o["distance"][ok], r["distance"][ok])
+        assert np.array_equal(o["p0"][ok], r["p0"][ok]) and np.array_equal(o["p1"][ok], r["p1"][ok])
+
+
+def test_directed_penetration_properties(oracle_lib):
+    """Depth along the EPA normal equals the EPA depth; along any direction it
+    is no smaller than the minimum depth (fcl::collide, directed mode)."""
+    from fclg import workloads
+    b = workloads.mixed(8000, seed=33)
+    sd = oracle_lib.signed_distance(b, threads=2)
+    ov = (sd["distance"] < -1e-5) & (sd["epa_status"] == 1)
+    r = oracle_lib.collide_directed(b, sd["normal"].astype(np.float32), threads=2)
+    m = ov & (r["epa_status"] == 0)
+    assert m.sum() > 1000
+    err = np.abs(r["distance"][m] - sd["distance"][m])
+    assert np.mean(err <= 1e-5) >= 0.99
+    rng = np.random.default_rng(4)
+    u = rng.normal(size=(b.n_pairs, 3))
+    u = (u / np.linalg.norm(u, axis=1, keepdims=True)).astype(np.float32)
+    r2 = oracle_lib.collide_directed(b, u, threads=2)
+    m2 = ov & (r2["epa_status"] == 0)
+    assert np.all(-r2["distance"][m2] >= -sd["distance"][m2] - 1e-6)
+    assert np.array_equal(r2["ok"] == 1, oracle_lib.collide(b, threads=2)["ok"] == 1)
