@@ -130,6 +130,18 @@ int fclg_set_shapes(fclg_context* ctx, const fclg_shape* shapes, uint32_t n_shap
 int fclg_set_shapes_device(fclg_context* ctx, const fclg_shape* d_shapes, uint32_t n_shapes,
                            const float* d_vertices_xyzw, uint64_t n_vertices);
 
+/* Edge graph of the convex hull of nv points (xyzw), the graph the support
+   walk climbs (fclg_tuning.support_walk): starts[6] = the extreme corner along
+   +x, -x, +y, -y, +z, -z; first[nv + 1] = row starts into adj; adj = the
+   neighbour corners of each vertex, rows ascending.  Points that are not
+   corners of the hull get empty rows.  Host work only (no device, no context).
+   Pass adj = NULL to learn *adj_len.  FCLG_E_INVALID when the points span no
+   volume, FCLG_E_TOO_LARGE when adj_cap is short.  No counterpart in the
+   reference's API: fcl::Convex derives the same graph from the face list its
+   caller supplies (geometry/shape/convex-inl.h:379-405, FindVertexNeighbors). */
+int fclg_hull_graph(const float* xyzw, uint32_t nv, uint32_t* starts, uint32_t* first, uint32_t* adj,
+                    uint32_t adj_cap, uint32_t* adj_len);
+
 /* Signed distance per pair: GJK separation distance and witness points for
    separated pairs, -EPA depth, witness points and contact normal for
    overlapping ones (GJKSolver::shapeSignedDistance, gjk_solver-inl.h:810-874;
@@ -234,8 +246,16 @@ int fclg_collide_directed_device(fclg_context* ctx, const fclg_pair* d_pairs, ui
    large_hull_vertices); pairs without a large hull run the GJK pass with
    gjk_lanes_small lanes per pair, the rest with gjk_lanes_large.  Zero
    fields keep the current value.  Defaults: bucketing on, 1 and 4 lanes,
-   128 vertices, 4 GJK and 5 EPA CTAs per SM (the EPA pass's first,
-   128-face layout). */
+   128 vertices, 4 GJK and 6 EPA CTAs per SM (the EPA pass's first,
+   128-face layout), support walk on.
+   support_walk: hulls of more than 32 vertices get their edge graph built on
+   the host when shapes are set (a quickhull per hull, spread over the host's
+   threads); a GJK / MPR launch with one lane per pair then finds a hull's
+   support by hill-climbing that graph from one of six cached axis-extreme
+   corners, the rule of Convex::findExtremeVertexViaNeighbours
+   (geometry/shape/convex-inl.h:201-283), instead of scanning every vertex.
+   Groups of several lanes and the EPA pass scan.  Both give the vertex of
+   maximal support value; they may differ only where several vertices tie. */
 typedef struct fclg_tuning {
   int32_t bucketing;            /* 1 on, -1 off, 0 unchanged */
   int32_t gjk_lanes_small;      /* 1, 2, 4, 8, 16 or 32 */
@@ -243,6 +263,7 @@ typedef struct fclg_tuning {
   int32_t large_hull_vertices;
   int32_t gjk_ctas_per_sm;
   int32_t epa_ctas_per_sm;
+  int32_t support_walk;         /* 1 on, -1 off, 0 unchanged */
 } fclg_tuning;
 int fclg_set_tuning(fclg_context* ctx, const fclg_tuning* tuning);
 int fclg_get_tuning(const fclg_context* ctx, fclg_tuning* tuning);

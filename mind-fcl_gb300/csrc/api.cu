@@ -8,7 +8,11 @@
 #include <string>
 #include <vector>
 
+#include <atomic>
+#include <thread>
+
 #include "fclg.h"
+#include "hull.h"
 #include "kernels.h"
 #include "mesh_build.h"
 #include "mesh_kernels.h"
@@ -26,6 +30,11 @@ struct fclg_context {
   const float4* verts = nullptr;
   uint32_t n_shapes = 0;
   uint64_t n_verts = 0;
+  // support walk: per-shape first entry of the hull's walk block (or kNoWalk), the blocks
+  uint32_t* walk_tab = nullptr;
+  float4* hull_ents = nullptr;
+  uint32_t walk_hulls = 0;
+  bool support_walk = true;
   // scratch handed from the GJK pass to the EPA pass
   uint32_t* epa_count = nullptr;  // [2]: work list, overflow list
   uint32_t* epa_list = nullptr;
@@ -125,11 +134,84 @@ int validate_shapes(fclg_context* c, const fclg_shape* s, uint32_t n, uint64_t n
 void release_shapes(fclg_context* c) {
   if (c->own_shapes) cudaFree(c->own_shapes);
   if (c->own_verts) cudaFree(c->own_verts);
+  if (c->walk_tab) cudaFree(c->walk_tab);
+  if (c->hull_ents) cudaFree(c->hull_ents);
+  c->walk_tab = nullptr;
+  c->hull_ents = nullptr;
+  c->walk_hulls = 0;
   c->own_shapes = c->own_verts = nullptr;
   c->shapes = nullptr;
   c->verts = nullptr;
   c->n_shapes = 0;
   c->n_verts = 0;
+}
+
+// Walk blocks of every hull above kWalkMinVertices (hull.h), built in
+// parallel over distinct vertex ranges and uploaded with a per-shape table.
+// A hull whose points span no volume, or whose graph does not fit a block,
+// keeps the vertex scan.
+int build_walks(fclg_context* c, const fclg_shape* s, uint32_t n, const float* verts) {
+  std::vector<uint32_t> tab(n, fclg::kNoWalk);
+  std::vector<uint64_t> keys;
+  for (uint32_t i = 0; i < n; ++i)
+    if (s[i].type == FCLG_CONVEX && s[i].vert_count > fclg::kWalkMinVertices)
+      keys.push_back(((uint64_t)s[i].vert_offset << 32) | s[i].vert_count);
+  if (keys.empty()) return FCLG_OK;
+  std::sort(keys.begin(), keys.end());
+  keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+  std::vector<std::vector<float>> blocks(keys.size());
+  std::atomic<size_t> next{0};
+  auto work = [&]() {
+    fclg::HullGraph g;
+    for (size_t k = next.fetch_add(1); k < keys.size(); k = next.fetch_add(1)) {
+      const float* v = verts + 4 * (size_t)(keys[k] >> 32);
+      const uint32_t nv = (uint32_t)keys[k];
+      if (!fclg::hull_graph(v, nv, g) || !fclg::pack_walk(v, g, blocks[k])) blocks[k].clear();
+    }
+  };
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t nt = std::min<size_t>({(size_t)hw, (size_t)64, keys.size() / 8 + 1});
+  std::vector<std::thread> pool;
+  for (size_t t = 1; t < nt; ++t) pool.emplace_back(work);
+  work();
+  for (auto& t : pool) t.join();
+  std::vector<uint32_t> base(keys.size(), fclg::kNoWalk);
+  uint64_t total = 0;
+  uint32_t built = 0;
+  for (size_t k = 0; k < keys.size(); ++k) {
+    const uint64_t ents = blocks[k].size() / 4;
+    if (ents == 0 || total + ents >= fclg::kNoWalk) continue;
+    base[k] = (uint32_t)total;
+    total += ents;
+    ++built;
+  }
+  if (total == 0) return FCLG_OK;
+  for (uint32_t i = 0; i < n; ++i) {
+    if (s[i].type != FCLG_CONVEX || s[i].vert_count <= fclg::kWalkMinVertices) continue;
+    const uint64_t key = ((uint64_t)s[i].vert_offset << 32) | s[i].vert_count;
+    tab[i] = base[std::lower_bound(keys.begin(), keys.end(), key) - keys.begin()];
+  }
+  std::vector<float> ents;
+  ents.reserve(4 * total);
+  for (size_t k = 0; k < keys.size(); ++k)
+    if (base[k] != fclg::kNoWalk) ents.insert(ents.end(), blocks[k].begin(), blocks[k].end());
+  FCLG_CUDA(c, cudaMalloc(&c->walk_tab, (size_t)n * sizeof(uint32_t)));
+  FCLG_CUDA(c, cudaMalloc(&c->hull_ents, total * sizeof(float4)));
+  FCLG_CUDA(c, cudaMemcpy(c->walk_tab, tab.data(), (size_t)n * sizeof(uint32_t), cudaMemcpyHostToDevice));
+  FCLG_CUDA(c, cudaMemcpy(c->hull_ents, ents.data(), total * sizeof(float4), cudaMemcpyHostToDevice));
+  c->walk_hulls = built;
+  return FCLG_OK;
+}
+
+// Batch arguments over the context's shapes.
+fclg::BatchArgs batch_args(const fclg_context* c) {
+  fclg::BatchArgs b{};
+  b.shapes = c->shapes;
+  b.verts = c->verts;
+  b.walk = c->support_walk ? c->walk_tab : nullptr;
+  b.hull = c->hull_ents;
+  b.n_shapes = c->n_shapes;
+  return b;
 }
 
 int ensure_epa(fclg_context* c, size_t n) {
@@ -241,9 +323,7 @@ int run_query(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_
     const int rc = ensure_epa(c, n);
     if (rc) return rc;
   }
-  fclg::BatchArgs b;
-  b.shapes = c->shapes;
-  b.verts = c->verts;
+  fclg::BatchArgs b = batch_args(c);
   b.pairs = reinterpret_cast<const float4*>(d_pairs);
   b.guess = nullptr;
   b.results = reinterpret_cast<float4*>(d_results);
@@ -381,6 +461,20 @@ int fclg_set_shapes(fclg_context* c, const fclg_shape* shapes, uint32_t n_shapes
   c->verts = static_cast<const float4*>(c->own_verts);
   c->n_shapes = n_shapes;
   c->n_verts = n_vertices;
+  return build_walks(c, shapes, n_shapes, vertices);
+}
+
+int fclg_hull_graph(const float* xyzw, uint32_t nv, uint32_t* starts, uint32_t* first, uint32_t* adj,
+                    uint32_t adj_cap, uint32_t* adj_len) {
+  if (!xyzw || !starts || !first || !adj_len) return FCLG_E_INVALID;
+  fclg::HullGraph g;
+  if (!fclg::hull_graph(xyzw, nv, g)) return FCLG_E_INVALID;
+  *adj_len = (uint32_t)g.adj.size();
+  std::copy(g.start, g.start + 6, starts);
+  std::copy(g.first.begin(), g.first.end(), first);
+  if (!adj) return FCLG_OK;
+  if (adj_cap < g.adj.size()) return FCLG_E_TOO_LARGE;
+  std::copy(g.adj.begin(), g.adj.end(), adj);
   return FCLG_OK;
 }
 
@@ -399,7 +493,13 @@ int fclg_set_shapes_device(fclg_context* c, const fclg_shape* d_shapes, uint32_t
   c->verts = reinterpret_cast<const float4*>(d_vertices);
   c->n_shapes = n_shapes;
   c->n_verts = n_vertices;
-  return FCLG_OK;
+  bool walks = false;
+  for (uint32_t i = 0; i < n_shapes && !walks; ++i)
+    walks = h[i].type == FCLG_CONVEX && h[i].vert_count > fclg::kWalkMinVertices;
+  if (!walks) return FCLG_OK;
+  std::vector<float> hv(4 * (size_t)n_vertices);
+  FCLG_CUDA(c, cudaMemcpy(hv.data(), d_vertices, hv.size() * sizeof(float), cudaMemcpyDeviceToHost));
+  return build_walks(c, h.data(), n_shapes, hv.data());
 }
 
 int fclg_distance(fclg_context* c, const fclg_pair* pairs, uint32_t n, const fclg_request* req,
@@ -445,6 +545,7 @@ int fclg_set_tuning(fclg_context* c, const fclg_tuning* t) {
   if (t->large_hull_vertices) c->large_hull = t->large_hull_vertices;
   if (t->gjk_ctas_per_sm) c->gjk_ctas_per_sm = t->gjk_ctas_per_sm;
   if (t->epa_ctas_per_sm) c->epa_ctas_per_sm = t->epa_ctas_per_sm;
+  if (t->support_walk) c->support_walk = t->support_walk > 0;
   return FCLG_OK;
 }
 
@@ -456,6 +557,7 @@ int fclg_get_tuning(const fclg_context* c, fclg_tuning* t) {
   t->large_hull_vertices = c->large_hull;
   t->gjk_ctas_per_sm = c->gjk_ctas_per_sm;
   t->epa_ctas_per_sm = c->epa_ctas_per_sm;
+  t->support_walk = c->support_walk ? 1 : -1;
   return FCLG_OK;
 }
 
@@ -704,9 +806,7 @@ extern "C" int fclg_distance_device_static(fclg_context* c, const fclg_pair* d_p
   if (rc) return rc;
   const cudaStream_t st = static_cast<cudaStream_t>(stream);
   const fclg::QueryParams prm = make_params(req, true);
-  fclg::BatchArgs b;
-  b.shapes = c->shapes;
-  b.verts = c->verts;
+  fclg::BatchArgs b = batch_args(c);
   b.pairs = reinterpret_cast<const float4*>(d_pairs);
   b.guess = nullptr;
   b.results = reinterpret_cast<float4*>(d_results);
@@ -747,9 +847,7 @@ int run_directed(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fl
   prm.use_mpr = 0;
   prm.analytic = 0;
   prm.directed = 1;
-  fclg::BatchArgs b;
-  b.shapes = c->shapes;
-  b.verts = c->verts;
+  fclg::BatchArgs b = batch_args(c);
   b.pairs = reinterpret_cast<const float4*>(d_pairs);
   b.guess = d_dirs;
   b.results = reinterpret_cast<float4*>(d_results);
@@ -890,16 +988,20 @@ extern "C" int fclg_autotune(fclg_context* c, const fclg_pair* d_pairs, uint32_t
   c->profiling = false;
   // candidates: GJK lanes for small / large hulls, the hull split, bucketing
   std::vector<fclg_tuning> cand;
+  // (the support walk only changes one-lane launches, and only when hulls have walk blocks)
   for (int ls : {1, 2, 4, 8})
-    for (int ll : {4, 8, 16})
-      for (int lh : {64, 128, 256}) {
-        fclg_tuning t = keep;
-        t.bucketing = 1;
-        t.gjk_lanes_small = ls;
-        t.gjk_lanes_large = ll;
-        t.large_hull_vertices = lh;
-        cand.push_back(t);
-      }
+    for (int ll : {1, 4, 8, 16})
+      for (int lh : {64, 128, 256})
+        for (int walk : {1, -1}) {
+          if (walk < 0 && (!c->walk_tab || (ls != 1 && ll != 1))) continue;
+          fclg_tuning t = keep;
+          t.bucketing = 1;
+          t.gjk_lanes_small = ls;
+          t.gjk_lanes_large = ll;
+          t.large_hull_vertices = lh;
+          t.support_walk = walk;
+          cand.push_back(t);
+        }
   {
     fclg_tuning t = keep;
     t.bucketing = -1;

@@ -66,8 +66,13 @@ __device__ __forceinline__ void closest_bary_origin(d3 a, d3 b, d3 c, double& u,
 
 // Shape types: the reference's GJKShapeType values (gjk_shape.h:9-28).
 enum : int32_t { kBox = 0, kSphere = 1, kCapsule = 3, kCylinder = 5, kConvex = 100 };
+// Decoded form of a convex hull that carries a walk block (never in fclg_shape).
+constexpr int32_t kConvexWalk = 101;
 
 // One shape as the kernels use it, decoded from the 32-byte fclg_shape.
+// No walk block: the convex support scans every vertex.
+constexpr uint32_t kNoWalk = 0xFFFFFFFFu;
+
 struct ShapeDev {
   int32_t type;
   uint32_t vofs, nv;
@@ -85,6 +90,22 @@ __device__ __forceinline__ ShapeDev load_shape(const int4* __restrict__ shapes, 
     s.p0 = 0.5f * p.x; s.p1 = 0.5f * p.y; s.p2 = 0.5f * p.z;
   } else {
     s.p0 = p.x; s.p1 = 0.5f * p.y; s.p2 = 0.f;
+  }
+  return s;
+}
+
+// load_shape for one-lane groups: a hull with a walk block (walk_tab: per-shape
+// first entry or kNoWalk; null for none) decodes as kConvexWalk with vofs = the
+// block's first entry.
+__device__ __forceinline__ ShapeDev load_shape(const int4* __restrict__ shapes, const uint32_t* __restrict__ walk_tab,
+                                               uint32_t i) {
+  ShapeDev s = load_shape(shapes, i);
+  if (walk_tab && s.type == kConvex) {
+    const uint32_t w = __ldg(walk_tab + i);
+    if (w != kNoWalk) {
+      s.type = kConvexWalk;
+      s.vofs = w;
+    }
   }
   return s;
 }

@@ -22,10 +22,11 @@ __global__ void __launch_bounds__(128, 4) directed_pass(BatchArgs b, QueryParams
       continue;
     }
     MinkowskiSupport<LANES> sup;
-    sup.A = load_shape(b.shapes, pr.a);
-    sup.B = load_shape(b.shapes, pr.b);
+    sup.A = load_shape(b.shapes, b.walk, pr.a);
+    sup.B = load_shape(b.shapes, b.walk, pr.b);
     sup.pose = pr.pose;
     sup.verts = b.verts;
+    sup.hull = b.hull;
     sup.g = g;
     // fcl::collide, useDirectedPenetration (collisionPenetrationMPR,
     // collision_penetration-inl.h:106-250): the boolean collide (closed

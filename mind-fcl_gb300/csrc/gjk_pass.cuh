@@ -75,10 +75,11 @@ __global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_pass(BatchArgs b, Quer
       continue;
     }
     MinkowskiSupport<LANES> sup;
-    sup.A = load_shape(b.shapes, pr.a);
-    sup.B = load_shape(b.shapes, pr.b);
+    sup.A = load_shape(b.shapes, LANES == 1 ? b.walk : nullptr, pr.a);
+    sup.B = load_shape(b.shapes, LANES == 1 ? b.walk : nullptr, pr.b);
     sup.pose = pr.pose;
     sup.verts = b.verts;
+    sup.hull = b.hull;
     sup.g = g;
     // GJKSolver's default guess (1, 0, 0), gjk_solver-inl.h:1129
     const f3 plain = mk3(1.f, 0.f, 0.f);

@@ -13,6 +13,8 @@ struct BatchArgs {
   const float4* verts;    // xyzw
   const float4* pairs;    // fclg_pair[n_pairs]
   const float* guess;     // optional float[n_pairs][3]: GJKSolver::gjk_guess per pair
+  const uint32_t* walk;   // optional [n_shapes]: first entry of each hull's walk block, or kNoWalk
+  const float4* hull;     // walk blocks (hull.h), read by one-lane groups
   float4* results;        // fclg_result[n_pairs]
   uint32_t n_pairs;
   uint32_t n_shapes;

@@ -14,7 +14,7 @@ enum class MprStatus : int { Intersect = 0, Separated = 1, Failed = 2 };
 // Interior point of a shape in its own frame: the vertex mean of a hull
 // (convex-inl.h:58-63, stored in fclg_shape.param[0:3]), the origin otherwise.
 __device__ __forceinline__ f3 load_interior(const int4* __restrict__ shapes, uint32_t i, int type) {
-  if (type != kConvex) return mk3(0.f, 0.f, 0.f);
+  if (type != kConvex && type != kConvexWalk) return mk3(0.f, 0.f, 0.f);
   const float4 p = __ldg(reinterpret_cast<const float4*>(shapes) + 2 * (size_t)i + 1);
   return mk3(p.x, p.y, p.z);
 }

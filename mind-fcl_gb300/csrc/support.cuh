@@ -68,8 +68,48 @@ __device__ __forceinline__ f3 convex_support(const float4* __restrict__ v, uint3
   return mk3(q.x, q.y, q.z);
 }
 
+// Hill climb over a walk block e (entries {x, y, z, link}, link = (row << 8) |
+// degree).  Start: the cached corner of the axis direction with the largest
+// d-component, the first of +x, -x, +y, -y, +z, -z on ties
+// (convex-inl.h:206-222).  Step: scan the current corner's row, skipping the
+// last two corners left behind; every strictly larger value moves the corner
+// (convex-inl.h:230-278).  Values strictly increase, so no corner repeats; the
+// pass count is bounded by the vertex count all the same.
+__device__ __forceinline__ f3 convex_walk(const float4* __restrict__ e, uint32_t nv, f3 d) {
+  int k = 0;
+  float m = d.x;
+  if (-d.x > m) { k = 1; m = -d.x; }
+  if (d.y > m) { k = 2; m = d.y; }
+  if (-d.y > m) { k = 3; m = -d.y; }
+  if (d.z > m) { k = 4; m = d.z; }
+  if (-d.z > m) k = 5;
+  float4 cur = __ldg(e + k);
+  float best = fmaf(d.z, cur.z, fmaf(d.y, cur.y, d.x * cur.x));
+  uint32_t link = __float_as_uint(cur.w);
+  uint32_t parent0 = link, parent1 = link;
+  for (uint32_t pass = 0; pass < nv; ++pass) {
+    const uint32_t row = link >> 8, deg = link & 0xFFu, from = link;
+    for (uint32_t j = 0; j < deg; ++j) {
+      const float4 q = __ldg(e + row + j);
+      const uint32_t ql = __float_as_uint(q.w);
+      if (ql == parent0 || ql == parent1) continue;
+      const float v = fmaf(d.z, q.z, fmaf(d.y, q.y, d.x * q.x));
+      if (v > best) {
+        parent1 = link;
+        link = ql;
+        best = v;
+        cur = q;
+      }
+    }
+    parent0 = from;
+    if (link == from) break;
+  }
+  return mk3(cur.x, cur.y, cur.z);
+}
+
+// pool: the vertex pool, or for kConvexWalk the walk blocks.
 template <int LANES>
-__device__ __forceinline__ f3 shape_support(const ShapeDev& s, const float4* __restrict__ verts, f3 d,
+__device__ __forceinline__ f3 shape_support(const ShapeDev& s, const float4* __restrict__ pool, f3 d,
                                             const Group<LANES>& g) {
   switch (s.type) {
     case kBox:
@@ -90,7 +130,10 @@ __device__ __forceinline__ f3 shape_support(const ShapeDev& s, const float4* __r
       return mk3(k * d.x, k * d.y, z);
     }
     case kConvex:
-      return convex_support<LANES>(verts + s.vofs, s.nv, d, g);
+      return convex_support<LANES>(pool + s.vofs, s.nv, d, g);
+    case kConvexWalk:
+      if constexpr (LANES == 1) return convex_walk(pool + s.vofs, s.nv, d);
+      return mk3(0.f, 0.f, 0.f);
     default:
       return mk3(0.f, 0.f, 0.f);
   }
@@ -103,9 +146,9 @@ __device__ __forceinline__ f3 shape_support(const ShapeDev& s, const float4* __r
 // instruction footprint small (measured: GJK pass 8 % faster; the warp-wide
 // EPA pass keeps the inlined form, which is faster there).
 template <int LANES>
-__device__ __noinline__ f3 shape_support_outline(const ShapeDev& s, const float4* __restrict__ verts, f3 d,
+__device__ __noinline__ f3 shape_support_outline(const ShapeDev& s, const float4* __restrict__ pool, f3 d,
                                                  const Group<LANES>& g) {
-  return shape_support<LANES>(s, verts, d, g);
+  return shape_support<LANES>(s, pool, d, g);
 }
 
 template <int LANES>
@@ -113,11 +156,12 @@ struct MinkowskiSupport {
   ShapeDev A, B;
   Pose pose;
   const float4* __restrict__ verts;
+  const float4* __restrict__ hull = nullptr;  // walk blocks of kConvexWalk shapes
   Group<LANES> g;
   __device__ __forceinline__ void operator()(f3 d, f3& pa, f3& pb) const {
     if constexpr (LANES < 32) {
-      pa = shape_support_outline<LANES>(A, verts, d, g);
-      pb = pose.apply(shape_support_outline<LANES>(B, verts, pose.rotT(-d), g));
+      pa = shape_support_outline<LANES>(A, A.type == kConvexWalk ? hull : verts, d, g);
+      pb = pose.apply(shape_support_outline<LANES>(B, B.type == kConvexWalk ? hull : verts, pose.rotT(-d), g));
     } else {
       pa = shape_support<LANES>(A, verts, d, g);
       pb = pose.apply(shape_support<LANES>(B, verts, pose.rotT(-d), g));

@@ -29,7 +29,7 @@ EXPORTS = [
     "fclg_warmstart_get_params", "fclg_warmstart_set_params", "fclg_warmstart_predict", "fclg_warmstart_forward",
     "fclg_warmstart_gradient", "fclg_warmstart_train", "fclg_set_warmstart", "fclg_warmstart_status",
     "fclg_autotune", "fclg_graph_create", "fclg_graph_launch", "fclg_graph_destroy",
-    "fclg_collide_directed", "fclg_collide_directed_device",
+    "fclg_collide_directed", "fclg_collide_directed_device", "fclg_hull_graph",
 ]
 
 STATIC_MAX_PAIRS = 16384  # FCLG_STATIC_MAX_PAIRS
@@ -46,7 +46,8 @@ class FclgError(RuntimeError):
 class Tuning(ctypes.Structure):
     _fields_ = [("bucketing", ctypes.c_int32), ("gjk_lanes_small", ctypes.c_int32),
                 ("gjk_lanes_large", ctypes.c_int32), ("large_hull_vertices", ctypes.c_int32),
-                ("gjk_ctas_per_sm", ctypes.c_int32), ("epa_ctas_per_sm", ctypes.c_int32)]
+                ("gjk_ctas_per_sm", ctypes.c_int32), ("epa_ctas_per_sm", ctypes.c_int32),
+                ("support_walk", ctypes.c_int32)]
 
 
 class Request(ctypes.Structure):
@@ -148,6 +149,8 @@ def load_library(path=LIB_PATH):
     lib.fclg_graph_launch.restype = i32
     lib.fclg_graph_destroy.argtypes = [vp]
     lib.fclg_graph_destroy.restype = None
+    lib.fclg_hull_graph.argtypes = [vp, u32, vp, vp, vp, u32, ctypes.POINTER(u32)]
+    lib.fclg_hull_graph.restype = i32
     _lib = lib
     return lib
 
@@ -255,7 +258,7 @@ class Context:
         """Fields of fclg_tuning by name; unspecified ones keep their value."""
         t = Tuning()
         for k, v in kw.items():
-            if k == "bucketing":
+            if k in ("bucketing", "support_walk") and isinstance(v, bool):
                 v = 1 if v else -1
             setattr(t, k, int(v))
         self._check(self.lib.fclg_set_tuning(self.h, ctypes.byref(t)), "fclg_set_tuning")
@@ -464,6 +467,28 @@ def mesh_collide(ctx, mesh_a, mesh_b, poses, max_contacts=1):
     ctx._check(ctx.lib.fclg_mesh_collide(ctx.h, mesh_a.h, mesh_b.h, _ptr(p), n, max_contacts, _ptr(flags),
                                          _ptr(counts), _ptr(pairs), _ptr(status)), "fclg_mesh_collide")
     return flags, counts, pairs, status
+
+
+def hull_graph(points):
+    """Edge graph of the convex hull of ``points`` [n, 3 or 4] (fclg_hull_graph,
+    host work): (starts[6], first[n + 1], adj), rows of adj ascending; None when
+    the points span no volume."""
+    lib = load_library()
+    p = np.asarray(points, np.float32)
+    n = len(p)
+    xyzw = np.zeros((n, 4), np.float32)
+    xyzw[:, :p.shape[1]] = p[:, :4]
+    starts = np.zeros(6, np.uint32)
+    first = np.zeros(n + 1, np.uint32)
+    m = ctypes.c_uint32(0)
+    rc = lib.fclg_hull_graph(_ptr(xyzw), n, _ptr(starts), _ptr(first), None, 0, ctypes.byref(m))
+    if rc != 0:
+        return None
+    adj = np.zeros(max(m.value, 1), np.uint32)
+    rc = lib.fclg_hull_graph(_ptr(xyzw), n, _ptr(starts), _ptr(first), _ptr(adj), len(adj), ctypes.byref(m))
+    if rc != 0:
+        raise FclgError("fclg_hull_graph failed (%d)" % rc)
+    return starts, first, adj[:m.value]
 
 
 def bvh_build(vertices, triangles):

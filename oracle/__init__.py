@@ -65,6 +65,10 @@ def _load():
         lib.orc_mesh_allpairs.restype = i
         lib.orc_tri_tri.argtypes = [vp, vp, vp]
         lib.orc_tri_tri.restype = i
+        lib.orc_set_walk.argtypes = [vp, i, vp]
+        lib.orc_set_walk.restype = None
+        lib.orc_support.argtypes = [vp, i, vp, i, vp, i, vp]
+        lib.orc_support.restype = i
         _lib = lib
     return _lib
 
@@ -101,33 +105,115 @@ def _prep(batch):
     return s, v, p
 
 
+# fcl::Convex walks hulls of more than this many vertices
+# (kMinVertCountForEdgeWalking, include/fcl/geometry/shape/convex.h:60-61).
+WALK_MIN_VERTICES = 32
+
+
+def neighbor_table(nv, faces):
+    """Convex::FindVertexNeighbors (convex-inl.h:379-405) over a face list
+    (an [m, k] array or sequences of vertex indices; consecutive vertices of a
+    face and its last and first are neighbours): the neighbors_ layout, int32
+    -- nv row offsets, then per vertex its neighbour count and the neighbours
+    ascending."""
+    if isinstance(faces, np.ndarray) and faces.ndim == 2:
+        f = faces.astype(np.int64)
+        a, b = f.reshape(-1), np.roll(f, -1, axis=1).reshape(-1)
+    else:
+        a = np.asarray([int(v) for face in faces for v in face], np.int64)
+        b = np.asarray([int(face[(k + 1) % len(face)]) for face in faces for k in range(len(face))], np.int64)
+    e = np.unique(np.concatenate([a * nv + b, b * nv + a]))  # sorted: by vertex, then neighbour
+    src, dst = e // nv, e % nv
+    deg = np.bincount(src, minlength=nv)
+    row = nv + np.concatenate([[0], np.cumsum(deg + 1)[:-1]])  # each row: count, then neighbours
+    table = np.zeros(nv + int(np.sum(deg + 1)), np.int32)
+    table[:nv] = row
+    table[row] = deg
+    starts = np.concatenate([[0], np.cumsum(deg)[:-1]])
+    table[row[src] + 1 + (np.arange(len(src)) - starts[src])] = dst
+    return table
+
+
+def walk_tables(batch, min_vertices=WALK_MIN_VERTICES, faces=None):
+    """Neighbour tables of the batch's hulls with more than min_vertices
+    vertices, as fcl::Convex builds them from a face list: faces[shape] where
+    given, else the triangles of the hull's qhull convex hull (scipy).
+    Returns (off int64[n_shapes], -1 = scan; nbr int32[])."""
+    from scipy.spatial import ConvexHull
+    s = batch.shapes
+    off = np.full(len(s), -1, np.int64)
+    parts, total, seen = [], 0, {}
+    for i in range(len(s)):
+        if int(s["type"][i]) != 100 or int(s["vert_count"][i]) <= min_vertices:
+            continue
+        o, c = int(s["vert_offset"][i]), int(s["vert_count"][i])
+        key = (o, c)
+        if faces is None and key in seen:
+            off[i] = seen[key]
+            continue
+        if faces is not None and i in faces:
+            f = faces[i]
+        else:
+            f = ConvexHull(np.asarray(batch.vertices[o:o + c, :3], np.float64)).simplices
+        t = neighbor_table(c, f)
+        off[i] = seen[key] = total
+        parts.append(t)
+        total += len(t)
+    nbr = np.concatenate(parts) if parts else np.zeros(1, np.int32)
+    return off, nbr
+
+
+class _Walk:
+    """Installs walk tables in the restatement for one call."""
+
+    def __init__(self, lib, tables, n_shapes):
+        self.lib, self.tables, self.n = lib, tables, n_shapes
+
+    def __enter__(self):
+        if self.tables is not None:
+            off, nbr = self.tables
+            assert len(off) == self.n
+            self.off = np.ascontiguousarray(off, np.int64)
+            self.nbr = np.ascontiguousarray(nbr, np.int32)
+            self.lib.orc_set_walk(_ptr(self.off), self.n, _ptr(self.nbr))
+        return self
+
+    def __exit__(self, *exc):
+        if self.tables is not None:
+            self.lib.orc_set_walk(None, 0, None)
+        return False
+
+
 def default_threads():
     return max(1, os.cpu_count() or 1)
 
 
 def signed_distance(batch, guess=None, threads=None, gjk_max_iter=0, gjk_tol=0.0, epa_max_faces=0,
-                    epa_max_iter=0, epa_tol=0.0):
-    """GJKSolver::shapeSignedDistance per pair (restatement)."""
+                    epa_max_iter=0, epa_tol=0.0, walk=None):
+    """GJKSolver::shapeSignedDistance per pair (restatement); walk = tables of
+    walk_tables() for the hill-climbing convex support, None for the scan."""
     lib = _load()
     s, v, p = _prep(batch)
     out = np.zeros(len(p), RESULT_DTYPE)
     g = None if guess is None else np.ascontiguousarray(guess, np.float32)
-    rc = lib.orc_signed_distance(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), _ptr(g), _ptr(out),
-                                 threads or default_threads(), gjk_max_iter, gjk_tol, epa_max_faces, epa_max_iter,
-                                 epa_tol)
+    with _Walk(lib, walk, len(s)):
+            rc = lib.orc_signed_distance(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), _ptr(g), _ptr(out),
+                                     threads or default_threads(), gjk_max_iter, gjk_tol, epa_max_faces,
+                                     epa_max_iter, epa_tol)
     assert rc == 0
     return out
 
 
-def collide(batch, want_contact=False, threads=None, analytic=True):
+def collide(batch, want_contact=False, threads=None, analytic=True, walk=None):
     """fcl::collide on shape pairs (restatement): the closed-form sphere-pair
     solvers (analytic=True, as fcl::collide dispatches), else MPR boolean or
-    GJK+EPA contact."""
+    GJK+EPA contact; walk as in signed_distance."""
     lib = _load()
     s, v, p = _prep(batch)
     out = np.zeros(len(p), RESULT_DTYPE)
-    rc = lib.orc_collide(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), int(want_contact), int(analytic), _ptr(out),
-                         threads or default_threads())
+    with _Walk(lib, walk, len(s)):
+        rc = lib.orc_collide(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), int(want_contact), int(analytic),
+                             _ptr(out), threads or default_threads())
     assert rc == 0
     return out
 
@@ -168,13 +254,26 @@ def ref_directed(batch, dirs, threads=None):
     return out
 
 
-def time_signed_distance(batch, threads=None):
+def support(batch, shape, dirs, walk=None):
+    """Support points [n, 3] of one shape of the batch for directions [n, 3]."""
+    lib = _load()
+    s, v, _ = _prep(batch)
+    d = np.ascontiguousarray(dirs, np.float64).reshape(-1, 3)
+    out = np.zeros((len(d), 3), np.float64)
+    with _Walk(lib, walk, len(s)):
+        assert lib.orc_support(_ptr(s), len(s), _ptr(v), int(shape), _ptr(d), len(d), _ptr(out)) == 0
+    return out
+
+
+def time_signed_distance(batch, threads=None, walk=None):
     """Seconds the restatement takes for the whole batch (wall clock, C++ side)."""
     lib = _load()
     s, v, p = _prep(batch)
     out = np.zeros(len(p), RESULT_DTYPE)
-    return lib.orc_time_signed_distance(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), _ptr(out),
-                                        threads or default_threads()), out
+    with _Walk(lib, walk, len(s)):
+        t = lib.orc_time_signed_distance(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), _ptr(out),
+                                         threads or default_threads())
+    return t, out
 
 
 def ref_signed_distance(batch, guess=None, threads=None, gjk_max_iter=0, gjk_tol=0.0):

@@ -53,12 +53,24 @@ struct OrcResult {
 
 int orc_result_size() { return (int)sizeof(OrcResult); }
 
+// Convex walk tables for the next query calls over n_shapes shapes: off[i] =
+// start of shape i's table in nbr (Convex::neighbors_ layout: nv row offsets,
+// each row a count then vertex indices), -1 for a scan.  Null clears them.
+void orc_set_walk(const int64_t* off, int n_shapes, const int32_t* nbr);
+
 }  // extern "C"
 
 namespace {
 
+// Neighbour tables for the convex walk (orc_set_walk): per shape the offset of
+// its table in g_walk_nbr, or -1.  Set before a query call, cleared after.
+const int64_t* g_walk_off = nullptr;
+const int32_t* g_walk_nbr = nullptr;
+int g_walk_n = 0;
+
 std::vector<orc::Shape> makeShapes(const ShapeRec* s, int n, const float* verts) {
   std::vector<orc::Shape> out((size_t)n);
+  const bool walk = g_walk_off && g_walk_nbr && g_walk_n == n;
   for (int i = 0; i < n; ++i) {
     orc::Shape& o = out[(size_t)i];
     o.type = s[i].type;
@@ -67,6 +79,7 @@ std::vector<orc::Shape> makeShapes(const ShapeRec* s, int n, const float* verts)
       o.verts = verts + 4 * (size_t)s[i].vert_offset;
       o.nv = (int)s[i].vert_count;
       o.interior = orc::convexMean(o.verts, o.nv);
+      if (walk && g_walk_off[i] >= 0) orc::initWalk(o, g_walk_nbr + g_walk_off[i]);
     }
   }
   return out;
@@ -128,6 +141,12 @@ orc::SolverParams params(int gjk_max_iter, double gjk_tol, int epa_max_faces, in
 }
 
 }  // namespace
+
+extern "C" void orc_set_walk(const int64_t* off, int n_shapes, const int32_t* nbr) {
+  g_walk_off = off;
+  g_walk_nbr = nbr;
+  g_walk_n = off ? n_shapes : 0;
+}
 
 extern "C" {
 
@@ -253,12 +272,32 @@ int orc_directed_raw(const void* shapes, int n_shapes, const float* verts, const
   return 0;
 }
 
-// Wall-clock seconds of orc_signed_distance over the pairs (for the CPU
-// baseline; excludes nothing but the call itself).
+// Support point of one shape for n directions (dirs, out: n x 3), through
+// the same shape set-up (and walk tables) as the queries.
+int orc_support(const void* shapes, int n_shapes, const float* verts, int shape, const double* dirs, int n,
+                double* out) {
+  if (shape < 0 || shape >= n_shapes) return -1;
+  const auto sh = makeShapes((const ShapeRec*)shapes, n_shapes, verts);
+  for (int i = 0; i < n; ++i) {
+    const orc::V3 p = orc::support(sh[(size_t)shape], orc::V3(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]));
+    for (int k = 0; k < 3; ++k) out[3 * i + k] = p[k];
+  }
+  return 0;
+}
+
+// Wall-clock seconds of the orc_signed_distance queries over the pairs (for
+// the CPU baseline).  Shape set-up (vertex means, the walk's cached axis
+// extremes) is outside the clock: fcl::Convex does it once at construction.
 double orc_time_signed_distance(const void* shapes, int n_shapes, const float* verts, const void* pairs, int n_pairs,
                                 OrcResult* out, int n_threads) {
+  if (n_pairs < 0 || n_shapes < 0) return -1;
+  const auto sh = makeShapes((const ShapeRec*)shapes, n_shapes, verts);
+  const PairRec* pr = (const PairRec*)pairs;
+  const orc::SolverParams sp = params(0, 0, 0, 0, 0);
   const auto t0 = std::chrono::steady_clock::now();
-  orc_signed_distance(shapes, n_shapes, verts, pairs, n_pairs, nullptr, out, n_threads, 0, 0, 0, 0, 0);
+  parallelFor(n_pairs, n_threads, [&](int b, int e) {
+    for (int i = b; i < e; ++i) fill(out[i], orc::signedDistance(makeDiff(sh, pr[i]), sp, nullptr), false);
+  });
   const auto t1 = std::chrono::steady_clock::now();
   return std::chrono::duration<double>(t1 - t0).count();
 }

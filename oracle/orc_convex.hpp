@@ -13,11 +13,11 @@
 // the restatement and the reference compiled through oracle/eigen_shim agree
 // bit for bit when both are built with -ffp-contract=off.
 //
-// Deliberate difference: Convex support always uses the naive O(V) scan
-// (include/fcl/geometry/shape/convex-inl.h:133-149).  For V > 32 the reference
-// hill-climbs over vertex neighbours (convex-inl.h:201-283), which on a convex
-// hull reaches the same maximum support value; only the vertex picked on an
-// exact tie can differ.
+// Convex support: the naive O(V) scan (include/fcl/geometry/shape/convex-inl.h:133-149)
+// unless the shape carries a neighbour table (Convex::neighbors_ layout,
+// convex-inl.h:379-405); then the reference's hill climb from six cached
+// axis-extreme vertices (convex-inl.h:153-283), which fcl::Convex uses for
+// hulls of more than 32 vertices.  Callers choose which shapes get a table.
 #pragma once
 
 #include <algorithm>
@@ -85,6 +85,8 @@ struct Shape {
   int32_t nv = 0;
   double p[3] = {0, 0, 0};       // box: side; sphere: radius; capsule/cylinder: radius, lz
   V3 interior;                   // convex: vertex mean; primitives: zero
+  const int32_t* nbr = nullptr;  // convex: neighbour table (walk), or null (scan)
+  int start[6] = {0, 0, 0, 0, 0, 0};  // walk: extreme vertex along +x, -x, +y, -y, +z, -z
 };
 
 // Convex interior point = vertex mean, convex-inl.h:58-63.
@@ -94,8 +96,61 @@ inline V3 convexMean(const float* v, int n) {
   return sum * (double)(1.0 / (double)n);
 }
 
+// Convex::findExtremeVertexIndexNaive, convex-inl.h:133-149 (first maximum).
+inline int convexScan(const float* v, int n, const V3& d) {
+  int best = 0;
+  double best_val = dot(d, V3(v[0], v[1], v[2]));
+  for (int i = 1; i < n; ++i) {
+    const double val = dot(d, V3(v[4 * i], v[4 * i + 1], v[4 * i + 2]));
+    if (val > best_val) { best = i; best_val = val; }
+  }
+  return best;
+}
+
+// Convex::initExtremeViaNeighborCache, convex-inl.h:153-199: the naive
+// extreme vertex along each signed unit axis.
+inline void initWalk(Shape& s, const int32_t* nbr) {
+  s.nbr = nbr;
+  const V3 axes[6] = {V3(1, 0, 0), V3(-1, 0, 0), V3(0, 1, 0), V3(0, -1, 0), V3(0, 0, 1), V3(0, 0, -1)};
+  for (int k = 0; k < 6; ++k) s.start[k] = convexScan(s.verts, s.nv, axes[k]);
+}
+
+// Convex::findExtremeVertexViaNeighbours, convex-inl.h:201-283.
+inline int convexWalk(const Shape& s, const V3& d) {
+  const V3 axes[6] = {V3(1, 0, 0), V3(-1, 0, 0), V3(0, 1, 0), V3(0, -1, 0), V3(0, 0, 1), V3(0, 0, -1)};
+  int init = -1;
+  double max_dot = 0;
+  for (int k = 0; k < 6; ++k) {
+    const double dv = dot(axes[k], d);
+    if (init < 0 || dv > max_dot) { init = s.start[k]; max_dot = dv; }
+  }
+  const float* v = s.verts;
+  const int32_t* nb = s.nbr;
+  int ext = init;
+  double ext_val = dot(d, V3(v[4 * ext], v[4 * ext + 1], v[4 * ext + 2]));
+  int parent0 = init, parent1 = init;
+  bool keep = true;
+  while (keep) {
+    keep = false;
+    const int first = nb[ext], count = nb[first], old = ext;
+    for (int j = first + 1; j <= first + count; ++j) {
+      const int n = nb[j];
+      if (n == parent0 || n == parent1) continue;
+      const double val = dot(d, V3(v[4 * n], v[4 * n + 1], v[4 * n + 2]));
+      if (val > ext_val) {
+        parent1 = ext;
+        keep = true;
+        ext = n;
+        ext_val = val;
+      }
+    }
+    parent0 = old;
+  }
+  return ext;
+}
+
 // Supports: gjk_shape.hpp:44-51 (box), :65-71 (sphere), :101-117 (capsule),
-// :161-177 (cylinder); convex naive scan convex-inl.h:133-149.
+// :161-177 (cylinder); convex: Convex::findExtremeVertex, convex-inl.h:111-121.
 inline V3 support(const Shape& s, const V3& d) {
   switch (s.type) {
     case kBox:
@@ -121,12 +176,7 @@ inline V3 support(const Shape& s, const V3& d) {
     }
     case kConvex: {
       const float* v = s.verts;
-      int best = 0;
-      double best_val = dot(d, V3(v[0], v[1], v[2]));
-      for (int i = 1; i < s.nv; ++i) {
-        const double val = dot(d, V3(v[4 * i], v[4 * i + 1], v[4 * i + 2]));
-        if (val > best_val) { best = i; best_val = val; }
-      }
+      const int best = s.nbr ? convexWalk(s, d) : convexScan(v, s.nv, d);
       return V3(v[4 * best], v[4 * best + 1], v[4 * best + 2]);
     }
     default:
