@@ -283,7 +283,7 @@ int fclg_autotune(fclg_context* ctx, const fclg_pair* d_pairs, uint32_t n_pairs,
    then replay with fclg_graph_launch after refilling d_pairs.  The capture
    allocates the query's scratch first; a graph goes stale (launch returns
    FCLG_E_INVALID) when the context later reallocates that scratch for a
-   larger batch.  No counterpart in the reference. */
+   larger batch or its shapes are set again.  No counterpart in the reference. */
 typedef struct fclg_graph fclg_graph;
 int fclg_graph_create(fclg_context* ctx, const fclg_pair* d_pairs, uint32_t n_pairs, const fclg_request* req,
                       fclg_result* d_results, int distance_query, fclg_graph** graph);

@@ -139,6 +139,7 @@ void release_shapes(fclg_context* c) {
   c->walk_tab = nullptr;
   c->hull_ents = nullptr;
   c->walk_hulls = 0;
+  c->scratch_epoch += 1;  // captured graphs hold the old shape pointers
   c->own_shapes = c->own_verts = nullptr;
   c->shapes = nullptr;
   c->verts = nullptr;

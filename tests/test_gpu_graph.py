@@ -4,7 +4,8 @@
 * A replayed graph gives the same bytes as the direct device query on the same
   pairs, also after the pair buffer is refilled between replays (same size).
 * A graph goes stale when the context reallocates its scratch for a larger
-  batch; launching it then fails with an error instead of touching freed memory.
+  batch or its shapes are set again; launching it then fails with an error
+  instead of touching freed memory.
 * The autotuned launch shape answers like the default one: collision flags
   identical, distances within 1e-5 m for >= 99.9 % of pairs (lane counts change
   the support scan's order, hence FP32 rounding, not the algorithm).
@@ -52,9 +53,14 @@ def test_graph_replay_matches_direct_query(torch):
             torch.cuda.synchronize()
             got = d_res.cpu().numpy().tobytes()
             assert got == _direct(torch, ctx, _dev(torch, pairs), n)
-        # a larger batch reallocates the scratch: the graph must refuse to run
-        big = workloads.mixed(3 * n, seed=workloads.SEED_BASE + 502)
-        ctx.set_batch(big)
+        # setting the shapes again frees the old shape (and walk) buffers: stale
+        ctx.set_batch(b)
+        with pytest.raises(FclgError, match="stale"):
+            g.launch()
+        g.close()
+        # a larger batch reallocates the scratch: a graph captured before it must refuse to run
+        g = ctx.graph(d_pairs.data_ptr(), n, d_res.data_ptr())
+        big = b.subset(np.concatenate([np.arange(n)] * 3))
         _direct(torch, ctx, _dev(torch, big.pairs), big.n_pairs)
         with pytest.raises(FclgError, match="stale"):
             g.launch()
