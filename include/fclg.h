@@ -247,7 +247,7 @@ int fclg_collide_directed_device(fclg_context* ctx, const fclg_pair* d_pairs, ui
    gjk_lanes_small lanes per pair, the rest with gjk_lanes_large.  Zero
    fields keep the current value.  Defaults: bucketing on, 1 and 4 lanes,
    128 vertices, 4 GJK and 6 EPA CTAs per SM (the EPA pass's first,
-   128-face layout), support walk on.
+   128-face layout), support walk off.
    support_walk: hulls of more than 32 vertices get their edge graph built on
    the host when shapes are set (a quickhull per hull, spread over the host's
    threads); a GJK / MPR launch with one lane per pair then finds a hull's
@@ -255,7 +255,10 @@ int fclg_collide_directed_device(fclg_context* ctx, const fclg_pair* d_pairs, ui
    corners, the rule of Convex::findExtremeVertexViaNeighbours
    (geometry/shape/convex-inl.h:201-283), instead of scanning every vertex.
    Groups of several lanes and the EPA pass scan.  Both give the vertex of
-   maximal support value; they may differ only where several vertices tie. */
+   maximal support value; they may differ only where several vertices tie.
+   Off by default: on GB300 the one-lane scan of an L1-resident hull measured
+   faster (lanes of a warp walk paths of different lengths); fclg_autotune
+   tries both. */
 typedef struct fclg_tuning {
   int32_t bucketing;            /* 1 on, -1 off, 0 unchanged */
   int32_t gjk_lanes_small;      /* 1, 2, 4, 8, 16 or 32 */

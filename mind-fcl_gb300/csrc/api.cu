@@ -34,7 +34,7 @@ struct fclg_context {
   uint32_t* walk_tab = nullptr;
   float4* hull_ents = nullptr;
   uint32_t walk_hulls = 0;
-  bool support_walk = true;
+  bool support_walk = false;
   // scratch handed from the GJK pass to the EPA pass
   uint32_t* epa_count = nullptr;  // [2]: work list, overflow list
   uint32_t* epa_list = nullptr;

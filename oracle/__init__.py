@@ -69,6 +69,8 @@ def _load():
         lib.orc_set_walk.restype = None
         lib.orc_support.argtypes = [vp, i, vp, i, vp, i, vp]
         lib.orc_support.restype = i
+        lib.orc_box_box.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+        lib.orc_box_box.restype = i
         _lib = lib
     return _lib
 
@@ -252,6 +254,16 @@ def ref_directed(batch, dirs, threads=None):
     assert lib.ref_directed(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), _ptr(d), _ptr(out),
                             threads or default_threads()) == 0
     return out
+
+
+def box_box(side1, R1, T1, side2, R2, T2):
+    """boxBox2 in FP64 on two posed boxes (world frame), as boxBoxIntersect calls
+    it: (code, normal, depth or separation, contacts [n, 4] = pos, depth)."""
+    lib = _load()
+    a = [np.ascontiguousarray(x, np.float64).reshape(-1) for x in (side1, R1, T1, side2, R2, T2)]
+    out = np.zeros(6 + 16)
+    n = lib.orc_box_box(*[_ptr(x) for x in a], _ptr(out))
+    return int(out[4]), out[0:3].copy(), float(out[3]), out[6:6 + 4 * n].reshape(n, 4).copy()
 
 
 def support(batch, shape, dirs, walk=None):

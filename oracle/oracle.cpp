@@ -272,6 +272,29 @@ int orc_directed_raw(const void* shapes, int n_shapes, const float* verts, const
   return 0;
 }
 
+// boxBox2 (box_box-inl.h:214-802) on two posed boxes in FP64, as
+// boxBoxIntersect calls it (maxc 4): out = normal[3], depth, code, count, then
+// count x (pos[3], depth).  Returns the contact count.
+int orc_box_box(const double* side1, const double* R1, const double* T1, const double* side2, const double* R2,
+                const double* T2, double* out) {
+  orc::BoxContact c[4];
+  orc::V3 normal;
+  double depth = 0, sep = 0;
+  int code = 0;
+  const int n = orc::boxBox2(orc::V3(side1[0], side1[1], side1[2]), R1, orc::V3(T1[0], T1[1], T1[2]),
+                             orc::V3(side2[0], side2[1], side2[2]), R2, orc::V3(T2[0], T2[1], T2[2]), normal, depth,
+                             code, 4, c, sep);
+  for (int k = 0; k < 3; ++k) out[k] = normal[k];
+  out[3] = code ? depth : sep;
+  out[4] = code;
+  out[5] = n;
+  for (int j = 0; j < n; ++j) {
+    for (int k = 0; k < 3; ++k) out[6 + 4 * j + k] = c[j].pos[k];
+    out[6 + 4 * j + 3] = c[j].depth;
+  }
+  return n;
+}
+
 // Support point of one shape for n directions (dirs, out: n x 3), through
 // the same shape set-up (and walk tables) as the queries.
 int orc_support(const void* shapes, int n_shapes, const float* verts, int shape, const double* dirs, int n,
