@@ -69,6 +69,10 @@ def parse():
                          "warm-start inference kernel alone on 2.24M arm pairs")
     ap.add_argument("--no-warm", action="store_true", help="skip the warm-start comparison")
     ap.add_argument("--poses", type=int, default=65536)
+    ap.add_argument("--configs", type=int, default=100_000, help="arm: joint configurations (7 x 32 pairs each)")
+    ap.add_argument("--sweep", action="store_true",
+                    help="convex workloads: time one query per launch layout (GJK lanes, hull split, support "
+                         "walk on / off) and print them as one JSON object instead of the bench line")
     return ap.parse_args()
 
 
@@ -459,13 +463,13 @@ def run_warmstart_kernel(args):
     return 0
 
 
-def rank_batch(workloads, workload, rank, pairs=N_PAIRS):
+def rank_batch(workloads, workload, rank, pairs=N_PAIRS, configs=100_000):
     """This rank's batch: every rank draws its own seeded batch of the same
     shape (weak scaling; pairs are independent, nothing is exchanged)."""
     if workload == "mixed":
         return workloads.mixed(pairs, seed=workloads.SEED_BASE + 1 + rank)
     if workload == "arm":
-        return workloads.arm(100_000, seed=workloads.SEED_BASE + 3 + 100 * rank)
+        return workloads.arm(configs, seed=workloads.SEED_BASE + 3 + 100 * rank)
     if workload == "pareto":
         return workloads.pareto(seed=workloads.SEED_BASE + 4 + 100 * rank)
     return workloads.plain_small(seed=workloads.SEED_BASE + 0 + 100 * rank)
@@ -483,6 +487,33 @@ def max_over_ranks(torch, ms, dev, world):
 def job_value(n_per_rank, world, ms):
     """Whole-job throughput: the units all ranks processed over the slowest rank's time."""
     return n_per_rank * world / (ms * 1e-3)
+
+
+SWEEP_LAYOUTS = [(1, 1, 128), (1, 4, 128), (1, 2, 128), (1, 1, 256), (2, 4, 128), (4, 8, 128)]
+
+
+def launch_sweep(args, torch, ctx, step, stream, n, t_set):
+    """Mean device time of one query per launch layout (GJK lanes for small /
+    large hulls, hull split) with the refilling one-lane GJK pass on and off
+    and the support walk on and off."""
+    rows = []
+    for walk, refill in ((False, True), (False, False), (True, True)):
+        for ls, ll, lh in SWEEP_LAYOUTS:
+            ctx.set_tuning(bucketing=True, gjk_lanes_small=ls, gjk_lanes_large=ll, large_hull_vertices=lh,
+                           support_walk=walk, gjk_refill=refill)
+            for _ in range(2):
+                step()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(5):
+                step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            rows.append({"walk": walk, "refill": refill, "lanes_small": ls, "lanes_large": ll, "large_hull": lh,
+                         "ms": e0.elapsed_time(e1) / 5})
+    print(json.dumps({"sweep": args.workload, "pairs": n, "set_shapes_s": t_set, "rows": rows}))
+    return 0
 
 
 def main():
@@ -505,16 +536,21 @@ def main():
     from fclg import workloads
     from fclg.api import Context
     gen, algo_bytes, workload_text = CONVEX_WORKLOADS[args.workload]
-    batch = rank_batch(workloads, args.workload, rank, args.pairs)
+    batch = rank_batch(workloads, args.workload, rank, args.pairs, args.configs)
     n = batch.n_pairs
     ctx = Context(local)
+    t_set = time.perf_counter()
     ctx.set_batch(batch)
+    t_set = time.perf_counter() - t_set
     stream = torch.cuda.current_stream(dev)
     d_pairs = torch.from_numpy(batch.pairs.view(np.uint8).copy()).to(dev)
     d_res = torch.empty(n * 48, dtype=torch.uint8, device=dev)
 
     def step():
         ctx.distance_device(d_pairs.data_ptr(), n, d_res.data_ptr(), None, stream.cuda_stream)
+
+    if args.sweep:
+        return launch_sweep(args, torch, ctx, step, stream, n, t_set)
 
     # launch shape chosen by the library's autotuner on this batch (untimed)
     tuning, tune_ms = ctx.autotune(d_pairs.data_ptr(), n, d_res.data_ptr())

@@ -247,7 +247,11 @@ int fclg_collide_directed_device(fclg_context* ctx, const fclg_pair* d_pairs, ui
    gjk_lanes_small lanes per pair, the rest with gjk_lanes_large.  Zero
    fields keep the current value.  Defaults: bucketing on, 1 and 4 lanes,
    128 vertices, 4 GJK and 6 EPA CTAs per SM (the EPA pass's first,
-   128-face layout), support walk off.
+   128-face layout), support walk off, GJK refill on.
+   gjk_refill: one-lane GJK launches of distance queries (and of collides
+   without MPR or closed-form pairs) keep every lane of a warp busy by handing
+   a lane whose pair has finished the next pair of its warp's share, instead
+   of letting 32 pairs wait for the slowest of them; answers are the same.
    support_walk: hulls of more than 32 vertices get their edge graph built on
    the host when shapes are set (a quickhull per hull, spread over the host's
    threads); a GJK / MPR launch with one lane per pair then finds a hull's
@@ -267,6 +271,7 @@ typedef struct fclg_tuning {
   int32_t gjk_ctas_per_sm;
   int32_t epa_ctas_per_sm;
   int32_t support_walk;         /* 1 on, -1 off, 0 unchanged */
+  int32_t gjk_refill;           /* 1 on, -1 off, 0 unchanged */
 } fclg_tuning;
 int fclg_set_tuning(fclg_context* ctx, const fclg_tuning* tuning);
 int fclg_get_tuning(const fclg_context* ctx, fclg_tuning* tuning);

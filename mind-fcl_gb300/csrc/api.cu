@@ -35,6 +35,7 @@ struct fclg_context {
   float4* hull_ents = nullptr;
   uint32_t walk_hulls = 0;
   bool support_walk = false;
+  bool gjk_refill = true;
   // scratch handed from the GJK pass to the EPA pass
   uint32_t* epa_count = nullptr;  // [2]: work list, overflow list
   uint32_t* epa_list = nullptr;
@@ -355,11 +356,12 @@ int run_query(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_
                            c->bk_small + 2 * fclg::kBucketKeys};
     FCLG_CUDA(c, fclg::launch_bucketing(b, bs, (uint32_t)c->large_hull, st));
     const int blocks = c->num_sms * c->gjk_ctas_per_sm;
-    FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes, bs.order, bs.ranges, blocks, st));
-    FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes_large, bs.order, bs.ranges + 2, blocks, st));
+    FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes, bs.order, bs.ranges, blocks, st, c->gjk_refill));
+    FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes_large, bs.order, bs.ranges + 2, blocks, st,
+                                  c->gjk_refill));
     c->launches += 5;
   } else {
-    FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes, nullptr, nullptr, 0, st));
+    FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes, nullptr, nullptr, 0, st, c->gjk_refill));
     c->launches += 1;
   }
   if (c->profiling) FCLG_CUDA(c, cudaEventRecord(c->ev[1], st));
@@ -547,6 +549,7 @@ int fclg_set_tuning(fclg_context* c, const fclg_tuning* t) {
   if (t->gjk_ctas_per_sm) c->gjk_ctas_per_sm = t->gjk_ctas_per_sm;
   if (t->epa_ctas_per_sm) c->epa_ctas_per_sm = t->epa_ctas_per_sm;
   if (t->support_walk) c->support_walk = t->support_walk > 0;
+  if (t->gjk_refill) c->gjk_refill = t->gjk_refill > 0;
   return FCLG_OK;
 }
 
@@ -559,6 +562,7 @@ int fclg_get_tuning(const fclg_context* c, fclg_tuning* t) {
   t->gjk_ctas_per_sm = c->gjk_ctas_per_sm;
   t->epa_ctas_per_sm = c->epa_ctas_per_sm;
   t->support_walk = c->support_walk ? 1 : -1;
+  t->gjk_refill = c->gjk_refill ? 1 : -1;
   return FCLG_OK;
 }
 
@@ -817,7 +821,7 @@ extern "C" int fclg_distance_device_static(fclg_context* c, const fclg_pair* d_p
   fclg::EpaQueue q{counts, reinterpret_cast<uint32_t*>(base + kStaticListOffset),
                    reinterpret_cast<float4*>(base + kStaticRecOffset)};
   if (prm.want_epa) FCLG_CUDA(c, cudaMemsetAsync(counts, 0, 2 * sizeof(uint32_t), st));
-  FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes, nullptr, nullptr, 0, st));
+  FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes, nullptr, nullptr, 0, st, c->gjk_refill));
   c->launches += 1;
   if (prm.want_epa) {
     fclg::EpaQueue ovf{counts + 1, reinterpret_cast<uint32_t*>(base + kStaticOvfOffset), nullptr};
@@ -993,16 +997,20 @@ extern "C" int fclg_autotune(fclg_context* c, const fclg_pair* d_pairs, uint32_t
   for (int ls : {1, 2, 4, 8})
     for (int ll : {1, 4, 8, 16})
       for (int lh : {64, 128, 256})
-        for (int walk : {1, -1}) {
-          if (walk < 0 && (!c->walk_tab || (ls != 1 && ll != 1))) continue;
-          fclg_tuning t = keep;
-          t.bucketing = 1;
-          t.gjk_lanes_small = ls;
-          t.gjk_lanes_large = ll;
-          t.large_hull_vertices = lh;
-          t.support_walk = walk;
-          cand.push_back(t);
-        }
+        for (int walk : {1, -1})
+          for (int refill : {1, -1}) {
+            // the walk and the refilling kernel only change one-lane launches
+            if (ls != 1 && ll != 1 && (walk < 0 || refill < 0)) continue;
+            if (walk < 0 && !c->walk_tab) continue;
+            fclg_tuning t = keep;
+            t.bucketing = 1;
+            t.gjk_lanes_small = ls;
+            t.gjk_lanes_large = ll;
+            t.large_hull_vertices = lh;
+            t.support_walk = walk;
+            t.gjk_refill = refill;
+            cand.push_back(t);
+          }
   {
     fclg_tuning t = keep;
     t.bucketing = -1;

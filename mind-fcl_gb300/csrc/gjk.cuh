@@ -368,6 +368,153 @@ __device__ FCLG_GJK_COLD bool extract_try_sub(const Simplex& s, f3& p0, f3& p1) 
   return true;
 }
 
+// GJK boolean (gjk.hpp:10-140) then, for a separating vertex, the minimum
+// distance loop (gjk_distance.hpp:10-105) as a machine that advances by one
+// support evaluation per step(): begin() sets it up, step() returns true once
+// o holds the answer.  The refilling GJK pass (gjk_pass.cuh) interleaves the
+// steps of 32 pairs per warp and hands a finished lane its next pair.  The
+// same decisions in the same order as gjk_evaluate / min_distance below (the
+// loop form, which the group-per-pair pass keeps: its register allocation
+// does not survive the machine form); the two passes' answers are compared
+// bit for bit in the tests.
+struct GjkRun {
+  Simplex s;
+  f3 d;        // boolean: search direction; distance: next direction
+  f3 cur;      // distance: current closest point of the simplex
+  float book;  // distance: |cur|
+  int phase;   // 0 first support, 1 boolean loop, 2 distance loop, 3 done
+  int it;      // iteration of the current loop
+  GjkOut o;
+
+  __device__ __forceinline__ void begin(f3 guess) {
+    o.point_valid = false;
+    o.iterations = 0;
+    o.p0 = o.p1 = mk3(0, 0, 0);
+    d = guess;
+    if (sqn(d) <= 0.f) d = mk3(1, 0, 0);
+    d = normalized(d);
+    phase = 0;
+    it = 0;
+  }
+
+  __device__ __forceinline__ bool done() {
+    phase = 3;
+    return true;
+  }
+
+  // gjk.hpp:112-140 for the undetermined outcomes (no progress, iteration limit)
+  __device__ __forceinline__ bool undetermined(int status, bool want_distance) {
+    o.status = status;
+    if (want_distance) o.point_valid = extract_try_sub(s, o.p0, o.p1);
+    return done();
+  }
+
+  __device__ __forceinline__ bool distance_result(bool valid) {
+    o.point_valid = valid && extract_no_sub(s, o.p0, o.p1);
+    return done();
+  }
+
+  // separated: the rank-1 simplex s seeds the distance loop (gjk_distance.hpp:10-40)
+  __device__ __forceinline__ bool enter_distance(float tol, int max_iter, bool want_distance) {
+    o.status = kGjkSeparated;
+    s.rank = 1;
+    if (!want_distance) return done();
+    if (update_simplex(s, cur, tol) != Upd::OK) return done();
+    book = nrm(cur);
+    if (book <= tol) return distance_result(true);
+    d = cur * (-1.f / book);
+    phase = 2;
+    it = 0;
+    if (max_iter <= 0) return done();
+    return false;
+  }
+
+  template <class Sup>
+  __device__ __forceinline__ bool step(const Sup& sup, float tol, int max_iter, bool want_distance) {
+    const float tol2 = tol * tol;
+    f3 pa, pb;
+    if (phase == 0) {
+      sup(d, pa, pb);
+      s.set(0, pa, pb);
+      s.rank = 1;
+      if (sqn(s.w[0]) <= tol2) {
+        o.status = kGjkIntersect;
+        return done();
+      }
+      if (dot(s.w[0], d) < 0.f) return enter_distance(tol, max_iter, want_distance);
+      d = -d;
+      phase = 1;
+      it = 0;
+      if (max_iter <= 0) return undetermined(kGjkIterLimit, want_distance);
+      return false;
+    }
+    if (phase == 1) {
+      o.iterations = it + 1;
+      sup(d, pa, pb);
+      const f3 w = pa - pb;
+      if (dot(w, d) < 0.f) {
+        s.set(0, pa, pb);  // the separating vertex seeds the distance simplex
+        return enter_distance(tol, max_iter, want_distance);
+      }
+      bool dup = false;
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (j < s.rank && sqn(s.w[j] - w) < tol2) dup = true;
+      if (dup) return undetermined(kGjkNoProgress, want_distance);
+      if (s.rank == 1) s.set(1, pa, pb);
+      else if (s.rank == 2) s.set(2, pa, pb);
+      else s.set(3, pa, pb);
+      s.rank += 1;
+      if (sqn(w) <= tol2) {
+        o.status = kGjkIntersect;
+        return done();
+      }
+      Proj st;
+      if (s.rank == 2) st = project2(s, d);
+      else if (s.rank == 3) st = project3(s, d, tol);
+      else st = project4(s, d, tol);
+      if (st == Proj::Failed) {
+        o.status = kGjkFailed;
+        return done();
+      }
+      if (st == Proj::Intersect) {
+        o.status = kGjkIntersect;
+        return done();
+      }
+      if (st == Proj::ZeroVolume) return undetermined(kGjkNoProgress, want_distance);
+      if (++it >= max_iter) return undetermined(kGjkIterLimit, want_distance);
+      return false;
+    }
+    // phase 2: one iteration of the minimum-distance loop (gjk_distance.hpp:41-105)
+    ++o.iterations;
+    sup(d, pa, pb);
+    const f3 w = pa - pb;
+    FCLG_GJK_TRACE(it, -1, dot(d, w - cur), 0.f);
+    if (dot(d, w - cur) < tol) return distance_result(true);
+    bool dup = false;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (j < s.rank && sqn(s.w[j] - w) < tol2) dup = true;
+    if (dup) return distance_result(true);
+    // s.rank is 1..3 here
+    if (s.rank == 1) s.set(1, pa, pb);
+    else if (s.rank == 2) s.set(2, pa, pb);
+    else s.set(3, pa, pb);
+    s.rank += 1;
+    const Upd st = update_simplex(s, cur, tol);
+    if (st == Upd::NoImprovement) return distance_result(true);
+    if (st != Upd::OK) return done();
+    const float nd = nrm(cur);
+    FCLG_GJK_TRACE(it, s.rank, nd, book - nd);
+    if (book - nd < tol) return distance_result(true);
+    if (nd < tol) return distance_result(true);
+    book = nd;
+    d = cur * (-1.f / book);
+    if (++it >= max_iter) return done();
+    return false;
+  }
+};
+
 // gjk_distance.hpp:10-105: minimum distance from a separating vertex.
 template <class Sup>
 __device__ __forceinline__ bool min_distance(const Sup& sup, Simplex& s, float tol, int max_iter, f3& p0, f3& p1,

@@ -1,4 +1,5 @@
-// GJK pass launcher: picks the lane count's instantiation (gjk_pass_l*.cu).
+// GJK pass launcher: picks the lane count's instantiation (gjk_pass_l*.cu),
+// or the refilling one-lane pass defined here.
 #include "gjk_pass.cuh"
 
 namespace fclg {
@@ -6,13 +7,81 @@ namespace fclg {
 FCLG_GJK_INSTANTIATE(1)
 FCLG_GJK_INSTANTIATE(2)
 
+// One lane per pair, pairs refilled per lane: every lane of a warp steps its
+// own pair's GJK run one support evaluation at a time (GjkRun), and a lane
+// whose pair is done takes the next one from its warp's share of the items
+// (warp w takes items 32 (w + k W) .. 32 (w + k W) + 31, k = 0, 1, ...,
+// W warps in the grid, in the order its lanes come free).  A warp's lanes so
+// stay busy until its share runs out, instead of each round of 32 pairs
+// waiting for its slowest pair.  For queries without MPR, closed-form pairs
+// or a warm start; the results equal gjk_pass<1>'s (the same GjkRun).
+__global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_refill(BatchArgs b, QueryParams prm, EpaQueue q,
+                                                               const uint32_t* __restrict__ order,
+                                                               const uint32_t* __restrict__ range) {
+  uint32_t begin = 0, end = b.n_pairs;
+  if (range) {
+    begin = range[0];
+    end = range[1];
+  }
+  const unsigned lane = threadIdx.x & 31u;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
+  const Group<1> g = Group<1>::make();
+  // GJKSolver's default guess (1, 0, 0), gjk_solver-inl.h:1129
+  const f3 plain = mk3(1.f, 0.f, 0.f);
+  MinkowskiSupport<1> sup;
+  sup.verts = b.verts;
+  sup.hull = b.hull;
+  sup.g = g;
+  GjkRun run;
+  uint32_t pid = 0;
+  bool live = false;
+  uint32_t next = 0;  // warp-uniform: next unassigned position in the warp's share
+  for (;;) {
+    const unsigned want = __ballot_sync(0xFFFFFFFFu, !live);
+    if (!live) {
+      const uint32_t k = next + (uint32_t)__popc(want & ((1u << lane) - 1u));
+      const uint64_t item = (uint64_t)begin + ((uint64_t)(k >> 5) * n_warps + warp) * 32u + (k & 31u);
+      if (item < end) {
+        pid = order ? order[item] : (uint32_t)item;
+        const PairDev pr = load_pair(b.pairs, pid);
+        if (pr.a >= b.n_shapes || pr.b >= b.n_shapes) {
+          store_invalid(b.results, pid);
+        } else {
+          sup.A = load_shape(b.shapes, b.walk, pr.a);
+          sup.B = load_shape(b.shapes, b.walk, pr.b);
+          sup.pose = pr.pose;
+          run.begin(-plain);
+          live = true;
+        }
+      }
+    }
+    next += (uint32_t)__popc(want);
+    if (__all_sync(0xFFFFFFFFu, !live)) {
+      // no lane holds a pair: stop once the warp's next position is past the share
+      const uint64_t first = (uint64_t)begin + ((uint64_t)(next >> 5) * n_warps + warp) * 32u + (next & 31u);
+      if (first >= end) break;
+      continue;
+    }
+    if (live && run.step(sup, prm.gjk_tol, prm.gjk_max_iter, prm.want_distance != 0)) {
+      finish_pair(b, prm, q, pid, run.o, run.s);
+      live = false;
+    }
+  }
+}
+
+
 cudaError_t launch_gjk(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q, int lanes,
-                       const uint32_t* order, const uint32_t* range, int blocks, cudaStream_t st) {
+                       const uint32_t* order, const uint32_t* range, int blocks, cudaStream_t st, bool refill) {
   if (b.n_pairs == 0) return cudaSuccess;
   const int threads = 128;
   if (blocks <= 0) {
     const uint64_t total = (uint64_t)b.n_pairs * (uint64_t)lanes;
     blocks = (int)((total + threads - 1) / threads);
+  }
+  if (refill && lanes == 1 && !prm.use_mpr && !prm.analytic && !b.guess) {
+    gjk_refill<<<blocks, threads, 0, st>>>(b, prm, q, order, range);
+    return cudaGetLastError();
   }
   switch (lanes) {
     case 1: return launch_gjk_lanes<1>(b, prm, q, order, range, blocks, st);

@@ -53,6 +53,35 @@ __device__ __forceinline__ void store_invalid(float4* out, uint32_t pid) {
 
 }  // namespace
 
+// The tail of a pair once its GJK run is over: the EPA hand-off for an
+// overlapping pair, else the result record (shared by both GJK kernels).
+__device__ __forceinline__ void finish_pair(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q,
+                                            uint32_t pid, const GjkOut& o, const Simplex& s) {
+  if (o.status == kGjkIntersect) {
+    if (prm.want_epa) {
+      const uint32_t slot = aggregated_slot(q.count);
+      q.list[slot] = pid;
+      write_simplex(q.rec, slot, s, o.iterations);
+      return;
+    }
+    store_result(b.results, pid, 0.f, mk3(0, 0, 1), mk3(0, 0, 0), mk3(0, 0, 0), kGjkIntersect,
+                 (uint32_t)o.iterations, true, true);
+    return;
+  }
+  if (!prm.want_distance) {
+    store_result(b.results, pid, 0.f, mk3(0, 0, 1), mk3(0, 0, 0), mk3(0, 0, 0), o.status, (uint32_t)o.iterations,
+                 false, o.status == kGjkSeparated);
+    return;
+  }
+  // shapeSignedDistance: valid only for a separation certificate with valid points
+  const bool ok = (o.status == kGjkSeparated) && o.point_valid;
+  const f3 dv = o.p1 - o.p0;
+  const float dist = ok ? nrm(dv) : -1.f;
+  f3 nrmv = normalized(dv);
+  if (!(sqn(nrmv) > 0.f)) nrmv = mk3(0, 0, 1);
+  store_result(b.results, pid, dist, nrmv, o.p0, o.p1, o.status, (uint32_t)o.iterations, false, ok);
+}
+
 #ifndef FCLG_GJK_MINB
 #define FCLG_GJK_MINB 4
 #endif
@@ -137,29 +166,7 @@ __global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_pass(BatchArgs b, Quer
       o = gjk_evaluate(sup, -plain, prm.gjk_tol, prm.gjk_max_iter, prm.want_distance != 0, s);
     }
     if (g.lane != 0) continue;
-    if (o.status == kGjkIntersect) {
-      if (prm.want_epa) {
-        const uint32_t slot = aggregated_slot(q.count);
-        q.list[slot] = pid;
-        write_simplex(q.rec, slot, s, o.iterations);
-        continue;
-      }
-      store_result(b.results, pid, 0.f, mk3(0, 0, 1), mk3(0, 0, 0), mk3(0, 0, 0), kGjkIntersect,
-                   (uint32_t)o.iterations, true, true);
-      continue;
-    }
-    if (!prm.want_distance) {
-      store_result(b.results, pid, 0.f, mk3(0, 0, 1), mk3(0, 0, 0), mk3(0, 0, 0), o.status, (uint32_t)o.iterations,
-                   false, o.status == kGjkSeparated);
-      continue;
-    }
-    // shapeSignedDistance: valid only for a separation certificate with valid points
-    const bool ok = (o.status == kGjkSeparated) && o.point_valid;
-    const f3 dv = o.p1 - o.p0;
-    const float dist = ok ? nrm(dv) : -1.f;
-    f3 nrmv = normalized(dv);
-    if (!(sqn(nrmv) > 0.f)) nrmv = mk3(0, 0, 1);
-    store_result(b.results, pid, dist, nrmv, o.p0, o.p1, o.status, (uint32_t)o.iterations, false, ok);
+    finish_pair(b, prm, q, pid, o, s);
   }
 }
 

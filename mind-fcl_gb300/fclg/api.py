@@ -47,7 +47,7 @@ class Tuning(ctypes.Structure):
     _fields_ = [("bucketing", ctypes.c_int32), ("gjk_lanes_small", ctypes.c_int32),
                 ("gjk_lanes_large", ctypes.c_int32), ("large_hull_vertices", ctypes.c_int32),
                 ("gjk_ctas_per_sm", ctypes.c_int32), ("epa_ctas_per_sm", ctypes.c_int32),
-                ("support_walk", ctypes.c_int32)]
+                ("support_walk", ctypes.c_int32), ("gjk_refill", ctypes.c_int32)]
 
 
 class Request(ctypes.Structure):
@@ -258,7 +258,7 @@ class Context:
         """Fields of fclg_tuning by name; unspecified ones keep their value."""
         t = Tuning()
         for k, v in kw.items():
-            if k in ("bucketing", "support_walk") and isinstance(v, bool):
+            if k in ("bucketing", "support_walk", "gjk_refill") and isinstance(v, bool):
                 v = 1 if v else -1
             setattr(t, k, int(v))
         self._check(self.lib.fclg_set_tuning(self.h, ctypes.byref(t)), "fclg_set_tuning")

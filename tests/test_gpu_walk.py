@@ -101,3 +101,43 @@ def test_autotune_considers_the_walk(gpu_ctx):
     best, ms = gpu_ctx.autotune(dp.data_ptr(), n, dr.data_ptr())
     assert best["support_walk"] in (1, -1) and ms > 0
     gpu_ctx.set_tuning(**keep)
+
+
+@pytest.mark.parametrize("workload,n", [("mixed", 200_000), ("pareto", 400_000), ("arm", 2000), ("plain_small", 4096)])
+def test_refill_pass_equals_group_pass(gpu_ctx, workload, n):
+    """gjk_refill (one lane per pair, lanes refilled as their pairs finish)
+    restates the same GJK as gjk_pass<1>: distance answers identical bit for
+    bit, at both lane layouts that use it, with and without bucketing."""
+    keep = gpu_ctx.get_tuning()
+    if workload == "arm":
+        b = workloads.arm(n, seed=workloads.SEED_BASE + 41)
+    else:
+        b = getattr(workloads, workload)(n, seed=workloads.SEED_BASE + 42) if workload != "plain_small" else \
+            workloads.plain_small(seed=workloads.SEED_BASE + 42)
+    gpu_ctx.set_batch(b)
+    try:
+        for bucketing in (True, False):
+            gpu_ctx.set_tuning(bucketing=bucketing, gjk_lanes_small=1, gjk_lanes_large=1, gjk_refill=False)
+            group = gpu_ctx.distance(b.pairs)
+            gpu_ctx.set_tuning(gjk_refill=True)
+            refill = gpu_ctx.distance(b.pairs)
+            assert np.array_equal(group.view(np.uint8), refill.view(np.uint8)), (workload, bucketing)
+    finally:
+        gpu_ctx.set_tuning(**keep)
+
+
+def test_refill_collide_with_contact_equals_group_pass(gpu_ctx):
+    """fcl::collide with penetration and without the closed-form solvers runs
+    the refilling pass too (GJK, then EPA from its simplex)."""
+    NO_ANALYTIC = 16
+    keep = gpu_ctx.get_tuning()
+    b = workloads.mixed(100_000, seed=workloads.SEED_BASE + 43)
+    gpu_ctx.set_batch(b)
+    try:
+        gpu_ctx.set_tuning(gjk_lanes_small=1, gjk_lanes_large=1, gjk_refill=False)
+        group = gpu_ctx.collide(b.pairs, make_request(flags=NO_ANALYTIC))
+        gpu_ctx.set_tuning(gjk_refill=True)
+        refill = gpu_ctx.collide(b.pairs, make_request(flags=NO_ANALYTIC))
+        assert np.array_equal(group.view(np.uint8), refill.view(np.uint8))
+    finally:
+        gpu_ctx.set_tuning(**keep)
