@@ -99,14 +99,18 @@ enum {
   FCLG_REQ_WARM_START = 1u << 2,    /* seed GJK with the learned direction model (fclg_warmstart_*) */
   FCLG_REQ_GJK_BOOLEAN = 1u << 3,   /* boolean collide by GJK instead of MPR (the reference's boolean
                                        fcl::collide runs MPR, falling back to GJK when MPR fails) */
-  FCLG_REQ_NO_ANALYTIC = 1u << 4    /* collide: sphere pairs by MPR / GJK+EPA instead of the closed-form
-                                       solvers fcl::collide dispatches to (sphere-sphere, -capsule,
-                                       -box, -cylinder; gjk_solver-inl.h:209-218) */
+  FCLG_REQ_NO_ANALYTIC = 1u << 4,   /* collide: sphere and box pairs by MPR / GJK+EPA instead of the
+                                       closed-form solvers fcl::collide dispatches to (sphere-sphere,
+                                       -capsule, -box, -cylinder, box-box; gjk_solver-inl.h:209-218) */
+  FCLG_REQ_INCREMENTAL = 1u << 5    /* fclg_collide_directed*: the incremental minimum-distance
+                                       penetration from the directions as hints instead of the
+                                       directed penetration along them */
 };
 /* fclg_result.status bit 16: the boolean was decided by MPR.  Bit 17: the
-   result came from a closed-form sphere-pair solver (contact normal, the
-   contact position +- depth / 2 along it as p_a / p_b; when apart, the
-   centre-based separation with p_a = p_b = 0). */
+   result came from a closed-form solver (sphere pairs, box-box: contact
+   normal, the contact position +- depth / 2 along it as p_a / p_b; when
+   apart, the centre-based separation (sphere pairs) or the gap along the
+   separating axis found (box pairs) with p_a = p_b = 0). */
 #define FCLG_STATUS_MPR (1 << 16)
 #define FCLG_STATUS_ANALYTIC (1 << 17)
 
@@ -234,8 +238,19 @@ int fclg_set_warmstart(fclg_context* ctx, fclg_warmstart* model);
    direction) and ok = 1 when the directed run succeeded; normal = the
    direction; p_a / p_b the directed witness points; status bit 18
    (FCLG_STATUS_DIRECTED) with the directed status + 1 in bits 8-15 (0 OK,
-   1 Failed, 2 FailedNoIntersect, 3 iteration limit). */
+   1 Failed, 2 FailedNoIntersect, 3 iteration limit).
+   With FCLG_REQ_INCREMENTAL in req->flags: CollisionRequest::
+   useIncrementalMinimumDistancePenetration instead -- for colliding pairs
+   MPR::IncrementalMinimumPenetrationDistance (cvx_collide/
+   mpr_incremental_penetration.hpp:10-333, 128 iterations, returning on the
+   first converged direction) from dirs[i] as the hint.  Per pair: distance =
+   -depth and ok = 1 when the run is OK or stopped at its iteration limit
+   (both valid penetrations for the reference); normal = the direction it
+   settled on (the hint when not ok); status bit 19 (FCLG_STATUS_INCREMENTAL)
+   with the incremental status + 1 in bits 8-15 (0 OK, 1 Failed,
+   2 FailedNoIntersect, 4 iteration limit). */
 #define FCLG_STATUS_DIRECTED (1 << 18)
+#define FCLG_STATUS_INCREMENTAL (1 << 19)
 int fclg_collide_directed(fclg_context* ctx, const fclg_pair* pairs, uint32_t n_pairs, const float* dirs,
                           const fclg_request* req, fclg_result* results);
 int fclg_collide_directed_device(fclg_context* ctx, const fclg_pair* d_pairs, uint32_t n_pairs, const float* d_dirs,

@@ -296,6 +296,7 @@ fclg::QueryParams make_params(const fclg_request* req, bool distance_query) {
   // shapeSignedDistance (the distance entry points) has no such path
   p.analytic = (!distance_query && !(fl & FCLG_REQ_NO_ANALYTIC)) ? 1 : 0;
   p.directed = 0;
+  p.incremental = 0;
   return p;
 }
 
@@ -852,6 +853,7 @@ int run_directed(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fl
   prm.use_mpr = 0;
   prm.analytic = 0;
   prm.directed = 1;
+  prm.incremental = (req && (req->flags & FCLG_REQ_INCREMENTAL)) ? 1 : 0;
   fclg::BatchArgs b = batch_args(c);
   b.pairs = reinterpret_cast<const float4*>(d_pairs);
   b.guess = d_dirs;

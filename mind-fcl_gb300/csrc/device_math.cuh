@@ -153,6 +153,8 @@ constexpr int32_t kStatusMpr = 1 << 16;
 constexpr int32_t kStatusAnalytic = 1 << 17;
 // Result status bit: MPR directed penetration ran (bits 8-15 its status + 1).
 constexpr int32_t kStatusDirected = 1 << 18;
+// Result status bit: MPR incremental penetration ran (bits 8-15 its status + 1).
+constexpr int32_t kStatusIncremental = 1 << 19;
 enum : int32_t { kEpaFailed = 0, kEpaOK = 1, kEpaTouching = 2, kEpaIterLimit = 3, kEpaMallocFailed = 4 };
 
 // 48-byte fclg_result written as three float4 stores.
@@ -175,6 +177,7 @@ struct QueryParams {
   int use_mpr;        // boolean collide: MPR first, GJK when MPR fails
   int analytic;       // collide: closed-form solvers for sphere pairs
   int directed;       // collide with MPR directed penetration along BatchArgs::guess (directed_pass.cu)
+  int incremental;    // directed_pass: the incremental penetration from BatchArgs::guess as the hint
   int want_epa;       // run EPA on overlapping pairs
 };
 

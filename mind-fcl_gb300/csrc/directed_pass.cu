@@ -1,8 +1,9 @@
-// fcl::collide in the directed penetration mode, one thread per pair: the
-// boolean collide (closed-form sphere solvers, else MPR with the GJK
-// fallback), then MPR directed penetration along the pair's escape direction
-// (collisionPenetrationMPR, collision_penetration-inl.h:106-250; directed MPR
-// mpr.hpp:495-701).  Its own kernel so that the distance pass keeps its
+// fcl::collide in the directed and the incremental penetration modes, one
+// thread per pair: the boolean collide (closed-form solvers, else MPR with the
+// GJK fallback), then MPR directed penetration along the pair's escape
+// direction, or the incremental minimum-distance penetration from it as a
+// hint (collisionPenetrationMPR, collision_penetration-inl.h:106-250; directed
+// MPR mpr.hpp:495-701; incremental mpr_incremental_penetration.hpp:10-333).  Its own kernel so that the distance pass keeps its
 // register allocation.
 #include "analytic.cuh"
 #include "gjk.cuh"
@@ -56,18 +57,27 @@ __global__ void __launch_bounds__(128, 4) directed_pass(BatchArgs b, QueryParams
     const f3 d = mk3(__ldg(b.guess + 3 * (size_t)pid), __ldg(b.guess + 3 * (size_t)pid + 1),
                      __ldg(b.guess + 3 * (size_t)pid + 2));
     float depth = -1.f;
-    f3 p0 = mk3(0, 0, 0), p1 = mk3(0, 0, 0);
+    f3 p0 = mk3(0, 0, 0), p1 = mk3(0, 0, 0), n = d;
     int ds = -1;
     uint32_t iters = 0;
+    bool ok = false;
     if (hit) {
+      // computePenetrationMPR (collision_penetration-inl.h:106-184), 128 iterations
       Mpr<MinkowskiSupport<LANES>> mpr{sup, 128, prm.epa_tol};
-      ds = mpr.directed(d, depth, p0, p1);
+      if (prm.incremental) {
+        f3 dir;
+        ds = mpr.incremental(d, depth, dir, p0, p1);
+        ok = ds == 0 || ds == 4;  // at the iteration limit still a valid penetration
+        if (ok) n = dir;
+      } else {
+        ds = mpr.directed(d, depth, p0, p1);
+        ok = ds == 0;
+      }
       iters = (uint32_t)mpr.iterations;
     }
     if (g.lane == 0) {
-      st |= kStatusDirected | ((ds + 1) << 8);
-      const bool ok = hit && ds == 0;
-      store_result(b.results, pid, ok ? -depth : -1.f, d, p0, p1, st, iters, hit, ok);
+      st |= (prm.incremental ? kStatusIncremental : kStatusDirected) | ((ds + 1) << 8);
+      store_result(b.results, pid, ok ? -depth : -1.f, n, p0, p1, st, iters, hit, ok);
     }
   }
 }

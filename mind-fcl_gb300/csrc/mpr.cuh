@@ -169,6 +169,128 @@ struct Mpr {
   }
 
   // mpr.hpp:33-185.  v0 is the interior point of the Minkowski difference.
+  // Incremental minimum-distance penetration from the unit hint d
+  // (mpr_incremental_penetration.hpp:176-288, return on the first converged
+  // subroutine, as fcl::collide calls it): explore d -- the MPR portal along
+  // d, refined until its supporting plane either converges (done) or bounds
+  // the depth along d below the depth along the portal normal (continue
+  // along that normal).  0 OK, 1 Failed, 2 FailedNoIntersect, 4 iteration
+  // limit (still a valid penetration); depth, direction and witness points.
+  __device__ int incremental(f3 d, float& depth, f3& dir, f3& p0, f3& p1) {
+    iterations = 0;
+    f3 v1 = mk3(0, 0, 0), v2 = v1, v3 = v1, d1 = v1, d2 = v1, d3 = v1;
+    float prev_lb = -1.f, prev_ub = -1.f;
+    for (int outer = 0; outer < max_iter; ++outer) {
+      f3 nd = d;
+      float lb = 0.f, ub = 0.f;
+      const int st = explore(d, v1, v2, v3, d1, d2, d3, lb, ub, nd, outer >= 1);
+      if (st == 0) {
+        d = nd;
+      } else if (st == 1) {
+        finish_incremental(d, v1, v2, v3, d1, d2, d3, lb, ub, depth, dir, p0, p1);
+        return 0;
+      } else if (st == 2) {
+        depth = ub;
+        dir = nd;
+        sup(nd, p0, p1);
+        return 0;
+      } else {
+        return st == 4 ? 2 : 1;
+      }
+      prev_lb = lb;
+      prev_ub = ub;
+    }
+    finish_incremental(d, v1, v2, v3, d1, d2, d3, prev_lb, prev_ub, depth, dir, p0, p1);
+    return 4;
+  }
+
+  // mpr_incremental_penetration.hpp:49-174: 0 new direction, 1 converged,
+  // 2 degenerated, 3 failed, 4 no intersection.  lb / ub bound the depth
+  // along d (:10-47).
+  __device__ int explore(f3 d, f3& v1, f3& v2, f3& v3, f3& d1, f3& d2, f3& d3, float& lb, float& ub, f3& nd,
+                         bool v123_valid) {
+    const f3 v0 = -d;
+    f3 init_dir = d;
+    const f3 init = support(init_dir);
+    if (dot(d, init) < 0.f) return 4;
+    if (!v123_valid) {
+      d1 = d;
+      v1 = init;
+      d2 = cross(v0, v1);
+      if (absnorm(d2) <= absnorm(v1) * tol) {
+        lb = dot(v1, d);
+        ub = lb;
+        nd = d;
+        return 2;
+      }
+      v2 = support(d2);
+      if (dot(d2, v2) < 0.f) return 4;
+      d3 = cross(v1, v2);
+      if (dot(d3, v0) > 0.f) {
+        f3 t = v1; v1 = v2; v2 = t;
+        t = d1; d1 = d2; d2 = t;
+        d3 = -d3;
+      }
+      v3 = support(d3);
+      if (dot(d3, v3) < 0.f) return 4;
+    }
+    const float m2 = fmaxf(sqn(v1), fmaxf(sqn(v2), sqn(v3)));
+    const f3 v0s = v0 * sqrtf(m2);
+    const int fp = find_portal(v0s, v1, v2, v3, d1, d2, d3);
+    if (fp == 0) return 3;
+    if (fp == 1) return 4;
+    for (int it = 0; it < max_iter; ++it) {
+      ++iterations;
+      f3 n = cross(v2 - v1, v3 - v1);
+      if (dot(n, d) < 0.f) {
+        f3 t = v2; v2 = v3; v3 = t;
+        t = d2; d2 = d3; d3 = t;
+        n = -n;
+      }
+      const f3 v4 = support(n);
+      const float ub_plane = dot(v4, n);
+      if (ub_plane < 0.f) return 4;
+      const float v1n = dot(v1, n), v4n = dot(v4, n);
+      const float ndd = dot(d, n);
+      if (!(fabsf(ndd) > 0.f)) {
+        lb = fmaxf(dot(v1, d), fmaxf(dot(v2, d), dot(v3, d)));
+        ub = lb;
+      } else {
+        lb = v1n / ndd;
+        ub = v4n / ndd;
+      }
+      if (lb > ub_plane + tol) {
+        nd = n;
+        return 0;
+      }
+      if (fabsf(v4n - v1n) <= tol) {
+        nd = n;
+        return 1;
+      }
+      update_portal(v0s, v4, n, v1, v2, v3, d1, d2, d3);
+    }
+    return 3;
+  }
+
+  // finalizeIncrementalPenetrationResult (mpr_incremental_penetration.hpp:300-333)
+  __device__ void finish_incremental(f3 d, f3 v1, f3 v2, f3 v3, f3 d1, f3 d2, f3 d3, float lb, float ub,
+                                     float& depth, f3& dir, f3& p0, f3& p1) const {
+    depth = ub;
+    dir = d;
+    const f3 o_proj = d * lb;
+    const f3 a12 = v2 - v1, a13 = v3 - v1;
+    const float area = nrm(cross(a12, a13));
+    const float w2 = nrm(cross(a13, v1 - o_proj)) / area;
+    const float w3 = nrm(cross(a12, v1 - o_proj)) / area;
+    const float w1 = 1.f - w2 - w3;
+    f3 pa1, pb1, pa2, pb2, pa3, pb3;
+    sup(d1, pa1, pb1);
+    sup(d2, pa2, pb2);
+    sup(d3, pa3, pb3);
+    p0 = (pa1 * w1 + pa2 * w2) + pa3 * w3;
+    p1 = (pb1 * w1 + pb2 * w2) + pb3 * w3;
+  }
+
   __device__ MprStatus intersect(f3 v0) {
     iterations = 0;
     if (sqn(v0) <= tol * tol) return MprStatus::Intersect;

@@ -16,6 +16,11 @@ LIB_PATH = os.path.join(PKG, "lib", "libfclg.so")
 FCLG_REQ_BOOLEAN_ONLY = 1
 FCLG_REQ_NO_EPA = 2
 FCLG_REQ_WARM_START = 4
+FCLG_REQ_GJK_BOOLEAN = 8
+FCLG_REQ_NO_ANALYTIC = 16
+FCLG_REQ_INCREMENTAL = 32
+FCLG_STATUS_DIRECTED = 1 << 18
+FCLG_STATUS_INCREMENTAL = 1 << 19
 
 # Every symbol include/fclg.h declares (checked by tests/test_abi.py).
 EXPORTS = [
@@ -284,7 +289,8 @@ class Context:
 
     def collide_directed(self, pairs, dirs, request=None):
         """fcl::collide, directed penetration mode, host arrays: dirs float[n][3] (unit,
-        shape b's escape direction in shape a's frame)."""
+        shape b's escape direction in shape a's frame); with FCLG_REQ_INCREMENTAL in the
+        request's flags the incremental minimum-distance mode from dirs as hints."""
         p = np.ascontiguousarray(pairs, PAIR_DTYPE)
         d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
         assert len(d) == len(p)

@@ -56,6 +56,10 @@ def _load():
         lib.orc_collide_directed.restype = i
         lib.orc_directed_raw.argtypes = [vp, i, vp, vp, i, vp, vp, i]
         lib.orc_directed_raw.restype = i
+        lib.orc_collide_incremental.argtypes = [vp, i, vp, vp, i, vp, vp, i]
+        lib.orc_collide_incremental.restype = i
+        lib.orc_incremental_raw.argtypes = [vp, i, vp, vp, i, vp, vp, i]
+        lib.orc_incremental_raw.restype = i
         lib.orc_collide.restype = i
         lib.orc_time_signed_distance.argtypes = [vp, i, vp, vp, i, vp, i]
         lib.orc_time_signed_distance.restype = d
@@ -89,6 +93,8 @@ def _load_ref():
         lib.ref_collide.argtypes = [vp, i, vp, vp, i, i, vp, i]
         lib.ref_directed.argtypes = [vp, i, vp, vp, i, vp, vp, i]
         lib.ref_directed.restype = i
+        lib.ref_incremental.argtypes = [vp, i, vp, vp, i, vp, vp, i]
+        lib.ref_incremental.restype = i
         lib.ref_collide.restype = i
         _ref = lib
     return _ref
@@ -242,6 +248,40 @@ def directed_raw(batch, dirs, threads=None):
     out = np.zeros(len(p), RESULT_DTYPE)
     assert lib.orc_directed_raw(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), _ptr(d), _ptr(out),
                                 threads or default_threads()) == 0
+    return out
+
+
+def collide_incremental(batch, dirs, threads=None):
+    """fcl::collide with useIncrementalMinimumDistancePenetration: boolean
+    collide, then MPR::IncrementalMinimumPenetrationDistance from the hint dirs
+    (unit, shape b's escape direction in shape a's frame) for colliding pairs;
+    epa_status = the incremental status, normal = the converged direction."""
+    return _dir_call("orc_collide_incremental", batch, dirs, threads)
+
+
+def incremental_raw(batch, dirs, threads=None):
+    """Restated incremental penetration on every pair (depth in distance)."""
+    return _dir_call("orc_incremental_raw", batch, dirs, threads)
+
+
+def ref_incremental(batch, dirs, threads=None):
+    """The reference's RunIncrementalMinimumPenetrationDistance on every pair."""
+    lib = _load_ref()
+    s, v, p = _prep(batch)
+    d = np.ascontiguousarray(dirs, np.float32)
+    out = np.zeros(len(p), RESULT_DTYPE)
+    assert lib.ref_incremental(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), _ptr(d), _ptr(out),
+                               threads or default_threads()) == 0
+    return out
+
+
+def _dir_call(name, batch, dirs, threads):
+    lib = _load()
+    s, v, p = _prep(batch)
+    d = np.ascontiguousarray(dirs, np.float32)
+    out = np.zeros(len(p), RESULT_DTYPE)
+    assert getattr(lib, name)(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), _ptr(d), _ptr(out),
+                              threads or default_threads()) == 0
     return out
 
 

@@ -272,6 +272,73 @@ int orc_directed_raw(const void* shapes, int n_shapes, const float* verts, const
   return 0;
 }
 
+// fcl::collide in the incremental minimum-distance penetration mode
+// (computePenetrationMPR with is_incremental, collision_penetration-inl.h:
+// 133-155): the boolean collide as in orc_collide_directed, then
+// MPR::IncrementalMinimumPenetrationDistance from the hint dirs[i] for
+// colliding pairs.  Result: ok = collide; distance = -depth and normal = the
+// converged direction when the run is OK or at its iteration limit (both
+// valid for the reference), else distance -1 and normal = the hint;
+// epa_status = the incremental status (0 OK, 1 Failed, 2 FailedNoIntersect,
+// 4 IterationLimit), -1 when not colliding.
+int orc_collide_incremental(const void* shapes, int n_shapes, const float* verts, const void* pairs, int n_pairs,
+                            const float* dirs, OrcResult* out, int n_threads) {
+  if (n_pairs < 0 || n_shapes < 0 || !dirs) return -1;
+  const auto sh = makeShapes((const ShapeRec*)shapes, n_shapes, verts);
+  const PairRec* pr = (const PairRec*)pairs;
+  const orc::SolverParams sp;
+  parallelFor(n_pairs, n_threads, [&](int b, int e) {
+    for (int i = b; i < e; ++i) {
+      const orc::MinkDiff md = makeDiff(sh, pr[i]);
+      OrcResult& r = out[i];
+      r = OrcResult{};
+      orc::AContact ac;
+      bool hit;
+      if (orc::analyticIntersect(*md.s0, *md.s1, md.to0, ac)) hit = ac.hit;
+      else hit = orc::intersect(md, sp, false, nullptr).ok;
+      const orc::V3 d(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]);
+      for (int k = 0; k < 3; ++k) r.normal[k] = d[k];
+      r.ok = hit ? 1 : 0;
+      r.distance = -1;
+      r.epa_status = -1;
+      if (!hit) continue;
+      orc::MPR mpr(128, sp.epa_tol);
+      orc::MPR::Incremental pd;
+      const int st = mpr.IncrementalPenetration(md, d, pd);
+      r.epa_status = st;
+      if (st == 0 || st == 4) {
+        r.distance = -pd.depth;
+        for (int k = 0; k < 3; ++k) { r.normal[k] = pd.dir[k]; r.p0[k] = pd.p0[k]; r.p1[k] = pd.p1[k]; }
+      }
+    }
+  });
+  return 0;
+}
+
+// The restated incremental penetration on every pair (no boolean gate), in
+// the layout of ref_incremental, for the bit-for-bit pin: distance = depth.
+int orc_incremental_raw(const void* shapes, int n_shapes, const float* verts, const void* pairs, int n_pairs,
+                        const float* dirs, OrcResult* out, int n_threads) {
+  if (n_pairs < 0 || n_shapes < 0 || !dirs) return -1;
+  const auto sh = makeShapes((const ShapeRec*)shapes, n_shapes, verts);
+  const PairRec* pr = (const PairRec*)pairs;
+  parallelFor(n_pairs, n_threads, [&](int b, int e) {
+    for (int i = b; i < e; ++i) {
+      const orc::MinkDiff md = makeDiff(sh, pr[i]);
+      OrcResult& r = out[i];
+      r = OrcResult{};
+      orc::MPR mpr(128, 1e-6);
+      orc::MPR::Incremental pd;
+      const int st = mpr.IncrementalPenetration(md, orc::V3(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]), pd);
+      r.epa_status = st;
+      r.distance = pd.depth;
+      for (int k = 0; k < 3; ++k) { r.normal[k] = pd.dir[k]; r.p0[k] = pd.p0[k]; r.p1[k] = pd.p1[k]; }
+      r.ok = (st == 0 || st == 4) ? 1 : 0;
+    }
+  });
+  return 0;
+}
+
 // boxBox2 (box_box-inl.h:214-802) on two posed boxes in FP64, as
 // boxBoxIntersect calls it (maxc 4): out = normal[3], depth, code, count, then
 // count x (pos[3], depth).  Returns the contact count.

@@ -1455,7 +1455,139 @@ class MPR {
     return 3;
   }
 
+ public:
+  // ------------------------------------------------------------------
+  // Incremental minimum-distance penetration (fcl::collide with
+  // useIncrementalMinimumDistancePenetration, collision_penetration-inl.h:133-155):
+  // mpr_incremental_penetration.hpp:176-288 (RunIncrementalMinimumPenetrationDistance,
+  // return_on_subroutine_converge = true), :49-174 (the explore subroutine),
+  // :10-47 (the distance bounds along the ray) and :300-333 (the witness
+  // points).  Status: 0 OK, 1 Failed, 2 FailedNoIntersect, 4 IterationLimit.
+  struct Incremental {
+    double depth = 0;
+    V3 dir, p0, p1;
+  };
+  int IncrementalPenetration(const MinkDiff& shape, const V3& init_direction, Incremental& out) const {
+    V3 d = init_direction;
+    V3 v1, v2, v3, d1, d2, d3;
+    V3 prev_dir = init_direction;
+    double prev_lb = -1, prev_ub = -1;
+    for (int outer = 0; outer < max_iter_; ++outer) {
+      V3 nd;
+      double lb = 0, ub = 0;
+      const int st = explore(shape, d, v1, v2, v3, d1, d2, d3, lb, ub, nd, outer >= 1);
+      if (st == 0) {
+        d = nd;
+      } else if (st == 1) {
+        finalizeIncremental(shape, d, v1, v2, v3, d1, d2, d3, lb, ub, out);
+        return 0;
+      } else if (st == 2) {
+        out.depth = ub;
+        out.dir = nd;
+        out.p0 = shape.support0(nd);
+        out.p1 = shape.support1(-nd);
+        return 0;
+      } else if (st == 4) {
+        return 2;
+      } else {
+        return 1;
+      }
+      prev_dir = nd;
+      prev_lb = lb;
+      prev_ub = ub;
+    }
+    (void)prev_dir;
+    finalizeIncremental(shape, d, v1, v2, v3, d1, d2, d3, prev_lb, prev_ub, out);
+    return 4;
+  }
+
  private:
+  // explore subroutine status: 0 NewDirection, 1 SubroutineConverge,
+  // 2 Degenerated, 3 Failed, 4 FailedNoIntersect
+  int explore(const MinkDiff& shape, const V3& d, V3& v1, V3& v2, V3& v3, V3& d1, V3& d2, V3& d3, double& lb,
+              double& ub, V3& nd, bool v123_valid) const {
+    const V3 v0 = -d;
+    V3 init_dir = d;
+    const V3 init = sup(shape, init_dir);
+    if (dot(d, init) < 0) return 4;
+    if (!v123_valid) {
+      d1 = d;
+      v1 = init;
+      d2 = cross(v0, v1);
+      if (absnorm(d2) <= absnorm(v1) * tol_) {
+        lb = dot(v1, d);
+        ub = lb;
+        nd = d;
+        return 2;
+      }
+      v2 = sup(shape, d2);
+      if (dot(d2, v2) < 0) return 4;
+      d3 = cross(v1, v2);
+      if (dot(d3, v0) > 0) {
+        std::swap(v1, v2);
+        std::swap(d1, d2);
+        d3 = d3 * -1.0;
+      }
+      v3 = sup(shape, d3);
+      if (dot(d3, v3) < 0) return 4;
+    }
+    V3 v0s = v0;
+    {
+      const double m2 = std::max(sqn(v1), std::max(sqn(v2), sqn(v3)));
+      v0s = v0s * std::sqrt(m2);
+    }
+    const int fp = findPortal(shape, v0s, v1, v2, v3, d1, d2, d3);
+    if (fp == 0) return 3;
+    if (fp == 1) return 4;
+    int it = 0;
+    while (it < max_iter_) {
+      it += 1;
+      V3 n = cross(v2 - v1, v3 - v1);
+      if (dot(n, d) < 0) {
+        std::swap(v2, v3);
+        std::swap(d2, d3);
+        n = n * -1.0;
+      }
+      const V3 v4 = sup(shape, n);
+      const double ub_plane = dot(v4, n);
+      if (ub_plane < 0) return 4;
+      const double v1n = dot(v1, n), v4n = dot(v4, n);
+      const double v14 = v4n - v1n;
+      const double ndd = dot(d, n);
+      if (std::abs(ndd) <= 0) {
+        lb = std::max(dot(v1, d), std::max(dot(v2, d), dot(v3, d)));
+        ub = lb;
+      } else {
+        lb = v1n / ndd;
+        ub = v4n / ndd;
+      }
+      if (lb > ub_plane + tol_) {
+        nd = n;
+        return 0;
+      }
+      if (std::abs(v14) <= tol_) {
+        nd = n;
+        return 1;
+      }
+      updatePortal(v0s, v4, n, v1, v2, v3, d1, d2, d3);
+    }
+    return 3;
+  }
+
+  static void finalizeIncremental(const MinkDiff& shape, const V3& d, const V3& v1, const V3& v2, const V3& v3,
+                                  const V3& d1, const V3& d2, const V3& d3, double lb, double ub, Incremental& out) {
+    out.depth = ub;
+    out.dir = d;
+    const V3 o_projected = d * lb;
+    const V3 a12 = v2 - v1, a13 = v3 - v1;
+    const double area = norm(cross(a12, a13));
+    const double w2 = norm(cross(a13, v1 - o_projected)) / area;
+    const double w3 = norm(cross(a12, v1 - o_projected)) / area;
+    const double w1 = 1.0 - w2 - w3;
+    out.p0 = (shape.support0(d1) * w1 + shape.support0(d2) * w2) + shape.support0(d3) * w3;
+    out.p1 = (shape.support1(-d1) * w1 + shape.support1(-d2) * w2) + shape.support1(-d3) * w3;
+  }
+
   static void finalizeDirected(const MinkDiff& shape, const V3& d, const V3& n, Directed& pd, const V3* v4) {
     pd.portal_normal = n;
     const double ndd = dot(d, n);

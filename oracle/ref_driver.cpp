@@ -247,4 +247,34 @@ int ref_directed(const void* shapes, int n_shapes, const float* verts, const voi
   return 0;
 }
 
+// The reference's MPR::RunIncrementalMinimumPenetrationDistance
+// (mpr_incremental_penetration.hpp:176-288) on every pair, with the
+// fcl::collide settings (128 iterations, 1e-6, return on the first
+// converged subroutine).
+int ref_incremental(const void* shapes, int n_shapes, const float* verts, const void* pairs, int n_pairs,
+                    const float* dirs, RefResult* out, int n_threads) {
+  const Prepared p = prepare((const ShapeRec*)shapes, n_shapes, verts);
+  const PairRec* pr = (const PairRec*)pairs;
+  parallelFor(n_pairs, n_threads, [&](int b, int e) {
+    for (int i = b; i < e; ++i) {
+      RefResult& r = out[i];
+      r = RefResult{};
+      const MinkowskiDiff<double> md = makeDiff(p, pr[i]);
+      const Vec d(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]);
+      typename MPR<double>::IncrementalMinimumPenetrationData data{};
+      const auto st = MPR<double>::RunIncrementalMinimumPenetrationDistance(md, d, data, 128, 1e-6, true);
+      r.epa_status = (int)st;
+      r.distance = data.minimum_penetration;
+      for (int k = 0; k < 3; ++k) {
+        r.normal[k] = data.penetration_direction[k];
+        r.p0[k] = data.p0_in_shape0_frame[k];
+        r.p1[k] = data.p1_in_shape0_frame[k];
+      }
+      r.ok = (st == MPR<double>::IncrementalPenetrationStatus::OK ||
+              st == MPR<double>::IncrementalPenetrationStatus::IterationLimit) ? 1 : 0;
+    }
+  });
+  return 0;
+}
+
 }  // extern "C"

@@ -174,3 +174,51 @@ def test_box_box_flags_and_depth_vs_sat(oracle_lib):
             over = np.sum(ha * np.abs(nrm)) + np.sum(hb * np.abs(Rf[i].T @ nrm)) - abs(nrm @ tf[i])
             assert -r["distance"][i] <= over + 1e-6, i
     assert hits > 1000
+
+
+def test_epa_depth_vs_box_box(oracle_lib):
+    """test/cvx_collide/test_epa2_with_gjk2.cpp:75-161 (testBoxPenetration) at
+    20 k poses: boxes of sides (2, 1, 0.5) and (1, 1, 1) at random poses in a
+    4 m cube; wherever boxBox2 reports contacts, EPA's depth may not exceed
+    boxBox2's separating-axis depth by more than 1e-4 (no mismatches)."""
+    from fclg import workloads
+    from fclg.layout import BOX, PAIR_DTYPE, SHAPE_DTYPE
+    rng = np.random.default_rng(77)
+    n = 20000
+
+    def rot(k):
+        q = rng.normal(size=(k, 4))
+        q /= np.linalg.norm(q, axis=1, keepdims=True)
+        w, x, y, z = q.T
+        return np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y),
+                         2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x),
+                         2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)], axis=1).reshape(k, 3, 3)
+
+    R1, R2 = rot(n), rot(n)
+    t1, t2 = rng.uniform(-2, 2, size=(n, 3)), rng.uniform(-2, 2, size=(n, 3))
+    # b in a's frame, rounded to the FP32 pair record; boxBox2 runs on the same rounded pose
+    R = np.einsum("nji,njk->nik", R1, R2).astype(np.float32).astype(np.float64)
+    t = np.einsum("nji,nj->ni", R1, t2 - t1).astype(np.float32).astype(np.float64)
+    side1, side2 = np.array([2.0, 1.0, 0.5]), np.ones(3)
+    sat_depth = np.full(n, np.nan)
+    for i in range(n):
+        code, _, depth, contacts = oracle_lib.box_box(side1, np.eye(3), np.zeros(3), side2, R[i], t[i])
+        if len(contacts) > 0:
+            sat_depth[i] = depth
+    hit = np.nonzero(~np.isnan(sat_depth))[0]
+    assert len(hit) > 1000
+    s = np.zeros(2, SHAPE_DTYPE)
+    s["type"] = BOX
+    s["param"][0, :3] = side1
+    s["param"][1, :3] = side2
+    p = np.zeros(len(hit), PAIR_DTYPE)
+    p["shape_a"], p["shape_b"] = 0, 1
+    p["rot"] = R[hit].reshape(-1, 9)
+    p["trans"] = t[hit]
+    b = workloads.Batch("box_pen", s, np.zeros((1, 4), np.float32), p, {})
+    o = oracle_lib.signed_distance(b)
+    ok = (o["ok"] == 1) & (o["distance"] < 0)
+    epa = -o["distance"]
+    mismatch = ok & (np.abs(sat_depth[hit] - epa) > 1e-4) & (sat_depth[hit] < epa)
+    assert mismatch.sum() == 0
+    assert ok.mean() > 0.99
