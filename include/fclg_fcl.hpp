@@ -23,8 +23,10 @@
 //   * Each call runs on a per-thread context of device 0 (setDevice() before
 //     the first call to change it).  One pair per call is a GPU round trip;
 //     BatchQuery runs many pairs per call and is the fast path.
-//   * Penetration modes: disabled (boolean) and the default GJK/EPA mode; the
-//     directed / incremental MPR modes are not declared.
+//   * Penetration modes: disabled (boolean), the default GJK/EPA mode, and
+//     the MPR directed / incremental minimum-distance modes
+//     (useDirectedPenetration / useIncrementalMinimumDistancePenetration,
+//     collision_request.h:74-79) for shape pairs.
 #pragma once
 
 #include <algorithm>
@@ -218,9 +220,23 @@ class CollisionRequest {
  public:
   CollisionRequest() : CollisionRequest(1) {}
   explicit CollisionRequest(std::size_t n_max_contacts) : num_max_contacts_(n_max_contacts) {}
-  void disablePenetration() { penetration_ = false; }
-  void useDefaultPenetration() { penetration_ = true; }
+  void disablePenetration() { penetration_ = false; mode_ = 0; }
+  void useDefaultPenetration() { penetration_ = true; mode_ = 0; }
+  // MPR penetration along (directed) or starting from (incremental) shape 2's
+  // escape direction in the world frame (collision_penetration-inl.h:106-250)
+  void useDirectedPenetration(const Vector3<S>& shape2_escape_direction_in_world) {
+    penetration_ = true;
+    mode_ = 1;
+    prior_ = shape2_escape_direction_in_world;
+  }
+  void useIncrementalMinimumDistancePenetration(const Vector3<S>& shape2_escape_direction_in_world_hint) {
+    penetration_ = true;
+    mode_ = 2;
+    prior_ = shape2_escape_direction_in_world_hint;
+  }
   bool isPenetrationEnabled() const { return penetration_; }
+  int mprPenetrationMode() const { return mode_; }  // 0 none, 1 directed, 2 incremental
+  const Vector3<S>& priorPenetrationDirection() const { return prior_; }
   std::size_t maxNumContacts() const { return num_max_contacts_; }
   void setMaxContactCount(std::size_t n) { num_max_contacts_ = n; }
   void setBinaryCollisionTolerance(S t) { binary_tol_ = t; }
@@ -231,6 +247,8 @@ class CollisionRequest {
  private:
   std::size_t num_max_contacts_;
   bool penetration_ = false;
+  int mode_ = 0;
+  Vector3<S> prior_;
   S binary_tol_ = S(1e-6), distance_tol_ = S(1e-6);
 };
 
@@ -422,6 +440,7 @@ class BatchQuery {
 
   // fcl::collide per pair (one contact per colliding pair with penetration).
   std::vector<CollisionResult<S>> collide(const CollisionRequest<S>& req) {
+    if (req.mprPenetrationMode() != 0) return collide_mpr(req);
     const uint32_t flags = req.isPenetrationEnabled() ? 0u : (uint32_t)FCLG_REQ_BOOLEAN_ONLY;
     std::vector<fclg_result> r = run(false, detail::make_request(flags, (double)req.binaryCollisionTolerance(),
                                                                  (double)req.distanceTolerance()));
@@ -435,6 +454,49 @@ class BatchQuery {
                               0.5f * (r[i].p_a[2] + r[i].p_b[2])};
         c.pos = frames_[i].world(mid);
         c.penetration_depth = (S)(-r[i].distance);
+      }
+      out[i].addContact(c);
+    }
+    return out;
+  }
+
+  // The MPR penetration modes (collisionPenetrationMPR): every colliding pair
+  // gets a contact; depth -1, position 0 and the given direction as normal
+  // where the MPR run failed, as the reference reports it.
+  std::vector<CollisionResult<S>> collide_mpr(const CollisionRequest<S>& req) {
+    std::vector<CollisionResult<S>> out(pairs_.size());
+    if (pairs_.empty()) return out;
+    const Vector3<S>& dw = req.priorPenetrationDirection();
+    std::vector<float> dirs(3 * pairs_.size());
+    for (std::size_t i = 0; i < pairs_.size(); ++i) {
+      const double* R = frames_[i].R;  // direction in shape 1's frame: R^T d
+      double a[3];
+      for (int k = 0; k < 3; ++k)
+        a[k] = R[k] * (double)dw[0] + R[3 + k] * (double)dw[1] + R[6 + k] * (double)dw[2];
+      const double l = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+      for (int k = 0; k < 3; ++k) dirs[3 * i + k] = (float)(l > 0 ? a[k] / l : a[k]);
+    }
+    fclg_request r = detail::make_request(req.mprPenetrationMode() == 2 ? (uint32_t)FCLG_REQ_INCREMENTAL : 0u,
+                                          (double)req.binaryCollisionTolerance(), (double)req.distanceTolerance());
+    std::vector<fclg_result> res(pairs_.size());
+    fclg_context* ctx = detail::thread_context();
+    detail::check(ctx, fclg_set_shapes(ctx, shapes_.data(), (uint32_t)shapes_.size(), verts_.data(), verts_.size() / 4),
+                  "fclg_set_shapes");
+    detail::check(ctx, fclg_collide_directed(ctx, pairs_.data(), (uint32_t)pairs_.size(), dirs.data(), &r, res.data()),
+                  "fclg_collide_directed");
+    for (std::size_t i = 0; i < res.size(); ++i) {
+      if (!res[i].collide || req.maxNumContacts() == 0) continue;
+      Contact<S> c(geoms_[i].first, geoms_[i].second, -1, -1);
+      if (res[i].ok) {
+        c.normal = frames_[i].rot(res[i].normal);
+        const float mid[3] = {0.5f * (res[i].p_a[0] + res[i].p_b[0]), 0.5f * (res[i].p_a[1] + res[i].p_b[1]),
+                              0.5f * (res[i].p_a[2] + res[i].p_b[2])};
+        c.pos = frames_[i].world(mid);
+        c.penetration_depth = (S)(-res[i].distance);
+      } else {
+        c.normal = dw;
+        c.pos = Vector3<S>(S(0), S(0), S(0));
+        c.penetration_depth = S(-1);
       }
       out[i].addContact(c);
     }

@@ -80,6 +80,30 @@ int main() {
   res.clear();
   CHECK(collide(&b1, at(0, 0, 0), &b2, at(0.5, 0, 0), zero_req, res) == 0, "no contacts requested");
 
+  // MPR penetration modes: b2 sits 0.2 deep on top of b1.  Directed along +z
+  // gives 0.2; incremental from a tilted hint settles on +z with 0.2.
+  CollisionRequest<S> dir_req;
+  dir_req.useDirectedPenetration(Vector3<S>(0, 0, 1));
+  res.clear();
+  collide(&b1, at(0, 0, 0), &b2, at(0.05, 0.02, 0.8), dir_req, res);
+  CHECK(res.isCollision(), "directed contact");
+  if (res.isCollision()) {
+    const auto& c = res.getContact(0);
+    CHECK(std::fabs(c.penetration_depth - 0.2) < 1e-4, "directed depth %.7f", c.penetration_depth);
+    CHECK(c.normal[2] > 0.9999, "directed normal %.4f %.4f %.4f", c.normal[0], c.normal[1], c.normal[2]);
+  }
+  CollisionRequest<S> inc_req;
+  const S h = S(1) / std::sqrt(S(1.04));
+  inc_req.useIncrementalMinimumDistancePenetration(Vector3<S>(S(0.2) * h, 0, h));
+  res.clear();
+  collide(&b1, at(0, 0, 0), &b2, at(0.05, 0.02, 0.8), inc_req, res);
+  CHECK(res.isCollision(), "incremental contact");
+  if (res.isCollision()) {
+    const auto& c = res.getContact(0);
+    CHECK(std::fabs(c.penetration_depth - 0.2) < 1e-4, "incremental depth %.7f", c.penetration_depth);
+    CHECK(c.normal[2] > 0.999, "incremental normal %.4f %.4f %.4f", c.normal[0], c.normal[1], c.normal[2]);
+  }
+
   // convex cube (8 vertices) against a sphere: distance 0.3
   auto verts = std::make_shared<std::vector<Vector3<S>>>();
   for (int i = 0; i < 8; ++i) verts->push_back(Vector3<S>((i & 1) ? 0.5 : -0.5, (i & 2) ? 0.5 : -0.5, (i & 4) ? 0.5 : -0.5));
