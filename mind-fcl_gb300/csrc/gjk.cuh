@@ -432,9 +432,11 @@ struct GjkRun {
   template <class Sup>
   __device__ __forceinline__ bool step(const Sup& sup, float tol, int max_iter, bool want_distance) {
     const float tol2 = tol * tol;
+    // every phase supports along d: one call site, so that lanes of a warp in
+    // different phases still evaluate their supports together
     f3 pa, pb;
+    sup(d, pa, pb);
     if (phase == 0) {
-      sup(d, pa, pb);
       s.set(0, pa, pb);
       s.rank = 1;
       if (sqn(s.w[0]) <= tol2) {
@@ -450,7 +452,6 @@ struct GjkRun {
     }
     if (phase == 1) {
       o.iterations = it + 1;
-      sup(d, pa, pb);
       const f3 w = pa - pb;
       if (dot(w, d) < 0.f) {
         s.set(0, pa, pb);  // the separating vertex seeds the distance simplex
@@ -487,7 +488,6 @@ struct GjkRun {
     }
     // phase 2: one iteration of the minimum-distance loop (gjk_distance.hpp:41-105)
     ++o.iterations;
-    sup(d, pa, pb);
     const f3 w = pa - pb;
     FCLG_GJK_TRACE(it, -1, dot(d, w - cur), 0.f);
     if (dot(d, w - cur) < tol) return distance_result(true);

@@ -7,6 +7,9 @@ namespace fclg {
 FCLG_GJK_INSTANTIATE(1)
 FCLG_GJK_INSTANTIATE(2)
 
+// Free lanes of a warp that trigger a refill of them all.
+constexpr int kRefillBatch = 8;
+
 // One lane per pair, pairs refilled per lane: every lane of a warp steps its
 // own pair's GJK run one support evaluation at a time (GjkRun), and a lane
 // whose pair is done takes the next one from its warp's share of the items
@@ -38,8 +41,11 @@ __global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_refill(BatchArgs b, Qu
   bool live = false;
   uint32_t next = 0;  // warp-uniform: next unassigned position in the warp's share
   for (;;) {
-    const unsigned want = __ballot_sync(0xFFFFFFFFu, !live);
-    if (!live) {
+    unsigned want = __ballot_sync(0xFFFFFFFFu, !live);
+    // refill in batches: the loads of a new pair stall the whole warp, so
+    // wait until a quarter of the lanes are free (or none is busy)
+    if (__popc(want) < kRefillBatch && want != 0xFFFFFFFFu) want = 0;
+    if (want & (1u << lane)) {
       const uint32_t k = next + (uint32_t)__popc(want & ((1u << lane) - 1u));
       const uint64_t item = (uint64_t)begin + ((uint64_t)(k >> 5) * n_warps + warp) * 32u + (k & 31u);
       if (item < end) {
