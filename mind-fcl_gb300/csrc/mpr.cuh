@@ -252,7 +252,7 @@ struct Mpr {
       if (ub_plane < 0.f) return 4;
       const float v1n = dot(v1, n), v4n = dot(v4, n);
       const float ndd = dot(d, n);
-      if (!(fabsf(ndd) > 0.f)) {
+      if (fabsf(ndd) <= 0.f) {  // as the reference tests it (a NaN takes the division)
         lb = fmaxf(dot(v1, d), fmaxf(dot(v2, d), dot(v3, d)));
         ub = lb;
       } else {
