@@ -35,7 +35,7 @@ struct fclg_context {
   float4* hull_ents = nullptr;
   uint32_t walk_hulls = 0;
   bool support_walk = false;
-  bool gjk_refill = true;
+  bool gjk_refill = false;
   // scratch handed from the GJK pass to the EPA pass
   uint32_t* epa_count = nullptr;  // [2]: work list, overflow list
   uint32_t* epa_list = nullptr;
