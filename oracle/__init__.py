@@ -29,7 +29,8 @@ _CXXFLAGS = ["-O3", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared"]
 def build(force=False):
     """Compile the restatement (always) and the reference driver (only where the
     reference sources exist)."""
-    srcs = [os.path.join(HERE, f) for f in ("oracle.cpp", "orc_convex.hpp", "orc_mesh.hpp") if
+    srcs = [os.path.join(HERE, f) for f in ("oracle.cpp", "orc_convex.hpp", "orc_mesh.hpp", "orc_analytic.hpp",
+                                            "orc_mesh_shape.hpp") if
             os.path.exists(os.path.join(HERE, f))]
     if force or not os.path.exists(LIB_PATH) or any(os.path.getmtime(s) > os.path.getmtime(LIB_PATH) for s in srcs):
         subprocess.check_call(["g++", *_CXXFLAGS, os.path.join(HERE, "oracle.cpp"), "-o", LIB_PATH, "-lpthread"])
@@ -75,6 +76,10 @@ def _load():
         lib.orc_support.restype = i
         lib.orc_box_box.argtypes = [vp, vp, vp, vp, vp, vp, vp]
         lib.orc_box_box.restype = i
+        lib.orc_mesh_shape_collide.argtypes = [vp, vp, vp, i, vp, vp, vp, i, i, i, vp, vp, vp, i]
+        lib.orc_mesh_shape_collide.restype = i
+        lib.orc_mesh_shape_all.argtypes = [vp, i, vp, i, vp, ctypes.c_uint32, vp, vp, i]
+        lib.orc_mesh_shape_all.restype = i
         _lib = lib
     return _lib
 
@@ -367,6 +372,38 @@ def mesh_collide(nodes_a, tris_a, nodes_b, tris_b, poses, max_contacts=1, pair_c
     assert lib.orc_mesh_collide(_ptr(na), _ptr(ta), _ptr(nb), _ptr(tb), _ptr(poses), n, int(max_contacts), cap,
                                 _ptr(flags), _ptr(counts), _ptr(pairs), threads or default_threads()) == 0
     return flags, counts, pairs
+
+
+def mesh_shape_collide(nodes, tris, batch, shape_ids, poses, max_contacts=1, pair_cap=None, threads=None):
+    """fcl::collide(mesh, shape) per query (MeshShapeIntersect, penetration
+    off): the batch's shape shape_ids[i] posed by poses[i] (12 floats) in the
+    mesh frame.  Returns (flags, counts, tri_ids[n, pair_cap])."""
+    lib = _load()
+    s, v, _ = _prep(batch)
+    ids = np.ascontiguousarray(shape_ids, np.uint32)
+    poses = np.ascontiguousarray(poses, np.float32).reshape(-1, 12)
+    n = len(poses)
+    cap = pair_cap if pair_cap is not None else max(max_contacts, 1)
+    flags = np.zeros(n, np.uint8)
+    counts = np.zeros(n, np.uint32)
+    out = np.full((n, cap), -1, np.int32)
+    nd = np.ascontiguousarray(nodes)
+    tr = np.ascontiguousarray(tris, np.float32)
+    assert lib.orc_mesh_shape_collide(_ptr(nd), _ptr(tr), _ptr(s), len(s), _ptr(v), _ptr(ids), _ptr(poses), n,
+                                      int(max_contacts), cap, _ptr(flags), _ptr(counts), _ptr(out),
+                                      threads or default_threads()) == 0
+    return flags, counts, out
+
+
+def mesh_shape_all(tris, batch, shape_id, pose, cap=1 << 20):
+    """Every colliding triangle of one query by brute force."""
+    lib = _load()
+    s, v, _ = _prep(batch)
+    tr = np.ascontiguousarray(tris, np.float32)
+    p = np.ascontiguousarray(pose, np.float32).reshape(12)
+    out = np.zeros(cap, np.int32)
+    n = lib.orc_mesh_shape_all(_ptr(tr), len(tr), _ptr(s), len(s), _ptr(v), int(shape_id), _ptr(p), _ptr(out), cap)
+    return out[:min(n, cap)]
 
 
 def mesh_allpairs(tris_a, tris_b, pose, cap=1 << 20):

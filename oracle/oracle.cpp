@@ -15,6 +15,7 @@
 #include "orc_analytic.hpp"
 #include "orc_convex.hpp"
 #include "orc_mesh.hpp"
+#include "orc_mesh_shape.hpp"
 
 namespace {
 
@@ -420,6 +421,52 @@ int orc_mesh_collide(const void* nodes_a, const float* tris_a, const void* nodes
     }
   });
   return 0;
+}
+
+// fcl::collide(mesh, shape) with penetration off per query: shape shape_ids[i]
+// posed by poses[i] (12 floats: rotation row-major, translation) in the mesh
+// frame (MeshShapeIntersect, bvh_solver-inl.h:6-72).  max_contacts 0: every
+// colliding triangle.  Writes flags, counts and up to pair_cap triangle ids
+// per query.
+int orc_mesh_shape_collide(const void* nodes, const float* tris, const void* shapes, int n_shapes,
+                           const float* verts, const uint32_t* shape_ids, const float* poses, int n, int max_contacts,
+                           int pair_cap, uint8_t* flags, uint32_t* counts, int32_t* tri_ids, int n_threads) {
+  const orc::MeshNode* nd = (const orc::MeshNode*)nodes;
+  const auto sh = makeShapes((const ShapeRec*)shapes, n_shapes, verts);
+  const orc::SolverParams sp;
+  parallelFor(n, n_threads, [&](int b, int e) {
+    std::vector<int> c;
+    for (int i = b; i < e; ++i) {
+      orc::Iso X;
+      for (int k = 0; k < 9; ++k) X.R[k] = poses[12 * (size_t)i + k];
+      X.t = orc::V3(poses[12 * (size_t)i + 9], poses[12 * (size_t)i + 10], poses[12 * (size_t)i + 11]);
+      const uint32_t si = shape_ids[i];
+      c.clear();
+      if (si < (uint32_t)n_shapes)
+        orc::meshShapeIntersect(nd, tris, sh[si], X, max_contacts > 0 ? (size_t)max_contacts : SIZE_MAX, sp, c);
+      flags[i] = c.empty() ? 0 : 1;
+      counts[i] = (uint32_t)c.size();
+      for (size_t k = 0; k < c.size() && k < (size_t)pair_cap; ++k) tri_ids[(size_t)pair_cap * i + k] = c[k];
+    }
+  });
+  return 0;
+}
+
+// Every colliding triangle of one query by brute force over all triangles.
+int orc_mesh_shape_all(const float* tris, int n_tris, const void* shapes, int n_shapes, const float* verts,
+                       uint32_t shape_id, const float* pose, int32_t* tri_ids, int cap) {
+  const auto sh = makeShapes((const ShapeRec*)shapes, n_shapes, verts);
+  const orc::SolverParams sp;
+  orc::Iso X;
+  for (int k = 0; k < 9; ++k) X.R[k] = pose[k];
+  X.t = orc::V3(pose[9], pose[10], pose[11]);
+  int cnt = 0;
+  for (int t = 0; t < n_tris; ++t)
+    if (orc::shapeTriangleIntersect(sh[shape_id], X, tris + 12 * (size_t)t, sp)) {
+      if (cnt < cap) tri_ids[cnt] = t;
+      ++cnt;
+    }
+  return cnt;
 }
 
 // Every colliding triangle pair of one pose by brute force (returns the count;

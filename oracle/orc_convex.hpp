@@ -77,7 +77,7 @@ struct Iso {
 
 // ----------------------------------------------------------------- shapes --
 // Shape type codes are GJKShapeType's values (include/fcl/cvx_collide/gjk_shape.h:9-28).
-enum ShapeType : int32_t { kBox = 0, kSphere = 1, kCapsule = 3, kCylinder = 5, kConvex = 100 };
+enum ShapeType : int32_t { kBox = 0, kSphere = 1, kCapsule = 3, kCylinder = 5, kConvex = 100, kTriangle = 101 };
 
 struct Shape {
   int32_t type = kSphere;
@@ -178,6 +178,14 @@ inline V3 support(const Shape& s, const V3& d) {
       const float* v = s.verts;
       const int best = s.nbr ? convexWalk(s, d) : convexScan(v, s.nv, d);
       return V3(v[4 * best], v[4 * best + 1], v[4 * best + 2]);
+    }
+    case kTriangle: {
+      // triangleSupport, geometry/shape/shape_gjk_interface-inl.h:17-39
+      const float* v = s.verts;
+      const V3 a(v[0], v[1], v[2]), b(v[4], v[5], v[6]), c(v[8], v[9], v[10]);
+      const double da = dot(d, a), db = dot(d, b), dc = dot(d, c);
+      if (da > db) return dc > da ? c : a;
+      return dc > db ? c : b;
     }
     default:
       return V3();

