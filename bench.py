@@ -62,10 +62,11 @@ def parse():
     ap.add_argument("--impl", default="fclg", choices=["fclg", "reference"])
     ap.add_argument("--pairs", type=int, default=N_PAIRS)
     ap.add_argument("--workload", default="mixed",
-                    choices=["mixed", "mesh", "pareto", "plain_small", "arm", "warmstart"],
+                    choices=["mixed", "mesh", "mesh_shape", "pareto", "plain_small", "arm", "warmstart"],
                     help="mixed: the headline convex-pair batch (with the warm-start comparison); mesh: the "
                          "50k x 50k-triangle BVH workload; pareto: 4M heavy-tailed hull pairs; plain_small: 4096 "
-                         "hull pairs; arm: 7-link arm x 32 obstacles, 100k configurations; warmstart: the "
+                         "hull pairs; arm: 7-link arm x 32 obstacles, 100k configurations; mesh_shape: the "
+                         "50k-triangle mesh against 65,536 mixed-shape queries; warmstart: the "
                          "warm-start inference kernel alone on 2.24M arm pairs")
     ap.add_argument("--no-warm", action="store_true", help="skip the warm-start comparison")
     ap.add_argument("--poses", type=int, default=65536)
@@ -420,6 +421,94 @@ def run_mesh(args):
     return 0
 
 
+MESH_SHAPE_WORKLOAD = ("mesh-shape BVH: the first geodesic sphere of the mesh-mesh workload (50,000 triangles) "
+                       "against 65,536 queries of 2,048 mixed shapes (sphere / box / capsule / cylinder / hull, "
+                       "sizes U[0.02, 0.4] m, hulls of log-uniform[8, 256] points), poses as the mesh-mesh "
+                       "workload's; fcl::collide(mesh, shape) with penetration off")
+
+
+def run_mesh_shape(args):
+    """Mesh-shape collides/s (fcl::collide(BVHModel, shape), its own JSON line)."""
+    import torch
+    from fclg import workloads
+    from fclg.api import Context, GpuMesh, mesh_shape_collide
+    import ctypes
+    rank, world, local = dist_env()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    mesh, _ = workloads.mesh_pair()
+    shapes = workloads.mixed(1024, seed=workloads.SEED_BASE + 61)
+    poses = workloads.mesh_poses(args.poses)
+    n = len(poses)
+    ids = (np.arange(n) % len(shapes.shapes)).astype(np.uint32)
+    ctx = Context(local)
+    ctx.set_batch(shapes)
+    gm = GpuMesh(ctx, mesh.vertices, mesh.triangles)
+    stream = torch.cuda.current_stream(dev)
+    d_poses = torch.from_numpy(poses).to(dev)
+    d_ids = torch.from_numpy(ids.view(np.int32)).to(dev)
+    out = {}
+    for cap in (1, 64):
+        d_flags = torch.empty(n, dtype=torch.uint8, device=dev)
+        d_counts = torch.empty(n, dtype=torch.int32, device=dev)
+        d_tris = torch.empty(n * cap, dtype=torch.int32, device=dev)
+        d_status = torch.empty(n, dtype=torch.int32, device=dev)
+
+        def step():
+            rc = ctx.lib.fclg_mesh_shape_collide_device(ctx.h, gm.h, ctypes.c_void_p(d_ids.data_ptr()),
+                                                        ctypes.c_void_p(d_poses.data_ptr()), n, cap,
+                                                        ctypes.c_void_p(d_flags.data_ptr()),
+                                                        ctypes.c_void_p(d_counts.data_ptr()),
+                                                        ctypes.c_void_p(d_tris.data_ptr()),
+                                                        ctypes.c_void_p(d_status.data_ptr()),
+                                                        ctypes.c_void_p(stream.cuda_stream))
+            assert rc == 0
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        launches0 = ctx.launch_count
+        with ClockSampler(local) as clk:
+            e0.record(stream)
+            for _ in range(args.steps):
+                step()
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / args.steps
+        flags = d_flags.cpu().numpy()
+        status = d_status.cpu().numpy()
+        t0 = time.perf_counter()
+        for _ in range(max(1, args.steps // 2)):
+            mesh_shape_collide(ctx, gm, ids, poses, max_contacts=cap)
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / max(1, args.steps // 2)
+        out[cap] = {"value": n / (ms * 1e-3), "ms_per_step": ms, "collide_fraction": float(flags.mean()),
+                    "incomplete": int(np.sum(status != 0)), "e2e": n / (e2e_ms * 1e-3),
+                    "gpu_launches": ctx.launch_count - launches0, "clocks": clk.summary()}
+    import oracle
+    oracle.build()
+    nodes, tris = gm.export()
+    sample = min(2048, n)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    oracle.mesh_shape_collide(nodes, tris, shapes, ids[:sample], poses[:sample], max_contacts=1, threads=threads)
+    cpu_s = time.perf_counter() - t0
+    line = {"metric": "mesh-shape collides/s (fcl::collide on BVHModel<OBBRSS> x shape)", "value": out[1]["value"],
+            "unit": "mesh-shape collides/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": out[1]["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (FP64 re-decision for sphere / box leaves)", "data": "synthetic",
+            "config": {"workload": MESH_SHAPE_WORKLOAD, "queries": n, "first_contact": out[1],
+                       "contacts_64": out[64]},
+            "gpu_launches": out[1]["gpu_launches"], "clocks": out[1]["clocks"],
+            "cpu_baseline": {"value": sample / cpu_s, "unit": "mesh-shape collides/s", "cores": threads,
+                             "kind": "port", "sample": "first %d queries, first-contact mode" % sample},
+            "e2e": {"value": out[1]["e2e"], "unit": "mesh-shape collides/s", "h2d_bytes_per_step": n * 52,
+                    "d2h_bytes_per_step": n * (1 + 4 + 4 + 4)}}
+    print(json.dumps(line))
+    gm.close()
+    ctx.close()
+    return 0
+
+
 def run_warmstart_kernel(args):
     """The warm-start inference kernels alone (tcgen05 and mma.sync) on the arm
     workload's 2.24M pairs, untrained weights (the cost does not depend on them)."""
@@ -522,6 +611,8 @@ def main():
         return run_reference(args)
     if args.workload == "mesh":
         return run_mesh(args)
+    if args.workload == "mesh_shape":
+        return run_mesh_shape(args)
     if args.workload == "warmstart":
         return run_warmstart_kernel(args)
     import torch

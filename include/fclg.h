@@ -370,6 +370,24 @@ int fclg_mesh_collide_device(fclg_context* ctx, const fclg_mesh* a, const fclg_m
                              uint32_t n_poses, uint32_t max_contacts, uint8_t* d_flags, uint32_t* d_counts,
                              int32_t* d_pairs, uint32_t* d_status, void* stream);
 
+/* Boolean collision of a mesh against shapes of the context (fcl::collide on
+   a BVHModel<OBBRSS> and a shape with penetration off:
+   OrientedNodeBVHSolver::MeshShapeIntersect, bvh_solver-inl.h:6-72, with the
+   shape-triangle tests GJKSolver::shapeTriangleIntersect picks,
+   gjk_solver-inl.h:451-591: sphere-triangle and box-triangle in closed form,
+   MPR for capsules, cylinders and hulls).  Query i: shape shape_ids[i] (of
+   fclg_set_shapes) posed by poses[i] (rotation row-major, then translation:
+   12 floats) in the mesh's frame.  A query stops after max_contacts colliding
+   triangles (1: first-contact mode).  Outputs per query: flags, counts,
+   tri_ids (max_contacts triangle ids) and, when not NULL, status (bit 0 stack
+   overflow, bit 1 round limit, bit 2 shape id out of range). */
+int fclg_mesh_shape_collide(fclg_context* ctx, const fclg_mesh* mesh, const uint32_t* shape_ids, const float* poses,
+                            uint32_t n, uint32_t max_contacts, uint8_t* flags, uint32_t* counts, int32_t* tri_ids,
+                            uint32_t* status);
+int fclg_mesh_shape_collide_device(fclg_context* ctx, const fclg_mesh* mesh, const uint32_t* d_shape_ids,
+                                   const float* d_poses, uint32_t n, uint32_t max_contacts, uint8_t* d_flags,
+                                   uint32_t* d_counts, int32_t* d_tri_ids, uint32_t* d_status, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -681,7 +681,6 @@ int fclg_mesh_collide(fclg_context* c, const fclg_mesh* a, const fclg_mesh* b, c
   const size_t need = b_poses + b_flags + b_counts + b_pairs + b_status;
   if (need > c->mesh_io_bytes) {
     if (c->mesh_io) cudaFree(c->mesh_io);
-  if (c->guess) cudaFree(c->guess);
     c->mesh_io = nullptr;
     c->mesh_io_bytes = 0;
     FCLG_CUDA(c, cudaSetDevice(c->device));
@@ -701,6 +700,79 @@ int fclg_mesh_collide(fclg_context* c, const fclg_mesh* a, const fclg_mesh* b, c
   FCLG_CUDA(c, cudaMemcpyAsync(flags, d_flags, n, cudaMemcpyDeviceToHost, c->stream));
   FCLG_CUDA(c, cudaMemcpyAsync(counts, d_counts, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
   FCLG_CUDA(c, cudaMemcpyAsync(pairs, d_pairs, (size_t)n * max_contacts * 8, cudaMemcpyDeviceToHost, c->stream));
+  if (status) FCLG_CUDA(c, cudaMemcpyAsync(status, d_status, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+  FCLG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return FCLG_OK;
+}
+
+int fclg_mesh_shape_collide_device(fclg_context* c, const fclg_mesh* mesh, const uint32_t* d_shape_ids,
+                                   const float* d_poses, uint32_t n, uint32_t max_contacts, uint8_t* d_flags,
+                                   uint32_t* d_counts, int32_t* d_tri_ids, uint32_t* d_status, void* stream) {
+  if (!c) return FCLG_E_INVALID;
+  if (!mesh) return fail(c, FCLG_E_INVALID, "null mesh");
+  if (n == 0) return FCLG_OK;
+  if (max_contacts == 0) return fail(c, FCLG_E_INVALID, "max_contacts must be >= 1");
+  if (!d_shape_ids || !d_poses || !d_flags || !d_counts || !d_tri_ids) return fail(c, FCLG_E_INVALID, "null pointer");
+  if (!c->shapes) return fail(c, FCLG_E_NO_SHAPES, "no shapes set");
+  if (mesh->device != c->device) return fail(c, FCLG_E_INVALID, "mesh on another device");
+  FCLG_CUDA(c, cudaSetDevice(c->device));
+  fclg::MeshShapeArgs m;
+  m.mesh = fclg::MeshDev{static_cast<const float4*>(mesh->nodes), static_cast<const float4*>(mesh->tris),
+                         mesh->n_nodes, mesh->n_tris};
+  m.shapes = c->shapes;
+  m.verts = c->verts;
+  m.n_shapes = c->n_shapes;
+  m.shape_ids = d_shape_ids;
+  m.poses = reinterpret_cast<const float4*>(d_poses);
+  m.n = n;
+  m.max_contacts = max_contacts;
+  m.gjk_tol = 1e-6f;
+  m.gjk_max_iter = 128;
+  m.flags = d_flags;
+  m.counts = d_counts;
+  m.tri_ids = d_tri_ids;
+  m.status = d_status;
+  clear_pending_error();
+  FCLG_CUDA(c, fclg::launch_mesh_shape(m, c->num_sms * 8, static_cast<cudaStream_t>(stream)));
+  c->launches += 1;
+  return FCLG_OK;
+}
+
+int fclg_mesh_shape_collide(fclg_context* c, const fclg_mesh* mesh, const uint32_t* shape_ids, const float* poses,
+                            uint32_t n, uint32_t max_contacts, uint8_t* flags, uint32_t* counts, int32_t* tri_ids,
+                            uint32_t* status) {
+  if (!c) return FCLG_E_INVALID;
+  if (n == 0) return FCLG_OK;
+  if (!shape_ids || !poses || !flags || !counts || !tri_ids) return fail(c, FCLG_E_INVALID, "null pointer");
+  if (max_contacts == 0) return fail(c, FCLG_E_INVALID, "max_contacts must be >= 1");
+  auto up16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
+  const size_t b_poses = up16((size_t)n * 48), b_ids = up16((size_t)n * 4), b_flags = up16(n),
+               b_counts = up16((size_t)n * 4), b_tris = up16((size_t)n * max_contacts * 4),
+               b_status = up16((size_t)n * 4);
+  const size_t need = b_poses + b_ids + b_flags + b_counts + b_tris + b_status;
+  if (need > c->mesh_io_bytes) {
+    if (c->mesh_io) cudaFree(c->mesh_io);
+    c->mesh_io = nullptr;
+    c->mesh_io_bytes = 0;
+    FCLG_CUDA(c, cudaSetDevice(c->device));
+    FCLG_CUDA(c, cudaMalloc(&c->mesh_io, need));
+    c->mesh_io_bytes = need;
+  }
+  char* p = static_cast<char*>(c->mesh_io);
+  float* d_poses = reinterpret_cast<float*>(p);
+  uint32_t* d_ids = reinterpret_cast<uint32_t*>(p += b_poses);
+  uint8_t* d_flags = reinterpret_cast<uint8_t*>(p += b_ids);
+  uint32_t* d_counts = reinterpret_cast<uint32_t*>(p += b_flags);
+  int32_t* d_tris = reinterpret_cast<int32_t*>(p += b_counts);
+  uint32_t* d_status = reinterpret_cast<uint32_t*>(p += b_tris);
+  FCLG_CUDA(c, cudaMemcpyAsync(d_poses, poses, (size_t)n * 48, cudaMemcpyHostToDevice, c->stream));
+  FCLG_CUDA(c, cudaMemcpyAsync(d_ids, shape_ids, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
+  const int rc = fclg_mesh_shape_collide_device(c, mesh, d_ids, d_poses, n, max_contacts, d_flags, d_counts, d_tris,
+                                                d_status, c->stream);
+  if (rc) return rc;
+  FCLG_CUDA(c, cudaMemcpyAsync(flags, d_flags, n, cudaMemcpyDeviceToHost, c->stream));
+  FCLG_CUDA(c, cudaMemcpyAsync(counts, d_counts, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
+  FCLG_CUDA(c, cudaMemcpyAsync(tri_ids, d_tris, (size_t)n * max_contacts * 4, cudaMemcpyDeviceToHost, c->stream));
   if (status) FCLG_CUDA(c, cudaMemcpyAsync(status, d_status, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
   FCLG_CUDA(c, cudaStreamSynchronize(c->stream));
   return FCLG_OK;

@@ -68,6 +68,9 @@ __device__ __forceinline__ void closest_bary_origin(d3 a, d3 b, d3 c, double& u,
 enum : int32_t { kBox = 0, kSphere = 1, kCapsule = 3, kCylinder = 5, kConvex = 100 };
 // Decoded form of a convex hull that carries a walk block (never in fclg_shape).
 constexpr int32_t kConvexWalk = 101;
+// A mesh triangle as a support shape (vofs: its first of three float4 in the
+// triangle soup; never in fclg_shape).
+constexpr int32_t kTriangle = 102;
 
 // One shape as the kernels use it, decoded from the 32-byte fclg_shape.
 // No walk block: the convex support scans every vertex.

@@ -25,4 +25,25 @@ struct MeshArgs {
 
 cudaError_t launch_mesh_collide(const MeshArgs& m, int blocks, cudaStream_t st);
 
+// Mesh against shapes of the context (mesh_shape.cu): query i = shape
+// shape_ids[i] posed by poses[i] in the mesh frame.
+struct MeshShapeArgs {
+  MeshDev mesh;
+  const int4* shapes;     // fclg_shape[n_shapes]
+  const float4* verts;    // hull vertices, xyzw
+  uint32_t n_shapes;
+  const uint32_t* shape_ids;  // [n]
+  const float4* poses;        // 3 float4 per query: rotation row-major, translation
+  uint32_t n;
+  uint32_t max_contacts;      // >= 1
+  float gjk_tol;              // MPR leaves (GJKSolver defaults 1e-6, 128)
+  int gjk_max_iter;
+  uint8_t* flags;             // [n]
+  uint32_t* counts;           // [n]
+  int32_t* tri_ids;           // [n][max_contacts]
+  uint32_t* status;           // [n] or null: bit 0 stack overflow, bit 1 round limit, bit 2 bad shape id
+};
+
+cudaError_t launch_mesh_shape(const MeshShapeArgs& m, int blocks, cudaStream_t st);
+
 }  // namespace fclg

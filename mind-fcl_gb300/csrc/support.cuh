@@ -134,6 +134,14 @@ __device__ __forceinline__ f3 shape_support(const ShapeDev& s, const float4* __r
     case kConvexWalk:
       if constexpr (LANES == 1) return convex_walk(pool + s.vofs, s.nv, d);
       return mk3(0.f, 0.f, 0.f);
+    case kTriangle: {
+      // triangleSupport, geometry/shape/shape_gjk_interface-inl.h:17-39
+      const float4 qa = __ldg(pool + s.vofs), qb = __ldg(pool + s.vofs + 1), qc = __ldg(pool + s.vofs + 2);
+      const f3 a = mk3(qa.x, qa.y, qa.z), b = mk3(qb.x, qb.y, qb.z), c = mk3(qc.x, qc.y, qc.z);
+      const float da = dot(d, a), db = dot(d, b), dc = dot(d, c);
+      if (da > db) return dc > da ? c : a;
+      return dc > db ? c : b;
+    }
     default:
       return mk3(0.f, 0.f, 0.f);
   }
@@ -156,12 +164,13 @@ struct MinkowskiSupport {
   ShapeDev A, B;
   Pose pose;
   const float4* __restrict__ verts;
-  const float4* __restrict__ hull = nullptr;  // walk blocks of kConvexWalk shapes
+  const float4* __restrict__ hull = nullptr;  // walk blocks of kConvexWalk shapes / triangle soup of kTriangle
   Group<LANES> g;
   __device__ __forceinline__ void operator()(f3 d, f3& pa, f3& pb) const {
     if constexpr (LANES < 32) {
-      pa = shape_support_outline<LANES>(A, A.type == kConvexWalk ? hull : verts, d, g);
-      pb = pose.apply(shape_support_outline<LANES>(B, B.type == kConvexWalk ? hull : verts, pose.rotT(-d), g));
+      pa = shape_support_outline<LANES>(A, (A.type == kConvexWalk || A.type == kTriangle) ? hull : verts, d, g);
+      pb = pose.apply(shape_support_outline<LANES>(B, (B.type == kConvexWalk || B.type == kTriangle) ? hull : verts,
+                                                   pose.rotT(-d), g));
     } else {
       pa = shape_support<LANES>(A, verts, d, g);
       pb = pose.apply(shape_support<LANES>(B, verts, pose.rotT(-d), g));

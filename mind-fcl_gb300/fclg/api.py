@@ -35,6 +35,7 @@ EXPORTS = [
     "fclg_warmstart_gradient", "fclg_warmstart_train", "fclg_set_warmstart", "fclg_warmstart_status",
     "fclg_autotune", "fclg_graph_create", "fclg_graph_launch", "fclg_graph_destroy",
     "fclg_collide_directed", "fclg_collide_directed_device", "fclg_hull_graph",
+    "fclg_mesh_shape_collide", "fclg_mesh_shape_collide_device",
 ]
 
 STATIC_MAX_PAIRS = 16384  # FCLG_STATIC_MAX_PAIRS
@@ -156,6 +157,10 @@ def load_library(path=LIB_PATH):
     lib.fclg_graph_destroy.restype = None
     lib.fclg_hull_graph.argtypes = [vp, u32, vp, vp, vp, u32, ctypes.POINTER(u32)]
     lib.fclg_hull_graph.restype = i32
+    lib.fclg_mesh_shape_collide.argtypes = [vp, vp, vp, vp, u32, u32, vp, vp, vp, vp]
+    lib.fclg_mesh_shape_collide.restype = i32
+    lib.fclg_mesh_shape_collide_device.argtypes = [vp, vp, vp, vp, u32, u32, vp, vp, vp, vp, vp]
+    lib.fclg_mesh_shape_collide_device.restype = i32
     _lib = lib
     return lib
 
@@ -460,6 +465,22 @@ class GpuMesh:
             self.close()
         except Exception:
             pass
+
+
+def mesh_shape_collide(ctx, mesh, shape_ids, poses, max_contacts=1):
+    """fcl::collide(mesh, shape) per query, penetration off: shapes of the
+    context's shape set, poses [n, 12] in the mesh frame.  Returns (flags,
+    counts, tri_ids [n, max_contacts], status)."""
+    ids = np.ascontiguousarray(shape_ids, np.uint32)
+    p = np.ascontiguousarray(poses, np.float32).reshape(-1, 12)
+    n = len(p)
+    flags = np.zeros(n, np.uint8)
+    counts = np.zeros(n, np.uint32)
+    tris = np.full((n, max_contacts), -1, np.int32)
+    status = np.zeros(n, np.uint32)
+    ctx._check(ctx.lib.fclg_mesh_shape_collide(ctx.h, mesh.h, _ptr(ids), _ptr(p), n, max_contacts, _ptr(flags),
+                                               _ptr(counts), _ptr(tris), _ptr(status)), "fclg_mesh_shape_collide")
+    return flags, counts, tris, status
 
 
 def mesh_collide(ctx, mesh_a, mesh_b, poses, max_contacts=1):

@@ -147,3 +147,44 @@ def test_mpr_leaves_agree_with_sphere_sweep(oracle_lib, small_mesh):
     f_on, _, _ = oracle_lib.mesh_shape_collide(nodes, tris, b, ids, on)
     assert f_far.sum() == 0
     assert f_on.mean() > 0.9
+
+
+def _sets(counts, ids, i):
+    return set(ids[i, :counts[i]].tolist())
+
+
+@pytest.mark.gpu
+def test_gpu_mesh_shape_vs_oracle(oracle_lib, small_mesh):
+    """The library's kernel (fclg_mesh_shape_collide) against the oracle on the
+    same tree: with room for every contact, the colliding triangle sets are
+    identical for spheres and boxes (FP32 tests re-decided in FP64 near their
+    thresholds) and for >= 99 % of the capsule / cylinder / hull queries (MPR
+    in FP32; the rest differ by triangles within rounding of contact); in
+    first-contact mode the flags agree likewise and the reported triangle is
+    one of the oracle's colliding set."""
+    from fclg.api import Context, GpuMesh, mesh_shape_collide
+    m = workloads.geodesic_sphere(10, 0.3, 0.01, seed=1)
+    b = shape_set()
+    ids, poses = queries(3000, seed=21)
+    ctx = Context(0)
+    try:
+        ctx.set_batch(b)
+        gm = GpuMesh(ctx, m.vertices, m.triangles)
+        nodes, tris = gm.export()
+        cap = 2048
+        fo, co, oo = oracle_lib.mesh_shape_collide(nodes, tris, b, ids, poses, max_contacts=0, pair_cap=cap)
+        fg, cg, og, st = mesh_shape_collide(ctx, gm, ids, poses, max_contacts=cap)
+        assert np.all(st == 0)
+        assert 0.2 < fo.mean() < 0.95
+        exact = ids < 2
+        same = np.array([_sets(co, oo, i) == _sets(cg, og, i) for i in range(len(ids))])
+        assert same[exact].all(), np.nonzero(exact & ~same)[0][:10]
+        assert same[~exact].mean() >= 0.99
+        f1, c1, o1, _ = mesh_shape_collide(ctx, gm, ids, poses, max_contacts=1)
+        assert np.array_equal(f1[exact], fo[exact])
+        assert np.mean(f1[~exact] == fo[~exact]) >= 0.995
+        both = (f1 == 1) & (fo == 1)
+        assert all(o1[i, 0] in _sets(co, oo, i) for i in np.nonzero(both & exact)[0])
+        gm.close()
+    finally:
+        ctx.close()
