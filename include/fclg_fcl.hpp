@@ -23,6 +23,7 @@
 //   * Each call runs on a per-thread context of device 0 (setDevice() before
 //     the first call to change it).  One pair per call is a GPU round trip;
 //     BatchQuery runs many pairs per call and is the fast path.
+//   * Mesh-mesh and mesh-shape pairs: boolean contacts with triangle indices.
 //   * Penetration modes: disabled (boolean), the default GJK/EPA mode, and
 //     the MPR directed / incremental minimum-distance modes
 //     (useDirectedPenetration / useIncrementalMinimumDistancePenetration,
@@ -556,6 +557,38 @@ class BatchQuery {
 
 namespace detail {
 
+// Mesh-shape collide with penetration off (MeshShapeIntersect): contacts
+// carry the mesh's triangle index (b1 when the mesh is o1, b2 otherwise).
+template <typename S, typename TFM, typename TFS>
+std::size_t mesh_shape_collide(const CollisionGeometry<S>* mesh, const TFM& tfm, const CollisionGeometry<S>* shape,
+                               const TFS& tfs, bool mesh_first, const CollisionRequest<S>& req,
+                               CollisionResult<S>& res) {
+  if (req.isPenetrationEnabled())
+    throw std::invalid_argument("fclg: mesh-shape contacts with penetration are not provided (boolean only)");
+  using M = BVHModel<OBBRSS<S>>;
+  const auto* m = static_cast<const M*>(mesh);
+  fclg_context* ctx = thread_context();
+  std::vector<fclg_shape> shapes;
+  std::vector<float> verts;
+  encode_shape(shape, shapes, verts);
+  check(ctx, fclg_set_shapes(ctx, shapes.data(), 1, verts.data(), verts.size() / 4), "fclg_set_shapes");
+  fclg_pair p{};
+  relative_pose(tfm, tfs, p);
+  float pose[12];
+  for (int i = 0; i < 9; ++i) pose[i] = p.rot[i];
+  for (int i = 0; i < 3; ++i) pose[9 + i] = p.trans[i];
+  const uint32_t cap = (uint32_t)std::max<std::size_t>(req.maxNumContacts(), 1);
+  const uint32_t id = 0;
+  uint8_t flag = 0;
+  uint32_t count = 0, status = 0;
+  std::vector<int32_t> tri((std::size_t)cap, -1);
+  check(ctx, fclg_mesh_shape_collide(ctx, m->device_mesh(ctx), &id, pose, 1, cap, &flag, &count, tri.data(), &status),
+        "fclg_mesh_shape_collide");
+  for (uint32_t k = 0; k < count && res.numContacts() < req.maxNumContacts(); ++k)
+    res.addContact(mesh_first ? Contact<S>(mesh, shape, tri[k], -1) : Contact<S>(shape, mesh, -1, tri[k]));
+  return res.numContacts();
+}
+
 // Mesh-mesh collide: contacts carry the triangle indices (b1, b2).
 template <typename S, typename TF1, typename TF2>
 std::size_t mesh_collide(const CollisionGeometry<S>* o1, const TF1& tf1, const CollisionGeometry<S>* o2,
@@ -592,7 +625,8 @@ std::size_t collide(const CollisionGeometry<S>* o1, const TF1& tf1, const Collis
   if (request.maxNumContacts() == 0) return 0;  // the reference warns and returns 0 (collision-inl.h:73-111)
   const bool m1 = o1->getNodeType() == BV_OBBRSS, m2 = o2->getNodeType() == BV_OBBRSS;
   if (m1 && m2) return detail::mesh_collide(o1, tf1, o2, tf2, request, result);
-  if (m1 || m2) throw std::invalid_argument("fclg: mesh-shape pairs are not provided");
+  if (m1) return detail::mesh_shape_collide(o1, tf1, o2, tf2, true, request, result);
+  if (m2) return detail::mesh_shape_collide(o2, tf2, o1, tf1, false, request, result);
   BatchQuery<S> q;
   q.add(o1, tf1, o2, tf2);
   CollisionResult<S> r = q.collide(request).front();

@@ -140,6 +140,19 @@ int main() {
   res.clear();
   CHECK(collide(&m1, at(0, 0, 0), &m2, at(2.5, 0, 0), mesh_req, res) == 0, "mesh apart");
 
+  // mesh-shape (MeshShapeIntersect): a sphere and a box crossing the mesh's
+  // surface collide, a sphere outside it does not
+  Sphere<S> ball(0.3);
+  CollisionRequest<S> ms_req(4);
+  res.clear();
+  CHECK(collide(&m1, at(0, 0, 0), &ball, at(1.1, 0, 0), ms_req, res) > 0, "mesh-sphere overlap");
+  for (const auto& c : res.getContacts()) CHECK(c.o1 == &m1 && c.b1 >= 0 && c.b1 < 8, "mesh-sphere triangle ids");
+  res.clear();
+  CHECK(collide(&m1, at(0, 0, 0), &ball, at(2.0, 0, 0), ms_req, res) == 0, "mesh-sphere apart");
+  res.clear();
+  CHECK(collide(&b1, at(0.9, 0, 0), &m1, at(0, 0, 0), ms_req, res) > 0, "box-mesh overlap");
+  for (const auto& c : res.getContacts()) CHECK(c.o2 == &m1 && c.b2 >= 0 && c.b2 < 8, "box-mesh triangle ids");
+
   if (failures == 0) std::printf("fcl_compat_test: all passed\n");
   return failures == 0 ? 0 : 1;
 }
