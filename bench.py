@@ -474,6 +474,7 @@ def run_mesh_shape(args):
                 step()
             e1.record(stream)
             torch.cuda.synchronize(dev)
+        launches = ctx.launch_count - launches0
         ms = e0.elapsed_time(e1) / args.steps
         flags = d_flags.cpu().numpy()
         status = d_status.cpu().numpy()
@@ -483,7 +484,7 @@ def run_mesh_shape(args):
         e2e_ms = (time.perf_counter() - t0) * 1e3 / max(1, args.steps // 2)
         out[cap] = {"value": n / (ms * 1e-3), "ms_per_step": ms, "collide_fraction": float(flags.mean()),
                     "incomplete": int(np.sum(status != 0)), "e2e": n / (e2e_ms * 1e-3),
-                    "gpu_launches": ctx.launch_count - launches0, "clocks": clk.summary()}
+                    "gpu_launches": launches, "clocks": clk.summary()}
     import oracle
     oracle.build()
     nodes, tris = gm.export()
