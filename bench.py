@@ -62,7 +62,7 @@ def parse():
     ap.add_argument("--impl", default="fclg", choices=["fclg", "reference"])
     ap.add_argument("--pairs", type=int, default=N_PAIRS)
     ap.add_argument("--workload", default="mixed",
-                    choices=["mixed", "mesh", "mesh_shape", "pareto", "plain_small", "arm", "warmstart"],
+                    choices=["mixed", "mesh", "mesh_shape", "scene", "pareto", "plain_small", "arm", "warmstart"],
                     help="mixed: the headline convex-pair batch (with the warm-start comparison); mesh: the "
                          "50k x 50k-triangle BVH workload; pareto: 4M heavy-tailed hull pairs; plain_small: 4096 "
                          "hull pairs; arm: 7-link arm x 32 obstacles, 100k configurations; mesh_shape: the "
@@ -71,6 +71,7 @@ def parse():
     ap.add_argument("--no-warm", action="store_true", help="skip the warm-start comparison")
     ap.add_argument("--poses", type=int, default=65536)
     ap.add_argument("--configs", type=int, default=100_000, help="arm: joint configurations (7 x 32 pairs each)")
+    ap.add_argument("--objects", type=int, default=100_000, help="scene: posed objects")
     ap.add_argument("--sweep", action="store_true",
                     help="convex workloads: time one query per launch layout (GJK lanes, hull split, support "
                          "walk on / off) and print them as one JSON object instead of the bench line")
@@ -510,6 +511,109 @@ def run_mesh_shape(args):
     return 0
 
 
+SCENE_WORKLOAD = ("scene: 100,000 posed objects (sphere / box / capsule / cylinder / hull, sizes U[0.02, 0.4] m, "
+                  "hulls of log-uniform[8, 256] points; uniform rotations, 20 % identity) in a cube at 0.25 "
+                  "objects per bounding-sphere volume; per step the broadphase (CollisionObject AABBs, every "
+                  "overlapping pair), the candidates' narrowphase records and the signed distance of every "
+                  "candidate")
+
+
+def run_scene(args):
+    """Scene objects/s through broadphase + narrowphase (its own JSON line)."""
+    import torch
+    import ctypes
+    from fclg import workloads
+    from fclg.api import Context
+    from fclg.layout import PAIR_DTYPE
+    rank, world, local = dist_env()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    b, ids, poses = workloads.scene(args.objects)
+    n = len(ids)
+    ctx = Context(local)
+    ctx.set_batch(b)
+    stream = torch.cuda.current_stream(dev)
+    vp = ctypes.c_void_p
+    d_ids = torch.from_numpy(ids.view(np.int32)).to(dev)
+    d_poses = torch.from_numpy(poses).to(dev)
+    cap = 16 * n
+    d_cand = torch.empty(2 * cap, dtype=torch.int32, device=dev)
+    d_cnt = torch.zeros(1, dtype=torch.int32, device=dev)
+    d_rec = torch.empty(cap * PAIR_DTYPE.itemsize, dtype=torch.uint8, device=dev)
+    d_res = torch.empty(cap * 48, dtype=torch.uint8, device=dev)
+    h_cnt = torch.zeros(1, dtype=torch.int32).pin_memory()
+
+    def step():
+        assert ctx.lib.fclg_broadphase_device(ctx.h, vp(d_ids.data_ptr()), vp(d_poses.data_ptr()), n,
+                                              vp(d_cand.data_ptr()), cap, vp(d_cnt.data_ptr()), None, None,
+                                              vp(stream.cuda_stream)) == 0
+        h_cnt.copy_(d_cnt, non_blocking=True)
+        stream.synchronize()
+        m = min(int(h_cnt.item()), cap)
+        assert ctx.lib.fclg_object_pairs_device(ctx.h, vp(d_ids.data_ptr()), vp(d_poses.data_ptr()),
+                                                vp(d_cand.data_ptr()), m, vp(d_rec.data_ptr()),
+                                                vp(stream.cuda_stream)) == 0
+        ctx.distance_device(d_rec.data_ptr(), m, d_res.data_ptr(), None, stream.cuda_stream)
+        return m
+
+    for _ in range(args.warmup):
+        m = step()
+    torch.cuda.synchronize(dev)
+    # broadphase alone
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        ctx.lib.fclg_broadphase_device(ctx.h, vp(d_ids.data_ptr()), vp(d_poses.data_ptr()), n,
+                                       vp(d_cand.data_ptr()), cap, vp(d_cnt.data_ptr()), None, None,
+                                       vp(stream.cuda_stream))
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    bp_ms = e0.elapsed_time(e1) / args.steps
+    launches0 = ctx.launch_count
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize(dev)
+        e0.record(stream)
+        for _ in range(args.steps):
+            m = step()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1) / args.steps
+    launches = ctx.launch_count - launches0
+    # CPU baseline: FP64 AABBs, sort-and-sweep, signed distance of the candidates
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    boxes = oracle.object_aabbs(b, ids, poses)
+    cand = oracle.sweep_pairs(boxes)
+    rec = np.zeros(len(cand), PAIR_DTYPE)
+    P = poses.astype(np.float64)
+    Ri, Rj = P[cand[:, 0], :9].reshape(-1, 3, 3), P[cand[:, 1], :9].reshape(-1, 3, 3)
+    rec["shape_a"], rec["shape_b"] = ids[cand[:, 0]], ids[cand[:, 1]]
+    rec["rot"] = np.einsum("nki,nkj->nij", Ri, Rj).reshape(-1, 9)
+    rec["trans"] = np.einsum("nki,nk->ni", Ri, P[cand[:, 1], 9:] - P[cand[:, 0], 9:])
+    q = workloads.Batch("scene_pairs", b.shapes, b.vertices, rec, {})
+    cpu_bp = time.perf_counter() - t0
+    walk = oracle.walk_tables(q)
+    cpu_np, _ = oracle.time_signed_distance(q, threads=threads, walk=walk)
+    cpu_s = cpu_bp + cpu_np
+    line = {"metric": "scene objects/s (broadphase + narrowphase signed distance)", "value": n / (ms * 1e-3),
+            "unit": "scene objects/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": SCENE_WORKLOAD, "objects": n, "candidate_pairs": m, "broadphase_ms": bp_ms,
+                       "candidate_pairs_per_s": m / (ms * 1e-3)},
+            "gpu_launches": launches, "clocks": clk.summary(),
+            "cpu_baseline": {"value": n / cpu_s, "unit": "scene objects/s", "cores": threads, "kind": "port",
+                             "sample": "the whole scene once: FP64 AABBs and sort-and-sweep on one thread "
+                                       "(%.2f s), candidates' signed distance on all threads (%.2f s)"
+                                       % (cpu_bp, cpu_np)},
+            "e2e": {"value": n / (ms * 1e-3), "unit": "scene objects/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 4, "note": "device-resident scene; one 4-byte count read per step"}}
+    print(json.dumps(line))
+    ctx.close()
+    return 0
+
+
 def run_warmstart_kernel(args):
     """The warm-start inference kernels alone (tcgen05 and mma.sync) on the arm
     workload's 2.24M pairs, untrained weights (the cost does not depend on them)."""
@@ -614,6 +718,8 @@ def main():
         return run_mesh(args)
     if args.workload == "mesh_shape":
         return run_mesh_shape(args)
+    if args.workload == "scene":
+        return run_scene(args)
     if args.workload == "warmstart":
         return run_warmstart_kernel(args)
     import torch

@@ -134,6 +134,30 @@ int fclg_set_shapes(fclg_context* ctx, const fclg_shape* shapes, uint32_t n_shap
 int fclg_set_shapes_device(fclg_context* ctx, const fclg_shape* d_shapes, uint32_t n_shapes,
                            const float* d_vertices_xyzw, uint64_t n_vertices);
 
+/* Broadphase over n posed objects -- object i is shape shape_ids[i] of
+   fclg_set_shapes posed by poses[i] (world rotation row-major, translation:
+   12 floats): every pair (i < j) whose world AABBs overlap (touching counts),
+   the pair set BinaryAABB_Tree::SelfCollision reports
+   (broadphase/binary_AABB_tree-inl.h) over CollisionObject::computeAABB's
+   boxes (narrowphase/collision_object-inl.h:141-154: the local AABB
+   translated for an identity rotation, else the cube of the local half
+   diagonal about the moved centre).  pairs receives up to cap pairs (2 x
+   u32, unordered); *n_pairs the total, which may exceed cap (call again with
+   room for all).  aabbs (nullable, device entry: two float4 arrays lo / hi of
+   n each; host entry: n x 6 floats lo, hi) receives the boxes.  The reference
+   walks a binary tree; this sorts by the lower x bound and sweeps. */
+int fclg_broadphase(fclg_context* ctx, const uint32_t* shape_ids, const float* poses, uint32_t n, uint32_t* pairs,
+                    uint32_t cap, uint32_t* n_pairs, float* aabbs);
+int fclg_broadphase_device(fclg_context* ctx, const uint32_t* d_shape_ids, const float* d_poses, uint32_t n,
+                           uint32_t* d_pairs, uint32_t cap, uint32_t* d_n_pairs, float* d_aabb_lo, float* d_aabb_hi,
+                           void* stream);
+/* Narrowphase records (fclg_pair) for m candidate object pairs (2 x u32 each):
+   shape_a = shape_ids[i], shape_b = shape_ids[j], the pose of j in i's frame
+   (X_i^-1 X_j), flags and pair_class 0; feeds fclg_distance_device /
+   fclg_collide_device straight from fclg_broadphase_device's output. */
+int fclg_object_pairs_device(fclg_context* ctx, const uint32_t* d_shape_ids, const float* d_poses,
+                             const uint32_t* d_candidates, uint32_t m, fclg_pair* d_pairs, void* stream);
+
 /* Edge graph of the convex hull of nv points (xyzw), the graph the support
    walk climbs (fclg_tuning.support_walk): starts[6] = the extreme corner along
    +x, -x, +y, -y, +z, -z; first[nv + 1] = row starts into adj; adj = the

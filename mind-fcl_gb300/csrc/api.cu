@@ -11,6 +11,7 @@
 #include <atomic>
 #include <thread>
 
+#include "broadphase.h"
 #include "fclg.h"
 #include "hull.h"
 #include "kernels.h"
@@ -35,6 +36,11 @@ struct fclg_context {
   float4* hull_ents = nullptr;
   uint32_t walk_hulls = 0;
   bool support_walk = false;
+  // broadphase scratch and host staging
+  void* bp_scratch = nullptr;
+  size_t bp_bytes = 0;
+  void* bp_io = nullptr;
+  size_t bp_io_bytes = 0;
   bool gjk_refill = false;
   // scratch handed from the GJK pass to the EPA pass
   uint32_t* epa_count = nullptr;  // [2]: work list, overflow list
@@ -439,6 +445,8 @@ void fclg_destroy(fclg_context* c) {
   if (c->bk_small) cudaFree(c->bk_small);
   if (c->mesh_io) cudaFree(c->mesh_io);
   if (c->guess) cudaFree(c->guess);
+  if (c->bp_scratch) cudaFree(c->bp_scratch);
+  if (c->bp_io) cudaFree(c->bp_io);
   if (c->stream) cudaStreamDestroy(c->stream);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -775,6 +783,102 @@ int fclg_mesh_shape_collide(fclg_context* c, const fclg_mesh* mesh, const uint32
   FCLG_CUDA(c, cudaMemcpyAsync(tri_ids, d_tris, (size_t)n * max_contacts * 4, cudaMemcpyDeviceToHost, c->stream));
   if (status) FCLG_CUDA(c, cudaMemcpyAsync(status, d_status, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
   FCLG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return FCLG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Broadphase (BinaryAABB_Tree::SelfCollision over CollisionObject AABBs).
+// ---------------------------------------------------------------------------
+
+int fclg_broadphase_device(fclg_context* c, const uint32_t* d_shape_ids, const float* d_poses, uint32_t n,
+                           uint32_t* d_pairs, uint32_t cap, uint32_t* d_n_pairs, float* d_aabb_lo, float* d_aabb_hi,
+                           void* stream) {
+  if (!c) return FCLG_E_INVALID;
+  if (!d_n_pairs || (n && (!d_shape_ids || !d_poses)) || (cap && !d_pairs))
+    return fail(c, FCLG_E_INVALID, "null pointer");
+  if (!c->shapes) return fail(c, FCLG_E_NO_SHAPES, "no shapes set");
+  FCLG_CUDA(c, cudaSetDevice(c->device));
+  const size_t need = fclg::broadphase_scratch_bytes(n, c->n_shapes);
+  if (need > c->bp_bytes) {
+    if (c->bp_scratch) cudaFree(c->bp_scratch);
+    c->bp_scratch = nullptr;
+    c->bp_bytes = 0;
+    FCLG_CUDA(c, cudaMalloc(&c->bp_scratch, need));
+    c->bp_bytes = need;
+  }
+  fclg::BroadphaseArgs a;
+  a.shapes = c->shapes;
+  a.verts = c->verts;
+  a.n_shapes = c->n_shapes;
+  a.shape_ids = d_shape_ids;
+  a.poses = reinterpret_cast<const float4*>(d_poses);
+  a.n = n;
+  a.pairs = d_pairs;
+  a.cap = cap;
+  a.count = d_n_pairs;
+  a.aabb_lo = reinterpret_cast<float4*>(d_aabb_lo);
+  a.aabb_hi = reinterpret_cast<float4*>(d_aabb_hi);
+  clear_pending_error();
+  FCLG_CUDA(c, fclg::launch_broadphase(a, c->bp_scratch, static_cast<cudaStream_t>(stream)));
+  c->launches += n ? (uint64_t)fclg::broadphase_launches() : 0;
+  return FCLG_OK;
+}
+
+int fclg_broadphase(fclg_context* c, const uint32_t* shape_ids, const float* poses, uint32_t n, uint32_t* pairs,
+                    uint32_t cap, uint32_t* n_pairs, float* aabbs) {
+  if (!c) return FCLG_E_INVALID;
+  if (!n_pairs || (n && (!shape_ids || !poses)) || (cap && !pairs)) return fail(c, FCLG_E_INVALID, "null pointer");
+  auto up256 = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t b_ids = up256((size_t)n * 4), b_poses = up256((size_t)n * 48), b_pairs = up256((size_t)cap * 8),
+               b_box = up256((size_t)n * 16), b_cnt = 256;
+  const size_t need = b_ids + b_poses + b_pairs + 2 * b_box + b_cnt;
+  FCLG_CUDA(c, cudaSetDevice(c->device));
+  if (need > c->bp_io_bytes) {
+    if (c->bp_io) cudaFree(c->bp_io);
+    c->bp_io = nullptr;
+    c->bp_io_bytes = 0;
+    FCLG_CUDA(c, cudaMalloc(&c->bp_io, need));
+    c->bp_io_bytes = need;
+  }
+  char* p = static_cast<char*>(c->bp_io);
+  uint32_t* d_ids = reinterpret_cast<uint32_t*>(p);
+  float* d_poses = reinterpret_cast<float*>(p += b_ids);
+  uint32_t* d_pairs = reinterpret_cast<uint32_t*>(p += b_poses);
+  float* d_lo = reinterpret_cast<float*>(p += b_pairs);
+  float* d_hi = reinterpret_cast<float*>(p += b_box);
+  uint32_t* d_cnt = reinterpret_cast<uint32_t*>(p += b_box);
+  if (n) {
+    FCLG_CUDA(c, cudaMemcpyAsync(d_ids, shape_ids, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
+    FCLG_CUDA(c, cudaMemcpyAsync(d_poses, poses, (size_t)n * 48, cudaMemcpyHostToDevice, c->stream));
+  }
+  const int rc = fclg_broadphase_device(c, d_ids, d_poses, n, d_pairs, cap, d_cnt, d_lo, d_hi, c->stream);
+  if (rc) return rc;
+  FCLG_CUDA(c, cudaMemcpyAsync(n_pairs, d_cnt, 4, cudaMemcpyDeviceToHost, c->stream));
+  FCLG_CUDA(c, cudaStreamSynchronize(c->stream));
+  const uint32_t got = std::min(*n_pairs, cap);
+  if (got) FCLG_CUDA(c, cudaMemcpy(pairs, d_pairs, (size_t)got * 8, cudaMemcpyDeviceToHost));
+  if (aabbs && n) {
+    std::vector<float> lo(4 * (size_t)n), hi(4 * (size_t)n);
+    FCLG_CUDA(c, cudaMemcpy(lo.data(), d_lo, lo.size() * 4, cudaMemcpyDeviceToHost));
+    FCLG_CUDA(c, cudaMemcpy(hi.data(), d_hi, hi.size() * 4, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; ++i)
+      for (int k = 0; k < 3; ++k) {
+        aabbs[6 * i + k] = lo[4 * i + k];
+        aabbs[6 * i + 3 + k] = hi[4 * i + k];
+      }
+  }
+  return FCLG_OK;
+}
+
+int fclg_object_pairs_device(fclg_context* c, const uint32_t* d_shape_ids, const float* d_poses,
+                             const uint32_t* d_candidates, uint32_t m, fclg_pair* d_pairs, void* stream) {
+  if (!c) return FCLG_E_INVALID;
+  if (m && (!d_shape_ids || !d_poses || !d_candidates || !d_pairs)) return fail(c, FCLG_E_INVALID, "null pointer");
+  FCLG_CUDA(c, cudaSetDevice(c->device));
+  clear_pending_error();
+  FCLG_CUDA(c, fclg::launch_object_pairs(d_shape_ids, d_poses, d_candidates, m, d_pairs,
+                                         static_cast<cudaStream_t>(stream)));
+  c->launches += m ? 1 : 0;
   return FCLG_OK;
 }
 

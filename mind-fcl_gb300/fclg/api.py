@@ -36,6 +36,7 @@ EXPORTS = [
     "fclg_autotune", "fclg_graph_create", "fclg_graph_launch", "fclg_graph_destroy",
     "fclg_collide_directed", "fclg_collide_directed_device", "fclg_hull_graph",
     "fclg_mesh_shape_collide", "fclg_mesh_shape_collide_device",
+    "fclg_broadphase", "fclg_broadphase_device", "fclg_object_pairs_device",
 ]
 
 STATIC_MAX_PAIRS = 16384  # FCLG_STATIC_MAX_PAIRS
@@ -161,6 +162,12 @@ def load_library(path=LIB_PATH):
     lib.fclg_mesh_shape_collide.restype = i32
     lib.fclg_mesh_shape_collide_device.argtypes = [vp, vp, vp, vp, u32, u32, vp, vp, vp, vp, vp]
     lib.fclg_mesh_shape_collide_device.restype = i32
+    lib.fclg_broadphase.argtypes = [vp, vp, vp, u32, vp, u32, ctypes.POINTER(u32), vp]
+    lib.fclg_broadphase.restype = i32
+    lib.fclg_broadphase_device.argtypes = [vp, vp, vp, u32, vp, u32, vp, vp, vp, vp]
+    lib.fclg_broadphase_device.restype = i32
+    lib.fclg_object_pairs_device.argtypes = [vp, vp, vp, vp, u32, vp, vp]
+    lib.fclg_object_pairs_device.restype = i32
     _lib = lib
     return lib
 
@@ -465,6 +472,25 @@ class GpuMesh:
             self.close()
         except Exception:
             pass
+
+
+def broadphase(ctx, shape_ids, poses, cap=None):
+    """Overlapping object pairs (fclg_broadphase): objects = (shape of the
+    context's set, world pose [12]).  Returns (pairs [m, 2] uint32 with i < j,
+    aabbs [n, 6] float32 lo / hi); retries with room for every pair."""
+    ids = np.ascontiguousarray(shape_ids, np.uint32)
+    p = np.ascontiguousarray(poses, np.float32).reshape(-1, 12)
+    n = len(p)
+    cap = 4 * n if cap is None else cap
+    aabbs = np.zeros((n, 6), np.float32)
+    while True:
+        pairs = np.zeros((max(cap, 1), 2), np.uint32)
+        m = ctypes.c_uint32(0)
+        ctx._check(ctx.lib.fclg_broadphase(ctx.h, _ptr(ids), _ptr(p), n, _ptr(pairs), cap, ctypes.byref(m),
+                                           _ptr(aabbs)), "fclg_broadphase")
+        if m.value <= cap:
+            return pairs[:m.value], aabbs
+        cap = m.value
 
 
 def mesh_shape_collide(ctx, mesh, shape_ids, poses, max_contacts=1):

@@ -213,6 +213,29 @@ def pareto(n_pairs=4_000_000, seed=SEED_BASE + 4, g_max=PARETO_G_MAX):
     return Batch("pareto", s, v, p, {"seed": seed, "g_max": g_max})
 
 
+def scene(n_objects=100_000, seed=SEED_BASE + 7, density=0.25, identity_fraction=0.2):
+    """A scene of posed objects for the broadphase feed: n_objects shapes of
+    the mixed workload's kinds and sizes (one shape per object), world poses
+    with uniform rotations (identity for identity_fraction of them: the
+    CollisionObject::computeAABB shortcut) and translations uniform in a cube
+    whose edge gives ``density`` objects per bounding-sphere volume.
+    Returns (Batch of the shapes, shape_ids [n] uint32, poses [n, 12] float32)."""
+    rng = _rng(seed)
+    choice = np.array([BOX, SPHERE, CAPSULE, CYLINDER, CONVEX], np.int32)
+    types = choice[np.minimum((rng.random(n_objects) * 5).astype(np.int64), 4)]
+    s, v, rho = _make_shapes(rng, types, 0.02, 0.4, lambda k: log_uniform_counts(rng, k, 8, 256))
+    vol = float(np.sum(4.0 / 3.0 * np.pi * rho ** 3)) / density
+    edge = vol ** (1.0 / 3.0)
+    R = random_rotations(rng, n_objects).reshape(-1, 9)
+    ident = rng.random(n_objects) < identity_fraction
+    R[ident] = np.eye(3).ravel()
+    t = (rng.random((n_objects, 3)) - 0.5) * edge
+    poses = np.concatenate([R, t], axis=1).astype(np.float32)
+    ids = np.arange(n_objects, dtype=np.uint32)
+    b = Batch("scene", s, v, np.zeros(0, PAIR_DTYPE), {"seed": seed, "edge": edge, "density": density})
+    return b, ids, poses
+
+
 def _rot(axis, ang):
     """Batched rotation matrices [n, 3, 3] about a coordinate axis."""
     c, s_ = np.cos(ang), np.sin(ang)

@@ -80,6 +80,12 @@ def _load():
         lib.orc_mesh_shape_collide.restype = i
         lib.orc_mesh_shape_all.argtypes = [vp, i, vp, i, vp, ctypes.c_uint32, vp, vp, i]
         lib.orc_mesh_shape_all.restype = i
+        lib.orc_object_aabbs.argtypes = [vp, i, vp, vp, vp, i, vp]
+        lib.orc_object_aabbs.restype = i
+        lib.orc_aabb_pairs.argtypes = [vp, i, vp, i]
+        lib.orc_aabb_pairs.restype = i
+        lib.orc_sweep_pairs.argtypes = [vp, i, vp, i]
+        lib.orc_sweep_pairs.restype = i
         _lib = lib
     return _lib
 
@@ -404,6 +410,43 @@ def mesh_shape_all(tris, batch, shape_id, pose, cap=1 << 20):
     out = np.zeros(cap, np.int32)
     n = lib.orc_mesh_shape_all(_ptr(tr), len(tr), _ptr(s), len(s), _ptr(v), int(shape_id), _ptr(p), _ptr(out), cap)
     return out[:min(n, cap)]
+
+
+def object_aabbs(batch, shape_ids, poses):
+    """CollisionObject::computeAABB per object in FP64: [n, 6] lo, hi."""
+    lib = _load()
+    s, v, _ = _prep(batch)
+    ids = np.ascontiguousarray(shape_ids, np.uint32)
+    p = np.ascontiguousarray(poses, np.float32).reshape(-1, 12)
+    out = np.zeros((len(p), 6), np.float64)
+    assert lib.orc_object_aabbs(_ptr(s), len(s), _ptr(v), _ptr(ids), _ptr(p), len(p), _ptr(out)) == 0
+    return out
+
+
+def aabb_pairs(boxes, cap=None):
+    """Every overlapping pair (i < j) of the boxes [n, 6] by brute force."""
+    lib = _load()
+    b = np.ascontiguousarray(boxes, np.float64).reshape(-1, 6)
+    cap = len(b) * 8 if cap is None else cap
+    while True:
+        out = np.zeros((max(cap, 1), 2), np.uint32)
+        m = lib.orc_aabb_pairs(_ptr(b), len(b), _ptr(out), cap)
+        if m <= cap:
+            return out[:m]
+        cap = m
+
+
+def sweep_pairs(boxes, cap=None):
+    """The overlapping pairs by sort-and-sweep (CPU baseline of the broadphase)."""
+    lib = _load()
+    b = np.ascontiguousarray(boxes, np.float64).reshape(-1, 6)
+    cap = len(b) * 8 if cap is None else cap
+    while True:
+        out = np.zeros((max(cap, 1), 2), np.uint32)
+        m = lib.orc_sweep_pairs(_ptr(b), len(b), _ptr(out), cap)
+        if m <= cap:
+            return out[:m]
+        cap = m
 
 
 def mesh_allpairs(tris_a, tris_b, pose, cap=1 << 20):

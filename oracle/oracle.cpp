@@ -452,6 +452,106 @@ int orc_mesh_shape_collide(const void* nodes, const float* tris, const void* sha
   return 0;
 }
 
+// CollisionObject::computeAABB (narrowphase/collision_object-inl.h:141-154)
+// of object i = shape ids[i] posed by poses[i] (12 floats, world), in FP64:
+// out[6 i ..] = lo, hi.  The local box is computeBV<AABB>(shape, identity)
+// (geometry/shape/utility-inl.h:70-219, 770-776; a hull's from its vertices,
+// convex-inl.h:76-87), its centre and half-diagonal radius as
+// computeLocalAABB stores them (box-inl.h:74-80).
+int orc_object_aabbs(const void* shapes, int n_shapes, const float* verts, const uint32_t* ids, const float* poses,
+                     int n, double* out) {
+  const ShapeRec* sr = (const ShapeRec*)shapes;
+  for (int i = 0; i < n; ++i) {
+    const uint32_t s = ids[i];
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    if (s < (uint32_t)n_shapes) {
+      const ShapeRec& r = sr[s];
+      const double p0 = r.param[0], p1 = r.param[1], p2 = r.param[2];
+      switch (r.type) {
+        case orc::kBox: hi[0] = 0.5 * p0; hi[1] = 0.5 * p1; hi[2] = 0.5 * p2; break;
+        case orc::kSphere: hi[0] = hi[1] = hi[2] = p0; break;
+        case orc::kCapsule: hi[0] = hi[1] = p0; hi[2] = 0.5 * p1 + p0; break;
+        case orc::kCylinder: hi[0] = hi[1] = p0; hi[2] = 0.5 * p1; break;
+        default: {
+          for (int k = 0; k < 3; ++k) { lo[k] = 1e300; hi[k] = -1e300; }
+          for (uint32_t v = 0; v < r.vert_count; ++v)
+            for (int k = 0; k < 3; ++k) {
+              const double x = verts[4 * ((size_t)r.vert_offset + v) + k];
+              lo[k] = std::min(lo[k], x);
+              hi[k] = std::max(hi[k], x);
+            }
+        }
+      }
+      if (r.type != orc::kConvex)
+        for (int k = 0; k < 3; ++k) lo[k] = -hi[k];
+    } else {
+      for (int k = 0; k < 3; ++k) { lo[k] = 1e300; hi[k] = -1e300; }
+      for (int k = 0; k < 3; ++k) { out[6 * i + k] = lo[k]; out[6 * i + 3 + k] = hi[k]; }
+      continue;
+    }
+    const float* P = poses + 12 * (size_t)i;
+    bool identity = true;
+    for (int k = 0; k < 9; ++k) identity = identity && std::abs((double)P[k] - ((k % 4 == 0) ? 1.0 : 0.0)) <= 1e-12;
+    const double t[3] = {P[9], P[10], P[11]};
+    if (identity) {
+      for (int k = 0; k < 3; ++k) { out[6 * i + k] = lo[k] + t[k]; out[6 * i + 3 + k] = hi[k] + t[k]; }
+      continue;
+    }
+    const double c[3] = {0.5 * (lo[0] + hi[0]), 0.5 * (lo[1] + hi[1]), 0.5 * (lo[2] + hi[2])};
+    const double d[3] = {lo[0] - c[0], lo[1] - c[1], lo[2] - c[2]};
+    const double rad = std::sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]);
+    for (int k = 0; k < 3; ++k) {
+      const double cw = (((double)P[3 * k] * c[0] + (double)P[3 * k + 1] * c[1]) + (double)P[3 * k + 2] * c[2]) + t[k];
+      out[6 * i + k] = cw - rad;
+      out[6 * i + 3 + k] = cw + rad;
+    }
+  }
+  return 0;
+}
+
+// Every pair (i < j) of boxes (6 values each, lo then hi) that overlap as
+// AABB::overlap decides (apart only if one starts past the other's end), by
+// brute force; returns the count, writes up to cap pairs.
+int orc_aabb_pairs(const double* box, int n, uint32_t* pairs, int cap) {
+  int m = 0;
+  for (int i = 0; i < n; ++i)
+    for (int j = i + 1; j < n; ++j) {
+      const double* a = box + 6 * (size_t)i;
+      const double* b = box + 6 * (size_t)j;
+      bool apart = false;
+      for (int k = 0; k < 3; ++k) apart = apart || a[k] > b[3 + k] || b[k] > a[3 + k];
+      if (apart) continue;
+      if (m < cap) { pairs[2 * m] = (uint32_t)i; pairs[2 * m + 1] = (uint32_t)j; }
+      ++m;
+    }
+  return m;
+}
+
+// The same pair set by sorting on the lower x bound and sweeping (the CPU
+// baseline of the broadphase; the reference walks a binary AABB tree, also
+// O(n log n + pairs)).
+int orc_sweep_pairs(const double* box, int n, uint32_t* pairs, int cap) {
+  std::vector<int> order((size_t)n);
+  for (int i = 0; i < n; ++i) order[(size_t)i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return box[6 * (size_t)a] < box[6 * (size_t)b]; });
+  int m = 0;
+  for (int k = 0; k < n; ++k) {
+    const double* a = box + 6 * (size_t)order[(size_t)k];
+    for (int q = k + 1; q < n; ++q) {
+      const double* b = box + 6 * (size_t)order[(size_t)q];
+      if (b[0] > a[3]) break;
+      if (a[1] > b[4] || b[1] > a[4] || a[2] > b[5] || b[2] > a[5]) continue;
+      if (m < cap) {
+        const uint32_t i = (uint32_t)order[(size_t)k], j = (uint32_t)order[(size_t)q];
+        pairs[2 * m] = std::min(i, j);
+        pairs[2 * m + 1] = std::max(i, j);
+      }
+      ++m;
+    }
+  }
+  return m;
+}
+
 // Every colliding triangle of one query by brute force over all triangles.
 int orc_mesh_shape_all(const float* tris, int n_tris, const void* shapes, int n_shapes, const float* verts,
                        uint32_t shape_id, const float* pose, int32_t* tri_ids, int cap) {
