@@ -1,5 +1,7 @@
 // GJK pass launcher: picks the lane count's instantiation (gjk_pass_l*.cu),
 // or the refilling one-lane pass defined here.
+#include <algorithm>
+
 #include "gjk_pass.cuh"
 
 namespace fclg {
@@ -9,6 +11,10 @@ FCLG_GJK_INSTANTIATE(2)
 
 // Free lanes of a warp that trigger a refill of them all.
 constexpr int kRefillBatch = 8;
+// CTAs per SM the refilling pass is compiled for (its register budget) and launched with.
+#ifndef FCLG_REFILL_MINB
+#define FCLG_REFILL_MINB 4
+#endif
 
 // One lane per pair, pairs refilled per lane: every lane of a warp steps its
 // own pair's GJK run one support evaluation at a time (GjkRun), and a lane
@@ -18,7 +24,7 @@ constexpr int kRefillBatch = 8;
 // stay busy until its share runs out, instead of each round of 32 pairs
 // waiting for its slowest pair.  For queries without MPR, closed-form pairs
 // or a warm start; the results equal gjk_pass<1>'s (the same GjkRun).
-__global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_refill(BatchArgs b, QueryParams prm, EpaQueue q,
+__global__ void __launch_bounds__(128, FCLG_REFILL_MINB) gjk_refill(BatchArgs b, QueryParams prm, EpaQueue q,
                                                                const uint32_t* __restrict__ order,
                                                                const uint32_t* __restrict__ range) {
   uint32_t begin = 0, end = b.n_pairs;
@@ -86,7 +92,13 @@ cudaError_t launch_gjk(const BatchArgs& b, const QueryParams& prm, const EpaQueu
     blocks = (int)((total + threads - 1) / threads);
   }
   if (refill && lanes == 1 && !prm.use_mpr && !prm.analytic && !b.guess) {
-    gjk_refill<<<blocks, threads, 0, st>>>(b, prm, q, order, range);
+    // a persistent grid: FCLG_REFILL_MINB CTAs on every SM
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess)
+      return cudaGetLastError();
+    const int grid = std::min<int>(blocks, sms * FCLG_REFILL_MINB);
+    gjk_refill<<<grid > 0 ? grid : 1, threads, 0, st>>>(b, prm, q, order, range);
     return cudaGetLastError();
   }
   switch (lanes) {

@@ -30,6 +30,10 @@ namespace {
 
 constexpr int kMsStack = 1024;
 constexpr int kMsWarps = 4;
+// CTAs per SM the kernel is compiled for (its register budget)
+#ifndef FCLG_MESH_SHAPE_MINB
+#define FCLG_MESH_SHAPE_MINB 4
+#endif
 constexpr int kMsMaxRounds = 1 << 22;  // bound against a corrupted tree
 
 struct MsSmem {
@@ -233,7 +237,7 @@ __device__ void shape_box(const ShapeDev& s, const float4* __restrict__ verts, u
 
 }  // namespace
 
-__global__ void __launch_bounds__(kMsWarps * 32) mesh_shape_kernel(MeshShapeArgs m) {
+__global__ void __launch_bounds__(kMsWarps * 32, FCLG_MESH_SHAPE_MINB) mesh_shape_kernel(MeshShapeArgs m) {
   __shared__ MsSmem smem_all[kMsWarps];
   MsSmem& S = smem_all[threadIdx.x >> 5];
   const unsigned lane = threadIdx.x & 31u;
