@@ -72,6 +72,9 @@ def parse():
     ap.add_argument("--poses", type=int, default=65536)
     ap.add_argument("--configs", type=int, default=100_000, help="arm: joint configurations (7 x 32 pairs each)")
     ap.add_argument("--objects", type=int, default=100_000, help="scene: posed objects")
+    ap.add_argument("--tuning", default=None,
+                    help="convex workloads: a fixed launch shape as JSON (fclg_tuning fields, e.g. "
+                         "'{\"gjk_refill\": 0, \"gjk_lanes_large\": 1}') instead of the autotuner's choice")
     ap.add_argument("--sweep", action="store_true",
                     help="convex workloads: time one query per launch layout (GJK lanes, hull split, support "
                          "walk on / off) and print them as one JSON object instead of the bench line")
@@ -750,8 +753,13 @@ def main():
     if args.sweep:
         return launch_sweep(args, torch, ctx, step, stream, n, t_set)
 
-    # launch shape chosen by the library's autotuner on this batch (untimed)
-    tuning, tune_ms = ctx.autotune(d_pairs.data_ptr(), n, d_res.data_ptr())
+    # launch shape chosen by the library's autotuner on this batch (untimed), or given
+    if args.tuning:
+        fixed = {k: (int(v) if not isinstance(v, bool) else v) for k, v in json.loads(args.tuning).items()}
+        ctx.set_tuning(**fixed)
+        tuning, tune_ms = ctx.get_tuning(), 0.0
+    else:
+        tuning, tune_ms = ctx.autotune(d_pairs.data_ptr(), n, d_res.data_ptr())
 
     def barrier():
         torch.cuda.synchronize(dev)
