@@ -151,6 +151,13 @@ int fclg_broadphase(fclg_context* ctx, const uint32_t* shape_ids, const float* p
 int fclg_broadphase_device(fclg_context* ctx, const uint32_t* d_shape_ids, const float* d_poses, uint32_t n,
                            uint32_t* d_pairs, uint32_t cap, uint32_t* d_n_pairs, float* d_aabb_lo, float* d_aabb_hi,
                            void* stream);
+/* Two object sets (BinaryAABB_Tree::TreeCollision; a one-object set is
+   SingleObjectCollision): every pair (i of the first set, j of the second)
+   whose world AABBs overlap, as fclg_broadphase defines them; pairs hold
+   (i, j) with i and j indices into their own sets.  Device pointers. */
+int fclg_broadphase_cross_device(fclg_context* ctx, const uint32_t* d_shape_ids_a, const float* d_poses_a,
+                                 uint32_t n_a, const uint32_t* d_shape_ids_b, const float* d_poses_b, uint32_t n_b,
+                                 uint32_t* d_pairs, uint32_t cap, uint32_t* d_n_pairs, void* stream);
 /* Narrowphase records (fclg_pair) for m candidate object pairs (2 x u32 each):
    shape_a = shape_ids[i], shape_b = shape_ids[j], the pose of j in i's frame
    (X_i^-1 X_j), flags and pair_class 0; feeds fclg_distance_device /

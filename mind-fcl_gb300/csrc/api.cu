@@ -41,6 +41,8 @@ struct fclg_context {
   size_t bp_bytes = 0;
   void* bp_io = nullptr;
   size_t bp_io_bytes = 0;
+  void* bp_join = nullptr;  // the two sets of a cross query, side by side
+  size_t bp_join_bytes = 0;
   bool gjk_refill = false;
   // scratch handed from the GJK pass to the EPA pass
   uint32_t* epa_count = nullptr;  // [2]: work list, overflow list
@@ -447,6 +449,7 @@ void fclg_destroy(fclg_context* c) {
   if (c->guess) cudaFree(c->guess);
   if (c->bp_scratch) cudaFree(c->bp_scratch);
   if (c->bp_io) cudaFree(c->bp_io);
+  if (c->bp_join) cudaFree(c->bp_join);
   if (c->stream) cudaStreamDestroy(c->stream);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -818,9 +821,66 @@ int fclg_broadphase_device(fclg_context* c, const uint32_t* d_shape_ids, const f
   a.count = d_n_pairs;
   a.aabb_lo = reinterpret_cast<float4*>(d_aabb_lo);
   a.aabb_hi = reinterpret_cast<float4*>(d_aabb_hi);
+  a.split = 0;
   clear_pending_error();
   FCLG_CUDA(c, fclg::launch_broadphase(a, c->bp_scratch, static_cast<cudaStream_t>(stream)));
   c->launches += n ? (uint64_t)fclg::broadphase_launches() : 0;
+  return FCLG_OK;
+}
+
+int fclg_broadphase_cross_device(fclg_context* c, const uint32_t* d_ids_a, const float* d_poses_a, uint32_t n_a,
+                                 const uint32_t* d_ids_b, const float* d_poses_b, uint32_t n_b, uint32_t* d_pairs,
+                                 uint32_t cap, uint32_t* d_n_pairs, void* stream) {
+  if (!c) return FCLG_E_INVALID;
+  if (!d_n_pairs || (n_a && (!d_ids_a || !d_poses_a)) || (n_b && (!d_ids_b || !d_poses_b)) || (cap && !d_pairs))
+    return fail(c, FCLG_E_INVALID, "null pointer");
+  if (!c->shapes) return fail(c, FCLG_E_NO_SHAPES, "no shapes set");
+  FCLG_CUDA(c, cudaSetDevice(c->device));
+  const cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const uint32_t n = n_a + n_b;
+  if (n_a == 0 || n_b == 0) {
+    FCLG_CUDA(c, cudaMemsetAsync(d_n_pairs, 0, 4, st));
+    return FCLG_OK;
+  }
+  const size_t b_ids = ((size_t)n * 4 + 255) & ~(size_t)255;
+  const size_t need = b_ids + (size_t)n * 48;
+  if (need > c->bp_join_bytes) {
+    if (c->bp_join) cudaFree(c->bp_join);
+    c->bp_join = nullptr;
+    c->bp_join_bytes = 0;
+    FCLG_CUDA(c, cudaMalloc(&c->bp_join, need));
+    c->bp_join_bytes = need;
+  }
+  uint32_t* ids = static_cast<uint32_t*>(c->bp_join);
+  float* poses = reinterpret_cast<float*>(static_cast<char*>(c->bp_join) + b_ids);
+  FCLG_CUDA(c, cudaMemcpyAsync(ids, d_ids_a, (size_t)n_a * 4, cudaMemcpyDeviceToDevice, st));
+  FCLG_CUDA(c, cudaMemcpyAsync(ids + n_a, d_ids_b, (size_t)n_b * 4, cudaMemcpyDeviceToDevice, st));
+  FCLG_CUDA(c, cudaMemcpyAsync(poses, d_poses_a, (size_t)n_a * 48, cudaMemcpyDeviceToDevice, st));
+  FCLG_CUDA(c, cudaMemcpyAsync(poses + 12 * (size_t)n_a, d_poses_b, (size_t)n_b * 48, cudaMemcpyDeviceToDevice, st));
+  const size_t scratch = fclg::broadphase_scratch_bytes(n, c->n_shapes);
+  if (scratch > c->bp_bytes) {
+    if (c->bp_scratch) cudaFree(c->bp_scratch);
+    c->bp_scratch = nullptr;
+    c->bp_bytes = 0;
+    FCLG_CUDA(c, cudaMalloc(&c->bp_scratch, scratch));
+    c->bp_bytes = scratch;
+  }
+  fclg::BroadphaseArgs a;
+  a.shapes = c->shapes;
+  a.verts = c->verts;
+  a.n_shapes = c->n_shapes;
+  a.shape_ids = ids;
+  a.poses = reinterpret_cast<const float4*>(poses);
+  a.n = n;
+  a.pairs = d_pairs;
+  a.cap = cap;
+  a.count = d_n_pairs;
+  a.aabb_lo = nullptr;
+  a.aabb_hi = nullptr;
+  a.split = n_a;
+  clear_pending_error();
+  FCLG_CUDA(c, fclg::launch_broadphase(a, c->bp_scratch, st));
+  c->launches += (uint64_t)fclg::broadphase_launches();
   return FCLG_OK;
 }
 

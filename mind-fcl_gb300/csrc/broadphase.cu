@@ -168,8 +168,8 @@ __global__ void radix_scatter_kernel(const uint32_t* __restrict__ key, const uin
 
 // The sweep: sorted box k against the boxes after it while they can overlap in x.
 __global__ void sweep_kernel(const uint32_t* __restrict__ order, const float4* __restrict__ lo,
-                             const float4* __restrict__ hi, uint32_t n, uint32_t* __restrict__ pairs, uint32_t cap,
-                             uint32_t* __restrict__ count) {
+                             const float4* __restrict__ hi, uint32_t n, uint32_t split, uint32_t* __restrict__ pairs,
+                             uint32_t cap, uint32_t* __restrict__ count) {
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const uint32_t i = order[k];
     const float4 la = __ldg(lo + i), ha = __ldg(hi + i);
@@ -180,10 +180,12 @@ __global__ void sweep_kernel(const uint32_t* __restrict__ order, const float4* _
       const float4 hb = __ldg(hi + j);
       // AABB::overlap (math/bv/AABB-inl.h): apart only if one box starts past the other's end
       if (la.y > hb.y || lb.y > ha.y || la.z > hb.z || lb.z > ha.z || la.x > hb.x) continue;
+      if (split && ((i < split) == (j < split))) continue;  // two sets: only pairs across them
       const uint32_t slot = atomicAdd(count, 1u);
       if (slot < cap) {
-        pairs[2 * (size_t)slot] = min(i, j);
-        pairs[2 * (size_t)slot + 1] = max(i, j);
+        const uint32_t lo_i = min(i, j), hi_i = max(i, j);
+        pairs[2 * (size_t)slot] = lo_i;
+        pairs[2 * (size_t)slot + 1] = split ? hi_i - split : hi_i;
       }
     }
   }
@@ -258,7 +260,7 @@ cudaError_t launch_broadphase(const BroadphaseArgs& a, void* scratch, cudaStream
     uint32_t* t = k0; k0 = k1; k1 = t;
     t = v0; v0 = v1; v1 = t;
   }
-  sweep_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(v0, lo, hi, n, a.pairs, a.cap, a.count);
+  sweep_kernel<<<(n + tb - 1) / tb, tb, 0, st>>>(v0, lo, hi, n, a.split, a.pairs, a.cap, a.count);
   return cudaGetLastError();
 }
 

@@ -18,6 +18,8 @@ struct BroadphaseArgs {
   uint32_t* count;            // [1] number of overlapping pairs (may exceed cap)
   float4* aabb_lo;            // optional [n]: the world AABBs
   float4* aabb_hi;
+  uint32_t split;             // 0: every pair; else objects [0, split) and [split, n) are two sets and only
+                              // pairs across them count, written as (index in the first, index in the second)
 };
 
 // Device scratch the launch needs (byte size; any 256-byte aligned buffer).

@@ -36,7 +36,7 @@ EXPORTS = [
     "fclg_autotune", "fclg_graph_create", "fclg_graph_launch", "fclg_graph_destroy",
     "fclg_collide_directed", "fclg_collide_directed_device", "fclg_hull_graph",
     "fclg_mesh_shape_collide", "fclg_mesh_shape_collide_device",
-    "fclg_broadphase", "fclg_broadphase_device", "fclg_object_pairs_device",
+    "fclg_broadphase", "fclg_broadphase_device", "fclg_object_pairs_device", "fclg_broadphase_cross_device",
 ]
 
 STATIC_MAX_PAIRS = 16384  # FCLG_STATIC_MAX_PAIRS
@@ -168,6 +168,8 @@ def load_library(path=LIB_PATH):
     lib.fclg_broadphase_device.restype = i32
     lib.fclg_object_pairs_device.argtypes = [vp, vp, vp, vp, u32, vp, vp]
     lib.fclg_object_pairs_device.restype = i32
+    lib.fclg_broadphase_cross_device.argtypes = [vp, vp, vp, u32, vp, vp, u32, vp, u32, vp, vp]
+    lib.fclg_broadphase_cross_device.restype = i32
     _lib = lib
     return lib
 

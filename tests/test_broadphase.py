@@ -137,3 +137,40 @@ def test_gpu_broadphase_feeds_the_narrowphase(oracle_lib):
         check_parity(got, oracle_lib.signed_distance(q), q)
     finally:
         ctx.close()
+
+
+@pytest.mark.gpu
+def test_gpu_broadphase_two_sets(oracle_lib):
+    """TreeCollision / SingleObjectCollision: the pairs across two object sets
+    equal the cross pairs of the joint self query."""
+    import ctypes
+    import torch
+    from fclg.api import Context, broadphase
+    b, ids, poses = workloads.scene(8000, seed=workloads.SEED_BASE + 73)
+    na = 3000
+    ctx = Context(0)
+    try:
+        ctx.set_batch(b)
+        joint, _ = broadphase(ctx, ids, poses)
+        want = {(int(i), int(j) - na) for i, j in joint.tolist() if i < na <= j}
+        vp = ctypes.c_void_p
+        dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+        da, pa, db, pb = dev(ids[:na].view(np.int32)), dev(poses[:na]), dev(ids[na:].view(np.int32)), dev(poses[na:])
+        cap = 1 << 16
+        out = torch.zeros(2 * cap, dtype=torch.int32, device="cuda")
+        cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+        assert ctx.lib.fclg_broadphase_cross_device(ctx.h, vp(da.data_ptr()), vp(pa.data_ptr()), na,
+                                                    vp(db.data_ptr()), vp(pb.data_ptr()), len(ids) - na,
+                                                    vp(out.data_ptr()), cap, vp(cnt.data_ptr()), None) == 0
+        m = int(cnt.item())
+        got = {tuple(p) for p in out[:2 * m].cpu().numpy().reshape(-1, 2).tolist()}
+        assert m == len(got) == len(want) and got == want and m > 100
+        # a single object against the set
+        assert ctx.lib.fclg_broadphase_cross_device(ctx.h, vp(da.data_ptr()), vp(pa.data_ptr()), 1,
+                                                    vp(db.data_ptr()), vp(pb.data_ptr()), len(ids) - na,
+                                                    vp(out.data_ptr()), cap, vp(cnt.data_ptr()), None) == 0
+        m1 = int(cnt.item())
+        one = {tuple(p) for p in out[:2 * m1].cpu().numpy().reshape(-1, 2).tolist()}
+        assert one == {p for p in want if p[0] == 0}
+    finally:
+        ctx.close()
