@@ -294,8 +294,8 @@ int fclg_collide_directed_device(fclg_context* ctx, const fclg_pair* d_pairs, ui
    fields keep the current value.  Defaults: bucketing on, 1 and 4 lanes,
    128 vertices, 4 GJK and 6 EPA CTAs per SM (the EPA pass's first,
    128-face layout), support walk off, GJK refill off.
-   gjk_refill: one-lane GJK launches of distance queries (and of collides
-   without MPR or closed-form pairs) keep every lane of a warp busy by handing
+   gjk_refill: one-lane GJK launches of distance queries, warm-started or not
+   (and of collides without MPR or closed-form pairs) keep every lane of a warp busy by handing
    a lane whose pair has finished the next pair of its warp's share, instead
    of letting 32 pairs wait for the slowest of them; answers are the same.
    On GB300 it pays where supports are costly (hulls of 64-256 vertices:

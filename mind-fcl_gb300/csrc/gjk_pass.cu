@@ -22,8 +22,9 @@ constexpr int kRefillBatch = 8;
 // (warp w takes items 32 (w + k W) .. 32 (w + k W) + 31, k = 0, 1, ...,
 // W warps in the grid, in the order its lanes come free).  A warp's lanes so
 // stay busy until its share runs out, instead of each round of 32 pairs
-// waiting for its slowest pair.  For queries without MPR, closed-form pairs
-// or a warm start; the results equal gjk_pass<1>'s (the same GjkRun).
+// waiting for its slowest pair -- which is also what lets a learned warm
+// start's shorter runs shorten the pass.  For queries without MPR or
+// closed-form pairs; the results equal gjk_pass<1>'s (the same decisions).
 __global__ void __launch_bounds__(128, FCLG_REFILL_MINB) gjk_refill(BatchArgs b, QueryParams prm, EpaQueue q,
                                                                const uint32_t* __restrict__ order,
                                                                const uint32_t* __restrict__ range) {
@@ -45,6 +46,8 @@ __global__ void __launch_bounds__(128, FCLG_REFILL_MINB) gjk_refill(BatchArgs b,
   GjkRun run;
   uint32_t pid = 0;
   bool live = false;
+  bool warm = false;   // the lane's run started from the learned direction
+  int warm_iters = 0;  // iterations of a warm run that is being redone from the plain direction
   uint32_t next = 0;  // warp-uniform: next unassigned position in the warp's share
   for (;;) {
     unsigned want = __ballot_sync(0xFFFFFFFFu, !live);
@@ -63,7 +66,15 @@ __global__ void __launch_bounds__(128, FCLG_REFILL_MINB) gjk_refill(BatchArgs b,
           sup.A = load_shape(b.shapes, b.walk, pr.a);
           sup.B = load_shape(b.shapes, b.walk, pr.b);
           sup.pose = pr.pose;
-          run.begin(-plain);
+          warm = b.guess != nullptr;
+          warm_iters = 0;
+          if (warm) {
+            const f3 guess = mk3(__ldg(b.guess + 3 * (size_t)pid), __ldg(b.guess + 3 * (size_t)pid + 1),
+                                 __ldg(b.guess + 3 * (size_t)pid + 2));
+            run.begin(-guess);
+          } else {
+            run.begin(-plain);
+          }
           live = true;
         }
       }
@@ -76,8 +87,23 @@ __global__ void __launch_bounds__(128, FCLG_REFILL_MINB) gjk_refill(BatchArgs b,
       continue;
     }
     if (live && run.step(sup, prm.gjk_tol, prm.gjk_max_iter, prm.want_distance != 0)) {
-      finish_pair(b, prm, q, pid, run.o, run.s);
-      live = false;
+      const GjkOut& o = run.o;
+      // a warm run stands for a separation certificate (with its points when
+      // distances are wanted) or for an overlap that needs no EPA; otherwise
+      // the pair is redone from the plain direction, both runs counted (as
+      // gjk_pass does)
+      const bool keep = (o.status == kGjkSeparated && (o.point_valid || !prm.want_distance)) ||
+                        (o.status == kGjkIntersect && !prm.want_epa);
+      if (warm && !keep) {
+        warm = false;
+        warm_iters = o.iterations;
+        run.begin(-plain);
+      } else {
+        GjkOut out = o;
+        out.iterations += warm_iters;
+        finish_pair(b, prm, q, pid, out, run.s);
+        live = false;
+      }
     }
   }
 }
@@ -91,7 +117,7 @@ cudaError_t launch_gjk(const BatchArgs& b, const QueryParams& prm, const EpaQueu
     const uint64_t total = (uint64_t)b.n_pairs * (uint64_t)lanes;
     blocks = (int)((total + threads - 1) / threads);
   }
-  if (refill && lanes == 1 && !prm.use_mpr && !prm.analytic && !b.guess) {
+  if (refill && lanes == 1 && !prm.use_mpr && !prm.analytic) {
     // a persistent grid: FCLG_REFILL_MINB CTAs on every SM
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=

@@ -46,8 +46,8 @@ cudaError_t launch_bucketing(const BatchArgs& b, const BucketScratch& s, uint32_
 // GJK pass over order[range[0] .. range[1]) (order / range may be null: all
 // pairs in index order) with `lanes` lanes per pair, as a persistent grid of
 // `blocks` CTAs (0: one CTA per 128 lanes of work, not persistent).  refill:
-// one-lane launches of queries without MPR, closed-form pairs or a warm start
-// run gjk_refill (lanes take new pairs as theirs finish) instead of gjk_pass<1>.
+// one-lane launches of queries without MPR or closed-form pairs run
+// gjk_refill (lanes take new pairs as theirs finish) instead of gjk_pass<1>.
 cudaError_t launch_gjk(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q, int lanes,
                        const uint32_t* order, const uint32_t* range, int blocks, cudaStream_t st,
                        bool refill = false);
