@@ -233,12 +233,12 @@ int ensure_epa(fclg_context* c, size_t n) {
   c->epa_ovf = nullptr;
   c->epa_rec = nullptr;
   c->epa_cap = 0;
+  c->scratch_epoch += 1;  // captured graphs hold the freed buffers, also if the allocation below fails
   const size_t cap = std::max<size_t>(n, 1024);
   FCLG_CUDA(c, cudaMalloc(&c->epa_list, cap * sizeof(uint32_t)));
   FCLG_CUDA(c, cudaMalloc(&c->epa_ovf, cap * sizeof(uint32_t)));
   FCLG_CUDA(c, cudaMalloc(&c->epa_rec, cap * fclg::kEpaRecordBytes));
   c->epa_cap = cap;
-  c->scratch_epoch += 1;
   return FCLG_OK;
 }
 
@@ -253,11 +253,11 @@ int ensure_bucket(fclg_context* c, size_t n) {
   c->bk_keys = nullptr;
   c->bk_order = nullptr;
   c->bk_cap = 0;
+  c->scratch_epoch += 1;
   const size_t cap = std::max<size_t>(n, 1024);
   FCLG_CUDA(c, cudaMalloc(&c->bk_keys, cap));
   FCLG_CUDA(c, cudaMalloc(&c->bk_order, cap * sizeof(uint32_t)));
   c->bk_cap = cap;
-  c->scratch_epoch += 1;
   return FCLG_OK;
 }
 
@@ -279,10 +279,10 @@ int ensure_guess(fclg_context* c, size_t n) {
   if (c->guess) cudaFree(c->guess);
   c->guess = nullptr;
   c->guess_cap = 0;
+  c->scratch_epoch += 1;
   const size_t cap = std::max<size_t>(n, 1024);
   FCLG_CUDA(c, cudaMalloc(&c->guess, cap * 3 * sizeof(float)));
   c->guess_cap = cap;
-  c->scratch_epoch += 1;
   return FCLG_OK;
 }
 
