@@ -279,7 +279,12 @@ int fclg_set_warmstart(fclg_context* ctx, fclg_warmstart* model);
    (both valid penetrations for the reference); normal = the direction it
    settled on (the hint when not ok); status bit 19 (FCLG_STATUS_INCREMENTAL)
    with the incremental status + 1 in bits 8-15 (0 OK, 1 Failed,
-   2 FailedNoIntersect, 4 iteration limit). */
+   2 FailedNoIntersect, 4 iteration limit).
+   With FCLG_REQ_INCREMENTAL | FCLG_REQ_WARM_START the hints are the unit
+   directions of the context's warm-start model (fclg_set_warmstart; dirs may
+   be NULL), so for this use it is trained on penetrating pairs' result
+   normals (shape b's escape direction).  FCLG_REQ_WARM_START without
+   FCLG_REQ_INCREMENTAL, or without a model, is FCLG_E_INVALID. */
 #define FCLG_STATUS_DIRECTED (1 << 18)
 #define FCLG_STATUS_INCREMENTAL (1 << 19)
 int fclg_collide_directed(fclg_context* ctx, const fclg_pair* pairs, uint32_t n_pairs, const float* dirs,

@@ -1078,12 +1078,23 @@ int run_directed(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fl
                  fclg_result* d_results, cudaStream_t st) {
   if (!c) return FCLG_E_INVALID;
   if (n == 0) return FCLG_OK;
-  if (!d_pairs || !d_dirs || !d_results) return fail(c, FCLG_E_INVALID, "null pair, direction or result pointer");
+  const bool learned = req && (req->flags & FCLG_REQ_WARM_START);
+  if (!d_pairs || (!d_dirs && !learned) || !d_results)
+    return fail(c, FCLG_E_INVALID, "null pair, direction or result pointer");
   if (!c->shapes) return fail(c, FCLG_E_NO_SHAPES, "no shapes set");
-  if (req && (req->flags & FCLG_REQ_WARM_START))
-    return fail(c, FCLG_E_INVALID, "directed penetration takes no warm start");
+  if (learned && !(req->flags & FCLG_REQ_INCREMENTAL))
+    return fail(c, FCLG_E_INVALID, "a learned direction seeds the incremental mode only (FCLG_REQ_INCREMENTAL)");
+  if (learned && !c->ws) return fail(c, FCLG_E_INVALID, "FCLG_REQ_WARM_START without a model (fclg_set_warmstart)");
   FCLG_CUDA(c, cudaSetDevice(c->device));
   clear_pending_error();
+  if (learned) {
+    // the model's directions are the hints: the incremental mode seeded by the learned direction
+    const int rc = ensure_guess(c, n);
+    if (rc) return rc;
+    FCLG_CUDA(c, fclg::warmstart_predict(c->ws, reinterpret_cast<const float4*>(d_pairs), n, c->guess, st));
+    c->launches += 1;
+    d_dirs = c->guess;
+  }
   fclg::QueryParams prm = make_params(req, false);
   prm.want_epa = 0;
   prm.use_mpr = 0;
@@ -1113,13 +1124,15 @@ extern "C" int fclg_collide_directed(fclg_context* c, const fclg_pair* pairs, ui
                                      const fclg_request* req, fclg_result* results) {
   if (!c) return FCLG_E_INVALID;
   if (n == 0) return FCLG_OK;
-  if (!pairs || !dirs || !results) return fail(c, FCLG_E_INVALID, "null pair, direction or result pointer");
+  const bool learned = req && (req->flags & FCLG_REQ_WARM_START);
+  if (!pairs || (!dirs && !learned) || !results) return fail(c, FCLG_E_INVALID, "null pair, direction or result pointer");
   int rc = ensure_io(c, n);
   if (!rc) rc = ensure_guess(c, n);
   if (rc) return rc;
   FCLG_CUDA(c, cudaMemcpyAsync(c->io_pairs, pairs, (size_t)n * sizeof(fclg_pair), cudaMemcpyHostToDevice, c->stream));
-  FCLG_CUDA(c, cudaMemcpyAsync(c->guess, dirs, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-  rc = run_directed(c, static_cast<const fclg_pair*>(c->io_pairs), n, c->guess, req,
+  if (!learned)
+    FCLG_CUDA(c, cudaMemcpyAsync(c->guess, dirs, (size_t)n * 3 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  rc = run_directed(c, static_cast<const fclg_pair*>(c->io_pairs), n, learned ? nullptr : c->guess, req,
                     static_cast<fclg_result*>(c->io_results), c->stream);
   if (rc) return rc;
   FCLG_CUDA(c, cudaMemcpyAsync(results, c->io_results, (size_t)n * sizeof(fclg_result), cudaMemcpyDeviceToHost,

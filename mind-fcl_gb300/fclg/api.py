@@ -304,14 +304,18 @@ class Context:
     def collide_directed(self, pairs, dirs, request=None):
         """fcl::collide, directed penetration mode, host arrays: dirs float[n][3] (unit,
         shape b's escape direction in shape a's frame); with FCLG_REQ_INCREMENTAL in the
-        request's flags the incremental minimum-distance mode from dirs as hints."""
+        request's flags the incremental minimum-distance mode from dirs as hints, and with
+        FCLG_REQ_INCREMENTAL | FCLG_REQ_WARM_START from the context's model's directions
+        (dirs None)."""
         p = np.ascontiguousarray(pairs, PAIR_DTYPE)
-        d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
-        assert len(d) == len(p)
+        d = None
+        if dirs is not None:
+            d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+            assert len(d) == len(p)
         out = np.zeros(len(p), RESULT_DTYPE)
         req = ctypes.byref(request) if request is not None else None
-        self._check(self.lib.fclg_collide_directed(self.h, _ptr(p), len(p), _ptr(d), req, _ptr(out)),
-                    "fclg_collide_directed")
+        self._check(self.lib.fclg_collide_directed(self.h, _ptr(p), len(p), _ptr(d) if d is not None else None,
+                                                   req, _ptr(out)), "fclg_collide_directed")
         return out
 
     def autotune(self, d_pairs, n, d_results, request=None, distance=True):

@@ -179,3 +179,71 @@ def test_trained_model_cuts_iterations_and_keeps_answers(torch):
         ws.close()
     finally:
         ctx.close()
+
+
+def test_learned_hints_seed_incremental_penetration(torch):
+    """Incremental minimum-distance penetration seeded by the learned direction
+    (FCLG_REQ_INCREMENTAL | FCLG_REQ_WARM_START): a model trained on the
+    escape normals of penetrating arm pairs predicts the hints on the device.
+    The answers are the reference algorithm's from those hints (flags exact
+    outside the 1e-6 m band; depth within 1e-5 m of the FP64 oracle's for
+    >= 99 % of pairs valid on both sides), and the learned hints land at
+    EPA's minimum depth more often than random unit hints do."""
+    import oracle
+    from fclg.api import (FCLG_REQ_INCREMENTAL, FCLG_STATUS_INCREMENTAL, Context, FclgError, WarmStart,
+                          make_request)
+    WARM = 4  # FCLG_REQ_WARM_START
+    ctx = Context(0)
+    try:
+        train = workloads.arm(3000, seed=workloads.SEED_BASE + 311)  # 672,000 pairs
+        ctx.set_batch(train)
+        res = _query(torch, ctx, _dev(torch, train.pairs), train.n_pairs, 0)
+        nrm = res["normal"].astype(np.float64)
+        ln = np.linalg.norm(nrm, axis=1)
+        keep = np.nonzero((res["ok"] == 1) & (res["distance"] < 0) & (np.abs(ln - 1) < 1e-3))[0]
+        assert len(keep) > 5000
+        d_tr = _dev(torch, train.pairs[keep])
+        d_lab = torch.from_numpy((nrm[keep] / ln[keep, None]).astype(np.float32)).cuda()
+        ws = WarmStart(workloads.ARM_CLASSES, seed=2)
+        losses = ws.train(d_tr.data_ptr(), d_lab.data_ptr(), len(keep), epochs=40, batch=1024, lr=2e-3)
+        assert losses[-1] < 0.5 * losses[0], losses
+
+        test = workloads.arm(400, seed=workloads.SEED_BASE + 312)
+        ctx.set_batch(test)
+        inc = make_request(flags=FCLG_REQ_INCREMENTAL | WARM)
+        with pytest.raises(FclgError):
+            ctx.collide_directed(test.pairs, None, inc)  # no model set
+        ctx.set_warmstart(ws)
+        with pytest.raises(FclgError):
+            ctx.collide_directed(test.pairs, None, make_request(flags=WARM))  # not incremental
+        got = ctx.collide_directed(test.pairs, None, inc)
+        d_te = _dev(torch, test.pairs)
+        d_g = torch.zeros(test.n_pairs * 3, dtype=torch.float32, device="cuda")
+        ws.predict(d_te.data_ptr(), test.n_pairs, d_g.data_ptr())
+        torch.cuda.synchronize()
+        hints = d_g.cpu().numpy().reshape(-1, 3)
+        ref = oracle.collide_incremental(test, hints)
+        sd = oracle.signed_distance(test)
+        assert np.all((got["status"] & FCLG_STATUS_INCREMENTAL) != 0)
+        outside = np.abs(sd["distance"]) > 1e-6
+        assert np.sum((got["collide"] != ref["ok"]) & outside) == 0
+        valid = lambda r: np.isin(r, (0, 4))
+        gst = ((got["status"] >> 8) & 0xFF).astype(np.int64) - 1
+        hit = (got["collide"] == 1) & (ref["ok"] == 1)
+        both = hit & valid(gst) & valid(ref["epa_status"])
+        assert both.sum() >= 0.97 * hit.sum() and hit.sum() > 500
+        err = np.abs(got["distance"][both].astype(np.float64) - ref["distance"][both])
+        assert np.mean(err <= 1e-5) >= 0.99
+
+        # learned against random hints: how often the run ends at EPA's depth
+        ov = both & (sd["epa_status"] == 1) & (sd["distance"] < 0)
+        at_min = lambda r: np.mean(np.abs(-r["distance"][ov].astype(np.float64) + sd["distance"][ov]) <= 1e-4)
+        rng = np.random.default_rng(13)
+        u = rng.normal(size=(test.n_pairs, 3))
+        u = (u / np.linalg.norm(u, axis=1, keepdims=True)).astype(np.float32)
+        rnd = ctx.collide_directed(test.pairs, u, make_request(flags=FCLG_REQ_INCREMENTAL))
+        assert at_min(got) > at_min(rnd), (at_min(got), at_min(rnd))
+        ctx.set_warmstart(None)
+        ws.close()
+    finally:
+        ctx.close()
