@@ -62,12 +62,13 @@ def parse():
     ap.add_argument("--impl", default="fclg", choices=["fclg", "reference"])
     ap.add_argument("--pairs", type=int, default=N_PAIRS)
     ap.add_argument("--workload", default="mixed",
-                    choices=["mixed", "mesh", "mesh_shape", "scene", "pareto", "plain_small", "arm", "warmstart"],
+                    choices=["mixed", "mesh", "mesh_shape", "scene", "ccd", "pareto", "plain_small", "arm", "warmstart"],
                     help="mixed: the headline convex-pair batch (with the warm-start comparison); mesh: the "
                          "50k x 50k-triangle BVH workload; pareto: 4M heavy-tailed hull pairs; plain_small: 4096 "
                          "hull pairs; arm: 7-link arm x 32 obstacles, 100k configurations; mesh_shape: the "
                          "50k-triangle mesh against 65,536 mixed-shape queries; warmstart: the "
-                         "warm-start inference kernel alone on 2.24M arm pairs")
+                         "warm-start inference kernel alone on 2.24M arm pairs; ccd: translational continuous "
+                         "collision of 1M mixed pairs")
     ap.add_argument("--no-warm", action="store_true", help="skip the warm-start comparison")
     ap.add_argument("--poses", type=int, default=65536)
     ap.add_argument("--configs", type=int, default=100_000, help="arm: joint configurations (7 x 32 pairs each)")
@@ -519,6 +520,96 @@ def run_mesh_shape(args):
     return 0
 
 
+CCD_WORKLOAD = ("translational CCD: 1M pairs of the mixed workload's kinds and sizes (sphere / box / capsule / "
+                "cylinder / hull of log-uniform[8, 256] points), start separations up to 3x the bounding-sphere "
+                "sum, shape a moving along a uniform unit axis by up to 2x that sum; one time-of-collision sample "
+                "per hit (kOneTocSample)")
+# compulsory bytes per CCD query: the mixed workload's hull / parameter / pose
+# bytes, the 16 B displacement and a 16 B result record
+CCD_ALGO_BYTES = 466.0
+
+
+def run_ccd(args):
+    """Translational CCD pair queries/s (fcl::translational_ccd, its own JSON line)."""
+    import torch
+    from fclg import workloads
+    from fclg.api import Context, FCLG_TOC_SAMPLE
+    rank, world, local = dist_env()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    b, disp = workloads.ccd(args.pairs, seed=workloads.SEED_BASE + 9 + 1000 * rank)
+    n = b.n_pairs
+    ctx = Context(local)
+    ctx.set_batch(b)
+    stream = torch.cuda.current_stream(dev)
+    d_pairs = torch.from_numpy(b.pairs.view(np.uint8).copy()).to(dev)
+    d_disp = torch.from_numpy(disp).to(dev)
+    d_res = torch.empty(n * 16, dtype=torch.uint8, device=dev)
+
+    def step():
+        ctx.translational_ccd_device(d_pairs.data_ptr(), n, d_disp.data_ptr(), d_res.data_ptr(),
+                                     toc_type=FCLG_TOC_SAMPLE, stream=stream.cuda_stream)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = ctx.launch_count
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+    launches = ctx.launch_count - launches0
+    if world > 1:
+        torch.distributed.barrier()
+    ms = max_over_ranks(torch, e0.elapsed_time(e1) / args.steps, dev, world)
+    res = d_res.cpu().numpy().view(np.uint32).reshape(n, 4)
+    hit = float(np.mean(res[:, 0] == 1))
+    # end to end: host arrays through fclg_translational_ccd (copies inside)
+    t0 = time.perf_counter()
+    e2e_steps = max(1, args.steps // 2)
+    for _ in range(e2e_steps):
+        ctx.translational_ccd(b.pairs, disp, toc_type=FCLG_TOC_SAMPLE)
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+    hbm, src = peaks()
+    achieved = n * CCD_ALGO_BYTES / (ms * 1e-3) / 1e9
+    line = {"metric": "translational CCD pair queries/s (fcl::translational_ccd, one toc sample)",
+            "value": world * n / (ms * 1e-3), "unit": "pair queries/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (box intervals f64)", "data": "synthetic",
+            "config": {"workload": CCD_WORKLOAD, "pairs_per_gpu": n, "hit_fraction": hit,
+                       "l2": "inputs larger than L2 (no flush)"},
+            "gpu_launches": launches, "clocks": clk.summary(),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": None, "peak_source": src,
+                         "kernel": "ccd_pass (swept-volume MPR, latency-bound)"},
+            "e2e": {"value": world * n / (e2e_ms * 1e-3), "unit": "pair queries/s",
+                    "h2d_bytes_per_step": n * (64 + 16), "d2h_bytes_per_step": n * 16}}
+    if rank == 0:
+        import oracle
+        oracle.build()
+        threads = os.cpu_count() or 1
+        sample = min(n, 200_000)
+        sb = workloads.Batch("ccd_sample", b.shapes, b.vertices, b.pairs[:sample], {})
+        reps, t0 = 0, time.perf_counter()
+        while True:
+            oracle.translational_ccd(sb, disp[:sample], oracle.TOC_SAMPLE, threads=threads)
+            reps += 1
+            if time.perf_counter() - t0 > 5.0:
+                break
+        cpu = reps * sample / (time.perf_counter() - t0)
+        line["cpu_baseline"] = {"value": cpu, "unit": "pair queries/s", "cores": threads, "kind": "port",
+                                "sample": "first %d pairs, repeated for >= 5 s" % sample}
+        print(json.dumps(line))
+    ctx.close()
+    return 0
+
+
 SCENE_WORKLOAD = ("scene: 100,000 posed objects (sphere / box / capsule / cylinder / hull, sizes U[0.02, 0.4] m, "
                   "hulls of log-uniform[8, 256] points; uniform rotations, 20 % identity) in a cube at 0.25 "
                   "objects per bounding-sphere volume; per step the broadphase (CollisionObject AABBs, every "
@@ -728,6 +819,8 @@ def main():
         return run_mesh_shape(args)
     if args.workload == "scene":
         return run_scene(args)
+    if args.workload == "ccd":
+        return run_ccd(args)
     if args.workload == "warmstart":
         return run_warmstart_kernel(args)
     import torch

@@ -424,6 +424,51 @@ int fclg_mesh_shape_collide_device(fclg_context* ctx, const fclg_mesh* mesh, con
                                    const float* d_poses, uint32_t n, uint32_t max_contacts, uint8_t* d_flags,
                                    uint32_t* d_counts, int32_t* d_tri_ids, uint32_t* d_status, void* stream);
 
+/* ---- translational continuous collision --------------------------------
+   Replaces fcl::translational_ccd(o1, tf1, o1_displacement, o2, tf2, request,
+   result) (narrowphase/continuous_collision.h:13-19) on shape pairs, through
+   ShapePairTranslationalCollisionSolver::RunShapePair
+   (narrowphase/detail/ccd/shape_pair_ccd-inl.h:113-160).  Per pair, shape a
+   moves from the pair's start along disp[i].axis (unit, shape a's frame; the
+   TranslationalDisplacement of ccd_typedef.h:11-15) by disp[i].distance
+   (>= 0); shape b stays at the pair's pose.  Box-box pairs always take the
+   box interval test (BoxPairTranslationalCCD::IsDisjoint); the other pairs
+   the swept-volume MPR, after that test on the shapes' local boxes for
+   FCLG_TOC_BOX. */
+typedef struct {
+  float axis[3];
+  float distance;
+} fclg_displacement;
+
+enum {  /* TimeOfCollisionRequestType (narrowphase/detail/ccd/ccd_request.h:11-17) */
+  FCLG_TOC_NONE = 0,    /* kNotRequested: the boolean alone (box-box pairs still report their interval) */
+  FCLG_TOC_BOX = 1,     /* kBoxApproximate: the local boxes' interval, then MPR */
+  FCLG_TOC_SAMPLE = 2   /* kOneTocSample: one time of collision from MPR's final portal */
+};
+
+typedef struct {            /* ContinuousCollisionRequest (ccd_request.h:19-31); 0 = default */
+  uint32_t toc_type;        /* FCLG_TOC_* */
+  int32_t max_gjk_iterations;       /* 128 */
+  float gjk_tolerance;              /* 1e-6 */
+  uint32_t reserved;
+  double zero_movement_tolerance;   /* 1e-4 */
+} fclg_ccd_request;
+
+typedef struct {     /* one ContinuousCollisionContact's verdict (ccd_contact.h) */
+  uint32_t collide;  /* 1: the moving shape touches the other somewhere on its path */
+  uint32_t status;   /* bits 0-1 swept MPR status (0 Intersect, 1 Separated, 2 Failed, 3 not run),
+                        bit 2 box interval test ran, bit 3 it found the boxes disjoint,
+                        bit 4 shape id out of range */
+  float toc_lower;   /* time of collision in [0, 1] as a fraction of the distance: */
+  float toc_upper;   /* the box interval, the one sample (lower = upper), or -1 when none */
+} fclg_ccd_result;
+
+int fclg_translational_ccd(fclg_context* ctx, const fclg_pair* pairs, uint32_t n_pairs, const fclg_displacement* disp,
+                           const fclg_ccd_request* req, fclg_ccd_result* results);
+int fclg_translational_ccd_device(fclg_context* ctx, const fclg_pair* d_pairs, uint32_t n_pairs,
+                                  const fclg_displacement* d_disp, const fclg_ccd_request* req,
+                                  fclg_ccd_result* d_results, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -33,6 +33,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <iostream>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -266,6 +267,55 @@ class CollisionResult {
 
  private:
   std::vector<Contact<S>> contacts_;
+};
+
+// ---- translational continuous collision (narrowphase/detail/ccd/) --------
+// TranslationalDisplacement and Interval (ccd_typedef.h:11-37).
+template <typename S>
+struct TranslationalDisplacement {
+  Vector3<S> unit_axis_in_shape1;
+  S scalar_displacement = S(0);
+};
+
+template <typename S>
+struct Interval {
+  S lower_bound = S(-1);
+  S upper_bound = S(-1);
+};
+
+// TimeOfCollisionRequestType and ContinuousCollisionRequest (ccd_request.h).
+enum class TimeOfCollisionRequestType { kNotRequested, kBoxApproximate, kOneTocSample };
+
+template <typename S>
+struct ContinuousCollisionRequest {
+  TimeOfCollisionRequestType request_type = TimeOfCollisionRequestType::kNotRequested;
+  std::size_t num_max_contacts = 1;
+  S zero_movement_tolerance = S(1e-4);
+  S gjk_tolerance = S(1e-6);
+  int max_gjk_iterations = 128;
+};
+
+// ContinuousCollisionContact / ContinuousCollisionResult (ccd_contact.h,
+// ccd_result.h): shape pairs give at most one contact, b1 = b2 = -1.
+template <typename S>
+struct ContinuousCollisionContact {
+  const CollisionGeometry<S>* o1 = nullptr;
+  const CollisionGeometry<S>* o2 = nullptr;
+  int b1 = -1, b2 = -1;
+  Interval<S> toc;
+};
+
+template <typename S>
+class ContinuousCollisionResult {
+ public:
+  void AddContact(const ContinuousCollisionContact<S>& c) { contacts_.push_back(c); }
+  void ClearContact() { contacts_.clear(); }
+  std::size_t num_contacts() const { return contacts_.size(); }
+  const std::vector<ContinuousCollisionContact<S>>& raw_contacts() const { return contacts_; }
+  bool TerminationConditionSatisfied(std::size_t n_max_contacts) const { return contacts_.size() >= n_max_contacts; }
+
+ private:
+  std::vector<ContinuousCollisionContact<S>> contacts_;
 };
 
 namespace detail {
@@ -504,6 +554,43 @@ class BatchQuery {
     return out;
   }
 
+  // fcl::translational_ccd per pair: shape 1 of pair i moving along
+  // displacement[i] (unit axis in its own frame) against shape 2.
+  std::vector<ContinuousCollisionResult<S>> translationalCcd(
+      const std::vector<TranslationalDisplacement<S>>& displacement, const ContinuousCollisionRequest<S>& req) {
+    std::vector<ContinuousCollisionResult<S>> out(pairs_.size());
+    if (pairs_.empty() || req.num_max_contacts == 0) return out;
+    if (displacement.size() != pairs_.size()) throw std::invalid_argument("one displacement per pair");
+    std::vector<fclg_displacement> disp(pairs_.size());
+    for (std::size_t i = 0; i < pairs_.size(); ++i) {
+      for (int k = 0; k < 3; ++k) disp[i].axis[k] = (float)displacement[i].unit_axis_in_shape1[k];
+      disp[i].distance = (float)displacement[i].scalar_displacement;
+    }
+    fclg_ccd_request r{};
+    r.toc_type = req.request_type == TimeOfCollisionRequestType::kBoxApproximate ? (uint32_t)FCLG_TOC_BOX
+                 : req.request_type == TimeOfCollisionRequestType::kOneTocSample ? (uint32_t)FCLG_TOC_SAMPLE
+                                                                                  : (uint32_t)FCLG_TOC_NONE;
+    r.max_gjk_iterations = req.max_gjk_iterations;
+    r.gjk_tolerance = (float)req.gjk_tolerance;
+    r.zero_movement_tolerance = (double)req.zero_movement_tolerance;
+    std::vector<fclg_ccd_result> res(pairs_.size());
+    fclg_context* ctx = detail::thread_context();
+    detail::check(ctx, fclg_set_shapes(ctx, shapes_.data(), (uint32_t)shapes_.size(), verts_.data(), verts_.size() / 4),
+                  "fclg_set_shapes");
+    detail::check(ctx, fclg_translational_ccd(ctx, pairs_.data(), (uint32_t)pairs_.size(), disp.data(), &r, res.data()),
+                  "fclg_translational_ccd");
+    for (std::size_t i = 0; i < res.size(); ++i) {
+      if (!res[i].collide) continue;
+      ContinuousCollisionContact<S> c;
+      c.o1 = geoms_[i].first;
+      c.o2 = geoms_[i].second;
+      c.toc.lower_bound = (S)res[i].toc_lower;
+      c.toc.upper_bound = (S)res[i].toc_upper;
+      out[i].AddContact(c);
+    }
+    return out;
+  }
+
   void clear() {
     pairs_.clear();
     frames_.clear();
@@ -633,6 +720,25 @@ std::size_t collide(const CollisionGeometry<S>* o1, const TF1& tf1, const Collis
   for (const auto& c : r.getContacts())
     if (result.numContacts() < request.maxNumContacts()) result.addContact(c);
   return r.numContacts();
+}
+
+// fcl::translational_ccd (narrowphase/continuous_collision.h:13-19) on shape
+// pairs; a BVHModel is not supported here and is reported as the reference
+// reports an unsupported pair (a warning, no contact).
+template <typename S, typename TF1, typename TF2>
+void translational_ccd(const CollisionGeometry<S>* o1, const TF1& tf1,
+                       const TranslationalDisplacement<S>& o1_displacement, const CollisionGeometry<S>* o2,
+                       const TF2& tf2, const ContinuousCollisionRequest<S>& request,
+                       ContinuousCollisionResult<S>& result) {
+  if (o1->getNodeType() == BV_OBBRSS || o2->getNodeType() == BV_OBBRSS) {
+    std::cerr << "Warning: translational CCD with a BVHModel is not supported\n";
+    return;
+  }
+  if (result.TerminationConditionSatisfied(request.num_max_contacts)) return;
+  BatchQuery<S> q;
+  q.add(o1, tf1, o2, tf2);
+  const auto r = q.translationalCcd({o1_displacement}, request).front();
+  for (const auto& c : r.raw_contacts()) result.AddContact(c);
 }
 
 // detail::GJKSolver<S>: shapeSignedDistance with the reference's defaults

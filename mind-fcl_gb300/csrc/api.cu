@@ -14,6 +14,7 @@
 #include "broadphase.h"
 #include "fclg.h"
 #include "hull.h"
+#include "ccd.h"
 #include "kernels.h"
 #include "mesh_build.h"
 #include "mesh_kernels.h"
@@ -83,6 +84,11 @@ struct fclg_context {
   size_t guess_cap = 0;
   // bumped whenever query scratch is reallocated (invalidates captured graphs)
   uint64_t scratch_epoch = 0;
+  // translational CCD: hull boxes of the current shapes (2 float4 each), host staging of displacements
+  float4* hull_aabb = nullptr;
+  bool hull_aabb_valid = false;
+  void* ccd_disp = nullptr;
+  size_t ccd_disp_cap = 0;
 };
 
 struct fclg_mesh {
@@ -148,6 +154,9 @@ void release_shapes(fclg_context* c) {
   c->walk_tab = nullptr;
   c->hull_ents = nullptr;
   c->walk_hulls = 0;
+  if (c->hull_aabb) cudaFree(c->hull_aabb);
+  c->hull_aabb = nullptr;
+  c->hull_aabb_valid = false;
   c->scratch_epoch += 1;  // captured graphs hold the old shape pointers
   c->own_shapes = c->own_verts = nullptr;
   c->shapes = nullptr;
@@ -450,6 +459,8 @@ void fclg_destroy(fclg_context* c) {
   if (c->bp_scratch) cudaFree(c->bp_scratch);
   if (c->bp_io) cudaFree(c->bp_io);
   if (c->bp_join) cudaFree(c->bp_join);
+  if (c->hull_aabb) cudaFree(c->hull_aabb);
+  if (c->ccd_disp) cudaFree(c->ccd_disp);
   if (c->stream) cudaStreamDestroy(c->stream);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -1301,5 +1312,85 @@ extern "C" int fclg_autotune(fclg_context* c, const fclg_pair* d_pairs, uint32_t
   if (rc) return rc;
   if (best) fclg_get_tuning(c, best);
   if (best_ms) *best_ms = best_t;
+  return FCLG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Translational continuous collision of shape pairs.
+// ---------------------------------------------------------------------------
+
+static_assert(sizeof(fclg_displacement) == 16, "displacement layout (read as float4)");
+static_assert(sizeof(fclg_ccd_result) == 16, "ccd result layout (written as float4)");
+static_assert(sizeof(fclg_ccd_request) == 24, "ccd request layout");
+static_assert(sizeof(fclg_ccd_result) <= sizeof(fclg_result), "ccd results share the query result staging");
+
+namespace {
+
+int run_ccd(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_displacement* d_disp,
+            const fclg_ccd_request* req, fclg_ccd_result* d_results, cudaStream_t st) {
+  if (!c) return FCLG_E_INVALID;
+  if (n == 0) return FCLG_OK;
+  if (!d_pairs || !d_disp || !d_results) return fail(c, FCLG_E_INVALID, "null pair, displacement or result pointer");
+  if (!c->shapes) return fail(c, FCLG_E_NO_SHAPES, "no shapes set");
+  fclg::CcdParams prm;
+  prm.toc_type = req ? (int)req->toc_type : fclg::kTocNone;
+  if (prm.toc_type < fclg::kTocNone || prm.toc_type > fclg::kTocSample)
+    return fail(c, FCLG_E_INVALID, "toc_type is not one of FCLG_TOC_*");
+  prm.max_iter = (req && req->max_gjk_iterations > 0) ? req->max_gjk_iterations : 128;
+  prm.tol = (req && req->gjk_tolerance > 0.f) ? req->gjk_tolerance : 1e-6f;
+  prm.zero_tol = (req && req->zero_movement_tolerance > 0.0) ? req->zero_movement_tolerance : 1e-4;
+  FCLG_CUDA(c, cudaSetDevice(c->device));
+  clear_pending_error();
+  if (prm.toc_type == fclg::kTocBox && !c->hull_aabb_valid) {
+    if (!c->hull_aabb) FCLG_CUDA(c, cudaMalloc(&c->hull_aabb, (size_t)c->n_shapes * 2 * sizeof(float4)));
+    FCLG_CUDA(c, fclg::launch_hull_aabbs(c->shapes, c->verts, c->n_shapes, c->hull_aabb, st));
+    c->launches += 1;
+    c->hull_aabb_valid = true;
+  }
+  fclg::BatchArgs b = batch_args(c);
+  b.pairs = reinterpret_cast<const float4*>(d_pairs);
+  b.results = nullptr;
+  b.n_pairs = n;
+  b.n_shapes = c->n_shapes;
+  FCLG_CUDA(c, fclg::launch_ccd(b, reinterpret_cast<const float4*>(d_disp), c->hull_aabb, prm,
+                                reinterpret_cast<float4*>(d_results), c->num_sms * c->gjk_ctas_per_sm, st));
+  c->launches += 1;
+  return FCLG_OK;
+}
+
+}  // namespace
+
+extern "C" int fclg_translational_ccd_device(fclg_context* c, const fclg_pair* d_pairs, uint32_t n,
+                                             const fclg_displacement* d_disp, const fclg_ccd_request* req,
+                                             fclg_ccd_result* d_results, void* stream) {
+  return run_ccd(c, d_pairs, n, d_disp, req, d_results, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int fclg_translational_ccd(fclg_context* c, const fclg_pair* pairs, uint32_t n,
+                                      const fclg_displacement* disp, const fclg_ccd_request* req,
+                                      fclg_ccd_result* results) {
+  if (!c) return FCLG_E_INVALID;
+  if (n == 0) return FCLG_OK;
+  if (!pairs || !disp || !results) return fail(c, FCLG_E_INVALID, "null pair, displacement or result pointer");
+  int rc = ensure_io(c, n);
+  if (rc) return rc;
+  if (n > c->ccd_disp_cap) {
+    if (c->ccd_disp) cudaFree(c->ccd_disp);
+    c->ccd_disp = nullptr;
+    c->ccd_disp_cap = 0;
+    const size_t cap = std::max<size_t>(n, 1024);
+    FCLG_CUDA(c, cudaMalloc(&c->ccd_disp, cap * sizeof(fclg_displacement)));
+    c->ccd_disp_cap = cap;
+  }
+  FCLG_CUDA(c, cudaMemcpyAsync(c->io_pairs, pairs, (size_t)n * sizeof(fclg_pair), cudaMemcpyHostToDevice, c->stream));
+  FCLG_CUDA(c, cudaMemcpyAsync(c->ccd_disp, disp, (size_t)n * sizeof(fclg_displacement), cudaMemcpyHostToDevice,
+                               c->stream));
+  // the results (16 bytes each) fit the staging of query results
+  rc = run_ccd(c, static_cast<const fclg_pair*>(c->io_pairs), n, static_cast<const fclg_displacement*>(c->ccd_disp),
+               req, static_cast<fclg_ccd_result*>(c->io_results), c->stream);
+  if (rc) return rc;
+  FCLG_CUDA(c, cudaMemcpyAsync(results, c->io_results, (size_t)n * sizeof(fclg_ccd_result), cudaMemcpyDeviceToHost,
+                               c->stream));
+  FCLG_CUDA(c, cudaStreamSynchronize(c->stream));
   return FCLG_OK;
 }

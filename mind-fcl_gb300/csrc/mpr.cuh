@@ -11,6 +11,15 @@ namespace fclg {
 
 enum class MprStatus : int { Intersect = 0, Separated = 1, Failed = 2 };
 
+// MPR::IntersectData (mpr.h:23-31) at an Intersect exit: the interior point,
+// the portal and the (unit) directions that found its vertices; `count` of
+// v1..v3 set (0: the interior point is at the origin; 1: the origin lies on
+// the segment v0 v1; 3: inside the tetrahedron v0 v1 v2 v3).
+struct MprPortal {
+  f3 v0, v1, v2, v3, d1, d2, d3;
+  int count;
+};
+
 // Interior point of a shape in its own frame: the vertex mean of a hull
 // (convex-inl.h:58-63, stored in fclg_shape.param[0:3]), the origin otherwise.
 __device__ __forceinline__ f3 load_interior(const int4* __restrict__ shapes, uint32_t i, int type) {
@@ -291,14 +300,22 @@ struct Mpr {
     p1 = (pb1 * w1 + pb2 * w2) + pb3 * w3;
   }
 
-  __device__ MprStatus intersect(f3 v0) {
+  // KEEP: the portal of an Intersect exit is written to *keep.
+  template <bool KEEP = false>
+  __device__ MprStatus intersect(f3 v0, MprPortal* keep = nullptr) {
     iterations = 0;
-    if (sqn(v0) <= tol * tol) return MprStatus::Intersect;
+    if (sqn(v0) <= tol * tol) {
+      if constexpr (KEEP) keep->v0 = v0, keep->count = 0;
+      return MprStatus::Intersect;
+    }
     f3 d1 = -v0;
     f3 v1 = support(d1);
     if (dot(d1, v1) < 0.f) return MprStatus::Separated;
     f3 d2 = cross(v0, v1);
-    if (absnorm(d2) <= absnorm(v0) * absnorm(v1) * tol) return MprStatus::Intersect;
+    if (absnorm(d2) <= absnorm(v0) * absnorm(v1) * tol) {
+      if constexpr (KEEP) keep->v0 = v0, keep->v1 = v1, keep->d1 = d1, keep->count = 1;
+      return MprStatus::Intersect;
+    }
     f3 v2 = support(d2);
     if (dot(d2, v2) < 0.f) return MprStatus::Separated;
     f3 d3 = cross(v1 - v0, v2 - v0);
@@ -320,7 +337,10 @@ struct Mpr {
         t = d2; d2 = d3; d3 = t;
         n = -n;
       }
-      if (!(dot(v1, n) < 0.f)) return MprStatus::Intersect;
+      if (!(dot(v1, n) < 0.f)) {
+        if constexpr (KEEP) *keep = MprPortal{v0, v1, v2, v3, d1, d2, d3, 3};
+        return MprStatus::Intersect;
+      }
       const f3 v4 = support(n);
       if (dot(v4, n) < 0.f) return MprStatus::Separated;
       if (fabsf(dot(v4 - v1, n)) < tol * absnorm(n)) return MprStatus::Separated;

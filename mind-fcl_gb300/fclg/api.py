@@ -37,7 +37,19 @@ EXPORTS = [
     "fclg_collide_directed", "fclg_collide_directed_device", "fclg_hull_graph",
     "fclg_mesh_shape_collide", "fclg_mesh_shape_collide_device",
     "fclg_broadphase", "fclg_broadphase_device", "fclg_object_pairs_device", "fclg_broadphase_cross_device",
+    "fclg_translational_ccd", "fclg_translational_ccd_device",
 ]
+
+# translational CCD (fclg_displacement, fclg_ccd_request, fclg_ccd_result)
+DISP_DTYPE = np.dtype([("axis", "<f4", (3,)), ("distance", "<f4")])
+CCD_RESULT_DTYPE = np.dtype([("collide", "<u4"), ("status", "<u4"), ("toc_lower", "<f4"), ("toc_upper", "<f4")])
+FCLG_TOC_NONE, FCLG_TOC_BOX, FCLG_TOC_SAMPLE = 0, 1, 2
+
+
+class CcdRequest(ctypes.Structure):
+    _fields_ = [("toc_type", ctypes.c_uint32), ("max_gjk_iterations", ctypes.c_int32),
+                ("gjk_tolerance", ctypes.c_float), ("reserved", ctypes.c_uint32),
+                ("zero_movement_tolerance", ctypes.c_double)]
 
 STATIC_MAX_PAIRS = 16384  # FCLG_STATIC_MAX_PAIRS
 
@@ -170,6 +182,10 @@ def load_library(path=LIB_PATH):
     lib.fclg_object_pairs_device.restype = i32
     lib.fclg_broadphase_cross_device.argtypes = [vp, vp, vp, u32, vp, vp, u32, vp, u32, vp, vp]
     lib.fclg_broadphase_cross_device.restype = i32
+    lib.fclg_translational_ccd.argtypes = [vp, vp, u32, vp, vp, vp]
+    lib.fclg_translational_ccd.restype = i32
+    lib.fclg_translational_ccd_device.argtypes = [vp, vp, u32, vp, vp, vp, vp]
+    lib.fclg_translational_ccd_device.restype = i32
     _lib = lib
     return lib
 
@@ -317,6 +333,28 @@ class Context:
         self._check(self.lib.fclg_collide_directed(self.h, _ptr(p), len(p), _ptr(d) if d is not None else None,
                                                    req, _ptr(out)), "fclg_collide_directed")
         return out
+
+    def translational_ccd(self, pairs, disp, toc_type=FCLG_TOC_NONE, max_gjk_iterations=0, gjk_tolerance=0.0,
+                          zero_movement_tolerance=0.0):
+        """fcl::translational_ccd on every pair, host arrays: disp = DISP_DTYPE rows or
+        float[n][4] (unit axis in shape a's frame, distance); CCD_RESULT_DTYPE out."""
+        p = np.ascontiguousarray(pairs, PAIR_DTYPE)
+        d = np.ascontiguousarray(disp, np.float32).reshape(-1, 4) if not isinstance(disp, np.ndarray) or \
+            disp.dtype != DISP_DTYPE else np.ascontiguousarray(disp).view(np.float32).reshape(-1, 4)
+        assert len(d) == len(p)
+        out = np.zeros(len(p), CCD_RESULT_DTYPE)
+        req = CcdRequest(toc_type, max_gjk_iterations, gjk_tolerance, 0, zero_movement_tolerance)
+        self._check(self.lib.fclg_translational_ccd(self.h, _ptr(p), len(p), _ptr(d), ctypes.byref(req), _ptr(out)),
+                    "fclg_translational_ccd")
+        return out
+
+    def translational_ccd_device(self, d_pairs, n, d_disp, d_results, toc_type=FCLG_TOC_NONE, stream=None):
+        """The device entry on device pointers (stream: a CUDA stream handle or None)."""
+        req = CcdRequest(toc_type, 0, 0.0, 0, 0.0)
+        self._check(self.lib.fclg_translational_ccd_device(self.h, ctypes.c_void_p(d_pairs), n, ctypes.c_void_p(d_disp),
+                                                           ctypes.byref(req), ctypes.c_void_p(d_results),
+                                                           ctypes.c_void_p(stream) if stream else None),
+                    "fclg_translational_ccd_device")
 
     def autotune(self, d_pairs, n, d_results, request=None, distance=True):
         """Times candidate launch shapes on the batch, keeps the fastest; returns (tuning dict, ms)."""

@@ -41,6 +41,8 @@ PARETO_CLASSES = 81
 ARM_LINKS, ARM_OBSTACLES = 7, 32
 ARM_CLASSES = ARM_LINKS * ARM_OBSTACLES
 MIXED_G_MAX = 1.92   # calibrated: 40 % overlap on the mixed workload
+CCD_G_MAX = 3.0      # translational CCD: start separations
+CCD_REACH = 2.0      # and displacements (bounding-sphere sums)
 PARETO_G_MAX = 1.66  # calibrated: 30 % overlap on the pareto workload
 
 
@@ -201,6 +203,26 @@ def mixed(n_pairs=1_000_000, seed=SEED_BASE + 1, g_max=MIXED_G_MAX):
     cls[[BOX, SPHERE, CAPSULE, CYLINDER, CONVEX]] = np.arange(5)
     p["pair_class"] = 5 * cls[s["type"][p["shape_a"]]] + cls[s["type"][p["shape_b"]]]
     return Batch("mixed", s, v, p, {"seed": seed, "g_max": g_max})
+
+
+def ccd(n_pairs=1_000_000, seed=SEED_BASE + 9, g_max=CCD_G_MAX, reach=CCD_REACH):
+    """Translational continuous collision: pairs of the mixed workload's kinds
+    and sizes, start separations as the mixed workload's at g_max, shape a
+    moving along a uniform random unit axis of its frame by up to `reach`
+    times the pair's bounding-sphere sum.  Returns (Batch, disp [n, 4]
+    float32: axis, distance)."""
+    rng = _rng(seed)
+    choice = np.array([BOX, SPHERE, CAPSULE, CYLINDER, CONVEX], np.int32)
+    types = choice[np.minimum((rng.random(2 * n_pairs) * 5).astype(np.int64), 4)]
+    s, v, rho = _make_shapes(rng, types, 0.02, 0.4, lambda k: log_uniform_counts(rng, k, 8, 256))
+    p = _pairs(rng, n_pairs, rho, g_max)
+    cls = np.zeros(CONVEX + 1, np.uint32)
+    cls[[BOX, SPHERE, CAPSULE, CYLINDER, CONVEX]] = np.arange(5)
+    p["pair_class"] = 5 * cls[s["type"][p["shape_a"]]] + cls[s["type"][p["shape_b"]]]
+    disp = np.zeros((n_pairs, 4), np.float32)
+    disp[:, :3] = unit_vectors(rng, n_pairs)
+    disp[:, 3] = rng.random(n_pairs) * reach * (rho[0::2] + rho[1::2])
+    return Batch("ccd", s, v, p, {"seed": seed, "g_max": g_max, "reach": reach}), disp
 
 
 def pareto(n_pairs=4_000_000, seed=SEED_BASE + 4, g_max=PARETO_G_MAX):

@@ -30,7 +30,7 @@ def build(force=False):
     """Compile the restatement (always) and the reference driver (only where the
     reference sources exist)."""
     srcs = [os.path.join(HERE, f) for f in ("oracle.cpp", "orc_convex.hpp", "orc_mesh.hpp", "orc_analytic.hpp",
-                                            "orc_mesh_shape.hpp") if
+                                            "orc_mesh_shape.hpp", "orc_ccd.hpp") if
             os.path.exists(os.path.join(HERE, f))]
     if force or not os.path.exists(LIB_PATH) or any(os.path.getmtime(s) > os.path.getmtime(LIB_PATH) for s in srcs):
         subprocess.check_call(["g++", *_CXXFLAGS, os.path.join(HERE, "oracle.cpp"), "-o", LIB_PATH, "-lpthread"])
@@ -106,6 +106,8 @@ def _load_ref():
         lib.ref_directed.restype = i
         lib.ref_incremental.argtypes = [vp, i, vp, vp, i, vp, vp, i]
         lib.ref_incremental.restype = i
+        lib.ref_swept_portal.argtypes = [vp, i, vp, vp, i, vp, i, ctypes.c_double, vp, i]
+        lib.ref_swept_portal.restype = i
         lib.ref_collide.restype = i
         _ref = lib
     return _ref
@@ -466,3 +468,70 @@ def tri_tri(p, q, pose):
     q = np.ascontiguousarray(q, np.float64).reshape(9)
     pose = np.ascontiguousarray(pose, np.float64).reshape(12)
     return bool(lib.orc_tri_tri(_ptr(p), _ptr(q), _ptr(pose)))
+
+
+# ------------------------------------------------------- translational CCD --
+CCD_DTYPE = np.dtype([("collide", np.int32), ("mpr_status", np.int32), ("box_tested", np.int32),
+                      ("reserved", np.int32), ("toc_lo", np.float64), ("toc_hi", np.float64)])
+TOC_NONE, TOC_BOX, TOC_SAMPLE = 0, 1, 2  # TimeOfCollisionRequestType order of the C ABI
+
+
+def translational_ccd(batch, disp, toc_type=TOC_NONE, zero_tol=1e-4, max_iter=128, tol=1e-6, threads=None):
+    """fcl::translational_ccd on every pair: shape a moving along disp[i] =
+    (unit axis in a's frame, distance) against shape b (CCD_DTYPE rows;
+    toc = (-1, -1) where the request computes none)."""
+    lib = _load()
+    s, v, p = _prep(batch)
+    d = np.ascontiguousarray(disp, np.float32).reshape(-1, 4)
+    assert len(d) == len(p)
+    out = np.zeros(len(p), CCD_DTYPE)
+    assert lib.orc_translational_ccd(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), _ptr(d), int(toc_type),
+                                     ctypes.c_double(zero_tol), int(max_iter), ctypes.c_double(tol), _ptr(out),
+                                     threads or default_threads()) == 0
+    return out
+
+
+def _portal(fn, batch, disp, max_iter, tol, threads):
+    s, v, p = _prep(batch)
+    d = np.ascontiguousarray(disp, np.float32).reshape(-1, 4)
+    out = np.zeros((len(p), 23))
+    assert fn(_ptr(s), len(s), _ptr(v), _ptr(p), len(p), _ptr(d), int(max_iter), ctypes.c_double(tol), _ptr(out),
+              threads or default_threads()) == 0
+    return out
+
+
+def swept_portal(batch, disp, max_iter=128, tol=1e-6, threads=None):
+    """The restated MPR on the swept-volume difference with its portal data
+    (rows of 23: status, count, v0, v1..v3, d1..d3; unset entries NaN)."""
+    return _portal(_load().orc_swept_portal, batch, disp, max_iter, tol, threads)
+
+
+def ref_swept_portal(batch, disp, max_iter=128, tol=1e-6, threads=None):
+    """The reference's MPR::Intersect with IntersectData on the same difference."""
+    return _portal(_load_ref().ref_swept_portal, batch, disp, max_iter, tol, threads)
+
+
+def box_axis(h1, d, h2, off):
+    """CheckEmptyTocIntervalOnAxis, scalar: (empty, lo, hi), unscaled."""
+    out = np.zeros(2)
+    e = _load().orc_box_axis(ctypes.c_double(h1), ctypes.c_double(d), ctypes.c_double(h2), ctypes.c_double(off),
+                             _ptr(out))
+    return bool(e), out[0], out[1]
+
+
+def box_axes3(h1, d, h2, off, zero_tol=1e-4):
+    """CheckEmptyTocIntervalOnAxis, three axes: (empty, lo, hi) scaled to [0, 1]."""
+    a = [np.ascontiguousarray(np.broadcast_to(x, 3), np.float64) for x in (h1, d, h2, off)]
+    out = np.zeros(2)
+    e = _load().orc_box_axes3(*[_ptr(x) for x in a], ctypes.c_double(zero_tol), _ptr(out))
+    return bool(e), out[0], out[1]
+
+
+def box_pair_ccd(h1, axis, dist, R, t, h2, zero_tol=1e-4):
+    """BoxPairTranslationalCCD::IsDisjoint with box 1 at the origin of its frame:
+    (disjoint, lo, hi); R row-major (box 2 in box 1), t box 2's centre."""
+    a = [np.ascontiguousarray(x, np.float64).reshape(-1) for x in (h1, axis, R, t, h2)]
+    out = np.zeros(2)
+    e = _load().orc_box_pair_ccd(_ptr(a[0]), _ptr(a[1]), ctypes.c_double(dist), _ptr(a[2]), _ptr(a[3]), _ptr(a[4]),
+                                 ctypes.c_double(zero_tol), _ptr(out))
+    return bool(e), out[0], out[1]

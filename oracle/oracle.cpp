@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "orc_analytic.hpp"
+#include "orc_ccd.hpp"
 #include "orc_convex.hpp"
 #include "orc_mesh.hpp"
 #include "orc_mesh_shape.hpp"
@@ -594,6 +595,96 @@ int orc_tri_tri(const double* p /* 9 */, const double* q /* 9 */, const double* 
                                 {q[3], q[4], q[5]}, {q[6], q[7], q[8]}, R, T)
              ? 1
              : 0;
+}
+
+// ------------------------------------------------------ translational CCD --
+// Per pair: shape a moving along disp[i] = (unit axis in a's frame, distance)
+// against shape b at the pair's pose (fcl::translational_ccd).
+struct OrcCcd {
+  int32_t collide, mpr_status, box_tested, reserved;
+  double toc_lo, toc_hi;
+};
+static_assert(sizeof(OrcCcd) == 32, "ccd layout");
+
+int orc_translational_ccd(const void* shapes, int n_shapes, const float* verts, const void* pairs, int n_pairs,
+                          const float* disp, int toc_type, double zero_tol, int max_iter, double tol, OrcCcd* out,
+                          int n_threads) {
+  if (n_pairs < 0 || n_shapes < 0 || !disp || toc_type < 0 || toc_type > 2) return -1;
+  const auto sh = makeShapes((const ShapeRec*)shapes, n_shapes, verts);
+  const PairRec* pr = (const PairRec*)pairs;
+  parallelFor(n_pairs, n_threads, [&](int b, int e) {
+    for (int i = b; i < e; ++i) {
+      const orc::MinkDiff md = makeDiff(sh, pr[i]);
+      const orc::V3 axis(disp[4 * (size_t)i], disp[4 * (size_t)i + 1], disp[4 * (size_t)i + 2]);
+      const orc::CcdOut o = orc::translationalCcd(*md.s0, *md.s1, md.to0, axis, disp[4 * (size_t)i + 3],
+                                                  (orc::TocRequest)toc_type, zero_tol, max_iter, tol);
+      out[i] = OrcCcd{o.collide ? 1 : 0, o.mpr_status, o.box_tested ? 1 : 0, 0, o.toc.lo, o.toc.hi};
+    }
+  });
+  return 0;
+}
+
+// MPR::Intersect on the swept-volume difference with its IntersectData, in
+// the layout of ref_swept_portal for the bit-for-bit pin: per pair 23
+// doubles = status, count, v0, v1, v2, v3, d1, d2, d3 (unset entries NaN).
+int orc_swept_portal(const void* shapes, int n_shapes, const float* verts, const void* pairs, int n_pairs,
+                     const float* disp, int max_iter, double tol, double* out, int n_threads) {
+  if (n_pairs < 0 || n_shapes < 0 || !disp) return -1;
+  const auto sh = makeShapes((const ShapeRec*)shapes, n_shapes, verts);
+  const PairRec* pr = (const PairRec*)pairs;
+  parallelFor(n_pairs, n_threads, [&](int b, int e) {
+    for (int i = b; i < e; ++i) {
+      orc::MinkDiff md = makeDiff(sh, pr[i]);
+      const orc::V3 axis(disp[4 * (size_t)i], disp[4 * (size_t)i + 1], disp[4 * (size_t)i + 2]);
+      md.swept = true;
+      md.sweep = axis * (double)disp[4 * (size_t)i + 3];
+      orc::MPR mpr(max_iter, tol);
+      orc::MPRPortal P;
+      const orc::MPRStatus st = mpr.Intersect(md, &P);
+      double* o = out + 23 * (size_t)i;
+      for (int k = 0; k < 23; ++k) o[k] = std::numeric_limits<double>::quiet_NaN();
+      o[0] = (double)(int)st;
+      o[1] = P.count;
+      for (int k = 0; k < 3; ++k) o[2 + k] = P.v0[k];
+      for (int j = 0; j < P.count; ++j)
+        for (int k = 0; k < 3; ++k) {
+          o[5 + 3 * j + k] = P.v[j][k];
+          o[14 + 3 * j + k] = P.d[j][k];
+        }
+    }
+  });
+  return 0;
+}
+
+// The box pieces alone, for the reference's interval tests
+// (test/ccd/test_box_pair_ccd.cpp): one axis (scalar, signed displacement,
+// unscaled interval), three axes (scaled), and a box pair.  Each returns
+// 1 when empty / disjoint and writes the interval to lo_hi.
+int orc_box_axis(double h1, double d, double h2, double off, double* lo_hi) {
+  orc::Interval t;
+  const bool e = orc::boxAxisEmptySigned(h1, d, h2, off, t);
+  lo_hi[0] = t.lo;
+  lo_hi[1] = t.hi;
+  return e ? 1 : 0;
+}
+
+int orc_box_axes3(const double* h1, const double* d, const double* h2, const double* off, double zero_tol,
+                  double* lo_hi) {
+  orc::Interval t;
+  const bool e = orc::boxAxes3Empty(h1, d, h2, off, t, zero_tol);
+  lo_hi[0] = t.lo;
+  lo_hi[1] = t.hi;
+  return e ? 1 : 0;
+}
+
+int orc_box_pair_ccd(const double* h1, const double* axis, double dist, const double* R, const double* t,
+                     const double* h2, double zero_tol, double* lo_hi) {
+  orc::Interval iv;
+  const bool e = orc::boxPairDisjoint(h1, orc::V3(axis[0], axis[1], axis[2]), dist, R, orc::V3(t[0], t[1], t[2]), h2,
+                                      zero_tol, iv);
+  lo_hi[0] = iv.lo;
+  lo_hi[1] = iv.hi;
+  return e ? 1 : 0;
 }
 
 }  // extern "C"

@@ -202,7 +202,15 @@ struct MinkDiff {
   const Shape* s0;
   const Shape* s1;
   Iso to0;
-  V3 support0(const V3& d) const { return orc::support(*s0, d); }
+  // Shape 0 swept along `sweep` (its frame) when `swept`: the ShapeSweptVolume
+  // support and interior of computeSupport / computeInterior
+  // (narrowphase/detail/gjk_solver_cvx-inl.h:90-107, 128-141).
+  bool swept = false;
+  V3 sweep;
+  V3 support0(const V3& d) const {
+    const V3 p = orc::support(*s0, d);
+    return (swept && dot(d, sweep) > 0) ? p + sweep : p;
+  }
   V3 support1(const V3& d) const { return to0.apply(orc::support(*s1, to0.rotT(d))); }
   V3 support(const V3& d) const { return support0(d) - support1(-d); }
   MinkVertex supportVertex(const V3& d) const {
@@ -211,7 +219,10 @@ struct MinkDiff {
     v.vertex = support0(d) - support1(-d);
     return v;
   }
-  V3 interior() const { return s0->interior - to0.apply(s1->interior); }
+  V3 interior() const {
+    const V3 i0 = swept ? s0->interior + sweep * 0.5 : s0->interior;
+    return i0 - to0.apply(s1->interior);
+  }
 };
 
 // -------------------------------------------------------------------- GJK --
@@ -1307,28 +1318,54 @@ class EPA {
 // -------------------------------------------------------------------- MPR --
 enum class MPRStatus : int { Intersect = 0, Separated = 1, Failed = 2 };
 
+// MPR::IntersectData (mpr.h:23-31) as the run leaves it: the interior point,
+// the portal and the directions that found its vertices; `count` = how many
+// of v1..v3 were set (the reference leaves the others NaN).
+struct MPRPortal {
+  V3 v0, v[3], d[3];
+  int count = 0;
+};
+
 class MPR {
  public:
   MPR(int max_iter, double tol) : max_iter_(max_iter), tol_(tol) {}
 
   // mpr.hpp:33-185
-  MPRStatus Intersect(const MinkDiff& shape) const {
+  MPRStatus Intersect(const MinkDiff& shape, MPRPortal* keep = nullptr) const {
     V3 v0 = shape.interior();
+    V3 d1, d2, d3, v1, v2, v3;
+    int count = 0;
+    const MPRStatus st = run(shape, v0, v1, v2, v3, d1, d2, d3, count);
+    if (keep) {
+      keep->v0 = v0;
+      keep->v[0] = v1; keep->v[1] = v2; keep->v[2] = v3;
+      keep->d[0] = d1; keep->d[1] = d2; keep->d[2] = d3;
+      keep->count = count;
+    }
+    return st;
+  }
+
+ private:
+  MPRStatus run(const MinkDiff& shape, const V3& v0, V3& v1, V3& v2, V3& v3, V3& d1, V3& d2, V3& d3,
+                int& count) const {
     if (sqn(v0) <= tol_ * tol_) return MPRStatus::Intersect;
-    V3 d1 = -v0;
-    V3 v1 = sup(shape, d1);
+    d1 = -v0;
+    v1 = sup(shape, d1);
+    count = 1;
     if (dot(d1, v1) < 0) return MPRStatus::Separated;
-    V3 d2 = cross(v0, v1);
+    d2 = cross(v0, v1);
     if (absnorm(d2) <= absnorm(v0) * absnorm(v1) * tol_) return MPRStatus::Intersect;
-    V3 v2 = sup(shape, d2);
+    v2 = sup(shape, d2);
+    count = 2;
     if (dot(d2, v2) < 0) return MPRStatus::Separated;
-    V3 d3 = cross(v1 - v0, v2 - v0);
+    d3 = cross(v1 - v0, v2 - v0);
     if (dot(d3, v0) > 0) {
       std::swap(v1, v2);
       std::swap(d1, d2);
       d3 = -d3;
     }
-    V3 v3 = sup(shape, d3);
+    v3 = sup(shape, d3);
+    count = 3;
     if (dot(d3, v3) < 0) return MPRStatus::Separated;
     const int fp = findPortal(shape, v0, v1, v2, v3, d1, d2, d3);
     if (fp == 0) return MPRStatus::Failed;

@@ -13,7 +13,9 @@
 // (convex-inl.h:58-63), and the GJKSolver bridge policies
 // ShapeSignedDistanceIndepImpl (gjk_solver-inl.h:810-863) and
 // ShapeIntersectIndepImpl (gjk_solver-inl.h:70-137).
+#include <cmath>
 #include <cstdint>
+#include <limits>
 #include <thread>
 #include <vector>
 
@@ -44,6 +46,11 @@ struct ConvexData {
 };
 
 Vec supportFn(const GJKGeometryData<double>& g, const Vec& d) {
+  if (g.shape_type == GJKShapeType::ShapeSweptVolume) {
+    // computeSupport's swept-volume case (narrowphase/detail/gjk_solver_cvx-inl.h:93-101)
+    const Vec p = supportFn(*static_cast<const GJKGeometryData<double>*>(g.user_ptr), d);
+    return (d.dot(g.vec3_data) > 0) ? Vec(p + g.vec3_data) : p;
+  }
   if (g.shape_type == GJKShapeType::Convex) {
     const ConvexData* c = static_cast<const ConvexData*>(g.user_ptr);
     int best = 0;
@@ -58,6 +65,8 @@ Vec supportFn(const GJKGeometryData<double>& g, const Vec& d) {
 }
 
 Vec interiorFn(const GJKGeometryData<double>& g) {
+  if (g.shape_type == GJKShapeType::ShapeSweptVolume)  // gjk_solver_cvx-inl.h:131-138
+    return Vec(interiorFn(*static_cast<const GJKGeometryData<double>*>(g.user_ptr)) + 0.5 * g.vec3_data);
   if (g.shape_type == GJKShapeType::Convex) return static_cast<const ConvexData*>(g.user_ptr)->mean;
   return basicGeometryInterior<double>(g);
 }
@@ -272,6 +281,46 @@ int ref_incremental(const void* shapes, int n_shapes, const float* verts, const 
       }
       r.ok = (st == MPR<double>::IncrementalPenetrationStatus::OK ||
               st == MPR<double>::IncrementalPenetrationStatus::IterationLimit) ? 1 : 0;
+    }
+  });
+  return 0;
+}
+
+// The reference's MPR::Intersect with IntersectData (cvx_collide/mpr.hpp:
+// 22-185) on the difference of shape a swept along disp[i] (unit axis in a's
+// frame, distance; TranslationalCollisionGJK::setupMinkowskiDiff,
+// narrowphase/detail/ccd/gjk_ccd-inl.h:7-18) and shape b: per pair 23
+// doubles = status, count of set portal vertices, v0, v1, v2, v3, d1, d2, d3.
+int ref_swept_portal(const void* shapes, int n_shapes, const float* verts, const void* pairs, int n_pairs,
+                     const float* disp, int max_iter, double tol, double* out, int n_threads) {
+  const Prepared p = prepare((const ShapeRec*)shapes, n_shapes, verts);
+  const PairRec* pr = (const PairRec*)pairs;
+  parallelFor(n_pairs, n_threads, [&](int b, int e) {
+    for (int i = b; i < e; ++i) {
+      MinkowskiDiff<double> md = makeDiff(p, pr[i]);
+      GJKGeometryData<double> swept;
+      swept.shape_type = GJKShapeType::ShapeSweptVolume;
+      swept.vec3_data = Vec(disp[4 * (size_t)i], disp[4 * (size_t)i + 1], disp[4 * (size_t)i + 2]) *
+                        (double)disp[4 * (size_t)i + 3];
+      swept.user_ptr = &p.geo[pr[i].shape_a];
+      md.shapes[0] = swept;
+      MPR<double> mpr(max_iter, tol);
+      MPR<double>::IntersectData data;
+      const auto st = mpr.Intersect(md, &data);
+      double* o = out + 23 * (size_t)i;
+      for (int k = 0; k < 23; ++k) o[k] = std::numeric_limits<double>::quiet_NaN();
+      o[0] = (double)(int)st;
+      const Vec* vs[3] = {&data.v1, &data.v2, &data.v3};
+      const Vec* ds[3] = {&data.v1_dir_in_support, &data.v2_dir_in_support, &data.v3_dir_in_support};
+      int count = 0;
+      while (count < 3 && !std::isnan((*vs[count])[0])) ++count;
+      o[1] = count;
+      for (int k = 0; k < 3; ++k) o[2 + k] = data.v0_interior[k];
+      for (int j = 0; j < count; ++j)
+        for (int k = 0; k < 3; ++k) {
+          o[5 + 3 * j + k] = (*vs[j])[k];
+          o[14 + 3 * j + k] = (*ds[j])[k];
+        }
     }
   });
   return 0;

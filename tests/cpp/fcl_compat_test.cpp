@@ -153,6 +153,47 @@ int main() {
   CHECK(collide(&b1, at(0.9, 0, 0), &m1, at(0, 0, 0), ms_req, res) > 0, "box-mesh overlap");
   for (const auto& c : res.getContacts()) CHECK(c.o2 == &m1 && c.b2 >= 0 && c.b2 < 8, "box-mesh triangle ids");
 
+  // translational CCD (test/ccd/test_shape_pair_interface.cpp): a sphere of
+  // radius 0.1 moving 1 along +x towards a sphere of radius 0.125 at x = 0.6
+  // hits; at x = 1.3 it stops short; moving along -x it never reaches it.  The
+  // sampled time puts the spheres in touch; two unit cubes 3 apart meet
+  // within the box interval [0.5, 1] of a motion of 4 along +x.
+  {
+    Sphere<S> a(0.1), b(0.125);
+    TranslationalDisplacement<S> mv;
+    mv.unit_axis_in_shape1 = Vector3<S>(1, 0, 0);
+    mv.scalar_displacement = 1.0;
+    ContinuousCollisionRequest<S> creq;
+    creq.request_type = TimeOfCollisionRequestType::kOneTocSample;
+    ContinuousCollisionResult<S> cres;
+    translational_ccd<S>(&a, at(0, 0, 0), mv, &b, at(0.6, 0, 0), creq, cres);
+    CHECK(cres.num_contacts() == 1, "ccd sphere hit");
+    if (cres.num_contacts() == 1) {
+      const S t = cres.raw_contacts()[0].toc.lower_bound;
+      CHECK(t >= 0 && t <= 1 && std::fabs(0.6 - t) <= 0.225 + 1e-5, "ccd sphere toc %.6f", t);
+      CHECK(cres.raw_contacts()[0].o1 == &a && cres.raw_contacts()[0].o2 == &b, "ccd contact objects");
+    }
+    ContinuousCollisionResult<S> far;
+    translational_ccd<S>(&a, at(0, 0, 0), mv, &b, at(1.3, 0, 0), creq, far);
+    CHECK(far.num_contacts() == 0, "ccd sphere stops short");
+    mv.unit_axis_in_shape1 = Vector3<S>(-1, 0, 0);
+    ContinuousCollisionResult<S> back;
+    translational_ccd<S>(&a, at(0, 0, 0), mv, &b, at(0.6, 0, 0), creq, back);
+    CHECK(back.num_contacts() == 0, "ccd sphere moving away");
+    Box<S> c1(1, 1, 1), c2(1, 1, 1);
+    mv.unit_axis_in_shape1 = Vector3<S>(1, 0, 0);
+    mv.scalar_displacement = 4.0;
+    ContinuousCollisionRequest<S> breq;
+    ContinuousCollisionResult<S> bres;
+    translational_ccd<S>(&c1, at(0, 0, 0), mv, &c2, at(3, 0, 0), breq, bres);
+    CHECK(bres.num_contacts() == 1, "ccd boxes hit");
+    if (bres.num_contacts() == 1)
+      CHECK(std::fabs(bres.raw_contacts()[0].toc.lower_bound - 0.5) < 1e-6 &&
+                std::fabs(bres.raw_contacts()[0].toc.upper_bound - 1.0) < 1e-6,
+            "ccd box interval [%.6f, %.6f]", bres.raw_contacts()[0].toc.lower_bound,
+            bres.raw_contacts()[0].toc.upper_bound);
+  }
+
   if (failures == 0) std::printf("fcl_compat_test: all passed\n");
   return failures == 0 ? 0 : 1;
 }
