@@ -543,6 +543,8 @@ def run_ccd(args):
     n = b.n_pairs
     ctx = Context(local)
     ctx.set_batch(b)
+    if args.tuning:
+        ctx.set_tuning(**{k: int(v) for k, v in json.loads(args.tuning).items()})
     stream = torch.cuda.current_stream(dev)
     d_pairs = torch.from_numpy(b.pairs.view(np.uint8).copy()).to(dev)
     d_disp = torch.from_numpy(disp).to(dev)
@@ -583,7 +585,7 @@ def run_ccd(args):
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (box intervals f64)", "data": "synthetic",
             "config": {"workload": CCD_WORKLOAD, "pairs_per_gpu": n, "hit_fraction": hit,
-                       "l2": "inputs larger than L2 (no flush)"},
+                       "l2": "inputs larger than L2 (no flush)", "tuning": ctx.get_tuning()},
             "gpu_launches": launches, "clocks": clk.summary(),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": None, "peak_source": src,

@@ -1352,7 +1352,18 @@ int run_ccd(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_di
   b.results = nullptr;
   b.n_pairs = n;
   b.n_shapes = c->n_shapes;
-  FCLG_CUDA(c, fclg::launch_ccd(b, reinterpret_cast<const float4*>(d_disp), c->hull_aabb, prm,
+  const uint32_t* order = nullptr;
+  if (c->bucketing) {
+    // shape-class order, as the distance query sorts its pairs
+    const int rc = ensure_bucket(c, n);
+    if (rc) return rc;
+    fclg::BucketScratch bs{c->bk_keys, c->bk_order, c->bk_small, c->bk_small + fclg::kBucketKeys,
+                           c->bk_small + 2 * fclg::kBucketKeys};
+    FCLG_CUDA(c, fclg::launch_bucketing(b, bs, (uint32_t)c->large_hull, st));
+    c->launches += 3;
+    order = bs.order;
+  }
+  FCLG_CUDA(c, fclg::launch_ccd(b, reinterpret_cast<const float4*>(d_disp), c->hull_aabb, prm, order,
                                 reinterpret_cast<float4*>(d_results), c->num_sms * c->gjk_ctas_per_sm, st));
   c->launches += 1;
   return FCLG_OK;

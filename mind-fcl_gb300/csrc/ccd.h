@@ -26,9 +26,9 @@ struct CcdParams {
 cudaError_t launch_hull_aabbs(const int4* shapes, const float4* verts, uint32_t n_shapes, float4* aabb,
                               cudaStream_t st);
 // One pass over b's pairs: disp[i] = (unit axis in a's frame, distance),
-// aabb = the hull boxes (read by the approximate request), out[i] =
-// fclg_ccd_result.
+// aabb = the hull boxes (read by the approximate request), order = the pairs
+// in shape-class order (or null: index order), out[i] = fclg_ccd_result.
 cudaError_t launch_ccd(const BatchArgs& b, const float4* disp, const float4* aabb, const CcdParams& prm,
-                       float4* out, int blocks, cudaStream_t st);
+                       const uint32_t* order, float4* out, int blocks, cudaStream_t st);
 
 }  // namespace fclg

@@ -9,7 +9,8 @@
 //     in FP32: shape a's support gains the displacement when the direction
 //     points along it, its interior point half of it; the boolean is MPR's
 //     Intersect, the one-sample time of collision the origin's barycentric
-//     weights in the final portal (FP64 from the FP32 portal).
+//     weights in the final portal.  Pairs run in shape-class order (the
+//     bucketing of the distance query) so that a warp runs one support pair.
 //   * Box intervals (BoxPairTranslationalCCD::IsDisjoint, ccd/box_pair_ccd-
 //     inl.h:112-393) in FP64 with explicitly rounded operations (no fused
 //     multiply-add), so that the decision and the interval equal the FP64
@@ -210,46 +211,34 @@ __device__ bool obb_pair_disjoint(const ShapeDev& A, uint32_t ia, const ShapeDev
   return box_pair_disjoint(h1, u, dist, R, t, h2, zero_tol, iv);
 }
 
-// computeOneTocSampleForIntersection (gjk_ccd-inl.h:106-187) in FP64.
-__device__ double toc_sample(const MprPortal& P, f3 sweep) {
-  constexpr double kV0Phase = 0.5;
-  const double v0[3] = {P.v0.x, P.v0.y, P.v0.z};
+// computeOneTocSampleForIntersection (gjk_ccd-inl.h:106-187), in FP32 like
+// the portal it reads.
+__device__ float toc_sample(const MprPortal& P, f3 sweep) {
+  constexpr float kV0Phase = 0.5f;
   if (P.count < 1) return kV0Phase;
-  const double v1[3] = {P.v1.x, P.v1.y, P.v1.z};
-  const double w[3] = {sweep.x, sweep.y, sweep.z};
-  auto phase = [&](f3 d) { return dot3(d.x, d.y, d.z, w[0], w[1], w[2]) > 0.0 ? 1.0 : 0.0; };
+  auto phase = [&](f3 d) { return dot(d, sweep) > 0.f ? 1.f : 0.f; };
   if (P.count < 3) {
-    const double n0 = sqrt(dot3(v0[0], v0[1], v0[2], v0[0], v0[1], v0[2]));
-    const double n1 = sqrt(dot3(v1[0], v1[1], v1[2], v1[0], v1[1], v1[2]));
-    const double n01 = n0 + n1;
-    if (n01 <= 0.0) return kV0Phase;
-    return (n1 / n01) * kV0Phase + (n0 / n01) * phase(P.d1);
+    const float n0 = sqrtf(sqn(P.v0)), n1 = sqrtf(sqn(P.v1));
+    const float n01 = n0 + n1;
+    if (n01 <= 0.f) return kV0Phase;
+    return (n1 * kV0Phase + n0 * phase(P.d1)) / n01;
   }
-  const double v2[3] = {P.v2.x, P.v2.y, P.v2.z}, v3[3] = {P.v3.x, P.v3.y, P.v3.z};
-  auto vol = [](const double a[3], const double b[3], const double c[3]) {
-    const double x = a[1] * b[2] - a[2] * b[1], y = a[2] * b[0] - a[0] * b[2], z = a[0] * b[1] - a[1] * b[0];
-    return fabs(x * c[0] + y * c[1] + z * c[2]);
-  };
-  double a1[3], a2[3], a3[3], e2[3], e3[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    a1[k] = v1[k] - v0[k];
-    a2[k] = v2[k] - v0[k];
-    a3[k] = v3[k] - v0[k];
-    e2[k] = v2[k] - v1[k];
-    e3[k] = v3[k] - v1[k];
-  }
-  const double o012 = vol(a1, a2, v0), o013 = vol(a1, a3, v0), o023 = vol(a2, a3, v0), o123 = vol(e2, e3, v1);
-  const double total = ((o012 + o013) + o023) + o123;
-  if (total <= 0.0) return 0.0;
-  return ((o123 * kV0Phase + o023 * phase(P.d1)) + o013 * phase(P.d2) + o012 * phase(P.d3)) / total;
+  const f3 a1 = P.v1 - P.v0, a2 = P.v2 - P.v0, a3 = P.v3 - P.v0;
+  const float o012 = fabsf(dot(cross(a1, a2), P.v0));
+  const float o013 = fabsf(dot(cross(a1, a3), P.v0));
+  const float o023 = fabsf(dot(cross(a2, a3), P.v0));
+  const float o123 = fabsf(dot(cross(P.v2 - P.v1, P.v3 - P.v1), P.v1));
+  const float total = ((o012 + o013) + o023) + o123;
+  if (total <= 0.f) return 0.f;
+  return (((o123 * kV0Phase + o023 * phase(P.d1)) + o013 * phase(P.d2)) + o012 * phase(P.d3)) / total;
 }
 
 __global__ void __launch_bounds__(128, 4) ccd_pass(BatchArgs b, const float4* __restrict__ disp,
                                                    const float4* __restrict__ aabb, CcdParams prm,
-                                                   float4* __restrict__ out) {
+                                                   const uint32_t* __restrict__ order, float4* __restrict__ out) {
   const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x; pid < b.n_pairs; pid += stride) {
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < b.n_pairs; k += stride) {
+    const uint32_t pid = order ? __ldg(order + k) : k;
     const PairDev pr = load_pair(b.pairs, pid);
     uint32_t st = kCcdNoMpr;
     bool hit = false;
@@ -295,7 +284,7 @@ __global__ void __launch_bounds__(128, 4) ccd_pass(BatchArgs b, const float4* __
       if (!hit) {
         lo = hi = -1.f;
       } else if (prm.toc_type == kTocSample) {
-        lo = hi = (float)toc_sample(P, sup.sweep);
+        lo = hi = toc_sample(P, sup.sweep);
       }
     }
     out[pid] = make_float4(__uint_as_float(hit ? 1u : 0u), __uint_as_float(st), lo, hi);
@@ -334,9 +323,9 @@ cudaError_t launch_hull_aabbs(const int4* shapes, const float4* verts, uint32_t 
 }
 
 cudaError_t launch_ccd(const BatchArgs& b, const float4* disp, const float4* aabb, const CcdParams& prm,
-                       float4* out, int blocks, cudaStream_t st) {
+                       const uint32_t* order, float4* out, int blocks, cudaStream_t st) {
   if (b.n_pairs == 0) return cudaSuccess;
-  ccd_pass<<<blocks, 128, 0, st>>>(b, disp, aabb, prm, out);
+  ccd_pass<<<blocks, 128, 0, st>>>(b, disp, aabb, prm, order, out);
   return cudaGetLastError();
 }
 
