@@ -441,7 +441,7 @@ def run_mesh_shape(args):
     """Mesh-shape collides/s (fcl::collide(BVHModel, shape), its own JSON line)."""
     import torch
     from fclg import workloads
-    from fclg.api import Context, GpuMesh, mesh_shape_collide
+    from fclg.api import Context, GpuMesh, mesh_shape_collide, mesh_shape_contacts
     import ctypes
     rank, world, local = dist_env()
     dev = torch.device("cuda", local)
@@ -458,20 +458,22 @@ def run_mesh_shape(args):
     d_poses = torch.from_numpy(poses).to(dev)
     d_ids = torch.from_numpy(ids.view(np.int32)).to(dev)
     out = {}
-    for cap in (1, 64):
+    for key, cap, pen in ((1, 1, False), (64, 64, False), ("contacts", 1, True)):
         d_flags = torch.empty(n, dtype=torch.uint8, device=dev)
         d_counts = torch.empty(n, dtype=torch.int32, device=dev)
         d_tris = torch.empty(n * cap, dtype=torch.int32, device=dev)
         d_status = torch.empty(n, dtype=torch.int32, device=dev)
+        d_con = torch.empty(n * cap * 8, dtype=torch.float32, device=dev)
 
         def step():
-            rc = ctx.lib.fclg_mesh_shape_collide_device(ctx.h, gm.h, ctypes.c_void_p(d_ids.data_ptr()),
-                                                        ctypes.c_void_p(d_poses.data_ptr()), n, cap,
-                                                        ctypes.c_void_p(d_flags.data_ptr()),
-                                                        ctypes.c_void_p(d_counts.data_ptr()),
-                                                        ctypes.c_void_p(d_tris.data_ptr()),
-                                                        ctypes.c_void_p(d_status.data_ptr()),
-                                                        ctypes.c_void_p(stream.cuda_stream))
+            vp = ctypes.c_void_p
+            common = (ctx.h, gm.h, vp(d_ids.data_ptr()), vp(d_poses.data_ptr()), n, cap, vp(d_flags.data_ptr()),
+                      vp(d_counts.data_ptr()), vp(d_tris.data_ptr()))
+            if pen:
+                rc = ctx.lib.fclg_mesh_shape_contacts_device(*common, vp(d_con.data_ptr()), vp(d_status.data_ptr()),
+                                                             vp(stream.cuda_stream))
+            else:
+                rc = ctx.lib.fclg_mesh_shape_collide_device(*common, vp(d_status.data_ptr()), vp(stream.cuda_stream))
             assert rc == 0
         for _ in range(args.warmup):
             step()
@@ -490,9 +492,12 @@ def run_mesh_shape(args):
         status = d_status.cpu().numpy()
         t0 = time.perf_counter()
         for _ in range(max(1, args.steps // 2)):
-            mesh_shape_collide(ctx, gm, ids, poses, max_contacts=cap)
+            if pen:
+                mesh_shape_contacts(ctx, gm, ids, poses, max_contacts=cap)
+            else:
+                mesh_shape_collide(ctx, gm, ids, poses, max_contacts=cap)
         e2e_ms = (time.perf_counter() - t0) * 1e3 / max(1, args.steps // 2)
-        out[cap] = {"value": n / (ms * 1e-3), "ms_per_step": ms, "collide_fraction": float(flags.mean()),
+        out[key] = {"value": n / (ms * 1e-3), "ms_per_step": ms, "collide_fraction": float(flags.mean()),
                     "incomplete": int(np.sum(status != 0)), "e2e": n / (e2e_ms * 1e-3),
                     "gpu_launches": launches, "clocks": clk.summary()}
     import oracle
@@ -508,7 +513,7 @@ def run_mesh_shape(args):
             "ms_per_step": out[1]["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 (FP64 re-decision for sphere / box leaves)", "data": "synthetic",
             "config": {"workload": MESH_SHAPE_WORKLOAD, "queries": n, "first_contact": out[1],
-                       "contacts_64": out[64]},
+                       "contacts_64": out[64], "first_contact_with_penetration": out["contacts"]},
             "gpu_launches": out[1]["gpu_launches"], "clocks": out[1]["clocks"],
             "cpu_baseline": {"value": sample / cpu_s, "unit": "mesh-shape collides/s", "cores": threads,
                              "kind": "port", "sample": "first %d queries, first-contact mode" % sample},

@@ -424,6 +424,24 @@ int fclg_mesh_shape_collide_device(fclg_context* ctx, const fclg_mesh* mesh, con
                                    const float* d_poses, uint32_t n, uint32_t max_contacts, uint8_t* d_flags,
                                    uint32_t* d_counts, int32_t* d_tri_ids, uint32_t* d_status, void* stream);
 
+/* The same with penetration on (a CollisionRequest with contacts,
+   ShapePairIntersectSolver::ShapeSimplexIntersect, narrowphase/detail/
+   shape_pair_intersect-inl.h:132-170): leaves other than spheres decide by
+   GJK, and every reported triangle gets its contact in contacts[n][max_contacts]
+   [8]: pos (3, mesh frame), normal (3, reversed as the reference's mesh-shape
+   contact meta does, bvh_solver-inl.h:56-61), penetration depth, and status
+   bits as a float's bits (0-7: EPA status + 1, 0 for the closed-form sphere;
+   bit 8: GJK or EPA gave no contact, which the reference would not have
+   added).  Sphere leaves are sphereTriangleIntersect's contact (its depth is
+   -(r - distance), as the reference writes it). */
+int fclg_mesh_shape_contacts(fclg_context* ctx, const fclg_mesh* mesh, const uint32_t* shape_ids, const float* poses,
+                             uint32_t n, uint32_t max_contacts, uint8_t* flags, uint32_t* counts, int32_t* tri_ids,
+                             float* contacts, uint32_t* status);
+int fclg_mesh_shape_contacts_device(fclg_context* ctx, const fclg_mesh* mesh, const uint32_t* d_shape_ids,
+                                    const float* d_poses, uint32_t n, uint32_t max_contacts, uint8_t* d_flags,
+                                    uint32_t* d_counts, int32_t* d_tri_ids, float* d_contacts, uint32_t* d_status,
+                                    void* stream);
+
 /* ---- translational continuous collision --------------------------------
    Replaces fcl::translational_ccd(o1, tf1, o1_displacement, o2, tf2, request,
    result) (narrowphase/continuous_collision.h:13-19) on shape pairs, through

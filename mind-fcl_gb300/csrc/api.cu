@@ -727,9 +727,9 @@ int fclg_mesh_collide(fclg_context* c, const fclg_mesh* a, const fclg_mesh* b, c
   return FCLG_OK;
 }
 
-int fclg_mesh_shape_collide_device(fclg_context* c, const fclg_mesh* mesh, const uint32_t* d_shape_ids,
-                                   const float* d_poses, uint32_t n, uint32_t max_contacts, uint8_t* d_flags,
-                                   uint32_t* d_counts, int32_t* d_tri_ids, uint32_t* d_status, void* stream) {
+static int run_mesh_shape(fclg_context* c, const fclg_mesh* mesh, const uint32_t* d_shape_ids, const float* d_poses,
+                          uint32_t n, uint32_t max_contacts, uint8_t* d_flags, uint32_t* d_counts, int32_t* d_tri_ids,
+                          float* d_contacts, uint32_t* d_status, void* stream) {
   if (!c) return FCLG_E_INVALID;
   if (!mesh) return fail(c, FCLG_E_INVALID, "null mesh");
   if (n == 0) return FCLG_OK;
@@ -754,15 +754,36 @@ int fclg_mesh_shape_collide_device(fclg_context* c, const fclg_mesh* mesh, const
   m.counts = d_counts;
   m.tri_ids = d_tri_ids;
   m.status = d_status;
+  m.contacts = d_contacts;
   clear_pending_error();
   FCLG_CUDA(c, fclg::launch_mesh_shape(m, c->num_sms * 8, static_cast<cudaStream_t>(stream)));
   c->launches += 1;
+  if (d_contacts) {
+    FCLG_CUDA(c, fclg::launch_mesh_contacts(m, c->num_sms, static_cast<cudaStream_t>(stream)));
+    c->launches += 1;
+  }
   return FCLG_OK;
 }
 
-int fclg_mesh_shape_collide(fclg_context* c, const fclg_mesh* mesh, const uint32_t* shape_ids, const float* poses,
-                            uint32_t n, uint32_t max_contacts, uint8_t* flags, uint32_t* counts, int32_t* tri_ids,
-                            uint32_t* status) {
+int fclg_mesh_shape_collide_device(fclg_context* c, const fclg_mesh* mesh, const uint32_t* d_shape_ids,
+                                   const float* d_poses, uint32_t n, uint32_t max_contacts, uint8_t* d_flags,
+                                   uint32_t* d_counts, int32_t* d_tri_ids, uint32_t* d_status, void* stream) {
+  return run_mesh_shape(c, mesh, d_shape_ids, d_poses, n, max_contacts, d_flags, d_counts, d_tri_ids, nullptr,
+                        d_status, stream);
+}
+
+int fclg_mesh_shape_contacts_device(fclg_context* c, const fclg_mesh* mesh, const uint32_t* d_shape_ids,
+                                    const float* d_poses, uint32_t n, uint32_t max_contacts, uint8_t* d_flags,
+                                    uint32_t* d_counts, int32_t* d_tri_ids, float* d_contacts, uint32_t* d_status,
+                                    void* stream) {
+  if (c && n && !d_contacts) return fail(c, FCLG_E_INVALID, "null contact pointer");
+  return run_mesh_shape(c, mesh, d_shape_ids, d_poses, n, max_contacts, d_flags, d_counts, d_tri_ids, d_contacts,
+                        d_status, stream);
+}
+
+static int mesh_shape_host(fclg_context* c, const fclg_mesh* mesh, const uint32_t* shape_ids, const float* poses,
+                           uint32_t n, uint32_t max_contacts, uint8_t* flags, uint32_t* counts, int32_t* tri_ids,
+                           float* contacts, uint32_t* status) {
   if (!c) return FCLG_E_INVALID;
   if (n == 0) return FCLG_OK;
   if (!shape_ids || !poses || !flags || !counts || !tri_ids) return fail(c, FCLG_E_INVALID, "null pointer");
@@ -770,8 +791,8 @@ int fclg_mesh_shape_collide(fclg_context* c, const fclg_mesh* mesh, const uint32
   auto up16 = [](size_t x) { return (x + 15) & ~(size_t)15; };
   const size_t b_poses = up16((size_t)n * 48), b_ids = up16((size_t)n * 4), b_flags = up16(n),
                b_counts = up16((size_t)n * 4), b_tris = up16((size_t)n * max_contacts * 4),
-               b_status = up16((size_t)n * 4);
-  const size_t need = b_poses + b_ids + b_flags + b_counts + b_tris + b_status;
+               b_status = up16((size_t)n * 4), b_contacts = contacts ? up16((size_t)n * max_contacts * 32) : 0;
+  const size_t need = b_poses + b_ids + b_flags + b_counts + b_tris + b_status + b_contacts;
   if (need > c->mesh_io_bytes) {
     if (c->mesh_io) cudaFree(c->mesh_io);
     c->mesh_io = nullptr;
@@ -787,17 +808,34 @@ int fclg_mesh_shape_collide(fclg_context* c, const fclg_mesh* mesh, const uint32
   uint32_t* d_counts = reinterpret_cast<uint32_t*>(p += b_flags);
   int32_t* d_tris = reinterpret_cast<int32_t*>(p += b_counts);
   uint32_t* d_status = reinterpret_cast<uint32_t*>(p += b_tris);
+  float* d_contacts = contacts ? reinterpret_cast<float*>(p += b_status) : nullptr;
   FCLG_CUDA(c, cudaMemcpyAsync(d_poses, poses, (size_t)n * 48, cudaMemcpyHostToDevice, c->stream));
   FCLG_CUDA(c, cudaMemcpyAsync(d_ids, shape_ids, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
-  const int rc = fclg_mesh_shape_collide_device(c, mesh, d_ids, d_poses, n, max_contacts, d_flags, d_counts, d_tris,
-                                                d_status, c->stream);
+  const int rc = run_mesh_shape(c, mesh, d_ids, d_poses, n, max_contacts, d_flags, d_counts, d_tris, d_contacts,
+                                d_status, c->stream);
   if (rc) return rc;
+  if (contacts)
+    FCLG_CUDA(c, cudaMemcpyAsync(contacts, d_contacts, (size_t)n * max_contacts * 32, cudaMemcpyDeviceToHost,
+                                 c->stream));
   FCLG_CUDA(c, cudaMemcpyAsync(flags, d_flags, n, cudaMemcpyDeviceToHost, c->stream));
   FCLG_CUDA(c, cudaMemcpyAsync(counts, d_counts, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
   FCLG_CUDA(c, cudaMemcpyAsync(tri_ids, d_tris, (size_t)n * max_contacts * 4, cudaMemcpyDeviceToHost, c->stream));
   if (status) FCLG_CUDA(c, cudaMemcpyAsync(status, d_status, (size_t)n * 4, cudaMemcpyDeviceToHost, c->stream));
   FCLG_CUDA(c, cudaStreamSynchronize(c->stream));
   return FCLG_OK;
+}
+
+int fclg_mesh_shape_collide(fclg_context* c, const fclg_mesh* mesh, const uint32_t* shape_ids, const float* poses,
+                            uint32_t n, uint32_t max_contacts, uint8_t* flags, uint32_t* counts, int32_t* tri_ids,
+                            uint32_t* status) {
+  return mesh_shape_host(c, mesh, shape_ids, poses, n, max_contacts, flags, counts, tri_ids, nullptr, status);
+}
+
+int fclg_mesh_shape_contacts(fclg_context* c, const fclg_mesh* mesh, const uint32_t* shape_ids, const float* poses,
+                             uint32_t n, uint32_t max_contacts, uint8_t* flags, uint32_t* counts, int32_t* tri_ids,
+                             float* contacts, uint32_t* status) {
+  if (c && n && !contacts) return fail(c, FCLG_E_INVALID, "null contact pointer");
+  return mesh_shape_host(c, mesh, shape_ids, poses, n, max_contacts, flags, counts, tri_ids, contacts, status);
 }
 
 // ---------------------------------------------------------------------------

@@ -143,10 +143,10 @@ __device__ __forceinline__ float point_to_plane(f3 p, f3 a, f3 b, f3 c) {
   return fabsf(dot(n * (1.f / nl), a - p));
 }
 
-template <int FMAX, int VMAX>
+template <int FMAX, int VMAX, class Sup = MinkowskiSupport<32>>
 struct EpaWarp {
   EpaSmem<FMAX, VMAX>& P;
-  const MinkowskiSupport<32>& sup;
+  const Sup& sup;
   float tol;
   unsigned lane;
   int nv, hw, live, fs_top;

@@ -36,14 +36,23 @@ struct MeshShapeArgs {
   const float4* poses;        // 3 float4 per query: rotation row-major, translation
   uint32_t n;
   uint32_t max_contacts;      // >= 1
-  float gjk_tol;              // MPR leaves (GJKSolver defaults 1e-6, 128)
+  float gjk_tol;              // MPR / GJK leaves (GJKSolver defaults 1e-6, 128)
   int gjk_max_iter;
   uint8_t* flags;             // [n]
   uint32_t* counts;           // [n]
   int32_t* tri_ids;           // [n][max_contacts]
   uint32_t* status;           // [n] or null: bit 0 stack overflow, bit 1 round limit, bit 2 bad shape id
+  // penetration on: leaves other than spheres decide by GJK (the test that
+  // feeds EPA), and contacts[n][max_contacts][8] receive pos (3), normal (3),
+  // depth and the EPA status bits of each reported triangle
+  float* contacts = nullptr;
+  float epa_tol = 1e-6f;      // GJKSolver defaults: 256 faces, 255 iterations, 1e-6
+  int epa_max_iter = 255;
 };
 
 cudaError_t launch_mesh_shape(const MeshShapeArgs& m, int blocks, cudaStream_t st);
+// The contacts of the triangles a penetration-mode launch reported
+// (mesh_contact.cu): sphere leaves in closed form, the others by GJK + EPA.
+cudaError_t launch_mesh_contacts(const MeshShapeArgs& m, int num_sms, cudaStream_t st);
 
 }  // namespace fclg

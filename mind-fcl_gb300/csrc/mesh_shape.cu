@@ -18,6 +18,7 @@
 // vertices).  The sphere and box leaf tests run in FP32 and are re-decided in
 // FP64 when a comparison sits within its rounding bound, so their verdicts
 // equal the FP64 ones; the MPR leaves run in FP32.
+#include "gjk.cuh"
 #include "kernels.h"
 #include "mesh_common.cuh"
 #include "mesh_kernels.h"
@@ -237,6 +238,7 @@ __device__ void shape_box(const ShapeDev& s, const float4* __restrict__ verts, u
 
 }  // namespace
 
+template <bool PEN>
 __global__ void __launch_bounds__(kMsWarps * 32, FCLG_MESH_SHAPE_MINB) mesh_shape_kernel(MeshShapeArgs m) {
   __shared__ MsSmem smem_all[kMsWarps];
   MsSmem& S = smem_all[threadIdx.x >> 5];
@@ -321,6 +323,15 @@ __global__ void __launch_bounds__(kMsWarps * 32, FCLG_MESH_SHAPE_MINB) mesh_shap
                 if (shp.type == kSphere) {
                   const int v = sphere_tri32(shp.p0, X.t, P1, P2, P3);
                   hit = v >= 0 ? v == 1 : sphere_tri64(shp.p0, dd(X.t), dd(P1), dd(P2), dd(P3));
+                } else if (PEN) {
+                  // with penetration the leaf is GJK's verdict, the test EPA starts from
+                  // (shapeTriangleIntersectImplRun, gjk_solver-inl.h:335-341; the box's
+                  // specialisation defers to it when a contact is wanted, :434-449)
+                  MinkowskiSupport<1> s2 = sup;
+                  s2.B.vofs = 3 * tri;
+                  Simplex s0;
+                  hit = gjk_evaluate(s2, mk3(-1.f, 0.f, 0.f), m.gjk_tol, m.gjk_max_iter, false, s0).status ==
+                        kGjkIntersect;
                 } else if (shp.type == kBox) {
                   const f3 w1 = Xi.apply(P1), w2 = Xi.apply(P2), w3 = Xi.apply(P3);
                   const int v = box_tri32(mk3(shp.p0, shp.p1, shp.p2), w1, w2, w3);
@@ -385,7 +396,8 @@ __global__ void __launch_bounds__(kMsWarps * 32, FCLG_MESH_SHAPE_MINB) mesh_shap
 
 cudaError_t launch_mesh_shape(const MeshShapeArgs& m, int blocks, cudaStream_t st) {
   if (m.n == 0) return cudaSuccess;
-  mesh_shape_kernel<<<blocks, kMsWarps * 32, 0, st>>>(m);
+  if (m.contacts) mesh_shape_kernel<true><<<blocks, kMsWarps * 32, 0, st>>>(m);
+  else mesh_shape_kernel<false><<<blocks, kMsWarps * 32, 0, st>>>(m);
   return cudaGetLastError();
 }
 

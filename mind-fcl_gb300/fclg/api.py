@@ -38,6 +38,7 @@ EXPORTS = [
     "fclg_mesh_shape_collide", "fclg_mesh_shape_collide_device",
     "fclg_broadphase", "fclg_broadphase_device", "fclg_object_pairs_device", "fclg_broadphase_cross_device",
     "fclg_translational_ccd", "fclg_translational_ccd_device",
+    "fclg_mesh_shape_contacts", "fclg_mesh_shape_contacts_device",
 ]
 
 # translational CCD (fclg_displacement, fclg_ccd_request, fclg_ccd_result)
@@ -182,6 +183,10 @@ def load_library(path=LIB_PATH):
     lib.fclg_object_pairs_device.restype = i32
     lib.fclg_broadphase_cross_device.argtypes = [vp, vp, vp, u32, vp, vp, u32, vp, u32, vp, vp]
     lib.fclg_broadphase_cross_device.restype = i32
+    lib.fclg_mesh_shape_contacts.argtypes = [vp, vp, vp, vp, u32, u32, vp, vp, vp, vp, vp]
+    lib.fclg_mesh_shape_contacts.restype = i32
+    lib.fclg_mesh_shape_contacts_device.argtypes = [vp, vp, vp, vp, u32, u32, vp, vp, vp, vp, vp, vp]
+    lib.fclg_mesh_shape_contacts_device.restype = i32
     lib.fclg_translational_ccd.argtypes = [vp, vp, u32, vp, vp, vp]
     lib.fclg_translational_ccd.restype = i32
     lib.fclg_translational_ccd_device.argtypes = [vp, vp, u32, vp, vp, vp, vp]
@@ -551,6 +556,25 @@ def mesh_shape_collide(ctx, mesh, shape_ids, poses, max_contacts=1):
     ctx._check(ctx.lib.fclg_mesh_shape_collide(ctx.h, mesh.h, _ptr(ids), _ptr(p), n, max_contacts, _ptr(flags),
                                                _ptr(counts), _ptr(tris), _ptr(status)), "fclg_mesh_shape_collide")
     return flags, counts, tris, status
+
+
+def mesh_shape_contacts(ctx, mesh, shape_ids, poses, max_contacts=1):
+    """fcl::collide(mesh, shape) per query with penetration on.  Returns
+    (flags, counts, tri_ids [n, max_contacts], contacts [n, max_contacts, 8]
+    float32 = pos, normal, depth, status bits (view the last column as
+    uint32), status)."""
+    ids = np.ascontiguousarray(shape_ids, np.uint32)
+    p = np.ascontiguousarray(poses, np.float32).reshape(-1, 12)
+    n = len(p)
+    flags = np.zeros(n, np.uint8)
+    counts = np.zeros(n, np.uint32)
+    tris = np.full((n, max_contacts), -1, np.int32)
+    con = np.zeros((n, max_contacts, 8), np.float32)
+    status = np.zeros(n, np.uint32)
+    ctx._check(ctx.lib.fclg_mesh_shape_contacts(ctx.h, mesh.h, _ptr(ids), _ptr(p), n, max_contacts, _ptr(flags),
+                                                _ptr(counts), _ptr(tris), _ptr(con), _ptr(status)),
+               "fclg_mesh_shape_contacts")
+    return flags, counts, tris, con, status
 
 
 def mesh_collide(ctx, mesh_a, mesh_b, poses, max_contacts=1):

@@ -403,6 +403,27 @@ def mesh_shape_collide(nodes, tris, batch, shape_ids, poses, max_contacts=1, pai
     return flags, counts, out
 
 
+def mesh_shape_contacts(nodes, tris, batch, shape_ids, poses, max_contacts=1, pair_cap=None, threads=None):
+    """fcl::collide(mesh, shape) with penetration on: per query (counts,
+    tri_ids[n, pair_cap], contacts[n, pair_cap, 8] = pos, normal (mesh frame,
+    the reference's reversed normal), depth, EPA status or -1 for a sphere)."""
+    lib = _load()
+    s, v, _ = _prep(batch)
+    ids = np.ascontiguousarray(shape_ids, np.uint32)
+    poses = np.ascontiguousarray(poses, np.float32).reshape(-1, 12)
+    n = len(poses)
+    cap = pair_cap if pair_cap is not None else max(max_contacts, 1)
+    counts = np.zeros(n, np.uint32)
+    out = np.full((n, cap), -1, np.int32)
+    con = np.zeros((n, cap, 8))
+    nd = np.ascontiguousarray(nodes)
+    tr = np.ascontiguousarray(tris, np.float32)
+    assert lib.orc_mesh_shape_contacts(_ptr(nd), _ptr(tr), _ptr(s), len(s), _ptr(v), _ptr(ids), _ptr(poses), n,
+                                       int(max_contacts), cap, _ptr(counts), _ptr(out), _ptr(con),
+                                       threads or default_threads()) == 0
+    return counts, out, con
+
+
 def mesh_shape_all(tris, batch, shape_id, pose, cap=1 << 20):
     """Every colliding triangle of one query by brute force."""
     lib = _load()

@@ -453,6 +453,38 @@ int orc_mesh_shape_collide(const void* nodes, const float* tris, const void* sha
   return 0;
 }
 
+// Mesh-shape collide with penetration on: per query up to max_contacts
+// contacts (pair_cap slots per query): tri_ids, contacts[8] = pos, normal,
+// depth, EPA status (-1 for the closed-form sphere).
+int orc_mesh_shape_contacts(const void* nodes, const float* tris, const void* shapes, int n_shapes,
+                            const float* verts, const uint32_t* shape_ids, const float* poses, int n, int max_contacts,
+                            int pair_cap, uint32_t* counts, int32_t* tri_ids, double* contacts, int n_threads) {
+  const orc::MeshNode* nd = (const orc::MeshNode*)nodes;
+  const auto sh = makeShapes((const ShapeRec*)shapes, n_shapes, verts);
+  const orc::SolverParams sp;
+  parallelFor(n, n_threads, [&](int b, int e) {
+    std::vector<orc::MsContact> c;
+    for (int i = b; i < e; ++i) {
+      orc::Iso X;
+      for (int k = 0; k < 9; ++k) X.R[k] = poses[12 * (size_t)i + k];
+      X.t = orc::V3(poses[12 * (size_t)i + 9], poses[12 * (size_t)i + 10], poses[12 * (size_t)i + 11]);
+      const uint32_t si = shape_ids[i];
+      c.clear();
+      if (si < (uint32_t)n_shapes)
+        orc::meshShapeContacts(nd, tris, sh[si], X, max_contacts > 0 ? (size_t)max_contacts : SIZE_MAX, sp, c);
+      counts[i] = (uint32_t)c.size();
+      for (size_t k = 0; k < c.size() && k < (size_t)pair_cap; ++k) {
+        tri_ids[(size_t)pair_cap * i + k] = c[k].tri;
+        double* o = contacts + 8 * ((size_t)pair_cap * i + k);
+        for (int j = 0; j < 3; ++j) { o[j] = c[k].pos[j]; o[3 + j] = c[k].normal[j]; }
+        o[6] = c[k].depth;
+        o[7] = c[k].epa_status;
+      }
+    }
+  });
+  return 0;
+}
+
 // CollisionObject::computeAABB (narrowphase/collision_object-inl.h:141-154)
 // of object i = shape ids[i] posed by poses[i] (12 floats, world), in FP64:
 // out[6 i ..] = lo, hi.  The local box is computeBV<AABB>(shape, identity)

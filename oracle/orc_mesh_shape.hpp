@@ -18,6 +18,8 @@
 #pragma once
 
 #include <algorithm>
+#include <cmath>
+#include <limits>
 #include <vector>
 
 #include "orc_convex.hpp"
@@ -203,6 +205,133 @@ inline void meshShapeIntersect(const MeshNode* nodes, const float* tris, const S
     const int t = -(n.child + 1);
     if (shapeTriangleIntersect(s, X, tris + 12 * (size_t)t, sp)) {
       contacts.push_back(t);
+      if (contacts.size() >= max_contacts) return;
+    }
+  }
+}
+
+// ---------------------------------------------------- penetration contacts --
+// ShapePairIntersectSolver::ShapeSimplexIntersect with penetration on
+// (narrowphase/detail/shape_pair_intersect-inl.h:132-170) for a triangle: the
+// contact of shapeTriangleIntersect (gjk_solver-inl.h:305-375, 405-449), its
+// normal reversed by the mesh-shape contact meta (bvh_solver-inl.h:56-61,
+// shape_pair_intersect-inl.h:19-26).  pos and normal in the mesh frame.
+struct MsContact {
+  int tri = -1;
+  V3 pos, normal;
+  double depth = 0;
+  int epa_status = -1;  // -1: closed form (sphere)
+};
+
+// sphereTriangleIntersect with its outputs (sphere_triangle-inl.h:107-191).
+inline bool sphereTriangleContact(double radius, const V3& center, const V3& P1, const V3& P2, const V3& P3, V3& pos,
+                                  V3& normal_out, double& depth) {
+  V3 normal = normalized(cross(P2 - P1, P3 - P1));
+  const double rt = radius + std::numeric_limits<double>::epsilon();
+  double dist = dot(center - P1, normal);
+  if (dist < 0) {
+    dist = -dist;
+    normal = -normal;
+  }
+  if (!(dist < rt)) return false;
+  bool has = false;
+  V3 cp;
+  if (projectInTriangle(P1, P2, P3, normal, center)) {
+    has = true;
+    cp = center - normal * dist;
+  } else {
+    const double r2 = rt * rt;
+    V3 near;
+    if (segmentSqrDistance(P1, P2, center, near) < r2) { has = true; cp = near; }
+    if (segmentSqrDistance(P2, P3, center, near) < r2) { has = true; cp = near; }
+    if (segmentSqrDistance(P3, P1, center, near) < r2) { has = true; cp = near; }
+  }
+  if (!has) return false;
+  const V3 ctc = cp - center;
+  const double d2 = sqn(ctc);
+  if (!(d2 < rt * rt)) return false;
+  pos = cp;
+  if (d2 > 0) {
+    normal_out = normalized(ctc);
+    depth = -(radius - std::sqrt(d2));
+  } else {
+    normal_out = -normal;
+    depth = -radius;
+  }
+  return true;
+}
+
+inline bool shapeTriangleContact(const Shape& s, const Iso& X, const float* tri_xyzw, const SolverParams& sp,
+                                 MsContact& c) {
+  const V3 P1(tri_xyzw[0], tri_xyzw[1], tri_xyzw[2]), P2(tri_xyzw[4], tri_xyzw[5], tri_xyzw[6]),
+      P3(tri_xyzw[8], tri_xyzw[9], tri_xyzw[10]);
+  if (s.type == kSphere) {
+    V3 pos, nrm;
+    double depth;
+    if (!sphereTriangleContact(s.p[0], X.t, P1, P2, P3, pos, nrm, depth)) return false;
+    c.pos = pos;
+    c.normal = -nrm;
+    c.depth = depth;
+    c.epa_status = -1;
+    return true;
+  }
+  Iso inv;
+  for (int r = 0; r < 3; ++r)
+    for (int k = 0; k < 3; ++k) inv.R[3 * r + k] = X.R[3 * k + r];
+  inv.t = -inv.rot(X.t);
+  Shape tri;
+  tri.type = kTriangle;
+  tri.verts = tri_xyzw;
+  tri.nv = 3;
+  tri.interior = (P1 + P2 + P3) / 3.0;
+  MinkDiff md;
+  md.s0 = &s;
+  md.s1 = &tri;
+  md.to0 = inv;
+  GJK gjk(sp.gjk_max_iter, sp.gjk_tol);
+  Simplex smp;
+  if (gjk.Evaluate(md, smp, V3(-1, 0, 0), nullptr) != GJKStatus::Intersect) return false;
+  EPA epa(sp.epa_max_faces, sp.epa_max_iter, sp.epa_tol);
+  double depth = 0;
+  V3 p0, p1;
+  const EPAStatus es = epa.Evaluate(smp, md, depth, p0, p1);
+  if (es == EPAStatus::Failed) return false;
+  V3 n = p0 - p1;
+  if (sqn(n) <= 0) n = V3(0, 0, 1);
+  else normalize(n);
+  c.pos = X.apply((p0 + p1) * 0.5);
+  c.normal = -X.rot(n);
+  c.depth = depth;
+  c.epa_status = (int)es;
+  return true;
+}
+
+// MeshShapeIntersect with penetration on: the traversal of meshShapeIntersect,
+// each leaf adding its contact.
+inline void meshShapeContacts(const MeshNode* nodes, const float* tris, const Shape& s, const Iso& X,
+                              size_t max_contacts, const SolverParams& sp, std::vector<MsContact>& contacts) {
+  contacts.clear();
+  if (max_contacts == 0) return;
+  const MeshNode sb = shapeBox(s, X);
+  Mat3 I;
+  for (int k = 0; k < 9; ++k) I.m[k] = (k % 4 == 0) ? 1.0 : 0.0;
+  const double T0[3] = {0, 0, 0};
+  std::vector<int> stack{0};
+  while (!stack.empty()) {
+    const int id = stack.back();
+    stack.pop_back();
+    const MeshNode& n = nodes[id];
+    if (!obbOverlap(I, T0, sb, n)) continue;
+    if (n.child >= 0) {
+      stack.push_back(n.child);
+      stack.push_back(n.child + 1);
+      continue;
+    }
+    const int t = -(n.child + 1);
+    MsContact c;
+    if (shapeTriangleContact(s, X, tris + 12 * (size_t)t, sp, c)) {
+      c.tri = t;
+      contacts.push_back(c);
       if (contacts.size() >= max_contacts) return;
     }
   }

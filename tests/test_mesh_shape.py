@@ -188,3 +188,91 @@ def test_gpu_mesh_shape_vs_oracle(oracle_lib, small_mesh):
         gm.close()
     finally:
         ctx.close()
+
+
+def test_penetration_contacts_known_answers(oracle_lib):
+    """Contacts with penetration on (ShapeSimplexIntersect): a sphere of
+    radius 0.1 centred 0.05 above the triangle's face touches it at the foot
+    of the centre with the reference's depth -(r - distance) = -0.05 and the
+    reversed centre-to-contact normal +z; a box of sides (0.2, 0.1, 0.3)
+    centred 0.1 above the face sinks 0.05 into it (EPA): depth 0.05, normal
+    +z, contact midway between the box's bottom face and the triangle."""
+    nodes, tris = _one_triangle_mesh()
+    b = shape_set(sphere_r=0.1)
+    poses = np.zeros((2, 12), np.float32)
+    poses[:, [0, 4, 8]] = 1
+    poses[0, 9:] = (0.2, 0.2, 0.05)
+    poses[1, 9:] = (0.3, 0.3, 0.1)
+    counts, tri, con = oracle_lib.mesh_shape_contacts(nodes, tris, b, np.array([0, 1], np.uint32), poses,
+                                                      max_contacts=4)
+    assert list(counts) == [1, 1] and tri[0, 0] == 0 and tri[1, 0] == 0
+    assert np.allclose(con[0, 0, :3], (0.2, 0.2, 0.0), atol=1e-9)
+    assert np.allclose(con[0, 0, 3:6], (0, 0, 1), atol=1e-9)
+    assert abs(con[0, 0, 6] + 0.05) < 1e-9 and con[0, 0, 7] == -1
+    assert abs(con[1, 0, 6] - 0.05) < 1e-6 and np.allclose(con[1, 0, 3:6], (0, 0, 1), atol=1e-6)
+    assert abs(con[1, 0, 2] + 0.025) < 1e-6 and con[1, 0, 7] == 1  # EPA OK
+
+
+def test_penetration_mode_hits_match_boolean(oracle_lib, small_mesh):
+    """With penetration on, spheres report the same triangles as the boolean
+    collide (the same closed-form test); the GJK-decided leaves of the other
+    shapes differ from the SAT / MPR ones only within rounding of contact
+    (<= 1 % of queries), and every EPA contact's depth is >= 0."""
+    nodes, tris = small_mesh
+    b = shape_set()
+    ids, poses = queries(600, seed=33)
+    f, c, o = oracle_lib.mesh_shape_collide(nodes, tris, b, ids, poses, max_contacts=0, pair_cap=2048)
+    cc, oo, con = oracle_lib.mesh_shape_contacts(nodes, tris, b, ids, poses, max_contacts=0, pair_cap=2048)
+    sph = ids == 0
+    assert np.array_equal(c[sph], cc[sph])
+    assert np.mean(c != cc) <= 0.01
+    valid = np.arange(2048)[None, :] < cc[:, None]
+    epa = valid & ~sph[:, None]
+    assert np.all(con[epa][:, 6] >= 0)
+    assert np.all(con[valid & sph[:, None]][:, 6] <= 0)
+
+
+@pytest.mark.gpu
+def test_gpu_mesh_shape_contacts_vs_oracle(oracle_lib, small_mesh):
+    """fclg_mesh_shape_contacts against the oracle on the same tree, room for
+    every contact: triangle sets equal for spheres and for >= 99 % of the
+    other queries; on common (query, triangle) pairs sphere contacts within
+    1e-5 (position, depth) and 1e-4 (normal), EPA contacts with depth within
+    1e-4 m and normals within 1e-2 of the oracle's for >= 99 % (FP32 EPA)."""
+    from fclg.api import Context, GpuMesh, mesh_shape_contacts
+    m = workloads.geodesic_sphere(10, 0.3, 0.01, seed=1)
+    b = shape_set()
+    ids, poses = queries(2000, seed=34)
+    ctx = Context(0)
+    try:
+        ctx.set_batch(b)
+        gm = GpuMesh(ctx, m.vertices, m.triangles)
+        nodes, tris = gm.export()
+        cap = 1024
+        co, oo, cono = oracle_lib.mesh_shape_contacts(nodes, tris, b, ids, poses, max_contacts=0, pair_cap=cap)
+        fg, cg, og, cong, st = mesh_shape_contacts(ctx, gm, ids, poses, max_contacts=cap)
+        gm.close()
+    finally:
+        ctx.close()
+    assert np.all(st == 0)
+    sph = ids == 0
+    same = np.array([_sets(co, oo, i) == _sets(cg, og, i) for i in range(len(ids))])
+    assert same[sph].all()
+    assert same[~sph].mean() >= 0.99
+    gstat = cong[:, :, 7].view(np.uint32)
+    dp, dn, sp_err = [], [], []
+    for i in np.nonzero(same & (co > 0))[0]:
+        ref = {int(t): cono[i, k] for k, t in enumerate(oo[i, :co[i]])}
+        for k in range(cg[i]):
+            r = ref[int(og[i, k])]
+            g = cong[i, k].astype(np.float64)
+            if sph[i]:
+                sp_err.append(max(np.abs(g[:3] - r[:3]).max(), abs(g[6] - r[6]), np.abs(g[3:6] - r[3:6]).max() * 0.1))
+            elif (gstat[i, k] & 256) == 0:
+                dp.append(abs(g[6] - r[6]))
+                dn.append(np.linalg.norm(g[3:6] - r[3:6]))
+    assert len(sp_err) > 100 and max(sp_err) <= 1e-5
+    dp, dn = np.array(dp), np.array(dn)
+    assert len(dp) > 100
+    assert np.mean(dp <= 1e-4) >= 0.99 and np.mean(dn <= 1e-2) >= 0.99
+    assert np.mean((gstat[:, :][np.arange(cap)[None, :] < cg[:, None]] & 256) != 0) <= 0.005
