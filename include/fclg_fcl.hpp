@@ -33,6 +33,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <iostream>
 #include <memory>
 #include <stdexcept>
@@ -650,8 +651,6 @@ template <typename S, typename TFM, typename TFS>
 std::size_t mesh_shape_collide(const CollisionGeometry<S>* mesh, const TFM& tfm, const CollisionGeometry<S>* shape,
                                const TFS& tfs, bool mesh_first, const CollisionRequest<S>& req,
                                CollisionResult<S>& res) {
-  if (req.isPenetrationEnabled())
-    throw std::invalid_argument("fclg: mesh-shape contacts with penetration are not provided (boolean only)");
   using M = BVHModel<OBBRSS<S>>;
   const auto* m = static_cast<const M*>(mesh);
   fclg_context* ctx = thread_context();
@@ -669,10 +668,40 @@ std::size_t mesh_shape_collide(const CollisionGeometry<S>* mesh, const TFM& tfm,
   uint8_t flag = 0;
   uint32_t count = 0, status = 0;
   std::vector<int32_t> tri((std::size_t)cap, -1);
-  check(ctx, fclg_mesh_shape_collide(ctx, m->device_mesh(ctx), &id, pose, 1, cap, &flag, &count, tri.data(), &status),
-        "fclg_mesh_shape_collide");
-  for (uint32_t k = 0; k < count && res.numContacts() < req.maxNumContacts(); ++k)
-    res.addContact(mesh_first ? Contact<S>(mesh, shape, tri[k], -1) : Contact<S>(shape, mesh, -1, tri[k]));
+  // The reference runs a shape-first pair as the mesh-first one (collision-inl.h:90-99): contacts name the
+  // mesh as o1 either way.
+  (void)mesh_first;
+  if (!req.isPenetrationEnabled()) {
+    check(ctx, fclg_mesh_shape_collide(ctx, m->device_mesh(ctx), &id, pose, 1, cap, &flag, &count, tri.data(),
+                                       &status),
+          "fclg_mesh_shape_collide");
+    for (uint32_t k = 0; k < count && res.numContacts() < req.maxNumContacts(); ++k)
+      res.addContact(Contact<S>(mesh, shape, tri[k], -1));
+    return res.numContacts();
+  }
+  // penetration on: contacts (mesh frame) mapped to the world by the mesh's transform
+  std::vector<float> con((std::size_t)cap * 8);
+  check(ctx, fclg_mesh_shape_contacts(ctx, m->device_mesh(ctx), &id, pose, 1, cap, &flag, &count, tri.data(),
+                                      con.data(), &status),
+        "fclg_mesh_shape_contacts");
+  for (uint32_t k = 0; k < count && res.numContacts() < req.maxNumContacts(); ++k) {
+    const float* q = con.data() + 8 * (std::size_t)k;
+    uint32_t st;
+    std::memcpy(&st, q + 7, 4);
+    if (st & (1u << 8)) continue;  // GJK / EPA found no contact: the reference adds none
+    Contact<S> c(mesh, shape, tri[k], -1);
+    for (int i = 0; i < 3; ++i) {
+      double w = (double)tfm.translation()(i), nw = 0;
+      for (int j = 0; j < 3; ++j) {
+        w += (double)tfm.linear()(i, j) * (double)q[j];
+        nw += (double)tfm.linear()(i, j) * (double)q[3 + j];
+      }
+      c.pos[i] = (S)w;
+      c.normal[i] = (S)nw;
+    }
+    c.penetration_depth = (S)q[6];
+    res.addContact(c);
+  }
   return res.numContacts();
 }
 

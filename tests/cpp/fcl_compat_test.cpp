@@ -151,7 +151,24 @@ int main() {
   CHECK(collide(&m1, at(0, 0, 0), &ball, at(2.0, 0, 0), ms_req, res) == 0, "mesh-sphere apart");
   res.clear();
   CHECK(collide(&b1, at(0.9, 0, 0), &m1, at(0, 0, 0), ms_req, res) > 0, "box-mesh overlap");
-  for (const auto& c : res.getContacts()) CHECK(c.o2 == &m1 && c.b2 >= 0 && c.b2 < 8, "box-mesh triangle ids");
+  // a shape-first pair runs as the mesh-first one: the mesh is o1 (collision-inl.h:90-99)
+  for (const auto& c : res.getContacts()) CHECK(c.o1 == &m1 && c.b1 >= 0 && c.b1 < 8, "box-mesh triangle ids");
+
+  // with penetration: a sphere of radius 0.3 centred 1.1 along +x from the octahedron's centre dips 0.2
+  // into its vertex region; contacts carry a depth and a unit normal
+  CollisionRequest<S> ms_pen(4);
+  ms_pen.useDefaultPenetration();
+  res.clear();
+  CHECK(collide(&m1, at(0, 0, 0), &ball, at(1.1, 0, 0), ms_pen, res) > 0, "mesh-sphere contact");
+  for (const auto& c : res.getContacts()) {
+    const S nn = std::sqrt(c.normal[0] * c.normal[0] + c.normal[1] * c.normal[1] + c.normal[2] * c.normal[2]);
+    CHECK(std::fabs(nn - 1) < 1e-4 && c.penetration_depth < 0 && c.penetration_depth > -0.3,
+          "mesh-sphere contact depth %.5f normal %.5f", (double)c.penetration_depth, (double)nn);
+  }
+  res.clear();
+  CHECK(collide(&m1, at(0, 0, 0), &b1, at(0.9, 0, 0), ms_pen, res) > 0, "mesh-box contact");
+  for (const auto& c : res.getContacts())
+    CHECK(c.penetration_depth > 0 && c.penetration_depth < 1.0, "mesh-box depth %.5f", (double)c.penetration_depth);
 
   // translational CCD (test/ccd/test_shape_pair_interface.cpp): a sphere of
   // radius 0.1 moving 1 along +x towards a sphere of radius 0.125 at x = 0.6
