@@ -250,7 +250,8 @@ cudaError_t launch_mesh_contacts(const MeshShapeArgs& m, int num_sms, cudaStream
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  mesh_contact_kernel<<<num_sms * 2, kMcWarps * 32, mc_smem_bytes(), st>>>(m);
+  // three 4-warp CTAs of 74 KB fit an SM's shared memory
+  mesh_contact_kernel<<<num_sms * 3, kMcWarps * 32, mc_smem_bytes(), st>>>(m);
   return cudaGetLastError();
 }
 
