@@ -271,3 +271,35 @@ def test_gpu_ccd_vs_oracle(toc):
         h = m & (got["collide"] == 1)
         sd = oracle.signed_distance(workloads.Batch("moved", b.shapes, b.vertices, moved[h], {}))
         assert np.mean((sd["ok"] == 1) & (sd["distance"] <= 1e-4)) >= 0.995
+
+
+@pytest.mark.gpu
+def test_gpu_ccd_edge_cases():
+    """An empty batch is a no-op; a pair naming a shape outside the set gets
+    collide 0, no interval and status bit 4 (shape id out of range) while its
+    neighbours are unaffected; zero displacement reduces to the static
+    collide (MPR flags of the oracle's static boolean)."""
+    from fclg.api import Context
+    b, d = workloads.ccd(2000, seed=workloads.SEED_BASE + 94)
+    ctx = Context(0)
+    try:
+        ctx.set_batch(b)
+        assert len(ctx.translational_ccd(b.pairs[:0], d[:0])) == 0
+        bad = b.pairs.copy()
+        bad["shape_b"][::7] = len(b.shapes) + 5
+        got = ctx.translational_ccd(bad, d, toc_type=2)
+        ref = ctx.translational_ccd(b.pairs, d, toc_type=2)
+        z = d.copy()
+        z[:, 3] = 0.0
+        still = ctx.translational_ccd(b.pairs, z)
+    finally:
+        ctx.close()
+    m = np.zeros(len(bad), bool)
+    m[::7] = True
+    assert np.all(got["collide"][m] == 0) and np.all((got["status"][m] & 16) != 0)
+    assert np.all(got["toc_lower"][m] == -1)
+    assert np.array_equal(got.view(np.uint8).reshape(len(bad), -1)[~m], ref.view(np.uint8).reshape(len(bad), -1)[~m])
+    static = oracle.collide(b, analytic=False)
+    sd = oracle.signed_distance(b)["distance"]
+    clear = np.abs(sd) > 1e-6
+    assert np.mean(still["collide"][clear] == static["ok"][clear]) >= 0.999
