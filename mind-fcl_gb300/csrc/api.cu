@@ -1402,7 +1402,7 @@ int run_ccd(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_di
     order = bs.order;
   }
   FCLG_CUDA(c, fclg::launch_ccd(b, reinterpret_cast<const float4*>(d_disp), c->hull_aabb, prm, order,
-                                reinterpret_cast<float4*>(d_results), c->num_sms * c->gjk_ctas_per_sm, st));
+                                reinterpret_cast<float4*>(d_results), c->num_sms, st));
   c->launches += 1;
   return FCLG_OK;
 }

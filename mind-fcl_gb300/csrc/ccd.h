@@ -29,6 +29,6 @@ cudaError_t launch_hull_aabbs(const int4* shapes, const float4* verts, uint32_t 
 // aabb = the hull boxes (read by the approximate request), order = the pairs
 // in shape-class order (or null: index order), out[i] = fclg_ccd_result.
 cudaError_t launch_ccd(const BatchArgs& b, const float4* disp, const float4* aabb, const CcdParams& prm,
-                       const uint32_t* order, float4* out, int blocks, cudaStream_t st);
+                       const uint32_t* order, float4* out, int num_sms, cudaStream_t st);
 
 }  // namespace fclg

@@ -233,7 +233,11 @@ __device__ float toc_sample(const MprPortal& P, f3 sweep) {
   return (((o123 * kV0Phase + o023 * phase(P.d1)) + o013 * phase(P.d2)) + o012 * phase(P.d3)) / total;
 }
 
-__global__ void __launch_bounds__(128, 4) ccd_pass(BatchArgs b, const float4* __restrict__ disp,
+#ifndef FCLG_CCD_MINB
+#define FCLG_CCD_MINB 5
+#endif
+
+__global__ void __launch_bounds__(128, FCLG_CCD_MINB) ccd_pass(BatchArgs b, const float4* __restrict__ disp,
                                                    const float4* __restrict__ aabb, CcdParams prm,
                                                    const uint32_t* __restrict__ order, float4* __restrict__ out) {
   const uint32_t stride = gridDim.x * blockDim.x;
@@ -323,9 +327,10 @@ cudaError_t launch_hull_aabbs(const int4* shapes, const float4* verts, uint32_t 
 }
 
 cudaError_t launch_ccd(const BatchArgs& b, const float4* disp, const float4* aabb, const CcdParams& prm,
-                       const uint32_t* order, float4* out, int blocks, cudaStream_t st) {
+                       const uint32_t* order, float4* out, int num_sms, cudaStream_t st) {
   if (b.n_pairs == 0) return cudaSuccess;
-  ccd_pass<<<blocks, 128, 0, st>>>(b, disp, aabb, prm, order, out);
+  // persistent: FCLG_CCD_MINB CTAs on every SM
+  ccd_pass<<<num_sms * FCLG_CCD_MINB, 128, 0, st>>>(b, disp, aabb, prm, order, out);
   return cudaGetLastError();
 }
 
