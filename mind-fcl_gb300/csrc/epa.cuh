@@ -419,6 +419,65 @@ struct EpaWarp {
     // recycle the patch's slots (pushed above the older free slots)
     for (int k = (int)lane; k < n_rem; k += 32) P.freestk[fs_top + k] = P.patch[k];
     __syncwarp();
+    bool err = false;
+    if (n_hz <= 32 && n_rem <= 32) {
+      // the usual case, one horizon edge per lane: phases A-C below with the
+      // edge in registers
+      const int k = (int)lane;
+      const bool on = k < n_hz;
+      uint32_t a = 0, b = 0, g = 0, t = 0;
+      if (on) {
+        const uint32_t hs = P.hz_s[k], he = P.hz_e[k];
+        const uint32_t fvs = P.fv[hs];
+        a = fvert(fvs, (int)he);
+        b = fvert(fvs, (int)(he == 2 ? 0 : he + 1));
+        g = P.fadj[hs][he];
+        t = (k < avail) ? P.freestk[avail - 1 - k] : (uint32_t)(hw + (k - avail));
+        P.hz_slot[k] = (uint16_t)t;
+      }
+      __syncwarp();
+      if (k < n_rem) {
+        const uint32_t f = P.patch[k];
+        P.fn[f].w = INFINITY;
+        P.fkey[f] = INFINITY;
+      }
+      if (on) {
+        P.start_at[a] = kNoSlot;
+        P.start_at[b] = kNoSlot;
+      }
+      __syncwarp();
+      FCLG_EPA_PHASE(5);
+      if (on) {
+        write_face(t, a, b, vnew);
+        P.fmark[t] = 0;
+        P.fadj[t][0] = (uint16_t)g;
+        const uint32_t gv = P.fv[g];
+        int gj = -1;
+#pragma unroll
+        for (int h = 0; h < 3; ++h)
+          if (fvert(gv, h) == b && fvert(gv, (h + 1) % 3) == a) gj = h;
+        if (gj < 0) err = true;
+        else P.fadj[g][gj] = (uint16_t)t;
+        if (atomicCAS(&P.start_at[a], kNoSlot, t) != kNoSlot) err = true;
+      }
+      __syncwarp();
+      if (on) {
+        const uint32_t u = P.start_at[b];
+        if (u == kNoSlot) {
+          err = true;
+        } else {
+          P.fadj[t][1] = (uint16_t)u;
+          P.fadj[u][2] = (uint16_t)t;
+        }
+      }
+      __syncwarp();
+      FCLG_EPA_PHASE(6);
+      if (__any_sync(0xFFFFFFFFu, err)) return 2;
+      live = new_live;
+      fs_top = avail > n_hz ? avail - n_hz : 0;
+      hw += fresh;
+      return 0;
+    }
     // Phase A: endpoints and outside neighbours of the horizon edges (the
     // patch slots are overwritten below); slots popped from the free stack.
     constexpr int kPer = (FMAX + 8 + 31) / 32;
@@ -445,7 +504,6 @@ struct EpaWarp {
     __syncwarp();
     FCLG_EPA_PHASE(5);
     // Phase B: write the fan (a, b, new) and re-point the outside neighbours.
-    bool err = false;
     j = 0;
     for (int k = (int)lane; k < n_hz; k += 32, ++j) {
       const uint32_t t = P.hz_slot[k];
