@@ -371,10 +371,11 @@ struct EpaWarp {
     FCLG_EPA_PHASE(3);
     int lo = 0, hi = 1;
     for (int round = 0; round < FMAX && lo < hi; ++round) {
-      for (int k = lo + (int)lane; k < hi; k += 32) {
-        const uint32_t f = P.patch[k];
-#pragma unroll
-        for (int e = 0; e < 3; ++e) {
+      // one (patch face, edge) per lane
+      for (int ke = 3 * lo + (int)lane; ke < 3 * hi; ke += 32) {
+        const uint32_t f = P.patch[ke / 3];
+        {
+          const int e = ke % 3;
           const uint32_t g = P.fadj[f][e];
           uint32_t m = P.fmark[g];
           if (m != kVis && m != kHid) {
