@@ -175,7 +175,7 @@ CONVEX_WORKLOADS = {
 MLP_FLOP_PER_PAIR = 2.0 * (28 * 256 + 2 * 256 * 256 + 256 * 3)
 # DRAM bytes (read + write) of the two EPA launches of one mixed-workload query
 # at 10^6 pairs, from one ncu capture (profiles/epa_pass_mixed_1M.md)
-EPA_TRAFFIC_MIXED_1M = (369.110272 + 29.940224 + 16.344064 + 0.022016) * 1e6
+EPA_TRAFFIC_MIXED_1M = (367.640320 + 40.247040 + 15.708416 + 0.013824) * 1e6
 
 
 def _to_dev(torch, arr, dev):
