@@ -243,13 +243,10 @@ size_t mc_smem_bytes() { return (size_t)kMcWarps * sizeof(EpaSmem<kMcF, kMcV>); 
 
 cudaError_t launch_mesh_contacts(const MeshShapeArgs& m, int num_sms, cudaStream_t st) {
   if (m.n == 0 || !m.contacts) return cudaSuccess;
-  static bool attr = false;
-  if (!attr) {
-    const cudaError_t e = cudaFuncSetAttribute(mesh_contact_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)mc_smem_bytes());
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  // per launch: the attribute belongs to the current device, and contexts may sit on different devices
+  const cudaError_t e = cudaFuncSetAttribute(mesh_contact_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)mc_smem_bytes());
+  if (e != cudaSuccess) return e;
   // three 4-warp CTAs of 74 KB fit an SM's shared memory
   mesh_contact_kernel<<<num_sms * 3, kMcWarps * 32, mc_smem_bytes(), st>>>(m);
   return cudaGetLastError();
