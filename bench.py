@@ -577,11 +577,17 @@ def run_ccd(args):
     ms = max_over_ranks(torch, e0.elapsed_time(e1) / args.steps, dev, world)
     res = d_res.cpu().numpy().view(np.uint32).reshape(n, 4)
     hit = float(np.mean(res[:, 0] == 1))
-    # end to end: host arrays through fclg_translational_ccd (copies inside)
+    # end to end: pinned host arrays through fclg_translational_ccd (copies inside)
+    from fclg.api import CCD_RESULT_DTYPE
+    from fclg.layout import PAIR_DTYPE
+    h_pairs = torch.from_numpy(b.pairs.view(np.uint8).copy()).pin_memory().numpy().view(PAIR_DTYPE)
+    h_disp = torch.from_numpy(disp.copy()).pin_memory().numpy()
+    h_out = torch.zeros(n * CCD_RESULT_DTYPE.itemsize, dtype=torch.uint8).pin_memory().numpy().view(CCD_RESULT_DTYPE)
+    ctx.translational_ccd(h_pairs, h_disp, toc_type=FCLG_TOC_SAMPLE, out=h_out)
     t0 = time.perf_counter()
     e2e_steps = max(1, args.steps // 2)
     for _ in range(e2e_steps):
-        ctx.translational_ccd(b.pairs, disp, toc_type=FCLG_TOC_SAMPLE)
+        ctx.translational_ccd(h_pairs, h_disp, toc_type=FCLG_TOC_SAMPLE, out=h_out)
     e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
     hbm, src = peaks()
     achieved = n * CCD_ALGO_BYTES / (ms * 1e-3) / 1e9

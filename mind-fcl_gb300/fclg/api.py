@@ -340,14 +340,17 @@ class Context:
         return out
 
     def translational_ccd(self, pairs, disp, toc_type=FCLG_TOC_NONE, max_gjk_iterations=0, gjk_tolerance=0.0,
-                          zero_movement_tolerance=0.0):
+                          zero_movement_tolerance=0.0, out=None):
         """fcl::translational_ccd on every pair, host arrays: disp = DISP_DTYPE rows or
-        float[n][4] (unit axis in shape a's frame, distance); CCD_RESULT_DTYPE out."""
+        float[n][4] (unit axis in shape a's frame, distance); CCD_RESULT_DTYPE out (or
+        written into `out`, e.g. a pinned array)."""
         p = np.ascontiguousarray(pairs, PAIR_DTYPE)
         d = np.ascontiguousarray(disp, np.float32).reshape(-1, 4) if not isinstance(disp, np.ndarray) or \
             disp.dtype != DISP_DTYPE else np.ascontiguousarray(disp).view(np.float32).reshape(-1, 4)
         assert len(d) == len(p)
-        out = np.zeros(len(p), CCD_RESULT_DTYPE)
+        if out is None:
+            out = np.zeros(len(p), CCD_RESULT_DTYPE)
+        assert out.dtype == CCD_RESULT_DTYPE and len(out) == len(p) and out.flags.c_contiguous
         req = CcdRequest(toc_type, max_gjk_iterations, gjk_tolerance, 0, zero_movement_tolerance)
         self._check(self.lib.fclg_translational_ccd(self.h, _ptr(p), len(p), _ptr(d), ctypes.byref(req), _ptr(out)),
                     "fclg_translational_ccd")

@@ -276,3 +276,16 @@ def test_gpu_mesh_shape_contacts_vs_oracle(oracle_lib, small_mesh):
     assert len(dp) > 100
     assert np.mean(dp <= 1e-4) >= 0.99 and np.mean(dn <= 1e-2) >= 0.99
     assert np.mean((gstat[:, :][np.arange(cap)[None, :] < cg[:, None]] & 256) != 0) <= 0.005
+    # first-contact mode: at most one contact, a triangle of the oracle's set, its contact as above
+    ctx = Context(0)
+    try:
+        ctx.set_batch(b)
+        gm = GpuMesh(ctx, m.vertices, m.triangles)
+        f1, c1, o1, con1, st1 = mesh_shape_contacts(ctx, gm, ids, poses, max_contacts=1)
+        gm.close()
+    finally:
+        ctx.close()
+    assert np.all(st1 == 0) and np.all(c1 <= 1)
+    hit = (c1 == 1) & (co > 0)
+    assert np.mean(f1[sph] == (co[sph] > 0)) == 1.0
+    assert all(int(o1[i, 0]) in _sets(co, oo, i) for i in np.nonzero(hit & sph)[0])
