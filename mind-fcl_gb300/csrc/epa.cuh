@@ -60,6 +60,27 @@ constexpr int kEpaOverflow = 16;
 // convergence tolerance.
 constexpr float kVisEps = 0.1f;
 
+// A pair's support data, one copy per warp in shared memory (read by
+// broadcast) instead of one per lane in local memory.
+struct EpaPairData {
+  ShapeDev A, B;
+  Pose pose;
+  const float4* verts;
+};
+
+// Support of A - B (MinkowskiSupport<32>'s) over the warp, reading the pair
+// from shared memory.
+struct SharedSupport32 {
+  const EpaPairData* d;
+  __device__ __forceinline__ void operator()(f3 dir, f3& pa, f3& pb) const {
+    const Group<32> g = Group<32>::make();
+    const ShapeDev A = d->A, B = d->B;
+    const Pose X = d->pose;
+    pa = shape_support<32>(A, d->verts, dir, g);
+    pb = X.apply(shape_support<32>(B, d->verts, X.rotT(-dir), g));
+  }
+};
+
 template <int FMAX, int VMAX>
 struct EpaSmem {
   float4 fn[FMAX];         // outward unit normal xyz, plane distance (inf: dead or degenerate)
@@ -77,6 +98,7 @@ struct EpaSmem {
   uint16_t hz_slot[FMAX + 8];
   uint32_t npatch;
   uint32_t nhz;             // horizon edges found by the flood fill
+  EpaPairData pair;         // the pair being run (SharedSupport32)
 };
 
 __device__ __forceinline__ uint32_t fvert(uint32_t packed, int k) { return (packed >> (8 * k)) & 0xFFu; }

@@ -43,13 +43,15 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) epa_pass(BatchArgs b, QueryP
       spb[i] = mk3(f[4 + 6 * i], f[5 + 6 * i], f[6 + 6 * i]);
     }
     const PairDev pr = load_pair(b.pairs, pid);
-    MinkowskiSupport<32> sup;
-    sup.A = load_shape(b.shapes, pr.a);
-    sup.B = load_shape(b.shapes, pr.b);
-    sup.pose = pr.pose;
-    sup.verts = b.verts;
-    sup.g = Group<32>::make();
-    EpaWarp<FMAX, VMAX> E{P, sup, prm.epa_tol, lane, 0, 0, 0, 0, 0u};
+    if (lane == 0) {
+      P.pair.A = load_shape(b.shapes, pr.a);
+      P.pair.B = load_shape(b.shapes, pr.b);
+      P.pair.pose = pr.pose;
+      P.pair.verts = b.verts;
+    }
+    __syncwarp();
+    const SharedSupport32 sup{&P.pair};
+    EpaWarp<FMAX, VMAX, SharedSupport32> E{P, sup, prm.epa_tol, lane, 0, 0, 0, 0, 0u};
     const EpaResult er =
         E.run(rank < 1 ? 1 : (rank > 4 ? 4 : rank), spa, spb, prm.epa_max_iter, max_faces, final_layout);
     if (lane == 0) {
