@@ -70,6 +70,7 @@ def parse():
                          "warm-start inference kernel alone on 2.24M arm pairs; ccd: translational continuous "
                          "collision of 1M mixed pairs")
     ap.add_argument("--no-warm", action="store_true", help="skip the warm-start comparison")
+    ap.add_argument("--no-mesh", action="store_true", help="skip the mesh-mesh block of the default line")
     ap.add_argument("--poses", type=int, default=65536)
     ap.add_argument("--configs", type=int, default=100_000, help="arm: joint configurations (7 x 32 pairs each)")
     ap.add_argument("--objects", type=int, default=100_000, help="scene: posed objects")
@@ -208,7 +209,7 @@ WARM_CASES = {
     # name: (training batch on held-out seeds, test batch, embedding classes)
     "mixed": (lambda w: w.mixed(2_000_000, seed=w.SEED_BASE + 1001), lambda w, a: w.mixed(a.pairs),
               lambda w: w.MIXED_CLASSES),
-    "arm": (lambda w: w.arm(9000, seed=w.SEED_BASE + 1003), lambda w, a: w.arm(10000), lambda w: w.ARM_CLASSES),
+    "arm": (lambda w: w.arm(9000, seed=w.SEED_BASE + 1003), lambda w, a: w.arm(a.configs), lambda w: w.ARM_CLASSES),
     "pareto": (lambda w: w.pareto(2_000_000, seed=w.SEED_BASE + 1004), lambda w, a: w.pareto(),
                lambda w: w.PARETO_CLASSES),
 }
@@ -255,6 +256,16 @@ def warm_start_block(args, torch, dev, stream, local, names):
         tuning_w, _ = ctx.autotune(d_te.data_ptr(), n, d_tmp.data_ptr(), request=make_request(flags=4))
         ms_w, rw = _time_queries(torch, ctx, d_te, n, 4, args.steps, args.warmup, stream, dev)
         tuning = {"plain": tuning_p, "warm": tuning_w}
+        # per-pass device times of both requests (events on the launch stream)
+        pass_ms = {}
+        for side, flags, tune in (("plain", 0, tuning_p), ("warm", 4, tuning_w)):
+            ctx.set_tuning(**tune)
+            ctx.set_profiling(True)
+            ctx.pass_times(reset=True)
+            _time_queries(torch, ctx, d_te, n, flags, 3, 1, stream, dev)
+            g_ms, e_ms, nq = ctx.pass_times(reset=True)
+            ctx.set_profiling(False)
+            pass_ms[side] = {"gjk_pass_ms": g_ms / max(nq, 1), "epa_pass_ms": e_ms / max(nq, 1)}
         del d_tmp
         # the tcgen05 inference kernel alone
         d_g = torch.empty(n * 3, dtype=torch.float32, device=dev)
@@ -276,6 +287,16 @@ def warm_start_block(args, torch, dev, stream, local, names):
         sep = (dp > 0) & (rp["ok"] == 1)
         err = np.abs(dp - dw)[sep]
         band = np.abs(dp) > 1e-6
+        # both answers against the exact distance: the FP64 oracle run to a
+        # 1e-12 tolerance on an evenly spaced subsample
+        import oracle
+        oracle.build()
+        sub = np.arange(0, n, max(1, n // 20000))
+        exact = oracle.signed_distance(test.subset(sub), gjk_max_iter=1000, gjk_tol=1e-12)
+        both = sep[sub] & (exact["ok"] == 1) & (exact["distance"] > 0)
+        ex = exact["distance"][both]
+        e_w = np.abs(dw[sub][both] - ex)
+        e_p = np.abs(dp[sub][both] - ex)
         tflops = MLP_FLOP_PER_PAIR * n / (ms_mlp * 1e-3) / 1e12
         out[name] = {
             "pairs": n, "train_samples": int(len(keep)), "train_epochs": 8, "train_s": round(train_s, 3),
@@ -287,6 +308,14 @@ def warm_start_block(args, torch, dev, stream, local, names):
             "flag_mismatches_outside_band": int(np.sum(((dp < 0) != (dw < 0)) & band)),
             "separation_diff_p99_5": float(np.percentile(err, 99.5)) if len(err) else 0.0,
             "separation_diff_max": float(err.max()) if len(err) else 0.0,
+            "separation_err_vs_exact": {
+                "pairs": int(both.sum()),
+                "warm_max": float(e_w.max()) if len(e_w) else 0.0,
+                "plain_max": float(e_p.max()) if len(e_p) else 0.0,
+                "warm_over_1e-5": int(np.sum(e_w > 1e-5)), "plain_over_1e-5": int(np.sum(e_p > 1e-5)),
+                "exact": "FP64 oracle, GJK tolerance 1e-12, 1000 iterations"},
+            "overlap_bit_identical": bool(np.array_equal(dp[dp < 0], dw[dp < 0])),
+            "pass_ms": pass_ms,
             "mlp_kernel": "tcgen05 (TMEM accumulators, bulk-async weight staging)", "mlp_ms": ms_mlp,
             "mlp_tflops": tflops, "mlp_frac": tflops / peak, "mlp_peak_source": peak_kind,
             "tuning": tuning,
@@ -316,6 +345,12 @@ def cpu_baseline(batch, threads):
 
 
 def run_reference(args):
+    """The reference's CPU path on the same 1M-pair batch, every step the whole
+    batch: GJKSolver::shapeSignedDistance in the FP64 restatement (bit-identical
+    to the reference compiled from its sources, tests/test_oracle.py) on all
+    host threads, hulls above 32 vertices walking their edge graphs as
+    fcl::Convex does (tables built outside the clock, as fcl::Convex builds
+    them at construction)."""
     rank, world, local = dist_env()
     if rank != 0:
         return 0
@@ -324,25 +359,25 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     import oracle
     oracle.build()
-    sample = batch.subset(np.arange(min(CPU_SAMPLE_PAIRS // 2, batch.n_pairs)))
-    walk = oracle.walk_tables(sample)
-    warm = sample.subset(np.arange(min(5000, sample.n_pairs)))
+    walk = oracle.walk_tables(batch)
+    warm = batch.subset(np.arange(min(20000, batch.n_pairs)))
     warm_walk = oracle.walk_tables(warm)
     for _ in range(max(args.warmup, 1)):
         oracle.time_signed_distance(warm, threads=threads, walk=warm_walk)
     total = 0.0
     for _ in range(args.steps):
-        secs, _ = oracle.time_signed_distance(sample, threads=threads, walk=walk)
+        secs, _ = oracle.time_signed_distance(batch, threads=threads, walk=walk)
         total += secs
-    value = sample.n_pairs * args.steps / total
+    value = batch.n_pairs * args.steps / total
     line = {
         "impl": "reference", "metric": BASELINE_METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "pairs_per_step": sample.n_pairs, "seed": batch.meta["seed"]},
+        "config": {"workload": WORKLOAD, "pairs_per_gpu": batch.n_pairs, "seed": batch.meta["seed"]},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "first %d pairs of the 1M mixed batch per step; hulls above 32 vertices "
-                                   "hill-climb their edge graphs as fcl::Convex does" % sample.n_pairs},
+                         "sample": "the whole %d-pair mixed batch every step (warm-up steps on its first %d "
+                                   "pairs); hulls above 32 vertices hill-climb their edge graphs as fcl::Convex "
+                                   "does" % (batch.n_pairs, warm.n_pairs)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -354,23 +389,42 @@ MESH_WORKLOAD = ("mesh-mesh BVH: two geodesic spheres of 50,000 triangles (radiu
                  "a 0.8 m ball, uniform rotation); boolean collide, first-contact and 64-contact modes")
 
 
-def run_mesh(args):
-    """BVH collides/s on the mesh-mesh workload (its own JSON line)."""
-    import torch
+def l2_copy_peak(torch, dev, stream):
+    """Copy bandwidth of a working set that stays in L2 (16 MB read + 16 MB
+    written, best of 50 back-to-back copies, CUDA events): the L2 analogue of
+    the HBM copy peak, measured here because no L2 figure is recorded."""
+    a = torch.empty(16 << 20, dtype=torch.uint8, device=dev)
+    b = torch.empty_like(a)
+    for _ in range(10):
+        b.copy_(a)
+    torch.cuda.synchronize(dev)
+    best = float("inf")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(50):
+        e0.record(stream)
+        b.copy_(a)
+        e1.record(stream)
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return 2 * a.numel() / (best * 1e-3) / 1e9
+
+
+def mesh_block(args, torch, dev, stream, local):
+    """BVH collides/s on the mesh-mesh workload, first-contact and 64-contact
+    modes: device-resident (events on the launch stream), end to end through
+    the host entry point, an L2 roofline from the kernel's own work counters
+    and the CPU baseline (the reference's traversal restated in FP64 over the
+    reference's own tree, all host threads)."""
     from fclg import workloads
-    from fclg.api import GpuMesh, mesh_collide
-    from fclg.api import Context
+    from fclg.api import Context, GpuMesh, mesh_collide
     import ctypes
-    rank, world, local = dist_env()
-    dev = torch.device("cuda", local)
-    torch.cuda.set_device(dev)
     ma, mb = workloads.mesh_pair()
     poses = workloads.mesh_poses(args.poses)
     ctx = Context(local)
     ga, gb = GpuMesh(ctx, ma.vertices, ma.triangles), GpuMesh(ctx, mb.vertices, mb.triangles)
-    stream = torch.cuda.current_stream(dev)
     n = len(poses)
     d_poses = torch.from_numpy(poses).to(dev)
+    l2_peak = l2_copy_peak(torch, dev, stream)
     out = {}
     for cap in (1, 64):
         d_flags = torch.empty(n, dtype=torch.uint8, device=dev)
@@ -386,9 +440,10 @@ def run_mesh(args):
                                                   ctypes.c_void_p(d_status.data_ptr()),
                                                   ctypes.c_void_p(stream.cuda_stream))
             assert rc == 0
-        for _ in range(args.warmup):
+        for _ in range(max(args.warmup, 3)):
             step()
         torch.cuda.synchronize(dev)
+        launches0 = ctx.launch_count
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(args.steps):
@@ -396,38 +451,77 @@ def run_mesh(args):
         e1.record(stream)
         torch.cuda.synchronize(dev)
         ms = e0.elapsed_time(e1) / args.steps
+        launches = ctx.launch_count - launches0
         flags = d_flags.cpu().numpy()
         status = d_status.cpu().numpy()
+        # the kernel's work for the roofline: one profiled step
+        ctx.set_profiling(True)
+        ctx.mesh_traffic(reset=True)
+        step()
+        node_pairs, tri_pairs = ctx.mesh_traffic(reset=True)
+        ctx.set_profiling(False)
+        algo = node_pairs * 128 + tri_pairs * 96
+        achieved = algo / (ms * 1e-3) / 1e9
         # end to end through the host entry point
-        t0 = time.perf_counter()
-        for _ in range(max(1, args.steps // 2)):
+        for _ in range(2):
             mesh_collide(ctx, ga, gb, poses, max_contacts=cap)
-        e2e_ms = (time.perf_counter() - t0) * 1e3 / max(1, args.steps // 2)
+        t0 = time.perf_counter()
+        reps = max(1, args.steps // 2)
+        for _ in range(reps):
+            mesh_collide(ctx, ga, gb, poses, max_contacts=cap)
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / reps
         out[cap] = {"value": n / (ms * 1e-3), "ms_per_step": ms, "collide_fraction": float(flags.mean()),
-                    "incomplete": int(np.sum(status != 0)), "e2e": n / (e2e_ms * 1e-3)}
-    # CPU baseline: the restated reference traversal over the same trees
+                    "mean_contacts": float(d_counts.float().mean().item()), "incomplete": int(np.sum(status != 0)),
+                    "gpu_launches": launches,
+                    "e2e": {"value": n / (e2e_ms * 1e-3), "unit": "BVH collides/s", "h2d_bytes_per_step": n * 48,
+                            "d2h_bytes_per_step": n * (1 + 4 + cap * 8 + 4)},
+                    "roofline": {"bound": "l2", "achieved": achieved, "peak": l2_peak, "unit": "GB/s",
+                                 "frac": achieved / l2_peak, "traffic": None,
+                                 "algorithmic_bytes": "%d node pairs x 128 B + %d triangle pairs x 96 B per launch"
+                                                      % (node_pairs, tri_pairs),
+                                 "peak_source": "L2-resident copy (16 MB + 16 MB) measured by bench.py"}}
+    # CPU baseline: the reference's traversal restated over the reference's own tree
     import oracle
     oracle.build()
-    na, ta = ga.export()
-    nb, tb = gb.export()
-    sample = poses[:4096]
     threads = os.cpu_count() or 1
+    A = (ma.vertices.astype(np.float64), ma.triangles)
+    B = (mb.vertices.astype(np.float64), mb.triangles)
+    sample = poses[:8192].astype(np.float64)
+    oracle.orc_mesh_collide_ref(A, B, sample[:256], 1, threads=threads)
     t0 = time.perf_counter()
-    oracle.mesh_collide(na, ta, nb, tb, sample, max_contacts=1, threads=threads)
+    oracle.orc_mesh_collide_ref(A, B, sample, 1, threads=threads)
     cpu_s = time.perf_counter() - t0
-    line = {"metric": BASELINE_METRIC, "value": out[1]["value"], "unit": "BVH collides/s", "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": out[1]["ms_per_step"],
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 triangle fallback)",
-            "data": "synthetic",
-            "config": {"workload": MESH_WORKLOAD, "poses": n, "first_contact": out[1], "contacts_64": out[64]},
-            "cpu_baseline": {"value": len(sample) / cpu_s, "unit": "BVH collides/s", "cores": threads,
-                             "kind": "port", "sample": "first %d poses, first-contact mode" % len(sample)},
-            "e2e": {"value": out[1]["e2e"], "unit": "BVH collides/s", "h2d_bytes_per_step": n * 48,
-                    "d2h_bytes_per_step": n * (1 + 4 + 8 + 4)}}
-    print(json.dumps(line))
     ga.close()
     gb.close()
     ctx.close()
+    return {"workload": MESH_WORKLOAD, "poses": n, "unit": "BVH collides/s", "first_contact": out[1],
+            "contacts_64": out[64],
+            "cpu_baseline": {"value": len(sample) / cpu_s, "unit": "BVH collides/s", "cores": threads,
+                             "kind": "port",
+                             "sample": "first %d poses, first-contact mode, the reference's MeshIntersect restated "
+                                       "in FP64 over its own OBBRSS trees (tree build outside the clock)"
+                                       % len(sample)}}
+
+
+def run_mesh(args):
+    """BVH collides/s on the mesh-mesh workload (its own JSON line)."""
+    import torch
+    rank, world, local = dist_env()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream(dev)
+    with ClockSampler(local) as clk:
+        m = mesh_block(args, torch, dev, stream, local)
+    fc = m["first_contact"]
+    line = {"metric": BASELINE_METRIC, "value": fc["value"], "unit": "BVH collides/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": fc["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (FP64 triangle fallback)", "data": "synthetic",
+            "config": {"workload": m["workload"], "poses": m["poses"], "first_contact": fc,
+                       "contacts_64": m["contacts_64"]},
+            "gpu_launches": fc["gpu_launches"], "roofline": fc["roofline"], "cpu_baseline": m["cpu_baseline"],
+            "e2e": fc["e2e"], "clocks": clk.summary()}
+    print(json.dumps(line))
     return 0
 
 
@@ -915,8 +1009,8 @@ def main():
     ms = max_over_ranks(torch, ms, dev, world)
     value = job_value(n, world, ms)
     graph_ms = None
-    if n <= 65536 and world == 1:
-        # small batches are launch-bound: the same query replayed as one CUDA graph
+    if world == 1:
+        # the same query replayed as one CUDA graph (small batches are launch-bound)
         g = ctx.graph(d_pairs.data_ptr(), n, d_res.data_ptr())
         g.launch(stream.cuda_stream)
         torch.cuda.synchronize(dev)
@@ -1005,6 +1099,8 @@ def main():
         if not args.no_warm and args.workload in ("mixed", "arm", "pareto"):
             names = ["mixed", "arm"] if args.workload == "mixed" else [args.workload]
             line["config"]["warm_start"] = warm_start_block(args, torch, dev, stream, local, names)
+        if not args.no_mesh and args.workload == "mixed" and world == 1:
+            line["config"]["mesh"] = mesh_block(args, torch, dev, stream, local)
         print(json.dumps(line))
     ctx.close()
     if world > 1:

@@ -90,7 +90,19 @@ typedef struct fclg_request {
   uint32_t flags;               /* FCLG_REQ_* */
   float gjk_tolerance;          /* 0: 1e-6 (CollisionRequest::binaryCollisionTolerance) */
   float epa_tolerance;          /* 0: 1e-6 (CollisionRequest::distanceTolerance) */
-  float reserved[2];
+  /* FCLG_REQ_WARM_START only.  A pair keeps the run from its learned
+     direction only when that run certifies separation within warm_probe
+     support evaluations (0: 3) and certifies its distance: the run's stop on a
+     small improvement (gjk_distance.hpp:78-90) waits until the duality gap
+     |v| - v^.w of its last support is at most warm_gap (0: 5e-6 m), so the
+     distance is within warm_gap (plus FP32 rounding) of the exact one.  Every
+     other pair (overlapping, probe exhausted, no certified distance) is redone
+     from the plain direction under the same certified stop (overlapping pairs
+     so get the plain GJK simplex and the plain EPA answer), and a pair that
+     even then has no certified distance once more under the reference's own
+     stop. */
+  float warm_gap;
+  uint32_t warm_probe;
 } fclg_request;
 
 enum {
@@ -196,13 +208,18 @@ int fclg_collide_device(fclg_context* ctx, const fclg_pair* d_pairs, uint32_t n_
 
 /* Signed distance on device pointers without any allocation in the call (no
    counterpart in the reference, whose per-pair solver keeps its polytope on
-   the stack).  Same results as fclg_distance_device; the overlapping pairs
-   handed from the GJK pass to the EPA pass are kept in a fixed device array of
-   the library instead of context buffers, so n_pairs is at most
-   FCLG_STATIC_MAX_PAIRS (larger batches return FCLG_E_TOO_LARGE; split them).
-   The first call on a device sets that array up (an address lookup): make it
-   before any stream capture.  Calls on one device share the array, so calls
-   that overlap in time on that device race; order them on one stream. */
+   the stack).  It runs the GJK pass unbucketed with the context's small-pair
+   lane count: the same results as fclg_distance_device with bucketing off
+   (fclg_tuning.bucketing = -1), and within the convex parity bar of the
+   default bucketed launch.  The overlapping pairs handed from the GJK pass to
+   the EPA pass are kept in a fixed device array of the library instead of
+   context buffers, so n_pairs is at most FCLG_STATIC_MAX_PAIRS (larger
+   batches return FCLG_E_TOO_LARGE; split them).  The first call on a device
+   sets that array up (an address lookup, cached for the device's primary
+   context; not valid across cudaDeviceReset): make it before any stream
+   capture.  Calls on one device share the array, so calls that overlap in
+   time on that device race; order them on one stream.  With profiling on,
+   fclg_pass_times covers these calls too. */
 #define FCLG_STATIC_MAX_PAIRS 16384u
 int fclg_distance_device_static(fclg_context* ctx, const fclg_pair* d_pairs, uint32_t n_pairs,
                                 const fclg_request* req, fclg_result* d_results, void* stream);
@@ -326,6 +343,9 @@ typedef struct fclg_tuning {
   int32_t epa_ctas_per_sm;
   int32_t support_walk;         /* 1 on, -1 off, 0 unchanged */
   int32_t gjk_refill;           /* 1 on, -1 off, 0 unchanged */
+  int32_t epa_resume;           /* 1 on (default), -1 off, 0 unchanged: a pair whose EPA polytope
+                                   outgrows the 128-face layout continues in the 256-face layout
+                                   from where it stopped instead of starting over (same answers) */
 } fclg_tuning;
 int fclg_set_tuning(fclg_context* ctx, const fclg_tuning* tuning);
 int fclg_get_tuning(const fclg_context* ctx, fclg_tuning* tuning);
@@ -379,9 +399,22 @@ typedef struct fclg_mesh_node { /* 64 bytes */
 
 /* Builds the hierarchy on the host only (no device, no context): 2 x
    n_triangles - 1 nodes, root first, and the triangle soup
-   (n_triangles x 3 x xyzw floats).  Returns FCLG_OK or FCLG_E_INVALID. */
+   (n_triangles x 3 x xyzw floats).  The tree is the reference's own
+   (BVHModel<OBBRSS<double>>::endModel with the default mean splitter: same
+   node slots, children and leaf triangles, built in FP64 from the FP32
+   vertices); each stored FP32 box contains its triangles.  Returns FCLG_OK or
+   FCLG_E_INVALID. */
 int fclg_bvh_build(const float* vertices_xyz, uint32_t n_vertices, const int32_t* triangles, uint32_t n_triangles,
                    fclg_mesh_node* nodes, float* triangles_xyzw);
+
+/* The FP64 |extent|^2 of each node's box as the reference's
+   BVHModel<OBBRSS<double>> computes it (OBB::size, math/bv/OBB-inl.h:153-156;
+   the mesh traversal descends into the pair's node with the larger value,
+   bvh_solver-inl.h:150-151) and the tree's depth (deepest level, root 0), on
+   the host only.  sizes (nullable) holds 2 x n_triangles - 1 values.  Returns
+   FCLG_OK or FCLG_E_INVALID. */
+int fclg_bvh_node_sizes(const float* vertices_xyz, uint32_t n_vertices, const int32_t* triangles,
+                        uint32_t n_triangles, double* sizes, uint32_t* depth);
 
 /* Builds the hierarchy over triangles (3 vertex indices each) and uploads
    it to the context's device. */
@@ -396,15 +429,24 @@ int fclg_mesh_export(const fclg_mesh* mesh, fclg_mesh_node* nodes, float* triang
 /* Boolean collision of mesh b posed by poses[i] (rotation row-major, then
    translation: 12 floats, b in a's frame) against mesh a.  A pose stops after
    max_contacts colliding triangle pairs (CollisionRequest::num_max_contacts;
-   1 is first-contact mode).  Outputs per pose: flags (1 if colliding),
-   counts, pairs (max_contacts x 2 triangle ids of a and b) and, when not
-   NULL, status (bit 0: the traversal stack overflowed, the pair set may be
-   incomplete; bit 1: round limit). */
+   1 is first-contact mode): the first max_contacts in the reference's own
+   traversal order, listed in that order, i.e. the reference's contact list.
+   Outputs per pose: flags (1 if colliding), counts, pairs (max_contacts x 2
+   triangle ids of a and b) and, when not NULL, status (bit 0: the traversal
+   stack overflowed, the pair set may be incomplete; bit 1: round limit).
+   FCLG_E_TOO_LARGE when the two trees' depths sum above 62 (the traversal
+   orders node pairs by a 64-bit path key). */
 int fclg_mesh_collide(fclg_context* ctx, const fclg_mesh* a, const fclg_mesh* b, const float* poses, uint32_t n_poses,
                       uint32_t max_contacts, uint8_t* flags, uint32_t* counts, int32_t* pairs, uint32_t* status);
 int fclg_mesh_collide_device(fclg_context* ctx, const fclg_mesh* a, const fclg_mesh* b, const float* d_poses,
                              uint32_t n_poses, uint32_t max_contacts, uint8_t* d_flags, uint32_t* d_counts,
                              int32_t* d_pairs, uint32_t* d_status, void* stream);
+/* Work of the mesh-mesh queries run while profiling is on
+   (fclg_set_profiling): node pairs whose boxes were tested and triangle pairs
+   tested, summed since the last reset (reset = 1 clears them); the inputs of
+   the traversal's bytes (64 B per node read, 48 B per triangle read).
+   Synchronises the device.  No counterpart in the reference. */
+int fclg_mesh_traffic(fclg_context* ctx, uint64_t* node_pairs, uint64_t* triangle_pairs, int reset);
 
 /* Boolean collision of a mesh against shapes of the context (fcl::collide on
    a BVHModel<OBBRSS> and a shape with penetration off:

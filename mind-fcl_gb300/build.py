@@ -11,14 +11,18 @@ import sys
 PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
-BUILD = os.path.join(PKG, "_build")
-LIB_DIR = os.path.join(PKG, "lib")
+# FCLG_BUILD_TAG builds a variant beside the default one (_build_<tag>/,
+# lib_<tag>/), FCLG_NVCC_FLAGS adds flags (e.g. -D overrides of the launch
+# constants); fclg.api loads a variant through FCLG_LIB.
+_TAG = os.environ.get("FCLG_BUILD_TAG", "")
+BUILD = os.path.join(PKG, "_build" + ("_" + _TAG if _TAG else ""))
+LIB_DIR = os.path.join(PKG, "lib" + ("_" + _TAG if _TAG else ""))
 LIB = os.path.join(LIB_DIR, "libfclg.so")
 
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-         "-I", os.path.join(ROOT, "include"), "-I", CSRC]
+         "-I", os.path.join(ROOT, "include"), "-I", CSRC] + os.environ.get("FCLG_NVCC_FLAGS", "").split()
 
 
 def sources():

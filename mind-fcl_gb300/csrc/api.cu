@@ -49,6 +49,9 @@ struct fclg_context {
   uint32_t* epa_count = nullptr;  // [2]: work list, overflow list
   uint32_t* epa_list = nullptr;
   uint32_t* epa_ovf = nullptr;
+  unsigned char* epa_resume = nullptr;  // polytope states handed from the small EPA layout to the large one
+  uint32_t epa_resume_cap = 0;
+  bool epa_resume_on = true;
   float4* epa_rec = nullptr;
   size_t epa_cap = 0;
   // device staging of the host-pointer entry points
@@ -78,6 +81,11 @@ struct fclg_context {
   // device staging of the host-pointer mesh entry point
   void* mesh_io = nullptr;
   size_t mesh_io_bytes = 0;
+  // per-warp contact buffers of mesh-mesh requests above the shared-memory buffer
+  void* mesh_cbuf = nullptr;
+  size_t mesh_cbuf_bytes = 0;
+  // mesh-mesh traffic counters while profiling: node pairs and triangle pairs tested
+  unsigned long long* mesh_ctr = nullptr;
   // learned warm start: the model and its per-pair directions
   fclg_warmstart* ws = nullptr;
   float* guess = nullptr;
@@ -95,8 +103,10 @@ struct fclg_mesh {
   int device = 0;
   void* nodes = nullptr;
   void* tris = nullptr;
+  void* sizes = nullptr;  // FP64 |extent|^2 per node (the traversal's descend key)
   uint32_t n_nodes = 0;
   uint32_t n_tris = 0;
+  uint32_t depth = 0;     // deepest node level (root 0)
 };
 
 namespace {
@@ -238,15 +248,23 @@ int ensure_epa(fclg_context* c, size_t n) {
   if (c->epa_list) cudaFree(c->epa_list);
   if (c->epa_ovf) cudaFree(c->epa_ovf);
   if (c->epa_rec) cudaFree(c->epa_rec);
+  if (c->epa_resume) cudaFree(c->epa_resume);
   c->epa_list = nullptr;
   c->epa_ovf = nullptr;
   c->epa_rec = nullptr;
+  c->epa_resume = nullptr;
+  c->epa_resume_cap = 0;
   c->epa_cap = 0;
   c->scratch_epoch += 1;  // captured graphs hold the freed buffers, also if the allocation below fails
   const size_t cap = std::max<size_t>(n, 1024);
   FCLG_CUDA(c, cudaMalloc(&c->epa_list, cap * sizeof(uint32_t)));
   FCLG_CUDA(c, cudaMalloc(&c->epa_ovf, cap * sizeof(uint32_t)));
   FCLG_CUDA(c, cudaMalloc(&c->epa_rec, cap * fclg::kEpaRecordBytes));
+  // states of the pairs that outgrow the small EPA layout (a few per cent of
+  // the overlapping pairs); pairs past the pool rerun from their simplex
+  const size_t resume_cap = std::min<size_t>(std::max<size_t>(cap / 16, 1024), 262144);
+  FCLG_CUDA(c, cudaMalloc(&c->epa_resume, resume_cap * fclg::kEpaResumeBytes));
+  c->epa_resume_cap = (uint32_t)resume_cap;
   c->epa_cap = cap;
   return FCLG_OK;
 }
@@ -295,6 +313,10 @@ int ensure_guess(fclg_context* c, size_t n) {
   return FCLG_OK;
 }
 
+// Defaults of fclg_request.warm_probe / warm_gap.
+constexpr int kWarmProbeDefault = 3;
+constexpr float kWarmGapDefault = 5e-6f;
+
 fclg::QueryParams make_params(const fclg_request* req, bool distance_query) {
   fclg::QueryParams p;
   p.gjk_tol = (req && req->gjk_tolerance > 0.f) ? req->gjk_tolerance : 1e-6f;
@@ -314,6 +336,10 @@ fclg::QueryParams make_params(const fclg_request* req, bool distance_query) {
   p.analytic = (!distance_query && !(fl & FCLG_REQ_NO_ANALYTIC)) ? 1 : 0;
   p.directed = 0;
   p.incremental = 0;
+  // a learned start keeps a pair only with a separation certificate found
+  // within warm_probe supports and a distance certified to warm_gap
+  p.warm_probe = (req && req->warm_probe) ? (int)req->warm_probe : kWarmProbeDefault;
+  p.warm_gap = (req && req->warm_gap > 0.f) ? req->warm_gap : kWarmGapDefault;
   return p;
 }
 
@@ -384,7 +410,8 @@ int run_query(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_
   }
   if (c->profiling) FCLG_CUDA(c, cudaEventRecord(c->ev[1], st));
   if (prm.want_epa) {
-    fclg::EpaQueue ovf{c->epa_count + 1, c->epa_ovf, nullptr};
+    fclg::EpaQueue ovf{c->epa_count + 1, c->epa_ovf, reinterpret_cast<float4*>(c->epa_resume),
+                       c->epa_resume_on ? c->epa_resume_cap : 0u};
     FCLG_CUDA(c, fclg::launch_epa(b, prm, q, ovf, c->num_sms, c->epa_ctas_per_sm, st));
     c->launches += prm.epa_max_faces > 128 ? 2 : 1;
     if (c->profiling) FCLG_CUDA(c, cudaEventRecord(c->ev[2], st));
@@ -448,6 +475,7 @@ void fclg_destroy(fclg_context* c) {
   if (c->epa_count) cudaFree(c->epa_count);
   if (c->epa_list) cudaFree(c->epa_list);
   if (c->epa_ovf) cudaFree(c->epa_ovf);
+  if (c->epa_resume) cudaFree(c->epa_resume);
   if (c->epa_rec) cudaFree(c->epa_rec);
   if (c->io_pairs) cudaFree(c->io_pairs);
   if (c->io_results) cudaFree(c->io_results);
@@ -455,6 +483,8 @@ void fclg_destroy(fclg_context* c) {
   if (c->bk_order) cudaFree(c->bk_order);
   if (c->bk_small) cudaFree(c->bk_small);
   if (c->mesh_io) cudaFree(c->mesh_io);
+  if (c->mesh_cbuf) cudaFree(c->mesh_cbuf);
+  if (c->mesh_ctr) cudaFree(c->mesh_ctr);
   if (c->guess) cudaFree(c->guess);
   if (c->bp_scratch) cudaFree(c->bp_scratch);
   if (c->bp_io) cudaFree(c->bp_io);
@@ -573,6 +603,7 @@ int fclg_set_tuning(fclg_context* c, const fclg_tuning* t) {
   if (t->epa_ctas_per_sm) c->epa_ctas_per_sm = t->epa_ctas_per_sm;
   if (t->support_walk) c->support_walk = t->support_walk > 0;
   if (t->gjk_refill) c->gjk_refill = t->gjk_refill > 0;
+  if (t->epa_resume) c->epa_resume_on = t->epa_resume > 0;
   return FCLG_OK;
 }
 
@@ -586,6 +617,7 @@ int fclg_get_tuning(const fclg_context* c, fclg_tuning* t) {
   t->epa_ctas_per_sm = c->epa_ctas_per_sm;
   t->support_walk = c->support_walk ? 1 : -1;
   t->gjk_refill = c->gjk_refill ? 1 : -1;
+  t->epa_resume = c->epa_resume_on ? 1 : -1;
   return FCLG_OK;
 }
 
@@ -610,6 +642,19 @@ int fclg_bvh_build(const float* vertices, uint32_t nv, const int32_t* tris, uint
   return FCLG_OK;
 }
 
+int fclg_bvh_node_sizes(const float* vertices, uint32_t nv, const int32_t* tris, uint32_t nt, double* sizes,
+                        uint32_t* depth) {
+  if (!vertices || !tris || nv == 0 || nt == 0 || nt > (1u << 29)) return FCLG_E_INVALID;
+  std::vector<fclg::MeshNodeRec> nn;
+  std::vector<float> soup;
+  std::vector<double> sz;
+  uint32_t d = 0;
+  if (fclg::build_obb_bvh(vertices, nv, tris, nt, nn, soup, &sz, &d) != 0) return FCLG_E_INVALID;
+  if (sizes) std::memcpy(sizes, sz.data(), sz.size() * sizeof(double));
+  if (depth) *depth = d;
+  return FCLG_OK;
+}
+
 int fclg_mesh_create(fclg_context* c, const float* vertices, uint32_t nv, const int32_t* tris, uint32_t nt,
                      fclg_mesh** out) {
   if (!c) return FCLG_E_INVALID;
@@ -618,7 +663,9 @@ int fclg_mesh_create(fclg_context* c, const float* vertices, uint32_t nv, const 
   if (nt > (1u << 29)) return fail(c, FCLG_E_TOO_LARGE, "too many triangles");
   std::vector<fclg::MeshNodeRec> nodes;
   std::vector<float> soup;
-  const int rc = fclg::build_obb_bvh(vertices, nv, tris, nt, nodes, soup);
+  std::vector<double> sizes;
+  uint32_t depth = 0;
+  const int rc = fclg::build_obb_bvh(vertices, nv, tris, nt, nodes, soup, &sizes, &depth);
   if (rc == -2) return fail(c, FCLG_E_INVALID, "triangle vertex index out of range");
   if (rc) return fail(c, FCLG_E_INVALID, "empty mesh");
   FCLG_CUDA(c, cudaSetDevice(c->device));
@@ -626,11 +673,14 @@ int fclg_mesh_create(fclg_context* c, const float* vertices, uint32_t nv, const 
   m->device = c->device;
   m->n_nodes = (uint32_t)nodes.size();
   m->n_tris = nt;
+  m->depth = depth;
   cudaError_t e = cudaMalloc(&m->nodes, nodes.size() * sizeof(fclg::MeshNodeRec));
   if (e == cudaSuccess) e = cudaMalloc(&m->tris, soup.size() * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&m->sizes, sizes.size() * sizeof(double));
   if (e == cudaSuccess)
     e = cudaMemcpy(m->nodes, nodes.data(), nodes.size() * sizeof(fclg::MeshNodeRec), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(m->tris, soup.data(), soup.size() * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(m->sizes, sizes.data(), sizes.size() * sizeof(double), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     fclg_mesh_destroy(m);
     return cuda_fail(c, e, "mesh upload");
@@ -644,6 +694,7 @@ void fclg_mesh_destroy(fclg_mesh* m) {
   cudaSetDevice(m->device);
   if (m->nodes) cudaFree(m->nodes);
   if (m->tris) cudaFree(m->tris);
+  if (m->sizes) cudaFree(m->sizes);
   delete m;
 }
 
@@ -673,10 +724,14 @@ int fclg_mesh_collide_device(fclg_context* c, const fclg_mesh* a, const fclg_mes
   if (max_contacts == 0) return fail(c, FCLG_E_INVALID, "max_contacts must be >= 1");
   if (!d_poses || !d_flags || !d_counts || !d_pairs) return fail(c, FCLG_E_INVALID, "null pointer");
   if (a->device != c->device || b->device != c->device) return fail(c, FCLG_E_INVALID, "mesh on another device");
+  // the traversal orders node pairs by a 64-bit path key: one bit per descent
+  if (a->depth + b->depth > 62) return fail(c, FCLG_E_TOO_LARGE, "BVH depths sum above 62");
   FCLG_CUDA(c, cudaSetDevice(c->device));
   fclg::MeshArgs m;
-  m.a = fclg::MeshDev{static_cast<const float4*>(a->nodes), static_cast<const float4*>(a->tris), a->n_nodes, a->n_tris};
-  m.b = fclg::MeshDev{static_cast<const float4*>(b->nodes), static_cast<const float4*>(b->tris), b->n_nodes, b->n_tris};
+  m.a = fclg::MeshDev{static_cast<const float4*>(a->nodes), static_cast<const float4*>(a->tris), a->n_nodes, a->n_tris,
+                      static_cast<const double*>(a->sizes)};
+  m.b = fclg::MeshDev{static_cast<const float4*>(b->nodes), static_cast<const float4*>(b->tris), b->n_nodes, b->n_tris,
+                      static_cast<const double*>(b->sizes)};
   m.poses = reinterpret_cast<const float4*>(d_poses);
   m.n_poses = n;
   m.max_contacts = max_contacts;
@@ -684,10 +739,50 @@ int fclg_mesh_collide_device(fclg_context* c, const fclg_mesh* a, const fclg_mes
   m.counts = d_counts;
   m.pairs = d_pairs;
   m.status = d_status;
-  const int blocks = c->num_sms * 8;
+  int blocks = c->num_sms * 8;
+  const int cbuf_len = fclg::mesh_contact_buffer_len(max_contacts);
+  if (cbuf_len > 0) {
+    // contact buffers in device memory, one per warp of a grid that fits at once
+    blocks = fclg::mesh_collide_resident_blocks(c->num_sms);
+    const size_t need = (size_t)fclg::mesh_collide_warps(blocks) * cbuf_len * (8 + 8);
+    if (need > ((size_t)8 << 30))
+      return fail(c, FCLG_E_TOO_LARGE, "max_contacts too large for the ordered contact buffers (8 GiB)");
+    if (need > c->mesh_cbuf_bytes) {
+      if (c->mesh_cbuf) cudaFree(c->mesh_cbuf);
+      c->mesh_cbuf = nullptr;
+      c->mesh_cbuf_bytes = 0;
+      FCLG_CUDA(c, cudaMalloc(&c->mesh_cbuf, need));
+      c->mesh_cbuf_bytes = need;
+    }
+    const size_t n_entries = (size_t)fclg::mesh_collide_warps(blocks) * cbuf_len;
+    m.cbuf_key = static_cast<unsigned long long*>(c->mesh_cbuf);
+    m.cbuf_pair = reinterpret_cast<int2*>(static_cast<char*>(c->mesh_cbuf) + n_entries * 8);
+    m.cbuf_len = (uint32_t)cbuf_len;
+  }
+  if (c->profiling) {
+    if (!c->mesh_ctr) {
+      FCLG_CUDA(c, cudaMalloc(&c->mesh_ctr, 2 * sizeof(unsigned long long)));
+      FCLG_CUDA(c, cudaMemset(c->mesh_ctr, 0, 2 * sizeof(unsigned long long)));
+    }
+    m.counters = c->mesh_ctr;
+  }
   clear_pending_error();
   FCLG_CUDA(c, fclg::launch_mesh_collide(m, blocks, static_cast<cudaStream_t>(stream)));
   c->launches += 1;
+  return FCLG_OK;
+}
+
+int fclg_mesh_traffic(fclg_context* c, uint64_t* node_pairs, uint64_t* triangle_pairs, int reset) {
+  if (!c) return FCLG_E_INVALID;
+  unsigned long long h[2] = {0, 0};
+  if (c->mesh_ctr) {
+    FCLG_CUDA(c, cudaSetDevice(c->device));
+    FCLG_CUDA(c, cudaDeviceSynchronize());
+    FCLG_CUDA(c, cudaMemcpy(h, c->mesh_ctr, sizeof h, cudaMemcpyDeviceToHost));
+    if (reset) FCLG_CUDA(c, cudaMemset(c->mesh_ctr, 0, sizeof h));
+  }
+  if (node_pairs) *node_pairs = h[0];
+  if (triangle_pairs) *triangle_pairs = h[1];
   return FCLG_OK;
 }
 
@@ -737,10 +832,12 @@ static int run_mesh_shape(fclg_context* c, const fclg_mesh* mesh, const uint32_t
   if (!d_shape_ids || !d_poses || !d_flags || !d_counts || !d_tri_ids) return fail(c, FCLG_E_INVALID, "null pointer");
   if (!c->shapes) return fail(c, FCLG_E_NO_SHAPES, "no shapes set");
   if (mesh->device != c->device) return fail(c, FCLG_E_INVALID, "mesh on another device");
+  // the traversal orders nodes by a 64-bit path key: one bit per descent
+  if (mesh->depth > 62) return fail(c, FCLG_E_TOO_LARGE, "BVH depth above 62");
   FCLG_CUDA(c, cudaSetDevice(c->device));
   fclg::MeshShapeArgs m;
   m.mesh = fclg::MeshDev{static_cast<const float4*>(mesh->nodes), static_cast<const float4*>(mesh->tris),
-                         mesh->n_nodes, mesh->n_tris};
+                         mesh->n_nodes, mesh->n_tris, static_cast<const double*>(mesh->sizes)};
   m.shapes = c->shapes;
   m.verts = c->verts;
   m.n_shapes = c->n_shapes;
@@ -755,8 +852,27 @@ static int run_mesh_shape(fclg_context* c, const fclg_mesh* mesh, const uint32_t
   m.tri_ids = d_tri_ids;
   m.status = d_status;
   m.contacts = d_contacts;
+  int blocks = c->num_sms * 8;
+  const int cbuf_len = fclg::mesh_contact_buffer_len(max_contacts);
+  if (cbuf_len > 0) {
+    // contact buffers in device memory, one per warp of a grid that fits at once
+    blocks = fclg::mesh_shape_resident_blocks(c->num_sms, d_contacts != nullptr);
+    const size_t n_entries = (size_t)fclg::mesh_shape_warps(blocks) * cbuf_len;
+    if (n_entries * 16 > ((size_t)8 << 30))
+      return fail(c, FCLG_E_TOO_LARGE, "max_contacts too large for the ordered contact buffers (8 GiB)");
+    if (n_entries * 16 > c->mesh_cbuf_bytes) {
+      if (c->mesh_cbuf) cudaFree(c->mesh_cbuf);
+      c->mesh_cbuf = nullptr;
+      c->mesh_cbuf_bytes = 0;
+      FCLG_CUDA(c, cudaMalloc(&c->mesh_cbuf, n_entries * 16));
+      c->mesh_cbuf_bytes = n_entries * 16;
+    }
+    m.cbuf_key = static_cast<unsigned long long*>(c->mesh_cbuf);
+    m.cbuf_val = reinterpret_cast<int2*>(static_cast<char*>(c->mesh_cbuf) + n_entries * 8);
+    m.cbuf_len = (uint32_t)cbuf_len;
+  }
   clear_pending_error();
-  FCLG_CUDA(c, fclg::launch_mesh_shape(m, c->num_sms * 8, static_cast<cudaStream_t>(stream)));
+  FCLG_CUDA(c, fclg::launch_mesh_shape(m, blocks, static_cast<cudaStream_t>(stream)));
   c->launches += 1;
   if (d_contacts) {
     FCLG_CUDA(c, fclg::launch_mesh_contacts(m, c->num_sms, static_cast<cudaStream_t>(stream)));
@@ -1060,7 +1176,10 @@ std::mutex g_static_mutex;
 unsigned char* g_static_base[kStaticMaxDevices] = {};
 
 // Address of g_static_scratch on the current device (c->device), looked up on
-// the first call for that device.
+// the first call for that device and cached per device ordinal.  The address
+// belongs to the device's primary context (the one the runtime API uses): a
+// cudaDeviceReset, or another context made current on the device, makes the
+// cached address stale, so this entry point must not be used across either.
 int static_scratch(fclg_context* c, unsigned char** out) {
   if (c->device < 0 || c->device >= kStaticMaxDevices) return fail(c, FCLG_E_INVALID, "device ordinal above 63");
   std::lock_guard<std::mutex> lock(g_static_mutex);
@@ -1106,13 +1225,24 @@ extern "C" int fclg_distance_device_static(fclg_context* c, const fclg_pair* d_p
   uint32_t* counts = reinterpret_cast<uint32_t*>(base);
   fclg::EpaQueue q{counts, reinterpret_cast<uint32_t*>(base + kStaticListOffset),
                    reinterpret_cast<float4*>(base + kStaticRecOffset)};
+  if (c->profiling) {  // the pass times of fclg_pass_times cover these calls too
+    const int prc = collect_times(c);
+    if (prc) return prc;
+  }
   if (prm.want_epa) FCLG_CUDA(c, cudaMemsetAsync(counts, 0, 2 * sizeof(uint32_t), st));
+  if (c->profiling) FCLG_CUDA(c, cudaEventRecord(c->ev[0], st));
   FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes, nullptr, nullptr, 0, st, c->gjk_refill));
   c->launches += 1;
+  if (c->profiling) FCLG_CUDA(c, cudaEventRecord(c->ev[1], st));
   if (prm.want_epa) {
     fclg::EpaQueue ovf{counts + 1, reinterpret_cast<uint32_t*>(base + kStaticOvfOffset), nullptr};
     FCLG_CUDA(c, fclg::launch_epa(b, prm, q, ovf, c->num_sms, c->epa_ctas_per_sm, st));
     c->launches += prm.epa_max_faces > 128 ? 2 : 1;
+    if (c->profiling) FCLG_CUDA(c, cudaEventRecord(c->ev[2], st));
+  }
+  if (c->profiling) {
+    c->ev_pending = true;
+    c->ev_epa = prm.want_epa != 0;
   }
   return FCLG_OK;
 }

@@ -182,6 +182,8 @@ struct QueryParams {
   int directed;       // collide with MPR directed penetration along BatchArgs::guess (directed_pass.cu)
   int incremental;    // directed_pass: the incremental penetration from BatchArgs::guess as the hint
   int want_epa;       // run EPA on overlapping pairs
+  int warm_probe;     // learned starts: supports the boolean phase gets to certify separation (0: no limit)
+  float warm_gap;     // learned starts: duality gap that certifies the distance (0: the reference's stop)
 };
 
 }  // namespace fclg

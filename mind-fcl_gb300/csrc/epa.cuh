@@ -149,6 +149,26 @@ struct EpaResult {
   float depth;
   f3 p0, p1;
   int iterations;
+  int resume_nv;  // kEpaOverflow: vertices of the polytope state to continue from
+};
+
+// Byte offsets of a polytope state written by a layout of F faces / V
+// vertices when it runs out of slots (the state before the iteration that
+// did not fit), read back by a larger layout, which continues from it: a
+// larger layout that had run from the start would hold the same state at the
+// same iteration (slots are assigned the same way until the smaller one
+// fills), so the answers equal a restart's.
+template <int F, int V>
+struct EpaResume {
+  static constexpr size_t kHead = 0;                  // int nv, hw, live, fs_top, iterations
+  static constexpr size_t kFn = 32;                   // float4 [F]
+  static constexpr size_t kFkey = kFn + 16 * F;       // float [F]
+  static constexpr size_t kFv = kFkey + 4 * F;        // uint32 [F]
+  static constexpr size_t kFadj = kFv + 4 * F;        // uint16 [F][4]
+  static constexpr size_t kFree = kFadj + 8 * F;      // uint16 [F]
+  static constexpr size_t kVw = (kFree + 2 * F + 15) & ~(size_t)15;  // float4 [V]
+  static constexpr size_t kVpa = kVw + 16 * V;        // float4 [V]
+  static constexpr size_t kBytes = kVpa + 16 * V;
 };
 
 // epa_polytope_utils.h:58-86
@@ -562,9 +582,72 @@ struct EpaWarp {
     return 0;
   }
 
+  // Writes the polytope state of a kEpaOverflow result (all lanes; layout
+  // RF / RV = this layout's capacity).
+  template <int RF, int RV>
+  __device__ void save(unsigned char* rec, const EpaResult& r) const {
+    using L = EpaResume<RF, RV>;
+    static_assert(RF == FMAX && RV == VMAX, "a state is written in its own layout's sizes");
+    if (lane == 0) {
+      int* h = reinterpret_cast<int*>(rec + L::kHead);
+      h[0] = r.resume_nv;
+      h[1] = hw;
+      h[2] = live;
+      h[3] = fs_top;
+      h[4] = r.iterations;
+    }
+    for (int i = (int)lane; i < hw; i += 32) {
+      reinterpret_cast<float4*>(rec + L::kFn)[i] = P.fn[i];
+      reinterpret_cast<float*>(rec + L::kFkey)[i] = P.fkey[i];
+      reinterpret_cast<uint32_t*>(rec + L::kFv)[i] = P.fv[i];
+      reinterpret_cast<uint2*>(rec + L::kFadj)[i] = *reinterpret_cast<const uint2*>(&P.fadj[i][0]);
+    }
+    for (int i = (int)lane; i < fs_top; i += 32) reinterpret_cast<uint16_t*>(rec + L::kFree)[i] = P.freestk[i];
+    for (int i = (int)lane; i < r.resume_nv; i += 32) {
+      reinterpret_cast<float4*>(rec + L::kVw)[i] = P.vw[i];
+      reinterpret_cast<float4*>(rec + L::kVpa)[i] = P.vpa[i];
+    }
+  }
+
+  // Continues a state written by a smaller layout (RF faces, RV vertices):
+  // loads it and runs the remaining iterations.
+  template <int RF, int RV>
+  __device__ EpaResult resume(const unsigned char* rec, int max_iter, int max_faces, bool overflow_is_final) {
+    using L = EpaResume<RF, RV>;
+    static_assert(RF <= FMAX && RV <= VMAX, "a state continues in a layout at least as large");
+    const int* h = reinterpret_cast<const int*>(rec + L::kHead);
+    nv = h[0];
+    hw = h[1];
+    live = h[2];
+    fs_top = h[3];
+    const int it0 = h[4];
+    for (int i = (int)lane; i < hw; i += 32) {
+      P.fn[i] = reinterpret_cast<const float4*>(rec + L::kFn)[i];
+      P.fkey[i] = reinterpret_cast<const float*>(rec + L::kFkey)[i];
+      P.fv[i] = reinterpret_cast<const uint32_t*>(rec + L::kFv)[i];
+      *reinterpret_cast<uint2*>(&P.fadj[i][0]) = reinterpret_cast<const uint2*>(rec + L::kFadj)[i];
+      P.fmark[i] = 0;
+    }
+    for (int i = (int)lane; i < fs_top; i += 32) P.freestk[i] = reinterpret_cast<const uint16_t*>(rec + L::kFree)[i];
+    for (int i = (int)lane; i < nv; i += 32) {
+      P.vw[i] = reinterpret_cast<const float4*>(rec + L::kVw)[i];
+      P.vpa[i] = reinterpret_cast<const float4*>(rec + L::kVpa)[i];
+    }
+    stamp = 0;
+    __syncwarp();
+    EpaResult r;
+    r.status = kEpaFailed;
+    r.depth = 0.f;
+    r.p0 = r.p1 = mk3(0, 0, 0);
+    r.iterations = it0;
+    r.resume_nv = 0;
+    iterate(it0, max_iter, max_faces, overflow_is_final, r);
+    return r;
+  }
+
   // Runs EPA from the GJK simplex (rank, pa[], pb[]).  When this layout runs
   // out of face or vertex slots before max_faces, the result is kEpaOverflow
-  // (rerun in a larger layout) unless overflow_is_final.
+  // (continued or rerun in a larger layout) unless overflow_is_final.
   __device__ EpaResult run(int rank, const f3* spa, const f3* spb, int max_iter, int max_faces,
                            bool overflow_is_final) {
     EpaResult r;
@@ -572,6 +655,7 @@ struct EpaWarp {
     r.depth = 0.f;
     r.p0 = r.p1 = mk3(0, 0, 0);
     r.iterations = 0;
+    r.resume_nv = 0;
     nv = 0;
     hw = 0;
     live = 0;
@@ -612,13 +696,19 @@ struct EpaWarp {
     if (done) return r;
     if (!ok) { r.status = kEpaFailed; return r; }
     __syncwarp();
-    for (int it = 0;;) {
+    iterate(0, max_iter, max_faces, overflow_is_final, r);
+    return r;
+  }
+
+  // The expansion loop from iteration `it` on the current polytope.
+  __device__ void iterate(int it, int max_iter, int max_faces, bool overflow_is_final, EpaResult& r) {
+    for (;;) {
       int bs;
       float bd;
       FCLG_EPA_PHASE(0);
       nearest(bs, bd);
       FCLG_EPA_PHASE(1);
-      if (bs == 0x7FFFFFFF || !(bd < INFINITY)) { r.status = kEpaFailed; return r; }
+      if (bs == 0x7FFFFFFF || !(bd < INFINITY)) { r.status = kEpaFailed; return; }
       const f3 n = ld3(P.fn[bs]);
       const uint32_t bfv = P.fv[bs];  // the slot may be reused by the expansion below
       f3 pa, pb;
@@ -629,12 +719,13 @@ struct EpaWarp {
       if (delta <= tol) {
         finalize(bfv, pa, pb, r);
         r.status = kEpaOK;
-        return r;
+        return;
       }
       if (nv >= VMAX) {
         finalize(bfv, pa, pb, r);
         r.status = overflow_is_final ? kEpaMallocFailed : kEpaOverflow;
-        return r;
+        r.resume_nv = nv;  // the support is not in the polytope yet
+        return;
       }
       push_vertex(pa, pb);
       __syncwarp();
@@ -642,11 +733,14 @@ struct EpaWarp {
       if (ex == 1 || (ex == 3 && overflow_is_final)) {
         finalize(bfv, pa, pb, r);
         r.status = kEpaMallocFailed;
-        return r;
+        return;
       }
       if (ex == 3) {
+        // the expansion stopped before changing the polytope: the state is
+        // the one before this iteration, without the new vertex
         r.status = kEpaOverflow;
-        return r;
+        r.resume_nv = nv - 1;
+        return;
       }
       if (ex == 2) {
         // The visible patch has no simple horizon at FP32 resolution.  Near
@@ -658,14 +752,14 @@ struct EpaWarp {
         } else {
           r.status = kEpaFailed;
         }
-        return r;
+        return;
       }
       ++it;
       r.iterations = it;
       if (it >= max_iter) {
         finalize(bfv, pa, pb, r);
         r.status = kEpaIterLimit;
-        return r;
+        return;
       }
     }
   }

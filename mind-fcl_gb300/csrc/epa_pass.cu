@@ -5,9 +5,27 @@
 
 namespace fclg {
 
+// Small layout: 128 faces / 72 vertices (~8.4 KB of shared memory per warp,
+// six 4-warp CTAs per SM; a polytope of 128 faces has about 66 vertices);
+// large layout: the reference's 256 faces (~18 KB per warp, three 4-warp CTAs
+// per SM).
+#ifndef FCLG_EPA_SMALL_V
+#define FCLG_EPA_SMALL_V 72
+#endif
+#ifndef FCLG_EPA_SMALL_MINB
+#define FCLG_EPA_SMALL_MINB 6
+#endif
+constexpr int kSmallF = 128, kSmallV = FCLG_EPA_SMALL_V, kSmallWarps = 4, kSmallMinB = FCLG_EPA_SMALL_MINB;
+#ifndef FCLG_EPA_LARGE_MINB
+#define FCLG_EPA_LARGE_MINB 3
+#endif
+constexpr int kLargeF = 256, kLargeV = 192, kLargeWarps = 4, kLargeMinB = FCLG_EPA_LARGE_MINB;
+static_assert(EpaResume<kSmallF, kSmallV>::kBytes <= kEpaResumeBytes, "resume record size");
+
 // EPA over the work list.  The small layout runs every listed pair and hands
-// the pairs whose polytope outgrows it to `ovf` (indices into the work list);
-// the large layout reruns those.
+// the pairs whose polytope outgrows it to `ovf` (indices into the work list),
+// the first ovf.resume_cap of them with their polytope state; the large
+// layout continues those from their state and reruns the rest.
 template <int FMAX, int VMAX, int WARPS, int MINB>
 __global__ void __launch_bounds__(WARPS * 32, MINB) epa_pass(BatchArgs b, QueryParams prm, EpaQueue q,
                                                             EpaQueue ovf, int large) {
@@ -52,13 +70,28 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) epa_pass(BatchArgs b, QueryP
     __syncwarp();
     const SharedSupport32 sup{&P.pair};
     EpaWarp<FMAX, VMAX, SharedSupport32> E{P, sup, prm.epa_tol, lane, 0, 0, 0, 0, 0u};
-    const EpaResult er =
-        E.run(rank < 1 ? 1 : (rank > 4 ? 4 : rank), spa, spb, prm.epa_max_iter, max_faces, final_layout);
-    if (lane == 0) {
-      if (er.status == kEpaOverflow) {
-        const uint32_t slot = atomicAdd(ovf.count, 1u);
+    EpaResult er;
+    if (large && k < ovf.resume_cap && FMAX >= kSmallF && VMAX >= kSmallV) {
+      er = E.template resume<kSmallF, kSmallV>(reinterpret_cast<const unsigned char*>(ovf.rec) +
+                                                   (size_t)k * kEpaResumeBytes,
+                                               prm.epa_max_iter, max_faces, final_layout);
+    } else {
+      er = E.run(rank < 1 ? 1 : (rank > 4 ? 4 : rank), spa, spb, prm.epa_max_iter, max_faces, final_layout);
+    }
+    if (er.status == kEpaOverflow) {
+      uint32_t slot = 0;
+      if (lane == 0) {
+        slot = atomicAdd(ovf.count, 1u);
         ovf.list[slot] = item;
-      } else {
+      }
+      slot = __shfl_sync(0xFFFFFFFFu, slot, 0);
+      if constexpr (FMAX == kSmallF && VMAX == kSmallV) {
+        if (slot < ovf.resume_cap)
+          E.template save<kSmallF, kSmallV>(reinterpret_cast<unsigned char*>(ovf.rec) + (size_t)slot * kEpaResumeBytes,
+                                            er);
+      }
+    } else if (lane == 0) {
+      {
         const int32_t status = kGjkIntersect | ((er.status + 1) << 8);
         const uint32_t iters = (uint32_t)(gjk_iters + er.iterations);
         if (er.status != kEpaFailed) {
@@ -73,22 +106,6 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) epa_pass(BatchArgs b, QueryP
     __syncwarp();
   }
 }
-
-// Small layout: 128 faces / 72 vertices (~8.4 KB of shared memory per warp,
-// six 4-warp CTAs per SM; a polytope of 128 faces has about 66 vertices);
-// large layout: the reference's 256 faces (~18 KB per warp, three 4-warp CTAs
-// per SM).
-#ifndef FCLG_EPA_SMALL_V
-#define FCLG_EPA_SMALL_V 72
-#endif
-#ifndef FCLG_EPA_SMALL_MINB
-#define FCLG_EPA_SMALL_MINB 6
-#endif
-constexpr int kSmallF = 128, kSmallV = FCLG_EPA_SMALL_V, kSmallWarps = 4, kSmallMinB = FCLG_EPA_SMALL_MINB;
-#ifndef FCLG_EPA_LARGE_MINB
-#define FCLG_EPA_LARGE_MINB 3
-#endif
-constexpr int kLargeF = 256, kLargeV = 192, kLargeWarps = 4, kLargeMinB = FCLG_EPA_LARGE_MINB;
 
 size_t epa_smem_bytes() { return (size_t)kSmallWarps * sizeof(EpaSmem<kSmallF, kSmallV>); }
 size_t epa_smem_bytes_large() { return (size_t)kLargeWarps * sizeof(EpaSmem<kLargeF, kLargeV>); }

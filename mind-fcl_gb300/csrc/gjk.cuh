@@ -384,9 +384,13 @@ struct GjkRun {
   float book;  // distance: |cur|
   int phase;   // 0 first support, 1 boolean loop, 2 distance loop, 3 done
   int it;      // iteration of the current loop
+  int probe;   // > 0: supports the boolean phase may take (gjk_evaluate's probe)
+  float cert;  // > 0: certified distance stop (min_distance's cert_gap)
   GjkOut o;
 
-  __device__ __forceinline__ void begin(f3 guess) {
+  __device__ __forceinline__ void begin(f3 guess, int probe_supports = 0, float cert_gap = 0.f) {
+    probe = probe_supports;
+    cert = cert_gap;
     o.point_valid = false;
     o.iterations = 0;
     o.p0 = o.p1 = mk3(0, 0, 0);
@@ -429,6 +433,18 @@ struct GjkRun {
     return false;
   }
 
+  // boolean iterations allowed: max_iter, or fewer under a probe
+  __device__ __forceinline__ int bool_iters(int max_iter) const {
+    return (probe > 0 && probe - 1 < max_iter) ? probe - 1 : max_iter;
+  }
+  __device__ __forceinline__ bool boolean_limit(int max_iter, bool want_distance) {
+    if (bool_iters(max_iter) < max_iter) {  // the learned start's probe ran out
+      o.status = kGjkIterLimit;
+      return done();
+    }
+    return undetermined(kGjkIterLimit, want_distance);
+  }
+
   template <class Sup>
   __device__ __forceinline__ bool step(const Sup& sup, float tol, int max_iter, bool want_distance) {
     const float tol2 = tol * tol;
@@ -447,7 +463,7 @@ struct GjkRun {
       d = -d;
       phase = 1;
       it = 0;
-      if (max_iter <= 0) return undetermined(kGjkIterLimit, want_distance);
+      if (bool_iters(max_iter) <= 0) return boolean_limit(max_iter, want_distance);
       return false;
     }
     if (phase == 1) {
@@ -483,14 +499,15 @@ struct GjkRun {
         return done();
       }
       if (st == Proj::ZeroVolume) return undetermined(kGjkNoProgress, want_distance);
-      if (++it >= max_iter) return undetermined(kGjkIterLimit, want_distance);
+      if (++it >= bool_iters(max_iter)) return boolean_limit(max_iter, want_distance);
       return false;
     }
     // phase 2: one iteration of the minimum-distance loop (gjk_distance.hpp:41-105)
     ++o.iterations;
     const f3 w = pa - pb;
-    FCLG_GJK_TRACE(it, -1, dot(d, w - cur), 0.f);
-    if (dot(d, w - cur) < tol) return distance_result(true);
+    const float gap = dot(d, w - cur);
+    FCLG_GJK_TRACE(it, -1, gap, 0.f);
+    if (gap < tol) return distance_result(true);
     bool dup = false;
 #pragma unroll
     for (int j = 0; j < 4; ++j)
@@ -506,7 +523,10 @@ struct GjkRun {
     if (st != Upd::OK) return done();
     const float nd = nrm(cur);
     FCLG_GJK_TRACE(it, s.rank, nd, book - nd);
-    if (book - nd < tol) return distance_result(true);
+    if (book - nd < tol) {
+      if (!(cert > 0.f) || gap <= cert) return distance_result(true);
+      if (!(book - nd > 0.f)) return done();  // no progress before the certificate: point_valid stays false
+    }
     if (nd < tol) return distance_result(true);
     book = nd;
     d = cur * (-1.f / book);
@@ -516,9 +536,15 @@ struct GjkRun {
 };
 
 // gjk_distance.hpp:10-105: minimum distance from a separating vertex.
+// cert_gap > 0 (runs from a learned start) replaces the reference's stop on a
+// small improvement with a certificate: the run ends on a small improvement
+// only once the duality gap of the last support, |v| - v^.w (an upper bound of
+// |v| - distance), is at most cert_gap, and gives up (returns false, so the
+// pair is redone from the plain start) when an iteration makes no progress
+// before that.
 template <class Sup>
 __device__ __forceinline__ bool min_distance(const Sup& sup, Simplex& s, float tol, int max_iter, f3& p0, f3& p1,
-                                             int& iters) {
+                                             int& iters, float cert_gap = 0.f) {
   f3 cur;
   if (update_simplex(s, cur, tol) != Upd::OK) return false;
   float book = nrm(cur);
@@ -530,8 +556,9 @@ __device__ __forceinline__ bool min_distance(const Sup& sup, Simplex& s, float t
     f3 pa, pb;
     sup(next, pa, pb);
     const f3 w = pa - pb;
-    FCLG_GJK_TRACE(it, -1, dot(next, w - cur), 0.f);
-    if (dot(next, w - cur) < tol) return extract_no_sub(s, p0, p1);
+    const float gap = dot(next, w - cur);
+    FCLG_GJK_TRACE(it, -1, gap, 0.f);
+    if (gap < tol) return extract_no_sub(s, p0, p1);
     bool dup = false;
 #pragma unroll
     for (int j = 0; j < 4; ++j)
@@ -547,7 +574,10 @@ __device__ __forceinline__ bool min_distance(const Sup& sup, Simplex& s, float t
     if (st != Upd::OK) return false;
     const float nd = nrm(cur);
     FCLG_GJK_TRACE(it, s.rank, nd, book - nd);
-    if (book - nd < tol) return extract_no_sub(s, p0, p1);
+    if (book - nd < tol) {
+      if (!(cert_gap > 0.f) || gap <= cert_gap) return extract_no_sub(s, p0, p1);
+      if (!(book - nd > 0.f)) return false;
+    }
     if (nd < tol) return extract_no_sub(s, p0, p1);
     book = nd;
     next = cur * (-1.f / book);
@@ -556,9 +586,13 @@ __device__ __forceinline__ bool min_distance(const Sup& sup, Simplex& s, float t
 }
 
 // gjk.hpp:10-140.  want_distance selects the MinSeparationDistanceOutput path.
+// probe > 0 (a learned start) allows the boolean phase that many support
+// evaluations to certify separation; past them the run ends with
+// kGjkIterLimit and no points (the pair is then redone from the plain start).
+// cert_gap: see min_distance.
 template <class Sup>
 __device__ __forceinline__ GjkOut gjk_evaluate(const Sup& sup, f3 guess, float tol, int max_iter, bool want_distance,
-                                               Simplex& s) {
+                                               Simplex& s, int probe = 0, float cert_gap = 0.f) {
   GjkOut o;
   o.point_valid = false;
   o.iterations = 0;
@@ -576,8 +610,9 @@ __device__ __forceinline__ GjkOut gjk_evaluate(const Sup& sup, f3 guess, float t
   int undetermined = -1;
   if (!separated) {
     d = -d;
+    const int bool_iters = (probe > 0 && probe - 1 < max_iter) ? probe - 1 : max_iter;
     int it = 0;
-    for (; it < max_iter; ++it) {
+    for (; it < bool_iters; ++it) {
       o.iterations = it + 1;
       sup(d, pa, pb);
       const f3 w = pa - pb;
@@ -605,13 +640,19 @@ __device__ __forceinline__ GjkOut gjk_evaluate(const Sup& sup, f3 guess, float t
       if (st == Proj::Intersect) { o.status = kGjkIntersect; return o; }
       if (st == Proj::ZeroVolume) { undetermined = kGjkNoProgress; break; }
     }
-    if (!separated && undetermined < 0) undetermined = kGjkIterLimit;
+    if (!separated && undetermined < 0) {
+      if (bool_iters < max_iter) {  // the learned start's probe ran out
+        o.status = kGjkIterLimit;
+        return o;
+      }
+      undetermined = kGjkIterLimit;
+    }
   } else {
     s.rank = 1;
   }
   if (separated) {
     o.status = kGjkSeparated;
-    if (want_distance) o.point_valid = min_distance(sup, s, tol, max_iter, o.p0, o.p1, o.iterations);
+    if (want_distance) o.point_valid = min_distance(sup, s, tol, max_iter, o.p0, o.p1, o.iterations, cert_gap);
     return o;
   }
   o.status = undetermined;

@@ -46,8 +46,8 @@ __global__ void __launch_bounds__(128, FCLG_REFILL_MINB) gjk_refill(BatchArgs b,
   GjkRun run;
   uint32_t pid = 0;
   bool live = false;
-  bool warm = false;   // the lane's run started from the learned direction
-  int warm_iters = 0;  // iterations of a warm run that is being redone from the plain direction
+  int stage = 0;       // 0 plain run; with a learned start: 1 learned, 2 plain certified, then 0
+  int done_iters = 0;  // iterations of the pair's earlier runs
   uint32_t next = 0;  // warp-uniform: next unassigned position in the warp's share
   for (;;) {
     unsigned want = __ballot_sync(0xFFFFFFFFu, !live);
@@ -66,12 +66,12 @@ __global__ void __launch_bounds__(128, FCLG_REFILL_MINB) gjk_refill(BatchArgs b,
           sup.A = load_shape(b.shapes, b.walk, pr.a);
           sup.B = load_shape(b.shapes, b.walk, pr.b);
           sup.pose = pr.pose;
-          warm = b.guess != nullptr;
-          warm_iters = 0;
-          if (warm) {
+          stage = b.guess != nullptr ? 1 : 0;
+          done_iters = 0;
+          if (stage == 1) {
             const f3 guess = mk3(__ldg(b.guess + 3 * (size_t)pid), __ldg(b.guess + 3 * (size_t)pid + 1),
                                  __ldg(b.guess + 3 * (size_t)pid + 2));
-            run.begin(-guess);
+            run.begin(-guess, prm.warm_probe, prm.warm_gap);
           } else {
             run.begin(-plain);
           }
@@ -88,19 +88,19 @@ __global__ void __launch_bounds__(128, FCLG_REFILL_MINB) gjk_refill(BatchArgs b,
     }
     if (live && run.step(sup, prm.gjk_tol, prm.gjk_max_iter, prm.want_distance != 0)) {
       const GjkOut& o = run.o;
-      // a warm run stands for a separation certificate (with its points when
-      // distances are wanted) or for an overlap that needs no EPA; otherwise
-      // the pair is redone from the plain direction, both runs counted (as
-      // gjk_pass does)
-      const bool keep = (o.status == kGjkSeparated && (o.point_valid || !prm.want_distance)) ||
-                        (o.status == kGjkIntersect && !prm.want_epa);
-      if (warm && !keep) {
-        warm = false;
-        warm_iters = o.iterations;
+      // the same three runs as gjk_pass: learned (kept on warm_keep), plain
+      // certified (kept unless uncertified), plain under the reference's stop
+      if (stage == 1 && !warm_keep(o, prm)) {
+        stage = 2;
+        done_iters += o.iterations;
+        run.begin(-plain, 0, prm.warm_gap);
+      } else if (stage == 2 && uncertified(o, prm)) {
+        stage = 0;
+        done_iters += o.iterations;
         run.begin(-plain);
       } else {
         GjkOut out = o;
-        out.iterations += warm_iters;
+        out.iterations += done_iters;
         finish_pair(b, prm, q, pid, out, run.s);
         live = false;
       }

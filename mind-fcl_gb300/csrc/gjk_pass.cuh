@@ -53,6 +53,20 @@ __device__ __forceinline__ void store_invalid(float4* out, uint32_t pid) {
 
 }  // namespace
 
+// A run from the learned direction stands for a separation certificate (with
+// certified points when distances are wanted) or for an overlap that needs no
+// EPA.
+__device__ __forceinline__ bool warm_keep(const GjkOut& o, const QueryParams& prm) {
+  return (o.status == kGjkSeparated && (o.point_valid || !prm.want_distance)) ||
+         (o.status == kGjkIntersect && !prm.want_epa);
+}
+
+// A separated run under the certified stop that ended without a certified
+// distance (no progress before the certificate, or the iteration limit).
+__device__ __forceinline__ bool uncertified(const GjkOut& o, const QueryParams& prm) {
+  return o.status == kGjkSeparated && prm.want_distance && !o.point_valid;
+}
+
 // The tail of a pair once its GJK run is over: the EPA hand-off for an
 // overlapping pair, else the result record (shared by both GJK kernels).
 __device__ __forceinline__ void finish_pair(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q,
@@ -149,18 +163,25 @@ __global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_pass(BatchArgs b, Quer
     Simplex s;
     GjkOut o;
     if (b.guess) {
-      // Learned direction first.  Overlapping pairs (their EPA must start
-      // from the plain simplex) and pairs without a separation certificate
-      // are rerun from the plain direction; both runs count as iterations.
+      // Learned direction first, for a separation certificate within
+      // warm_probe supports and a distance certified to warm_gap.  A pair it
+      // does not settle (overlapping: its EPA must start from the plain
+      // simplex; probe exhausted; no certified distance) is rerun from the
+      // plain direction with the same certified stop, and a pair that even
+      // then gets no certified distance is rerun once more under the
+      // reference's own stop.  Every run counts as iterations.
       const f3 guess = mk3(__ldg(b.guess + 3 * (size_t)pid), __ldg(b.guess + 3 * (size_t)pid + 1),
                            __ldg(b.guess + 3 * (size_t)pid + 2));
-      o = gjk_evaluate(sup, -guess, prm.gjk_tol, prm.gjk_max_iter, prm.want_distance != 0, s);
-      const bool keep = (o.status == kGjkSeparated && (o.point_valid || !prm.want_distance)) ||
-                        (o.status == kGjkIntersect && !prm.want_epa);
-      if (!keep) {
-        const int warm_iters = o.iterations;
-        o = gjk_evaluate(sup, -plain, prm.gjk_tol, prm.gjk_max_iter, prm.want_distance != 0, s);
-        o.iterations += warm_iters;
+      o = gjk_evaluate(sup, -guess, prm.gjk_tol, prm.gjk_max_iter, prm.want_distance != 0, s, prm.warm_probe,
+                       prm.warm_gap);
+      if (!warm_keep(o, prm)) {
+        int done_iters = o.iterations;
+        o = gjk_evaluate(sup, -plain, prm.gjk_tol, prm.gjk_max_iter, prm.want_distance != 0, s, 0, prm.warm_gap);
+        if (uncertified(o, prm)) {
+          done_iters += o.iterations;
+          o = gjk_evaluate(sup, -plain, prm.gjk_tol, prm.gjk_max_iter, prm.want_distance != 0, s);
+        }
+        o.iterations += done_iters;
       }
     } else {
       o = gjk_evaluate(sup, -plain, prm.gjk_tol, prm.gjk_max_iter, prm.want_distance != 0, s);

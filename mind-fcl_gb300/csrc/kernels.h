@@ -25,9 +25,13 @@ struct BatchArgs {
 struct EpaQueue {
   uint32_t* count;        // [1]
   uint32_t* list;         // [capacity] pair indices
-  float4* rec;            // [capacity][7] final GJK simplex (rank, support points)
+  float4* rec;            // [capacity][7] final GJK simplex (rank, support points); for the overflow
+                          // list: [resume_cap] polytope states (kEpaResumeBytes each) or null
+  uint32_t resume_cap = 0;  // overflow list: states the pool holds (the rest restart from the simplex)
 };
 constexpr size_t kEpaRecordBytes = 7 * sizeof(float4);
+// Bytes of one small-layout polytope state handed to the large layout (epa.cuh EpaResume).
+constexpr size_t kEpaResumeBytes = 6688;
 
 // Scratch of the bucketing pass: pairs sorted by shape class (bucket.cu).
 constexpr int kShapeClasses = 6;  // box, sphere, capsule, cylinder, convex <= big_nv, convex > big_nv

@@ -14,10 +14,14 @@ struct MeshNodeRec {
 };
 static_assert(sizeof(MeshNodeRec) == 64, "node layout");
 
-// Builds the tree (2 * nt - 1 nodes, root 0) and the triangle soup (3 x xyzw
-// per triangle, in input order).  Returns 0, or -1 for an empty mesh, -2 for a
-// vertex index out of range.
+// Builds the reference's OBBRSS tree (2 * nt - 1 nodes, root 0, children of
+// a node in adjacent slots) with FP32 boxes that contain their triangles, and
+// the triangle soup (3 x xyzw per triangle, in input order).  sizes (if not
+// null) receives each node's FP64 |extent|^2 as the reference computes it,
+// depth (if not null) the deepest node's level (root 0).  Returns 0, or -1
+// for an empty mesh, -2 for a vertex index out of range.
 int build_obb_bvh(const float* vertices_xyz, uint32_t nv, const int32_t* tris, uint32_t nt,
-                  std::vector<MeshNodeRec>& nodes, std::vector<float>& tri_xyzw);
+                  std::vector<MeshNodeRec>& nodes, std::vector<float>& tri_xyzw, std::vector<double>* sizes = nullptr,
+                  uint32_t* depth = nullptr);
 
 }  // namespace fclg

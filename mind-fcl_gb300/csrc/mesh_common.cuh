@@ -69,6 +69,76 @@ __device__ __forceinline__ bool obb_overlap(const Pose& P, const Node& A, const 
   return true;
 }
 
+// Ordered traversal (both mesh kernels).  A pending node (pair) carries its
+// path key: the descent choices from the root, one bit per step (0 = the
+// child the reference visits first), left-aligned above a sentinel bit, so
+// that two keys compare as unsigned integers as their places in the
+// reference's depth-first visiting order.  Paths hold at most 62 steps.
+constexpr unsigned long long kRootKey = 1ull << 63;
+constexpr unsigned long long kNoKey = ~0ull;
+
+__device__ __forceinline__ unsigned long long child_key(unsigned long long k, unsigned later) {
+  const unsigned long long low = k & (~k + 1ull);  // sentinel
+  return (k & ~low) | (later ? low : 0ull) | (low >> 1);
+}
+
+__device__ __forceinline__ int pow2_at_least(int n) {
+  int p = 2;
+  while (p < n) p <<= 1;
+  return p;
+}
+
+// Sorts the first n2 (a power of two, n2 >= 2) buffer entries by key,
+// ascending: a bitonic network, the warp's lanes taking the compare-exchange
+// pairs of each step.
+__device__ __forceinline__ void warp_sort_keys(unsigned long long* key, int2* val, int n2, unsigned lane) {
+  for (int k = 2; k <= n2; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = (int)lane; i < n2; i += 32) {
+        const int l = i ^ j;
+        if (l > i) {
+          const unsigned long long ki = key[i], kl = key[l];
+          const bool up = (i & k) == 0;
+          if (up ? (ki > kl) : (ki < kl)) {
+            key[i] = kl;
+            key[l] = ki;
+            const int2 t = val[i];
+            val[i] = val[l];
+            val[l] = t;
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// Contacts kept in key order: entries [0, found) of (key, value) with
+// max_contacts + 32 slots.  After a round appended its hits, keep() sorts and
+// cuts to max_contacts once the buffer holds that many, and returns the key of
+// the last kept contact (kNoKey while fewer).
+__device__ __forceinline__ unsigned long long keep_first(unsigned long long* key, int2* val, int& found, int cap,
+                                                         unsigned lane, unsigned long long last) {
+  if (found < cap) return last;
+  const int n2 = pow2_at_least(found);
+  for (int i = found + (int)lane; i < n2; i += 32) key[i] = kNoKey;
+  __syncwarp();
+  warp_sort_keys(key, val, n2, lane);
+  found = cap;
+  const unsigned long long l = key[cap - 1];
+  __syncwarp();
+  return l;
+}
+
+// Final order of a buffer that never filled (found < max_contacts).
+__device__ __forceinline__ void sort_found(unsigned long long* key, int2* val, int found, int cap, unsigned lane) {
+  if (found <= 0 || found >= cap) return;
+  const int n2 = pow2_at_least(found);
+  for (int i = found + (int)lane; i < n2; i += 32) key[i] = kNoKey;
+  __syncwarp();
+  warp_sort_keys(key, val, n2, lane);
+}
+
 __device__ __forceinline__ f3 ldv(const float4* __restrict__ tris, uint32_t t, int k) {
   const float4 q = __ldg(tris + 3 * (size_t)t + k);
   return mk3(q.x, q.y, q.z);

@@ -10,6 +10,7 @@ struct MeshDev {
   const float4* tris;   // 3 float4 per triangle (x, y, z, 0)
   uint32_t n_nodes;
   uint32_t n_tris;
+  const double* size;   // [n_nodes] FP64 |extent|^2 of the reference's box (the descend key)
 };
 
 struct MeshArgs {
@@ -20,10 +21,24 @@ struct MeshArgs {
   uint8_t* flags;         // [n_poses]
   uint32_t* counts;       // [n_poses]
   int32_t* pairs;         // [n_poses][max_contacts][2] triangle ids (a, b)
-  uint32_t* status;       // [n_poses] or null: bit 0 stack overflow, bit 1 round limit
+  uint32_t* status;       // [n_poses] or null: bit 0 stack overflow, bit 1 round limit, bit 2 path too long
+  // per-warp contact buffers for max_contacts above the shared-memory buffer
+  // (mesh_contact_buffer_len entries per warp, mesh_collide_warps warps)
+  unsigned long long* cbuf_key = nullptr;
+  int2* cbuf_pair = nullptr;
+  uint32_t cbuf_len = 0;
+  // optional traffic counters (profiling): [0] node pairs whose boxes were
+  // tested, [1] triangle pairs tested
+  unsigned long long* counters = nullptr;
 };
 
 cudaError_t launch_mesh_collide(const MeshArgs& m, int blocks, cudaStream_t st);
+// Global contact-buffer entries per warp a request with max_contacts needs (0:
+// it fits in shared memory), and the warps a launch of `blocks` CTAs runs.
+int mesh_contact_buffer_len(uint32_t max_contacts);
+int mesh_collide_warps(int blocks);
+// CTAs of the mesh-mesh kernel that fit on the device at once.
+int mesh_collide_resident_blocks(int num_sms);
 
 // Mesh against shapes of the context (mesh_shape.cu): query i = shape
 // shape_ids[i] posed by poses[i] in the mesh frame.
@@ -48,9 +63,17 @@ struct MeshShapeArgs {
   float* contacts = nullptr;
   float epa_tol = 1e-6f;      // GJKSolver defaults: 256 faces, 255 iterations, 1e-6
   int epa_max_iter = 255;
+  // per-warp contact buffers for max_contacts above the shared-memory buffer
+  // (mesh_contact_buffer_len entries per warp, mesh_shape_warps warps)
+  unsigned long long* cbuf_key = nullptr;
+  int2* cbuf_val = nullptr;
+  uint32_t cbuf_len = 0;
 };
 
 cudaError_t launch_mesh_shape(const MeshShapeArgs& m, int blocks, cudaStream_t st);
+int mesh_shape_warps(int blocks);
+// CTAs of the mesh-shape kernel that fit on the device at once.
+int mesh_shape_resident_blocks(int num_sms, bool penetration);
 // The contacts of the triangles a penetration-mode launch reported
 // (mesh_contact.cu): sphere leaves in closed form, the others by GJK + EPA.
 cudaError_t launch_mesh_contacts(const MeshShapeArgs& m, int num_sms, cudaStream_t st);

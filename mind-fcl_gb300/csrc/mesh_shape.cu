@@ -11,11 +11,14 @@
 // (box_triangle-inl.h) for boxes, MPR::Intersect on (shape, triangle) for the
 // rest.  A query stops once it has max_contacts colliding triangles.
 //
-// GPU layout: as the mesh-mesh kernel -- node ids on a per-warp stack in
-// shared memory, up to 32 popped per round (one per lane), children pushed with
-// a warp prefix sum, contacts recorded in lane order.  The shape's box is
-// built once per query (a hull's extent by a warp reduction over its
-// vertices).  The sphere and box leaf tests run in FP32 and are re-decided in
+// GPU layout: as the mesh-mesh kernel -- node ids with their path keys on a
+// per-warp stack in shared memory kept in the reference's visiting order (the
+// second child first), up to 32 popped per round (one per lane) while 64
+// slots stay free, children pushed back above the entries that follow their
+// parent; colliding triangles go to a per-warp buffer with their keys and the
+// first max_contacts of the reference's order are kept and written in that
+// order.  The shape's box is built once per query (a hull's extent by a warp
+// reduction over its vertices).  The sphere and box leaf tests run in FP32 and are re-decided in
 // FP64 when a comparison sits within its rounding bound, so their verdicts
 // equal the FP64 ones; the MPR leaves run in FP32.
 #include "gjk.cuh"
@@ -29,7 +32,9 @@ namespace fclg {
 
 namespace {
 
-constexpr int kMsStack = 1024;
+constexpr int kMsStack = 512;
+constexpr int kMsPathRoom = 64;     // slots kept for a depth-first descent (path length <= 62)
+constexpr int kMsSmemContacts = 128;  // in-shared-memory contact buffer (max_contacts <= 96)
 constexpr int kMsWarps = 4;
 // CTAs per SM the kernel is compiled for (its register budget)
 #ifndef FCLG_MESH_SHAPE_MINB
@@ -39,6 +44,9 @@ constexpr int kMsMaxRounds = 1 << 22;  // bound against a corrupted tree
 
 struct MsSmem {
   uint32_t node[kMsStack];
+  unsigned long long key[kMsStack];
+  unsigned long long ckey[kMsSmemContacts];
+  int2 cval[kMsSmemContacts];
 };
 
 struct D3 {
@@ -245,6 +253,13 @@ __global__ void __launch_bounds__(kMsWarps * 32, FCLG_MESH_SHAPE_MINB) mesh_shap
   const unsigned lane = threadIdx.x & 31u;
   const uint32_t gw = blockIdx.x * kMsWarps + (threadIdx.x >> 5);
   const uint32_t nw = gridDim.x * kMsWarps;
+  const int cap = (int)m.max_contacts;
+  unsigned long long* ckey = S.ckey;
+  int2* cval = S.cval;
+  if (pow2_at_least(cap + 32) > kMsSmemContacts) {
+    ckey = m.cbuf_key + (size_t)gw * m.cbuf_len;
+    cval = m.cbuf_val + (size_t)gw * m.cbuf_len;
+  }
   for (uint32_t q = gw; q < m.n; q += nw) {
     Pose X;  // the shape in the mesh frame
     {
@@ -294,28 +309,43 @@ __global__ void __launch_bounds__(kMsWarps * 32, FCLG_MESH_SHAPE_MINB) mesh_shap
       sup.g = Group<1>::make();
       const f3 interior_a = load_interior(m.shapes, sid, shp.type);
 
-      if (lane == 0) S.node[0] = 0;
+      if (lane == 0) {
+        S.node[0] = 0;
+        S.key[0] = kRootKey;
+      }
       int size = 1;
+      unsigned long long last = kNoKey;  // key of the max_contacts-th kept contact once the buffer is full
       __syncwarp();
-      for (int round = 0; size > 0 && found < (int)m.max_contacts; ++round) {
+      for (int round = 0; size > 0; ++round) {
         if (round >= kMsMaxRounds) { status |= 2u; break; }
+        // the earliest pending node comes after every kept contact: done
+        if (found >= cap && S.key[size - 1] > last) break;
         int k = size < 32 ? size : 32;
-        if (k > kMsStack - size) k = kMsStack - size;  // room for two children per popped node
-        if (k <= 0) { status |= 1u; break; }
-        const bool active = (int)lane < k;
+        const int room = kMsStack - kMsPathRoom - size;
+        if (k > room) k = room > 1 ? room : 1;
+        if (size + k > kMsStack) { status |= 1u; break; }  // unreachable: a descent needs <= 62 slots
+        const bool popped = (int)lane < k;
         uint32_t id = 0;
-        if (active) id = S.node[size - 1 - lane];
+        unsigned long long key = kNoKey;
+        if (popped) {
+          id = S.node[size - 1 - lane];
+          key = S.key[size - 1 - lane];
+        }
         size -= k;
         __syncwarp();
         int push = 0;
         bool hit = false;
         uint32_t child = 0, tri = 0;
-        if (active && id < m.mesh.n_nodes) {
+        if (popped && key < last && id < m.mesh.n_nodes) {
           const Node N = load_node(m.mesh.nodes, id);
           if (obb_overlap(I, SB, N)) {
             if (N.child >= 0) {
-              push = 2;
-              child = (uint32_t)N.child;
+              if ((key & 1ull) == 0ull) {
+                push = 2;
+                child = (uint32_t)N.child;
+              } else {
+                status |= 8u;  // path longer than the key holds (rejected on the host)
+              }
             } else {
               tri = (uint32_t)(-(N.child + 1));
               if (tri < m.mesh.n_tris) {
@@ -361,37 +391,57 @@ __global__ void __launch_bounds__(kMsWarps * 32, FCLG_MESH_SHAPE_MINB) mesh_shap
             }
           }
         }
+        // Children go back above the entries that follow their parent (lane j's
+        // below those of lanes < j), the second child on top: the reference
+        // pushes the first child, then the second, and pops the second first.
         int incl = push;
 #pragma unroll
         for (int off = 1; off < 32; off <<= 1) {
-          const int t = __shfl_up_sync(0xFFFFFFFFu, incl, off);
-          if ((int)lane >= off) incl += t;
+          const int t = __shfl_down_sync(0xFFFFFFFFu, incl, off);
+          if ((int)lane + off < 32) incl += t;
         }
-        const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+        const int total = __shfl_sync(0xFFFFFFFFu, incl, 0);
         if (push) {
-          // the second child on top: popped first, as the reference's stack does
           const int o = size + incl - push;
-          S.node[o] = child;
           S.node[o + 1] = child + 1;
+          S.key[o + 1] = child_key(key, 0);
+          S.node[o] = child;
+          S.key[o] = child_key(key, 1);
         }
         size += total;
         const unsigned hm = __ballot_sync(0xFFFFFFFFu, hit);
         if (hit) {
           const int slot = found + __popc(hm & ((1u << lane) - 1u));
-          if (slot < (int)m.max_contacts) m.tri_ids[(size_t)q * m.max_contacts + slot] = (int32_t)tri;
+          ckey[slot] = key;
+          cval[slot] = make_int2((int)tri, 0);
         }
         found += __popc(hm);
         __syncwarp();
+        if (hm) last = keep_first(ckey, cval, found, cap, lane, last);
       }
+      sort_found(ckey, cval, found, cap, lane);
+      for (int i = (int)lane; i < found; i += 32) m.tri_ids[(size_t)q * m.max_contacts + i] = cval[i].x;
+      __syncwarp();
     }
     if (lane == 0) {
-      const uint32_t cnt = found < (int)m.max_contacts ? (uint32_t)found : m.max_contacts;
+      const uint32_t cnt = (uint32_t)found;
       m.counts[q] = cnt;
       m.flags[q] = cnt > 0 ? 1 : 0;
       if (m.status) m.status[q] = status | (sid < m.n_shapes ? 0u : 4u);
     }
     __syncwarp();
   }
+}
+
+int mesh_shape_warps(int blocks) { return blocks * kMsWarps; }
+
+int mesh_shape_resident_blocks(int num_sms, bool penetration) {
+  int per_sm = 0;
+  const cudaError_t e =
+      penetration ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mesh_shape_kernel<true>, kMsWarps * 32, 0)
+                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mesh_shape_kernel<false>, kMsWarps * 32, 0);
+  if (e != cudaSuccess || per_sm < 1) per_sm = 1;
+  return num_sms * per_sm;
 }
 
 cudaError_t launch_mesh_shape(const MeshShapeArgs& m, int blocks, cudaStream_t st) {

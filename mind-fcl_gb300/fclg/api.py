@@ -11,7 +11,7 @@ import numpy as np
 from .layout import PAIR_DTYPE, RESULT_DTYPE, SHAPE_DTYPE
 
 PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-LIB_PATH = os.path.join(PKG, "lib", "libfclg.so")
+LIB_PATH = os.environ.get("FCLG_LIB") or os.path.join(PKG, "lib", "libfclg.so")
 
 FCLG_REQ_BOOLEAN_ONLY = 1
 FCLG_REQ_NO_EPA = 2
@@ -28,8 +28,8 @@ EXPORTS = [
     "fclg_set_shapes", "fclg_set_shapes_device",
     "fclg_distance", "fclg_distance_device", "fclg_distance_device_static", "fclg_collide", "fclg_collide_device",
     "fclg_set_launch", "fclg_set_tuning", "fclg_get_tuning", "fclg_launch_count", "fclg_set_profiling",
-    "fclg_pass_times", "fclg_bvh_build", "fclg_mesh_create", "fclg_mesh_destroy", "fclg_mesh_info", "fclg_mesh_export",
-    "fclg_mesh_collide", "fclg_mesh_collide_device",
+    "fclg_pass_times", "fclg_bvh_build", "fclg_bvh_node_sizes", "fclg_mesh_create", "fclg_mesh_destroy", "fclg_mesh_info", "fclg_mesh_export",
+    "fclg_mesh_collide", "fclg_mesh_collide_device", "fclg_mesh_traffic",
     "fclg_warmstart_create", "fclg_warmstart_destroy", "fclg_warmstart_last_error", "fclg_warmstart_param_count",
     "fclg_warmstart_get_params", "fclg_warmstart_set_params", "fclg_warmstart_predict", "fclg_warmstart_forward",
     "fclg_warmstart_gradient", "fclg_warmstart_train", "fclg_set_warmstart", "fclg_warmstart_status",
@@ -67,14 +67,14 @@ class Tuning(ctypes.Structure):
     _fields_ = [("bucketing", ctypes.c_int32), ("gjk_lanes_small", ctypes.c_int32),
                 ("gjk_lanes_large", ctypes.c_int32), ("large_hull_vertices", ctypes.c_int32),
                 ("gjk_ctas_per_sm", ctypes.c_int32), ("epa_ctas_per_sm", ctypes.c_int32),
-                ("support_walk", ctypes.c_int32), ("gjk_refill", ctypes.c_int32)]
+                ("support_walk", ctypes.c_int32), ("gjk_refill", ctypes.c_int32), ("epa_resume", ctypes.c_int32)]
 
 
 class Request(ctypes.Structure):
     _fields_ = [("gjk_max_iterations", ctypes.c_uint32), ("epa_max_faces", ctypes.c_uint32),
                 ("epa_max_iterations", ctypes.c_uint32), ("flags", ctypes.c_uint32),
                 ("gjk_tolerance", ctypes.c_float), ("epa_tolerance", ctypes.c_float),
-                ("reserved", ctypes.c_float * 2)]
+                ("warm_gap", ctypes.c_float), ("warm_probe", ctypes.c_uint32)]
 
 
 _lib = None
@@ -122,6 +122,8 @@ def load_library(path=LIB_PATH):
     lib.fclg_pass_times.restype = i32
     lib.fclg_bvh_build.argtypes = [vp, u32, vp, u32, vp, vp]
     lib.fclg_bvh_build.restype = i32
+    lib.fclg_bvh_node_sizes.argtypes = [vp, u32, vp, u32, vp, ctypes.POINTER(u32)]
+    lib.fclg_bvh_node_sizes.restype = i32
     lib.fclg_mesh_create.argtypes = [vp, vp, u32, vp, u32, ctypes.POINTER(vp)]
     lib.fclg_mesh_create.restype = i32
     lib.fclg_mesh_destroy.argtypes = [vp]
@@ -134,6 +136,8 @@ def load_library(path=LIB_PATH):
     lib.fclg_mesh_collide.restype = i32
     lib.fclg_mesh_collide_device.argtypes = [vp, vp, vp, vp, u32, u32, vp, vp, vp, vp, vp]
     lib.fclg_mesh_collide_device.restype = i32
+    lib.fclg_mesh_traffic.argtypes = [vp, ctypes.POINTER(u64), ctypes.POINTER(u64), i32]
+    lib.fclg_mesh_traffic.restype = i32
     lib.fclg_warmstart_create.argtypes = [i32, u32, u32, ctypes.POINTER(vp)]
     lib.fclg_warmstart_create.restype = i32
     lib.fclg_warmstart_destroy.argtypes = [vp]
@@ -204,9 +208,12 @@ def _ptr(a):
     return ctypes.c_void_p(a.ctypes.data) if a is not None else None
 
 
-def make_request(flags=0, gjk_tol=0.0, epa_tol=0.0, gjk_max_iter=0, epa_max_faces=0, epa_max_iter=0):
+def make_request(flags=0, gjk_tol=0.0, epa_tol=0.0, gjk_max_iter=0, epa_max_faces=0, epa_max_iter=0,
+                 warm_gap=0.0, warm_probe=0):
     r = Request()
     r.flags = flags
+    r.warm_gap = warm_gap
+    r.warm_probe = warm_probe
     r.gjk_tolerance = gjk_tol
     r.epa_tolerance = epa_tol
     r.gjk_max_iterations = gjk_max_iter
@@ -298,7 +305,7 @@ class Context:
         """Fields of fclg_tuning by name; unspecified ones keep their value."""
         t = Tuning()
         for k, v in kw.items():
-            if k in ("bucketing", "support_walk", "gjk_refill") and isinstance(v, bool):
+            if k in ("bucketing", "support_walk", "gjk_refill", "epa_resume") and isinstance(v, bool):
                 v = 1 if v else -1
             setattr(t, k, int(v))
         self._check(self.lib.fclg_set_tuning(self.h, ctypes.byref(t)), "fclg_set_tuning")
@@ -317,6 +324,14 @@ class Context:
         self._check(self.lib.fclg_pass_times(self.h, ctypes.byref(g), ctypes.byref(e), ctypes.byref(q), int(reset)),
                     "fclg_pass_times")
         return g.value, e.value, q.value
+
+    def mesh_traffic(self, reset=True):
+        """(node pairs, triangle pairs) tested by mesh-mesh queries run while
+        profiling was on, since the last reset."""
+        a, b = ctypes.c_uint64(), ctypes.c_uint64()
+        self._check(self.lib.fclg_mesh_traffic(self.h, ctypes.byref(a), ctypes.byref(b), int(reset)),
+                    "fclg_mesh_traffic")
+        return a.value, b.value
 
     @property
     def launch_count(self):
@@ -613,6 +628,20 @@ def hull_graph(points):
     if rc != 0:
         raise FclgError("fclg_hull_graph failed (%d)" % rc)
     return starts, first, adj[:m.value]
+
+
+def bvh_node_sizes(vertices, triangles):
+    """Host-only: each node's FP64 |extent|^2 (the traversal's descend key) and
+    the tree depth."""
+    lib = load_library()
+    v = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+    t = np.ascontiguousarray(triangles, np.int32).reshape(-1, 3)
+    sizes = np.zeros(2 * len(t) - 1)
+    depth = ctypes.c_uint32(0)
+    rc = lib.fclg_bvh_node_sizes(_ptr(v), len(v), _ptr(t), len(t), _ptr(sizes), ctypes.byref(depth))
+    if rc != 0:
+        raise FclgError("fclg_bvh_node_sizes failed (%d)" % rc)
+    return sizes, depth.value
 
 
 def bvh_build(vertices, triangles):

@@ -15,6 +15,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libfcl_ref.so")
+REF_MESH_PATH = os.path.join(HERE, "_ref", "libfcl_ref_mesh.so")
 
 RESULT_DTYPE = np.dtype(
     [("distance", "<f8"), ("p0", "<f8", (3,)), ("p1", "<f8", (3,)), ("normal", "<f8", (3,)),
@@ -34,9 +35,8 @@ def build(force=False):
             os.path.exists(os.path.join(HERE, f))]
     if force or not os.path.exists(LIB_PATH) or any(os.path.getmtime(s) > os.path.getmtime(LIB_PATH) for s in srcs):
         subprocess.check_call(["g++", *_CXXFLAGS, os.path.join(HERE, "oracle.cpp"), "-o", LIB_PATH, "-lpthread"])
-    ref_root = os.environ.get("REF_ROOT", "/root/reference")
-    if os.path.isdir(os.path.join(ref_root, "include", "fcl", "cvx_collide")):
-        subprocess.check_call(["bash", os.path.join(HERE, "build_ref.sh")])
+    # the recipe decides where the reference sources are and skips when absent
+    subprocess.check_call(["bash", os.path.join(HERE, "build_ref.sh")])
 
 
 _lib = None
@@ -68,6 +68,10 @@ def _load():
         lib.orc_mesh_collide.restype = i
         lib.orc_mesh_allpairs.argtypes = [vp, i, vp, i, vp, vp, i]
         lib.orc_mesh_allpairs.restype = i
+        lib.orc_ref_tree.argtypes = [vp, vp, i, vp, vp, vp]
+        lib.orc_ref_tree.restype = i
+        lib.orc_ref_mesh_collide.argtypes = [vp, vp, i, vp, vp, i, vp, i, i, vp, vp, i, i]
+        lib.orc_ref_mesh_collide.restype = i
         lib.orc_tri_tri.argtypes = [vp, vp, vp]
         lib.orc_tri_tri.restype = i
         lib.orc_set_walk.argtypes = [vp, i, vp]
@@ -111,6 +115,36 @@ def _load_ref():
         lib.ref_collide.restype = i
         _ref = lib
     return _ref
+
+
+def ref_mesh_available():
+    return os.path.exists(REF_MESH_PATH)
+
+
+_ref_mesh = None
+
+
+def _load_ref_mesh():
+    global _ref_mesh
+    if _ref_mesh is None:
+        lib = ctypes.CDLL(REF_MESH_PATH)
+        vp, i = ctypes.c_void_p, ctypes.c_int
+        lib.refm_build.argtypes = [vp, i, vp, i]
+        lib.refm_build.restype = vp
+        lib.refm_free.argtypes = [vp]
+        lib.refm_free.restype = None
+        lib.refm_num_nodes.argtypes = [vp]
+        lib.refm_num_nodes.restype = i
+        lib.refm_export.argtypes = [vp, vp, vp]
+        lib.refm_export.restype = None
+        lib.refm_mesh_collide.argtypes = [vp, vp, vp, i, i, vp, vp, i, i]
+        lib.refm_mesh_collide.restype = i
+        lib.refm_analytic.argtypes = [vp, vp, vp, i, vp, vp, i]
+        lib.refm_analytic.restype = i
+        lib.refm_mesh_shape_collide.argtypes = [vp, i, vp, vp, i, vp, i, i, vp, i, i, vp, vp, i, i]
+        lib.refm_mesh_shape_collide.restype = i
+        _ref_mesh = lib
+    return _ref_mesh
 
 
 def _ptr(a):
@@ -556,3 +590,144 @@ def box_pair_ccd(h1, axis, dist, R, t, h2, zero_tol=1e-4):
     e = _load().orc_box_pair_ccd(_ptr(a[0]), _ptr(a[1]), ctypes.c_double(dist), _ptr(a[2]), _ptr(a[3]), _ptr(a[4]),
                                  ctypes.c_double(zero_tol), _ptr(out))
     return bool(e), out[0], out[1]
+
+
+# ------------------------------------------------ mesh: the reference's tree --
+
+def _mesh_arrays(vertices, triangles):
+    V = np.ascontiguousarray(vertices, np.float64).reshape(-1, 3)
+    T = np.ascontiguousarray(triangles, np.int32).reshape(-1, 3)
+    return V, T
+
+
+def ref_tree(vertices, triangles):
+    """The reference's own BVHModel<OBBRSS<double>> over the mesh (compiled
+    reference): (f64[n, 16] = axis row-major 9, To 3, extent 3, size;
+    i32[n, 3] = first_child, first_primitive, num_primitives)."""
+    lib = _load_ref_mesh()
+    V, T = _mesh_arrays(vertices, triangles)
+    h = lib.refm_build(_ptr(V), len(V), _ptr(T), len(T))
+    assert h, "reference BVH build failed"
+    try:
+        n = lib.refm_num_nodes(h)
+        f64 = np.zeros((n, 16))
+        i32 = np.zeros((n, 3), np.int32)
+        lib.refm_export(h, _ptr(f64), _ptr(i32))
+    finally:
+        lib.refm_free(h)
+    return f64, i32
+
+
+def orc_tree(vertices, triangles):
+    """The restated build of the same tree: (f64, i32, primitive order)."""
+    lib = _load()
+    V, T = _mesh_arrays(vertices, triangles)
+    n = max(2 * len(T) - 1, 0)
+    f64 = np.zeros((n, 16))
+    i32 = np.zeros((n, 3), np.int32)
+    prim = np.zeros(len(T), np.uint32)
+    assert lib.orc_ref_tree(_ptr(V), _ptr(T), len(T), _ptr(f64), _ptr(i32), _ptr(prim)) == n
+    return f64, i32, prim
+
+
+def _collide_out(n, stride):
+    return np.zeros(n, np.int32), np.full((n, max(stride, 1), 2), -1, np.int32)
+
+
+def ref_mesh_collide(mesh_a, mesh_b, poses, max_contacts=1, stride=None, threads=None):
+    """The compiled reference's MeshIntersect per pose (mesh a at the identity,
+    mesh b posed by poses[i]: 12 values, rotation row-major then translation)
+    with CollisionRequest(max_contacts).  Returns (counts, pairs[n, stride, 2])
+    in the reference's contact order."""
+    lib = _load_ref_mesh()
+    Va, Ta = _mesh_arrays(*mesh_a)
+    Vb, Tb = _mesh_arrays(*mesh_b)
+    P = np.ascontiguousarray(poses, np.float64).reshape(-1, 12)
+    stride = max_contacts if stride is None else stride
+    ha = lib.refm_build(_ptr(Va), len(Va), _ptr(Ta), len(Ta))
+    hb = lib.refm_build(_ptr(Vb), len(Vb), _ptr(Tb), len(Tb))
+    assert ha and hb
+    try:
+        counts, pairs = _collide_out(len(P), stride)
+        assert lib.refm_mesh_collide(ha, hb, _ptr(P), len(P), int(max_contacts), _ptr(counts), _ptr(pairs),
+                                     max(stride, 1), threads or default_threads()) == 0
+    finally:
+        lib.refm_free(ha)
+        lib.refm_free(hb)
+    return counts, pairs
+
+
+def orc_mesh_collide_ref(mesh_a, mesh_b, poses, max_contacts=1, stride=None, threads=None):
+    """The restated MeshIntersect over the restated reference trees (same
+    interface as ref_mesh_collide)."""
+    lib = _load()
+    Va, Ta = _mesh_arrays(*mesh_a)
+    Vb, Tb = _mesh_arrays(*mesh_b)
+    P = np.ascontiguousarray(poses, np.float64).reshape(-1, 12)
+    stride = max_contacts if stride is None else stride
+    counts, pairs = _collide_out(len(P), stride)
+    assert lib.orc_ref_mesh_collide(_ptr(Va), _ptr(Ta), len(Ta), _ptr(Vb), _ptr(Tb), len(Tb), _ptr(P), len(P),
+                                    int(max_contacts), _ptr(counts), _ptr(pairs), max(stride, 1),
+                                    threads or default_threads()) == 0
+    return counts, pairs
+
+
+ANALYTIC_SHAPE_DTYPE = np.dtype([("type", "<i4"), ("pad", "<i4"), ("p", "<f8", (3,))])
+
+
+def ref_analytic(types_a, params_a, types_b, params_b, poses, threads=None):
+    """The compiled reference's GJKSolver::shapeIntersect with contacts on
+    closed-form pairs (types 0 sphere, 1 box, 2 capsule, 3 cylinder; params:
+    radius / full sides / radius and full length), shape a at the identity and
+    shape b posed by poses[i].  Returns (count[n] (-1: not a closed-form pair),
+    contacts[n, 4, 7] = normal 3, pos 3, depth)."""
+    lib = _load_ref_mesh()
+    n = len(types_a)
+    A = np.zeros(n, ANALYTIC_SHAPE_DTYPE)
+    B = np.zeros(n, ANALYTIC_SHAPE_DTYPE)
+    A["type"], A["p"] = types_a, params_a
+    B["type"], B["p"] = types_b, params_b
+    P = np.ascontiguousarray(poses, np.float64).reshape(-1, 12)
+    out = np.zeros((n, 4, 7))
+    ret = np.zeros(n, np.int32)
+    assert lib.refm_analytic(_ptr(A), _ptr(B), _ptr(P), n, _ptr(out), _ptr(ret), threads or default_threads()) == 0
+    return ret, out
+
+
+def ref_mesh_shape_collide(mesh, batch, shape_id, poses, max_contacts=1, stride=None, threads=None):
+    """The compiled reference's MeshShapeIntersect of a mesh (vertices,
+    triangles) against one shape of `batch` (sphere, box, capsule, cylinder or
+    convex hull; a hull gets scipy's triangulated hull faces) posed by
+    poses[i] in the mesh frame.  Returns (counts, tris[n, stride]) in the
+    reference's order."""
+    from fclg.layout import BOX, CAPSULE, CONVEX, CYLINDER, SPHERE
+    lib = _load_ref_mesh()
+    s = batch.shapes[shape_id]
+    t = int(s["type"])
+    code = {SPHERE: 0, BOX: 1, CAPSULE: 2, CYLINDER: 3, CONVEX: 4}[t]
+    params = np.ascontiguousarray(s["param"][:3], np.float64)
+    hv = np.zeros((1, 3))
+    faces = np.zeros(1, np.int32)
+    n_faces = 0
+    if t == CONVEX:
+        from scipy.spatial import ConvexHull
+        hv = np.ascontiguousarray(batch.vertices[s["vert_offset"]:s["vert_offset"] + s["vert_count"], :3],
+                                  np.float64)
+        hull = ConvexHull(hv)
+        n_faces = len(hull.simplices)
+        faces = np.concatenate([np.full((n_faces, 1), 3), hull.simplices], 1).astype(np.int32).ravel()
+    V, T = _mesh_arrays(*mesh)
+    P = np.ascontiguousarray(poses, np.float64).reshape(-1, 12)
+    stride = max_contacts if stride is None else stride
+    h = lib.refm_build(_ptr(V), len(V), _ptr(T), len(T))
+    assert h
+    try:
+        counts = np.zeros(len(P), np.int32)
+        tris = np.full((len(P), max(stride, 1)), -1, np.int32)
+        rc = lib.refm_mesh_shape_collide(h, code, _ptr(params), _ptr(hv), len(hv), _ptr(faces), n_faces, len(faces),
+                                         _ptr(P), len(P), int(max_contacts), _ptr(counts), _ptr(tris),
+                                         max(stride, 1), threads or default_threads())
+        assert rc == 0
+    finally:
+        lib.refm_free(h)
+    return counts, tris

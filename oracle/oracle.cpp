@@ -618,6 +618,67 @@ int orc_mesh_allpairs(const float* tris_a, int n_a, const float* tris_b, int n_b
   return (int)c.size();
 }
 
+// The reference's OBBRSS tree over nt triangles (FP64 vertices, restated
+// BVHModel<OBBRSS<double>>::endModel).  Returns the node count (2 nt - 1);
+// f64 (may be null): per node axis (9, row-major), To, extent, size; i32 (may
+// be null): first_child, first_primitive, num_primitives; prim (may be null):
+// the primitive order after the build.
+int orc_ref_tree(const double* V, const int32_t* T, int nt, double* f64, int32_t* i32, uint32_t* prim) {
+  std::vector<orc::RefNode> nodes;
+  std::vector<uint32_t> pr;
+  orc::buildRefTree(V, T, nt, nodes, pr);
+  for (size_t i = 0; i < nodes.size(); ++i) {
+    const orc::RefNode& n = nodes[i];
+    if (f64) {
+      double* d = f64 + 16 * i;
+      for (int k = 0; k < 9; ++k) d[k] = n.axis[k];
+      for (int k = 0; k < 3; ++k) {
+        d[9 + k] = n.To[k];
+        d[12 + k] = n.extent[k];
+      }
+      d[15] = n.size;
+    }
+    if (i32) {
+      i32[3 * i] = n.first_child;
+      i32[3 * i + 1] = n.first_primitive;
+      i32[3 * i + 2] = n.num_primitives;
+    }
+  }
+  if (prim)
+    for (int i = 0; i < nt; ++i) prim[i] = pr[i];
+  return (int)nodes.size();
+}
+
+// MeshIntersect per pose over the reference's own trees, rebuilt here from the
+// FP64 vertices (restated endModel): mesh a at the identity, mesh b posed by
+// poses[i] (12 doubles: rotation row-major, translation).  counts[i] = the
+// number of contacts (at most max_contacts), pairs[i][k] = (b1, b2) of contact
+// k in the reference's order, for k < stride.
+int orc_ref_mesh_collide(const double* Va, const int32_t* Ta, int nta, const double* Vb, const int32_t* Tb, int ntb,
+                         const double* poses, int n_poses, int max_contacts, int32_t* counts, int32_t* pairs,
+                         int stride, int n_threads) {
+  if (nta <= 0 || ntb <= 0 || max_contacts <= 0) return -1;
+  std::vector<orc::RefNode> na, nb;
+  std::vector<uint32_t> pa, pb;
+  orc::buildRefTree(Va, Ta, nta, na, pa);
+  orc::buildRefTree(Vb, Tb, ntb, nb, pb);
+  parallelFor(n_poses, n_threads, [&](int b, int e) {
+    std::vector<std::pair<int, int>> c;
+    for (int i = b; i < e; ++i) {
+      orc::Mat3 R;
+      for (int k = 0; k < 9; ++k) R.m[k] = poses[12 * (size_t)i + k];
+      const double T[3] = {poses[12 * (size_t)i + 9], poses[12 * (size_t)i + 10], poses[12 * (size_t)i + 11]};
+      orc::meshIntersectRef(na.data(), Va, Ta, nb.data(), Vb, Tb, R, T, (size_t)max_contacts, c);
+      counts[i] = (int32_t)c.size();
+      for (size_t k = 0; k < c.size() && (int)k < stride; ++k) {
+        pairs[2 * ((size_t)stride * i + k)] = c[k].first;
+        pairs[2 * ((size_t)stride * i + k) + 1] = c[k].second;
+      }
+    }
+  });
+  return 0;
+}
+
 // One triangle-triangle verdict (intersect_Triangle, boolean).
 int orc_tri_tri(const double* p /* 9 */, const double* q /* 9 */, const double* pose /* 12 */) {
   orc::Mat3 R;

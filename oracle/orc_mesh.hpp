@@ -3,13 +3,16 @@
 // FP64 restatement of mind-fcl's OBB BVH-vs-BVH boolean collision
 // (OrientedNodeBVHSolver::MeshIntersect with penetration off): the OBB overlap
 // test, the triangle-triangle separating-axis test, and the traversal order.
-// The BVH itself is an input (the flattened tree the GPU library builds), so
-// the oracle and the GPU traverse the same tree; the set of colliding triangle
-// pairs does not depend on the tree.
+// meshIntersect traverses a given flattened FP32 tree (the one the GPU
+// library builds); buildRefTree / meshIntersectRef restate the reference's
+// own FP64 OBBRSS tree and traverse it exactly as the reference does, so that
+// the order of reported contacts, and with it the contacts a capped request
+// keeps, follow the reference's.
 #pragma once
 
 #include <cmath>
 #include <cstdint>
+#include <limits>
 #include <utility>
 #include <vector>
 
@@ -190,6 +193,314 @@ inline void meshIntersect(const MeshNode* na, const float* tri_a, const MeshNode
     } else {
       stack.emplace_back(task.first, b.child);
       stack.emplace_back(task.first, b.child + 1);
+    }
+  }
+}
+
+// ------------------------------------------------ the reference's OBBRSS tree --
+//
+// FP64 restatement of BVHModel<OBBRSS<double>>::endModel on a triangle mesh
+// (geometry/bvh/BVH_model-inl.h:403-440 buildTreeIterativeImpl, :450-570
+// iterativeBuildTree) with the default mean splitter: each node's OBB is fitted
+// by FitImpl<S, OBBRSS<S>> (geometry/bvh/detail/BV_fitter-inl.h:323-345:
+// getCovariance, eigen_old, axisFromEigen, getExtentAndCenter), the split
+// vector is the OBB's first axis (BV_splitter-inl.h:449-454), the split value
+// the mean of the triangle centroids projected on it (computeSplitValue_mean,
+// :464-506), a triangle goes right when its centroid projects above it
+// (ApplyImpl<OBBRSS>, :411-415), an empty side falls back to half / half, and
+// the children take the next two node slots (left first) with the left
+// subtree built first.  Only the OBB half of OBBRSS is kept: the traversal's
+// overlap test and the split read only the OBB (OBBRSS-inl.h:114-116, 132-137).
+struct RefNode {
+  double axis[9];  // row-major; columns are the box axes (OBB::axis)
+  double To[3];
+  double extent[3];
+  double size;     // extent.squaredNorm() (OBB::size, OBB-inl.h:153-156)
+  int first_child, first_primitive, num_primitives;
+};
+
+// geometry-inl.h:712-767 (triangles only)
+inline void refCovariance(const double* V, const int32_t* T, const uint32_t* idx, int n, double M[9]) {
+  double S1[3] = {0, 0, 0};
+  double S2[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  int n_points = 0;
+  for (int i = 0; i < n; ++i) {
+    const int32_t* t = T + 3 * (size_t)idx[i];
+    const double* p1 = V + 3 * (size_t)t[0];
+    const double* p2 = V + 3 * (size_t)t[1];
+    const double* p3 = V + 3 * (size_t)t[2];
+    for (int k = 0; k < 3; ++k) S1[k] += (p1[k] + p2[k]) + p3[k];
+    S2[0][0] += (p1[0] * p1[0] + p2[0] * p2[0] + p3[0] * p3[0]);
+    S2[1][1] += (p1[1] * p1[1] + p2[1] * p2[1] + p3[1] * p3[1]);
+    S2[2][2] += (p1[2] * p1[2] + p2[2] * p2[2] + p3[2] * p3[2]);
+    S2[0][1] += (p1[0] * p1[1] + p2[0] * p2[1] + p3[0] * p3[1]);
+    S2[0][2] += (p1[0] * p1[2] + p2[0] * p2[2] + p3[0] * p3[2]);
+    S2[1][2] += (p1[1] * p1[2] + p2[1] * p2[2] + p3[1] * p3[2]);
+    n_points += 3;
+  }
+  M[0] = S2[0][0] - S1[0] * S1[0] / n_points;
+  M[4] = S2[1][1] - S1[1] * S1[1] / n_points;
+  M[8] = S2[2][2] - S1[2] * S1[2] / n_points;
+  M[1] = S2[0][1] - S1[0] * S1[1] / n_points;
+  M[5] = S2[1][2] - S1[1] * S1[2] / n_points;
+  M[2] = S2[0][2] - S1[0] * S1[2] / n_points;
+  M[3] = M[1];
+  M[6] = M[2];
+  M[7] = M[5];
+}
+
+// eigen_old, geometry-inl.h:236-337: cyclic Jacobi with the Numerical-Recipes
+// threshold schedule.  vout receives the rotation's rows as its columns
+// (row-major here: vout[3 * r + c] = v[c][r]); dout the eigenvalues.  Both
+// stay untouched when 50 sweeps do not clear the off-diagonal.
+inline void refEigenOld(const double m[9], double dout[3], double vout[9]) {
+  double R[9];
+  for (int k = 0; k < 9; ++k) R[k] = m[k];
+  auto Rr = [&](int r, int c) -> double& { return R[3 * r + c]; };
+  const int n = 3;
+  double b[3], z[3], d[3];
+  double v[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  for (int ip = 0; ip < n; ++ip) {
+    b[ip] = d[ip] = Rr(ip, ip);
+    z[ip] = 0;
+  }
+  for (int i = 0; i < 50; ++i) {
+    double sm = 0;
+    for (int ip = 0; ip < n; ++ip)
+      for (int iq = ip + 1; iq < n; ++iq) sm += std::abs(Rr(ip, iq));
+    if (sm == 0.0) {
+      for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r) vout[3 * r + c] = v[c][r];
+      for (int k = 0; k < 3; ++k) dout[k] = d[k];
+      return;
+    }
+    const double tresh = (i < 3) ? 0.2 * sm / (n * n) : 0.0;
+    for (int ip = 0; ip < n; ++ip) {
+      for (int iq = ip + 1; iq < n; ++iq) {
+        double g = 100.0 * std::abs(Rr(ip, iq));
+        if (i > 3 && std::abs(d[ip]) + g == std::abs(d[ip]) && std::abs(d[iq]) + g == std::abs(d[iq])) {
+          Rr(ip, iq) = 0.0;
+        } else if (std::abs(Rr(ip, iq)) > tresh) {
+          double h = d[iq] - d[ip];
+          double t;
+          if (std::abs(h) + g == std::abs(h)) {
+            t = (Rr(ip, iq)) / h;
+          } else {
+            const double theta = 0.5 * h / (Rr(ip, iq));
+            t = 1.0 / (std::abs(theta) + std::sqrt(1.0 + theta * theta));
+            if (theta < 0.0) t = -t;
+          }
+          const double c = 1.0 / std::sqrt(1 + t * t);
+          const double s = t * c;
+          const double tau = s / (1.0 + c);
+          h = t * Rr(ip, iq);
+          z[ip] -= h;
+          z[iq] += h;
+          d[ip] -= h;
+          d[iq] += h;
+          Rr(ip, iq) = 0.0;
+          auto rot = [&](double& x, double& y) {
+            const double gg = x, hh = y;
+            x = gg - s * (hh + gg * tau);
+            y = hh + s * (gg - hh * tau);
+          };
+          for (int j = 0; j < ip; ++j) rot(Rr(j, ip), Rr(j, iq));
+          for (int j = ip + 1; j < iq; ++j) rot(Rr(ip, j), Rr(j, iq));
+          for (int j = iq + 1; j < n; ++j) rot(Rr(ip, j), Rr(iq, j));
+          for (int j = 0; j < n; ++j) rot(v[j][ip], v[j][iq]);
+        }
+      }
+    }
+    for (int ip = 0; ip < n; ++ip) {
+      b[ip] += z[ip];
+      d[ip] = b[ip];
+      z[ip] = 0.0;
+    }
+  }
+}
+
+// axisFromEigen (Matrix3 form), geometry-inl.h:339-366: columns 0 and 1 are
+// the eigenvector rows of the largest and middle eigenvalue, column 2 their
+// cross product.
+inline void refAxisFromEigen(const double E[9], const double s[3], double axis[9]) {
+  int mn, md, mx;
+  if (s[0] > s[1]) {
+    mx = 0;
+    mn = 1;
+  } else {
+    mn = 0;
+    mx = 1;
+  }
+  if (s[2] < s[mn]) {
+    md = mn;
+    mn = 2;
+  } else if (s[2] > s[mx]) {
+    md = mx;
+    mx = 2;
+  } else {
+    md = 2;
+  }
+  double c0[3], c1[3];
+  for (int k = 0; k < 3; ++k) {
+    c0[k] = E[3 * mx + k];
+    c1[k] = E[3 * md + k];
+  }
+  for (int k = 0; k < 3; ++k) {
+    axis[3 * k] = c0[k];
+    axis[3 * k + 1] = c1[k];
+  }
+  axis[2] = c0[1] * c1[2] - c0[2] * c1[1];
+  axis[5] = c0[2] * c1[0] - c0[0] * c1[2];
+  axis[8] = c0[0] * c1[1] - c0[1] * c1[0];
+}
+
+// FitImpl<S, OBBRSS<S>>::run, OBB half (BV_fitter-inl.h:323-345) with
+// getExtentAndCenter_mesh (geometry-inl.h:147-182).
+inline void refFitObb(const double* V, const int32_t* T, const uint32_t* idx, int n, RefNode& nd) {
+  double M[9], s[3] = {0, 0, 0}, E[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  refCovariance(V, T, idx, n, M);
+  refEigenOld(M, s, E);
+  refAxisFromEigen(E, s, nd.axis);
+  const double big = std::numeric_limits<double>::max();
+  double mn[3] = {big, big, big}, mx[3] = {-big, -big, -big};
+  for (int i = 0; i < n; ++i) {
+    const int32_t* t = T + 3 * (size_t)idx[i];
+    for (int j = 0; j < 3; ++j) {
+      const double* p = V + 3 * (size_t)t[j];
+      double proj[3];
+      for (int k = 0; k < 3; ++k)
+        proj[k] = (nd.axis[k] * p[0] + nd.axis[3 + k] * p[1]) + nd.axis[6 + k] * p[2];
+      for (int k = 0; k < 3; ++k) {
+        if (proj[k] > mx[k]) mx[k] = proj[k];
+        if (proj[k] < mn[k]) mn[k] = proj[k];
+      }
+    }
+  }
+  double o[3];
+  for (int k = 0; k < 3; ++k) o[k] = (mx[k] + mn[k]) / 2;
+  for (int r = 0; r < 3; ++r) nd.To[r] = (nd.axis[3 * r] * o[0] + nd.axis[3 * r + 1] * o[1]) + nd.axis[3 * r + 2] * o[2];
+  for (int k = 0; k < 3; ++k) nd.extent[k] = (mx[k] - mn[k]) / 2;
+  nd.size = (nd.extent[0] * nd.extent[0] + nd.extent[1] * nd.extent[1]) + nd.extent[2] * nd.extent[2];
+}
+
+inline void buildRefTree(const double* V, const int32_t* T, int nt, std::vector<RefNode>& nodes,
+                         std::vector<uint32_t>& prim) {
+  nodes.clear();
+  prim.resize(nt);
+  for (int i = 0; i < nt; ++i) prim[i] = (uint32_t)i;
+  if (nt <= 0) return;
+  nodes.reserve(2 * (size_t)nt - 1);
+  struct Task {
+    int node, first, count;
+  };
+  std::vector<Task> tasks;
+  nodes.emplace_back();
+  tasks.push_back({0, 0, nt});
+  while (!tasks.empty()) {
+    const Task task = tasks.back();
+    tasks.pop_back();
+    uint32_t* cur = prim.data() + task.first;
+    RefNode fitted;
+    refFitObb(V, T, cur, task.count, fitted);
+    fitted.first_primitive = task.first;
+    fitted.num_primitives = task.count;
+    fitted.first_child = 0;
+    nodes[task.node] = fitted;
+    if (task.count == 1) {
+      nodes[task.node].first_child = -((int)cur[0] + 1);
+      continue;
+    }
+    // computeSplitValue_mean on the first OBB axis
+    const double sv[3] = {fitted.axis[0], fitted.axis[3], fitted.axis[6]};
+    double c[3] = {0.0, 0.0, 0.0};
+    for (int i = 0; i < task.count; ++i) {
+      const int32_t* t = T + 3 * (size_t)cur[i];
+      const double* p1 = V + 3 * (size_t)t[0];
+      const double* p2 = V + 3 * (size_t)t[1];
+      const double* p3 = V + 3 * (size_t)t[2];
+      for (int k = 0; k < 3; ++k) c[k] += ((p1[k] + p2[k]) + p3[k]) / 3;
+    }
+    const double split_value = ((c[0] * sv[0] + c[1] * sv[1]) + c[2] * sv[2]) / task.count;
+    int c1 = 0;
+    for (int i = 0; i < task.count; ++i) {
+      const int32_t* t = T + 3 * (size_t)cur[i];
+      const double* p1 = V + 3 * (size_t)t[0];
+      const double* p2 = V + 3 * (size_t)t[1];
+      const double* p3 = V + 3 * (size_t)t[2];
+      double p[3];
+      for (int k = 0; k < 3; ++k) p[k] = ((p1[k] + p2[k]) + p3[k]) / 3.0;
+      if (!(((sv[0] * p[0] + sv[1] * p[1]) + sv[2] * p[2]) > split_value)) {
+        std::swap(cur[i], cur[c1]);
+        ++c1;
+      }
+    }
+    if (c1 == 0 || c1 == task.count) c1 = task.count / 2;
+    const int left = (int)nodes.size();
+    nodes.emplace_back();
+    nodes.emplace_back();
+    nodes[task.node].first_child = left;
+    tasks.push_back({left + 1, task.first + c1, task.count - c1});
+    tasks.push_back({left, task.first, c1});
+  }
+}
+
+// overlap(R0, T0, OBB b1, OBB b2) on the FP64 nodes (OBB-inl.h:305-316).
+inline bool refObbOverlap(const Mat3& R0, const double T0[3], const RefNode& b1, const RefNode& b2) {
+  const double* A1 = b1.axis;
+  const double* A2 = b2.axis;
+  double R0b2[9];
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c)
+      R0b2[3 * r + c] = (R0.m[3 * r] * A2[c] + R0.m[3 * r + 1] * A2[3 + c]) + R0.m[3 * r + 2] * A2[6 + c];
+  Mat3 R;
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c)
+      R.m[3 * r + c] = (A1[r] * R0b2[c] + A1[3 + r] * R0b2[3 + c]) + A1[6 + r] * R0b2[6 + c];
+  double Tt[3];
+  for (int r = 0; r < 3; ++r)
+    Tt[r] = (((R0.m[3 * r] * b2.To[0] + R0.m[3 * r + 1] * b2.To[1]) + R0.m[3 * r + 2] * b2.To[2]) + T0[r]) - b1.To[r];
+  double Tv[3];
+  for (int c = 0; c < 3; ++c) Tv[c] = (Tt[0] * A1[c] + Tt[1] * A1[3 + c]) + Tt[2] * A1[6 + c];
+  return !obbDisjoint(R, Tv, b1.extent, b2.extent);
+}
+
+// MeshIntersect (bvh_solver-inl.h:74-164) over the reference's own FP64 trees
+// and FP64 vertices: contacts (b1, b2) in the order the reference adds them,
+// at most max_contacts.
+inline void meshIntersectRef(const RefNode* na, const double* Va, const int32_t* Ta, const RefNode* nb,
+                             const double* Vb, const int32_t* Tb, const Mat3& R, const double T[3],
+                             size_t max_contacts, std::vector<std::pair<int, int>>& contacts) {
+  contacts.clear();
+  if (max_contacts == 0) return;
+  auto vtx = [](const double* V, const int32_t* Tr, int t, int k) {
+    const double* p = V + 3 * (size_t)Tr[3 * (size_t)t + k];
+    return P3{p[0], p[1], p[2]};
+  };
+  std::vector<std::pair<int, int>> stack;
+  stack.emplace_back(0, 0);
+  while (!stack.empty()) {
+    const std::pair<int, int> task = stack.back();
+    stack.pop_back();
+    const RefNode& a = na[task.first];
+    const RefNode& b = nb[task.second];
+    if (!refObbOverlap(R, T, a, b)) continue;
+    const bool la = a.first_child < 0, lb = b.first_child < 0;
+    if (la && lb) {
+      const int ta = -(a.first_child + 1), tb = -(b.first_child + 1);
+      if (intersectTriangle(vtx(Va, Ta, ta, 0), vtx(Va, Ta, ta, 1), vtx(Va, Ta, ta, 2), vtx(Vb, Tb, tb, 0),
+                            vtx(Vb, Tb, tb, 1), vtx(Vb, Tb, tb, 2), R, T)) {
+        contacts.emplace_back(ta, tb);
+        if (contacts.size() >= max_contacts) return;
+      }
+      continue;
+    }
+    const bool go_a = lb || (!la && a.size > b.size);
+    if (go_a) {
+      stack.emplace_back(a.first_child, task.second);
+      stack.emplace_back(a.first_child + 1, task.second);
+    } else {
+      stack.emplace_back(task.first, b.first_child);
+      stack.emplace_back(task.first, b.first_child + 1);
     }
   }
 }

@@ -425,3 +425,24 @@ def test_invalid_shapes_rejected(gpu_ctx):
         gpu_ctx.set_shapes(s, np.zeros((4, 4), np.float32))
     with pytest.raises(FclgError, match="unsupported type"):
         gpu_ctx.set_shapes(_sh(7, 1.0), np.zeros((1, 4), np.float32))
+
+
+def test_epa_resume_equals_restart(gpu_ctx):
+    """A pair whose EPA polytope outgrows the 128-face layout continues in the
+    256-face layout from its saved state (fclg_tuning.epa_resume, the
+    default); rerunning it from the GJK simplex instead gives byte-identical
+    results, since both layouts assign slots the same way until the smaller
+    one fills."""
+    b = workloads.mixed(200000, seed=workloads.SEED_BASE + 51)
+    gpu_ctx.set_batch(b)
+    keep = gpu_ctx.get_tuning()
+    try:
+        gpu_ctx.set_tuning(epa_resume=True)
+        resumed = gpu_ctx.distance(b.pairs)
+        gpu_ctx.set_tuning(epa_resume=False)
+        restarted = gpu_ctx.distance(b.pairs)
+    finally:
+        gpu_ctx.set_tuning(**keep)
+    assert resumed.tobytes() == restarted.tobytes()
+    # the batch does reach the large layout (about 64 expansions fill 128 faces)
+    assert np.sum((resumed["distance"] < 0) & (resumed["iterations"] > 90)) > 100

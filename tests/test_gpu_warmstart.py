@@ -15,18 +15,16 @@
 * Training and the gain: a model trained on the GPU on plain-GJK directions
   of held-out arm configurations lowers the mean GJK iteration count of
   unseen configurations by >= 25 % against plain initialisation.
-* Answers: warm-started GPU results against the FP64 oracle started from the
-  same directions meet the convex parity bar (flags exact outside the 1e-6 m
-  band, separation within 1e-5 m for >= 99.5 % of pairs and 1e-3 m for all).
-  Against plain initialisation: collision flags identical outside the band,
-  overlapping pairs bit-identical (they rerun from the plain direction),
-  separation within 1e-5 m for >= 99.5 % of pairs and within 5e-3 m for all.
-  The last bound is the reference algorithm's own dependence on the start
-  direction: its distance loop stops when one iteration improves the bound
-  by less than the tolerance (gjk_distance.hpp:78-90), which on curved or
-  near-parallel features can happen up to ~2e-3 m from the optimum, for
-  either start (measured on 10^6 mixed pairs: max 1.9e-3 m, neither start
-  closer to a tight solve more often).
+* Answers: a warm-started pair keeps its run only with a certified distance
+  (the run's small-improvement stop waits for a duality gap <= 5e-6 m), so
+  every warm separation lies within 1e-5 m of the exact distance (the FP64
+  oracle run to a 1e-12 tolerance), over all pairs.  Against plain
+  initialisation: validity and collision flags identical outside the 1e-6 m
+  band, overlapping pairs bit-identical (they rerun from the plain
+  direction); separations differ from the plain ones by at most the plain
+  answer's own distance from the exact one (the reference's loop stops when
+  one iteration improves the bound by less than the tolerance,
+  gjk_distance.hpp:78-90, which on curved features leaves up to ~1e-3 m).
 """
 import numpy as np
 import pytest
@@ -147,23 +145,20 @@ def test_trained_model_cuts_iterations_and_keeps_answers(torch):
         # overlapping pairs rerun from the plain direction: same EPA answer
         assert np.array_equal(dp[ov], dw[ov])
         sep = ~ov & (plain["ok"] == 1)
-        err = np.abs(dp - dw)[sep]
-        assert np.mean(err <= 1e-5) >= 0.995 and err.max() <= 5e-3
-        # the warm answers are the reference algorithm's answers from the same start
+        # every warm separation within 1e-5 m of the exact distance
         import oracle
-        d_g = torch.zeros(test.n_pairs * 3, dtype=torch.float32, device="cuda")
-        ws.predict(d_te.data_ptr(), test.n_pairs, d_g.data_ptr())
-        torch.cuda.synchronize()
-        guess = d_g.cpu().numpy().reshape(-1, 3)
         sub = np.arange(0, test.n_pairs, 4)
-        ref = oracle.signed_distance(test.subset(sub), guess=guess[sub])
-        both = (ref["ok"] == 1) & (warm["ok"][sub] == 1)
-        assert both.mean() >= 0.999
-        rd, gd = ref["distance"], warm["distance"][sub].astype(np.float64)
-        out = np.abs(rd) > 1e-6
-        assert np.array_equal((rd < 0)[out & both], (gd < 0)[out & both])
-        e = np.abs(rd - gd)[both & (rd > 0)]
-        assert np.mean(e <= 1e-5) >= 0.995 and e.max() <= 1e-3
+        exact = oracle.signed_distance(test.subset(sub), gjk_max_iter=1000, gjk_tol=1e-12)
+        both = (exact["ok"] == 1) & sep[sub]
+        assert both.mean() >= 0.9 * sep[sub].mean()
+        ex = exact["distance"][both]
+        e_warm = np.abs(dw[sub][both] - ex)
+        e_plain = np.abs(dp[sub][both] - ex)
+        print("warm vs exact: max %.3g, over 1e-5: %d of %d; plain vs exact: max %.3g, over 1e-5: %d"
+              % (e_warm.max(), np.sum(e_warm > 1e-5), len(e_warm), e_plain.max(), np.sum(e_plain > 1e-5)))
+        assert e_warm.max() <= 1e-5, e_warm.max()
+        # warm and plain differ by no more than the plain answer's own error
+        assert np.all(np.abs(dw[sub][both] - dp[sub][both]) <= e_plain + 1e-5)
         it_p = plain["iterations"][sep].astype(np.float64).mean()
         it_w = warm["iterations"][sep].astype(np.float64).mean()
         assert it_w <= 0.75 * it_p, (it_p, it_w)

@@ -6,11 +6,15 @@ OrientedNodeBVHSolver::MeshIntersect, bvh_solver-inl.h:74-164) against brute
 force over all triangle pairs, plus the oracle's triangle-triangle test
 against an independent interval-overlap test.
 
-GPU: the warp-per-pose kernel through the C ABI against the oracle on the
-same trees: first-contact flags identical; with a contact cap, the reported
-triangle pairs are exactly the colliding set when it is smaller than the
-cap, otherwise cap-many members of it.
+GPU: the warp-per-pose kernel through the C ABI against the restated
+reference traversal over the reference's own tree (oracle/orc_mesh.hpp
+meshIntersectRef, pinned to the compiled reference by tests/test_mesh_ref.py)
+and against the reference's own golden lists: per pose the contact count and
+the ordered (b1, b2) list identical, for first contact, a cap of 64, a cap
+above the shared-memory buffer and every contact.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -94,50 +98,69 @@ def test_tri_tri_vs_independent(oracle_lib):
     assert agree == 3000
 
 
-def _check_gpu_vs_oracle(oracle_lib, ctx, mesh_a, mesh_b, poses, cap):
+def _gpu_lists(ctx, va, ta, vb, tb, poses, cap):
     from fclg.api import GpuMesh, mesh_collide
-    ga, gb = GpuMesh(ctx, mesh_a.vertices, mesh_a.triangles), GpuMesh(ctx, mesh_b.vertices, mesh_b.triangles)
-    na, ta = ga.export()
-    nb, tb = gb.export()
-    # first-contact mode
-    f, c, p, st = mesh_collide(ctx, ga, gb, poses, max_contacts=1)
-    of, oc, op = oracle_lib.mesh_collide(na, ta, nb, tb, poses, max_contacts=1)
+    ga, gb = GpuMesh(ctx, va, ta), GpuMesh(ctx, vb, tb)
+    try:
+        f, c, p, st = mesh_collide(ctx, ga, gb, poses, max_contacts=cap)
+    finally:
+        ga.close()
+        gb.close()
     assert np.all(st == 0)
-    assert np.array_equal(f, of)
-    # capped full mode, against every colliding pair: the complete set where
-    # it is smaller than the cap, else each reported pair confirmed by the FP64
-    # triangle test
-    f, c, p, st = mesh_collide(ctx, ga, gb, poses, max_contacts=cap)
-    af, ac, ap = oracle_lib.mesh_collide(na, ta, nb, tb, poses, max_contacts=0, pair_cap=cap)
-    assert np.all(st == 0)
-    assert np.array_equal(f, af)
-    for i in range(len(poses)):
-        got = list(map(tuple, p[i, :c[i]]))
-        assert len(set(got)) == len(got)
-        if ac[i] < cap:
-            assert c[i] == ac[i] and set(got) == set(map(tuple, ap[i, :ac[i]]))
-        else:
-            assert c[i] == cap
-            for x, y in got:
-                assert oracle_lib.tri_tri(ta[x, :, :3], tb[y, :, :3], poses[i])
-    ga.close()
-    gb.close()
-    return f.mean()
+    assert np.array_equal(f, (c > 0).astype(np.uint8))
+    return c, p
+
+
+def _check_gpu_vs_oracle(oracle_lib, ctx, mesh_a, mesh_b, poses, caps=(1, 64)):
+    """The kernel's contact lists equal, pose by pose and in order, the
+    restated reference traversal's over the reference's own tree."""
+    A = (mesh_a.vertices.astype(np.float64), mesh_a.triangles)
+    B = (mesh_b.vertices.astype(np.float64), mesh_b.triangles)
+    rate = None
+    for cap in caps:
+        c, p = _gpu_lists(ctx, mesh_a.vertices, mesh_a.triangles, mesh_b.vertices, mesh_b.triangles, poses, cap)
+        oc, op = oracle_lib.orc_mesh_collide_ref(A, B, poses.astype(np.float64), cap)
+        assert np.array_equal(c.astype(np.int32), oc)
+        for i in range(len(poses)):
+            assert np.array_equal(p[i, :c[i]], op[i, :oc[i]]), (cap, i)
+        if rate is None:
+            rate = (c > 0).mean()
+    return rate
 
 
 @pytest.mark.gpu
 def test_gpu_mesh_small_vs_oracle(gpu_ctx, oracle_lib):
     a = workloads.geodesic_sphere(10, 0.3, 0.05, seed=1)
     b = workloads.geodesic_sphere(8, 0.3, 0.05, seed=2)
-    rate = _check_gpu_vs_oracle(oracle_lib, gpu_ctx, a, b, workloads.mesh_poses(1500, seed=6), cap=64)
+    rate = _check_gpu_vs_oracle(oracle_lib, gpu_ctx, a, b, workloads.mesh_poses(1500, seed=6), caps=(1, 64, 200))
     assert 0.2 < rate < 0.95
 
 
 @pytest.mark.gpu
 def test_gpu_mesh_full_size_vs_oracle(gpu_ctx, oracle_lib):
     a, b = workloads.mesh_pair()
-    rate = _check_gpu_vs_oracle(oracle_lib, gpu_ctx, a, b, workloads.mesh_poses(600, seed=7), cap=64)
+    rate = _check_gpu_vs_oracle(oracle_lib, gpu_ctx, a, b, workloads.mesh_poses(600, seed=7))
     assert 0.2 < rate < 0.99
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ("env_rob", "spheres"))
+def test_gpu_mesh_reference_golden(gpu_ctx, name):
+    """The reference's own contact lists (tests/golden/mesh_ref.npz: its test
+    meshes env.obj / rob.obj and bumpy spheres), first contact, cap 64 and
+    every contact: counts and ordered (b1, b2) lists identical."""
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "mesh_ref.npz"))
+    va, ta, vb, tb = (g[name + "/" + k] for k in ("va", "ta", "vb", "tb"))
+    poses = g[name + "/poses"]
+    for tag, cap, n in (("cap1", 1, len(poses)), ("cap64", 64, len(poses)), ("all", None, 48)):
+        counts = g["%s/%s/counts" % (name, tag)]
+        flat = g["%s/%s/pairs" % (name, tag)]
+        cap = cap or max(int(counts.max()), 1)
+        c, p = _gpu_lists(gpu_ctx, va, ta, vb, tb, poses[:n], cap)
+        assert np.array_equal(c.astype(np.int32), counts)
+        off = np.concatenate([[0], np.cumsum(counts)])
+        for i in range(n):
+            assert np.array_equal(p[i, :c[i]], flat[off[i]:off[i + 1]]), (tag, i)
 
 
 @pytest.mark.gpu

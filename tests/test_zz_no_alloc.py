@@ -44,9 +44,14 @@ def test_static_matches_device_entry_twice():
         d_pairs = torch.from_numpy(b.pairs.view(np.uint8).copy()).cuda()
         n = b.n_pairs
         first = _run(ctx.distance_device_static, d_pairs, n, torch)
+        # device memory around the bare call only (its output buffer made beforehand)
+        d_res = torch.zeros(n * RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+        torch.cuda.synchronize()
         free_before = torch.cuda.mem_get_info()[0]
-        second = _run(ctx.distance_device_static, d_pairs, n, torch)
+        ctx.distance_device_static(d_pairs.data_ptr(), n, d_res.data_ptr())
+        torch.cuda.synchronize()
         assert torch.cuda.mem_get_info()[0] == free_before
+        second = d_res.cpu().numpy().view(RESULT_DTYPE).copy()
         # the two calls in a row agree bit for bit
         assert first.tobytes() == second.tobytes()
         assert (first["distance"] < 0).mean() > 0.3  # the EPA pass ran on a real share of the batch
