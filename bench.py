@@ -71,6 +71,7 @@ def parse():
                          "collision of 1M mixed pairs")
     ap.add_argument("--no-warm", action="store_true", help="skip the warm-start comparison")
     ap.add_argument("--no-mesh", action="store_true", help="skip the mesh-mesh block of the default line")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 plain-method block of the default line")
     ap.add_argument("--poses", type=int, default=65536)
     ap.add_argument("--configs", type=int, default=100_000, help="arm: joint configurations (7 x 32 pairs each)")
     ap.add_argument("--objects", type=int, default=100_000, help="scene: posed objects")
@@ -203,6 +204,55 @@ def _time_queries(torch, ctx, d_pairs, n, flags, steps, warmup, stream, dev):
     e1.record(stream)
     torch.cuda.synchronize(dev)
     return e0.elapsed_time(e1) / max(steps, 1), d_res.cpu().numpy().view(RESULT_DTYPE).copy()
+
+
+def fp64_block(args, torch, dev, stream, local):
+    """The plain method in FP64 on the GPU (fclg_distance64: shapeDistance per
+    pair, one thread per pair) beside the FP32 kernels on the plain-method
+    workload: 4096 pairs of 32-vertex hulls (the reference's small case) and
+    262,144 pairs of the same kind.  Device time per query, inputs resident."""
+    from fclg import workloads
+    from fclg.api import FCLG_REQ_NO_EPA, Context
+    from fclg.layout import GJK_SEPARATED, RESULT64_DTYPE
+    out = {"what": "GJKSolver<double>::shapeDistance on the GPU in FP64 (thread per pair) vs the FP32 GJK "
+                   "distance (no EPA) and the FP32 signed distance (GJK + EPA), same pairs, device-resident"}
+    for n in (4096, 262_144):
+        batch = workloads.plain_small(n)
+        ctx = Context(local)
+        ctx.set_batch(batch)
+        d_pairs = torch.from_numpy(batch.pairs.view(np.uint8).copy()).to(dev)
+        d64 = torch.empty(n * 64, dtype=torch.uint8, device=dev)
+
+        def step64():
+            ctx.distance64_device(d_pairs.data_ptr(), n, d64.data_ptr(), None, stream.cuda_stream)
+
+        for _ in range(max(3, args.warmup)):
+            step64()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = max(5, args.steps)
+        e0.record(stream)
+        for _ in range(reps):
+            step64()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms64 = e0.elapsed_time(e1) / reps
+        r64 = d64.cpu().numpy().view(RESULT64_DTYPE)
+        ms_gjk, r_gjk = _time_queries(torch, ctx, d_pairs, n, FCLG_REQ_NO_EPA, reps, 3, stream, dev)
+        ms_full, _ = _time_queries(torch, ctx, d_pairs, n, 0, reps, 3, stream, dev)
+        sep = (r64["ok"] == 1) & ((r64["status"] & 0xFF) == GJK_SEPARATED) & (r_gjk["ok"] == 1)
+        err = np.abs(r_gjk["distance"][sep].astype(np.float64) - r64["distance"][sep])
+        out["pairs_%d" % n] = {
+            "fp64_ms": ms64, "fp64_queries_per_s": n / (ms64 * 1e-3),
+            "fp32_gjk_distance_ms": ms_gjk, "fp32_gjk_distance_queries_per_s": n / (ms_gjk * 1e-3),
+            "fp32_signed_distance_ms": ms_full, "fp32_signed_distance_queries_per_s": n / (ms_full * 1e-3),
+            "fp32_over_fp64_gjk_speedup": ms64 / ms_gjk,
+            "separated_pairs": int(sep.sum()),
+            "fp32_vs_fp64_distance_err_max": float(err.max(initial=0.0)),
+            "fp32_vs_fp64_distance_err_p99": float(np.percentile(err, 99)) if err.size else 0.0,
+        }
+        ctx.close()
+    return out
 
 
 WARM_CASES = {
@@ -1101,6 +1151,8 @@ def main():
             line["config"]["warm_start"] = warm_start_block(args, torch, dev, stream, local, names)
         if not args.no_mesh and args.workload == "mixed" and world == 1:
             line["config"]["mesh"] = mesh_block(args, torch, dev, stream, local)
+        if not args.no_fp64 and args.workload == "mixed" and world == 1:
+            line["config"]["fp64_plain"] = fp64_block(args, torch, dev, stream, local)
         print(json.dumps(line))
     ctx.close()
     if world > 1:

@@ -206,6 +206,39 @@ int fclg_collide(fclg_context* ctx, const fclg_pair* pairs, uint32_t n_pairs, co
 int fclg_collide_device(fclg_context* ctx, const fclg_pair* d_pairs, uint32_t n_pairs, const fclg_request* req,
                         fclg_result* d_results, void* stream);
 
+/* Separation distance in FP64 on the GPU: the GJK path of
+   GJKSolver<double>::shapeDistance (ShapeDistanceIndepImpl,
+   narrowphase/detail/gjk_solver-inl.h:760-798), one thread per pair running
+   the reference's GJK boolean and GJK distance (cvx_collide/gjk.hpp:10-360,
+   gjk_distance.hpp:10-559) in FP64, every operation rounded on its own in the
+   reference's order, from the guess (1, 0, 0).  The FP32 inputs (shapes,
+   vertices, poses) are taken exactly as FP64.  Every pair runs GJK: the
+   closed-form specialisations shapeDistance has for sphere pairs and
+   capsule-capsule (gjk_solver-inl.h:900-1000) are not taken.  A separated
+   pair with valid witness points gets ok = 1, distance = |p_a - p_b| and the
+   points (shape a's frame); every other pair gets ok = 0 and distance -1 (a
+   separated pair whose witness extraction failed included: the reference
+   returns its unset witness points there), collide = 1 when GJK reported an
+   intersection.  req may be NULL (tolerance 1e-6, 128 iterations). */
+typedef struct fclg_request64 {
+  double gjk_tolerance;         /* 0: 1e-6 (GJKSolver::gjk_tolerance) */
+  uint32_t gjk_max_iterations;  /* 0: 128 */
+  uint32_t reserved;
+} fclg_request64;
+typedef struct fclg_result64 { /* 64 bytes */
+  double distance;
+  double p_a[3];
+  double p_b[3];
+  int32_t status;        /* GJK_Status (cvx_collide/gjk.h:13-28) */
+  uint16_t iterations;   /* GJK boolean + distance iterations */
+  uint8_t collide;
+  uint8_t ok;
+} fclg_result64;
+int fclg_distance64(fclg_context* ctx, const fclg_pair* pairs, uint32_t n_pairs, const fclg_request64* req,
+                    fclg_result64* results);
+int fclg_distance64_device(fclg_context* ctx, const fclg_pair* d_pairs, uint32_t n_pairs, const fclg_request64* req,
+                           fclg_result64* d_results, void* stream);
+
 /* Signed distance on device pointers without any allocation in the call (no
    counterpart in the reference, whose per-pair solver keeps its polytope on
    the stack).  It runs the GJK pass unbucketed with the context's small-pair

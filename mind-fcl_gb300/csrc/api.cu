@@ -577,6 +577,46 @@ int fclg_collide_device(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, c
   return run_query(c, d_pairs, n, req, d_results, static_cast<cudaStream_t>(stream), false);
 }
 
+int fclg_distance64_device(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_request64* req,
+                           fclg_result64* d_results, void* stream) {
+  if (!c) return FCLG_E_INVALID;
+  if (n == 0) return FCLG_OK;
+  if (!d_pairs || !d_results) return fail(c, FCLG_E_INVALID, "null pair or result pointer");
+  if (!c->shapes) return fail(c, FCLG_E_NO_SHAPES, "no shapes set");
+  FCLG_CUDA(c, cudaSetDevice(c->device));
+  clear_pending_error();
+  fclg::BatchArgs b = batch_args(c);
+  b.pairs = reinterpret_cast<const float4*>(d_pairs);
+  b.guess = nullptr;
+  b.results = nullptr;
+  b.n_pairs = n;
+  b.n_shapes = c->n_shapes;
+  const double tol = (req && req->gjk_tolerance > 0.) ? req->gjk_tolerance : 1e-6;
+  const int max_iter = (req && req->gjk_max_iterations) ? (int)req->gjk_max_iterations : 128;
+  FCLG_CUDA(c, fclg::launch_gjk64(b, tol, max_iter, reinterpret_cast<double*>(d_results), c->num_sms * 16,
+                                  static_cast<cudaStream_t>(stream)));
+  c->launches += 1;
+  return FCLG_OK;
+}
+
+int fclg_distance64(fclg_context* c, const fclg_pair* pairs, uint32_t n, const fclg_request64* req,
+                    fclg_result64* results) {
+  if (!c) return FCLG_E_INVALID;
+  if (n == 0) return FCLG_OK;
+  if (!pairs || !results) return fail(c, FCLG_E_INVALID, "null pair or result pointer");
+  // the staging of FP32 results, sized up to hold the 64-byte records
+  int rc = ensure_io(c, ((size_t)n * sizeof(fclg_result64) + sizeof(fclg_result) - 1) / sizeof(fclg_result));
+  if (rc) return rc;
+  FCLG_CUDA(c, cudaMemcpyAsync(c->io_pairs, pairs, (size_t)n * sizeof(fclg_pair), cudaMemcpyHostToDevice, c->stream));
+  rc = fclg_distance64_device(c, static_cast<const fclg_pair*>(c->io_pairs), n, req,
+                              static_cast<fclg_result64*>(c->io_results), c->stream);
+  if (rc) return rc;
+  FCLG_CUDA(c, cudaMemcpyAsync(results, c->io_results, (size_t)n * sizeof(fclg_result64), cudaMemcpyDeviceToHost,
+                               c->stream));
+  FCLG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return FCLG_OK;
+}
+
 int fclg_set_warmstart(fclg_context* c, fclg_warmstart* model) {
   if (!c) return FCLG_E_INVALID;
   if (model && fclg::warmstart_device(model) != c->device)
@@ -1491,6 +1531,8 @@ static_assert(sizeof(fclg_displacement) == 16, "displacement layout (read as flo
 static_assert(sizeof(fclg_ccd_result) == 16, "ccd result layout (written as float4)");
 static_assert(sizeof(fclg_ccd_request) == 24, "ccd request layout");
 static_assert(sizeof(fclg_ccd_result) <= sizeof(fclg_result), "ccd results share the query result staging");
+static_assert(sizeof(fclg_result64) == 64, "fclg_result64 layout (written as 8 doubles)");
+static_assert(sizeof(fclg_request64) == 16, "fclg_request64 layout");
 
 namespace {
 

@@ -57,6 +57,9 @@ cudaError_t launch_gjk(const BatchArgs& b, const QueryParams& prm, const EpaQueu
                        bool refill = false);
 // fcl::collide with directed penetration along b.guess (directed_pass.cu).
 cudaError_t launch_directed(const BatchArgs& b, const QueryParams& prm, int blocks, cudaStream_t st);
+// GJKSolver<double>::shapeDistance per pair in FP64, one thread per pair, as a
+// grid of at most `blocks` CTAs of 128 (fp64_pass.cu); out = fclg_result64[n_pairs].
+cudaError_t launch_gjk64(const BatchArgs& b, double tol, int max_iter, double* out, int blocks, cudaStream_t st);
 cudaError_t prepare_epa();
 // EPA over q's list: the small-polytope pass, then (when max_faces exceeds it)
 // the large pass over the pairs ovf collected.  ovf.count must be zero and

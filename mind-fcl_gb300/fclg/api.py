@@ -8,7 +8,7 @@ import os
 
 import numpy as np
 
-from .layout import PAIR_DTYPE, RESULT_DTYPE, SHAPE_DTYPE
+from .layout import PAIR_DTYPE, RESULT64_DTYPE, RESULT_DTYPE, SHAPE_DTYPE
 
 PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.environ.get("FCLG_LIB") or os.path.join(PKG, "lib", "libfclg.so")
@@ -27,6 +27,7 @@ EXPORTS = [
     "fclg_create", "fclg_destroy", "fclg_last_error", "fclg_version", "fclg_built_arch",
     "fclg_set_shapes", "fclg_set_shapes_device",
     "fclg_distance", "fclg_distance_device", "fclg_distance_device_static", "fclg_collide", "fclg_collide_device",
+    "fclg_distance64", "fclg_distance64_device",
     "fclg_set_launch", "fclg_set_tuning", "fclg_get_tuning", "fclg_launch_count", "fclg_set_profiling",
     "fclg_pass_times", "fclg_bvh_build", "fclg_bvh_node_sizes", "fclg_mesh_create", "fclg_mesh_destroy", "fclg_mesh_info", "fclg_mesh_export",
     "fclg_mesh_collide", "fclg_mesh_collide_device", "fclg_mesh_traffic",
@@ -77,6 +78,12 @@ class Request(ctypes.Structure):
                 ("warm_gap", ctypes.c_float), ("warm_probe", ctypes.c_uint32)]
 
 
+class Request64(ctypes.Structure):
+    """fclg_request64: the parameters of the FP64 separation distance."""
+    _fields_ = [("gjk_tolerance", ctypes.c_double), ("gjk_max_iterations", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
+
 _lib = None
 
 
@@ -101,10 +108,11 @@ def load_library(path=LIB_PATH):
     lib.fclg_set_shapes.restype = i32
     lib.fclg_set_shapes_device.argtypes = [vp, vp, u32, vp, u64]
     lib.fclg_set_shapes_device.restype = i32
-    for name in ("fclg_distance", "fclg_collide"):
+    for name in ("fclg_distance", "fclg_collide", "fclg_distance64"):
         getattr(lib, name).argtypes = [vp, vp, u32, vp, vp]
         getattr(lib, name).restype = i32
-    for name in ("fclg_distance_device", "fclg_distance_device_static", "fclg_collide_device"):
+    for name in ("fclg_distance_device", "fclg_distance_device_static", "fclg_collide_device",
+                 "fclg_distance64_device"):
         getattr(lib, name).argtypes = [vp, vp, u32, vp, vp, vp]
         getattr(lib, name).restype = i32
     lib.fclg_set_launch.argtypes = [vp, i32, i32]
@@ -208,6 +216,13 @@ def _ptr(a):
     return ctypes.c_void_p(a.ctypes.data) if a is not None else None
 
 
+def make_request64(gjk_tol=0.0, gjk_max_iter=0):
+    r = Request64()
+    r.gjk_tolerance = gjk_tol
+    r.gjk_max_iterations = gjk_max_iter
+    return r
+
+
 def make_request(flags=0, gjk_tol=0.0, epa_tol=0.0, gjk_max_iter=0, epa_max_faces=0, epa_max_iter=0,
                  warm_gap=0.0, warm_probe=0):
     r = Request()
@@ -277,6 +292,17 @@ class Context:
     def distance(self, pairs, request=None, out=None):
         """Signed distance per pair (host arrays in and out)."""
         return self._host_query(self.lib.fclg_distance, pairs, request, out)
+
+    def distance64(self, pairs, request=None, out=None):
+        """The GJK path of GJKSolver<double>::shapeDistance per pair in FP64 on the GPU
+        (RESULT64_DTYPE out; request: a Request64 or None)."""
+        if out is None:
+            out = np.zeros(len(pairs), RESULT64_DTYPE)
+        return self._host_query(self.lib.fclg_distance64, pairs, request, out)
+
+    def distance64_device(self, d_pairs, n, d_results, request=None, stream=0):
+        """Asynchronous FP64 separation distance on device pointers (fclg_result64 out)."""
+        self._dev_query(self.lib.fclg_distance64_device, d_pairs, n, d_results, request, stream)
 
     def collide(self, pairs, request=None, out=None):
         """fcl::collide per pair (host arrays in and out)."""

@@ -28,7 +28,14 @@ RESULT_DTYPE = np.dtype(
      ("status", "<i4"), ("iterations", "<u2"), ("collide", "u1"), ("ok", "u1")],
     align=False,
 )
+# fclg_result64: the FP64 separation distance (fclg_distance64)
+RESULT64_DTYPE = np.dtype(
+    [("distance", "<f8"), ("p_a", "<f8", (3,)), ("p_b", "<f8", (3,)), ("status", "<i4"), ("iterations", "<u2"),
+     ("collide", "u1"), ("ok", "u1")],
+    align=False,
+)
 assert SHAPE_DTYPE.itemsize == 32 and PAIR_DTYPE.itemsize == 64 and RESULT_DTYPE.itemsize == 48
+assert RESULT64_DTYPE.itemsize == 64
 
 # Status word of fclg_result: bits 0-7 GJK_Status (gjk.h:13-28), bits 8-15
 # EPA_Status + 1 (epa.h:14; 0 = EPA not run), bit 16 = capacity overflow.

@@ -69,6 +69,13 @@ def test_forward_matches_oracle(torch):
         assert rel.max() <= bound and np.median(rel) <= med, (kind, rel.max(), np.median(rel))
     rel = np.linalg.norm(outs["tcgen05"] - outs["mma.sync"], axis=1) / scale
     assert np.median(rel) <= 2e-3, np.median(rel)
+    # a ragged batch (an odd number of 128-pair tiles, the last one partial)
+    # gives each pair the same outputs, bit for bit
+    m = n - 165
+    d_y = torch.zeros(m * 3, dtype=torch.float32, device="cuda")
+    ws.predict(d_pairs.data_ptr(), m, d_y.data_ptr(), normalize=False)
+    ws.status()
+    assert np.array_equal(d_y.cpu().numpy().reshape(m, 3), outs["tcgen05"][:m])
     # normalised output is the unit direction of the raw one
     d_u = torch.zeros(n * 3, dtype=torch.float32, device="cuda")
     ws.predict(d_pairs.data_ptr(), n, d_u.data_ptr(), normalize=True)
