@@ -46,7 +46,7 @@ struct fclg_context {
   size_t bp_join_bytes = 0;
   bool gjk_refill = false;
   // scratch handed from the GJK pass to the EPA pass
-  uint32_t* epa_count = nullptr;  // [2]: work list, overflow list
+  uint32_t* epa_count = nullptr;  // [4]: work list, overflow list, entries taken by the two EPA launches
   uint32_t* epa_list = nullptr;
   uint32_t* epa_ovf = nullptr;
   unsigned char* epa_resume = nullptr;  // polytope states handed from the small EPA layout to the large one
@@ -376,11 +376,12 @@ int run_query(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_
   b.n_pairs = n;
   b.n_shapes = c->n_shapes;
   fclg::EpaQueue q{c->epa_count, c->epa_list, c->epa_rec};
+  q.next = c->epa_count + 2;
   if (c->profiling) {
     const int rc = collect_times(c);
     if (rc) return rc;
   }
-  if (prm.want_epa) FCLG_CUDA(c, cudaMemsetAsync(c->epa_count, 0, 2 * sizeof(uint32_t), st));
+  if (prm.want_epa) FCLG_CUDA(c, cudaMemsetAsync(c->epa_count, 0, 4 * sizeof(uint32_t), st));
   if (c->bucketing) {
     const int rc = ensure_bucket(c, n);
     if (rc) return rc;
@@ -411,7 +412,7 @@ int run_query(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_
   if (c->profiling) FCLG_CUDA(c, cudaEventRecord(c->ev[1], st));
   if (prm.want_epa) {
     fclg::EpaQueue ovf{c->epa_count + 1, c->epa_ovf, reinterpret_cast<float4*>(c->epa_resume),
-                       c->epa_resume_on ? c->epa_resume_cap : 0u};
+                       c->epa_resume_on ? c->epa_resume_cap : 0u, c->epa_count + 3};
     FCLG_CUDA(c, fclg::launch_epa(b, prm, q, ovf, c->num_sms, c->epa_ctas_per_sm, st));
     c->launches += prm.epa_max_faces > 128 ? 2 : 1;
     if (c->profiling) FCLG_CUDA(c, cudaEventRecord(c->ev[2], st));
@@ -460,7 +461,7 @@ int fclg_create(fclg_context** out, int device) {
   c->device = device;
   c->num_sms = prop.multiProcessorCount;
   if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaMalloc(&c->epa_count, 2 * sizeof(uint32_t)) != cudaSuccess || fclg::prepare_epa() != cudaSuccess) {
+      cudaMalloc(&c->epa_count, 4 * sizeof(uint32_t)) != cudaSuccess || fclg::prepare_epa() != cudaSuccess) {
     fclg_destroy(c);
     return FCLG_E_CUDA;
   }
@@ -1265,17 +1266,18 @@ extern "C" int fclg_distance_device_static(fclg_context* c, const fclg_pair* d_p
   uint32_t* counts = reinterpret_cast<uint32_t*>(base);
   fclg::EpaQueue q{counts, reinterpret_cast<uint32_t*>(base + kStaticListOffset),
                    reinterpret_cast<float4*>(base + kStaticRecOffset)};
+  q.next = counts + 2;
   if (c->profiling) {  // the pass times of fclg_pass_times cover these calls too
     const int prc = collect_times(c);
     if (prc) return prc;
   }
-  if (prm.want_epa) FCLG_CUDA(c, cudaMemsetAsync(counts, 0, 2 * sizeof(uint32_t), st));
+  if (prm.want_epa) FCLG_CUDA(c, cudaMemsetAsync(counts, 0, 4 * sizeof(uint32_t), st));
   if (c->profiling) FCLG_CUDA(c, cudaEventRecord(c->ev[0], st));
   FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes, nullptr, nullptr, 0, st, c->gjk_refill));
   c->launches += 1;
   if (c->profiling) FCLG_CUDA(c, cudaEventRecord(c->ev[1], st));
   if (prm.want_epa) {
-    fclg::EpaQueue ovf{counts + 1, reinterpret_cast<uint32_t*>(base + kStaticOvfOffset), nullptr};
+    fclg::EpaQueue ovf{counts + 1, reinterpret_cast<uint32_t*>(base + kStaticOvfOffset), nullptr, 0u, counts + 3};
     FCLG_CUDA(c, fclg::launch_epa(b, prm, q, ovf, c->num_sms, c->epa_ctas_per_sm, st));
     c->launches += prm.epa_max_faces > 128 ? 2 : 1;
     if (c->profiling) FCLG_CUDA(c, cudaEventRecord(c->ev[2], st));

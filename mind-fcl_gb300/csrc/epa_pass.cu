@@ -39,7 +39,17 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) epa_pass(BatchArgs b, QueryP
   // layout runs under the request's limit and overflows at its own capacity.
   const bool final_layout = large || prm.epa_max_faces <= FMAX;
   const int max_faces = (final_layout && prm.epa_max_faces > FMAX) ? FMAX : prm.epa_max_faces;
-  for (uint32_t k = gw; k < n; k += nw) {
+  // Pairs differ in EPA iterations by an order of magnitude, so each warp
+  // takes its next entry from a shared counter as it finishes one, and the
+  // warps end together (results do not depend on which warp runs a pair).
+  uint32_t* next = large ? ovf.next : q.next;
+  auto take = [&](uint32_t done) -> uint32_t {
+    if (!next) return done + nw;
+    uint32_t k = 0;
+    if (lane == 0) k = atomicAdd(next, 1u);
+    return __shfl_sync(0xFFFFFFFFu, k, 0);
+  };
+  for (uint32_t k = next ? take(0) : gw; k < n; k = take(k)) {
     const uint32_t item = large ? ovf.list[k] : k;
     const uint32_t pid = q.list[item];
     const float4* r = q.rec + 7 * (size_t)item;

@@ -99,7 +99,17 @@ __device__ __forceinline__ void finish_pair(const BatchArgs& b, const QueryParam
 #ifndef FCLG_GJK_MINB
 #define FCLG_GJK_MINB 4
 #endif
-template <int LANES>
+// Kernel variants: PLAIN compiles the GJK run from the plain direction only
+// (queries without closed-form pairs, MPR or a learned start: the distance
+// entry points), which keeps the kernel's code small enough for the
+// instruction cache; FULL compiles every path and selects by prm / b.guess.
+// Both give the same results on the queries PLAIN serves.
+enum : int { kPassPlain = 0, kPassFull = 1 };
+#ifndef FCLG_GJK_PLAIN_VARIANT
+#define FCLG_GJK_PLAIN_VARIANT 1
+#endif
+
+template <int LANES, int MODE>
 __global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_pass(BatchArgs b, QueryParams prm, EpaQueue q,
                                                    const uint32_t* __restrict__ order,
                                                    const uint32_t* __restrict__ range) {
@@ -126,7 +136,7 @@ __global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_pass(BatchArgs b, Quer
     sup.g = g;
     // GJKSolver's default guess (1, 0, 0), gjk_solver-inl.h:1129
     const f3 plain = mk3(1.f, 0.f, 0.f);
-    if (prm.analytic) {
+    if (MODE == kPassFull && prm.analytic) {
       // fcl::collide: closed-form solvers for sphere pairs (gjk_solver-inl.h:209-218)
       AnalyticContact ac;
       if (analytic_contact(sup.A, sup.B, pr.pose, ac)) {
@@ -144,7 +154,7 @@ __global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_pass(BatchArgs b, Quer
       }
     }
     int mpr_iters = 0;
-    if (prm.use_mpr) {
+    if (MODE == kPassFull && prm.use_mpr) {
       // fcl::collide without contact: MPR decides, GJK only when MPR fails
       // (ShapeIntersectIndepImpl::run, gjk_solver-inl.h:86-97)
       Mpr<MinkowskiSupport<LANES>> mpr{sup, prm.gjk_max_iter, prm.gjk_tol};
@@ -162,7 +172,7 @@ __global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_pass(BatchArgs b, Quer
     }
     Simplex s;
     GjkOut o;
-    if (b.guess) {
+    if (MODE == kPassFull && b.guess) {
       // Learned direction first, for a separation certificate within
       // warm_probe supports and a distance certified to warm_gap.  A pair it
       // does not settle (overlapping: its EPA must start from the plain
@@ -192,7 +202,8 @@ __global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_pass(BatchArgs b, Quer
 }
 
 
-// Launches gjk_pass<LANES> (defined in the translation unit that instantiates LANES).
+// Launches gjk_pass<LANES, ...> (defined in the translation unit that instantiates LANES): the
+// PLAIN variant when the query has no closed-form pairs, MPR or learned start.
 template <int LANES>
 cudaError_t launch_gjk_lanes(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q, const uint32_t* order,
                              const uint32_t* range, int blocks, cudaStream_t st);
@@ -201,7 +212,10 @@ cudaError_t launch_gjk_lanes(const BatchArgs& b, const QueryParams& prm, const E
   template <>                                                                                                \
   cudaError_t launch_gjk_lanes<L>(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q,             \
                                   const uint32_t* order, const uint32_t* range, int blocks, cudaStream_t st) { \
-    gjk_pass<L><<<blocks, 128, 0, st>>>(b, prm, q, order, range);                                            \
+    if (FCLG_GJK_PLAIN_VARIANT && !prm.analytic && !prm.use_mpr && !b.guess)                                 \
+      gjk_pass<L, kPassPlain><<<blocks, 128, 0, st>>>(b, prm, q, order, range);                              \
+    else                                                                                                     \
+      gjk_pass<L, kPassFull><<<blocks, 128, 0, st>>>(b, prm, q, order, range);                               \
     return cudaGetLastError();                                                                               \
   }
 

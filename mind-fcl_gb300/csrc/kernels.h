@@ -28,6 +28,9 @@ struct EpaQueue {
   float4* rec;            // [capacity][7] final GJK simplex (rank, support points); for the overflow
                           // list: [resume_cap] polytope states (kEpaResumeBytes each) or null
   uint32_t resume_cap = 0;  // overflow list: states the pool holds (the rest restart from the simplex)
+  uint32_t* next = nullptr;  // zero before the EPA pass over this list: the count of entries its warps have
+                             // taken (each warp takes its next entry there as it finishes one); null: each
+                             // warp takes every (warps in the grid)-th entry
 };
 constexpr size_t kEpaRecordBytes = 7 * sizeof(float4);
 // Bytes of one small-layout polytope state handed to the large layout (epa.cuh EpaResume).
