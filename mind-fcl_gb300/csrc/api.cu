@@ -20,6 +20,10 @@
 #include "mesh_kernels.h"
 #include "warmstart.h"
 
+// Counters of a query (fclg_context::epa_count): EPA work list and overflow
+// list lengths, entries taken by the two EPA launches and by the two GJK launches.
+constexpr int kQueueCounters = 6;
+
 struct fclg_context {
   int device = 0;
   int num_sms = 0;
@@ -46,7 +50,8 @@ struct fclg_context {
   size_t bp_join_bytes = 0;
   bool gjk_refill = false;
   // scratch handed from the GJK pass to the EPA pass
-  uint32_t* epa_count = nullptr;  // [4]: work list, overflow list, entries taken by the two EPA launches
+  uint32_t* epa_count = nullptr;  // [6]: work list, overflow list; entries taken by the two EPA launches,
+                                  // then by the two GJK launches
   uint32_t* epa_list = nullptr;
   uint32_t* epa_ovf = nullptr;
   unsigned char* epa_resume = nullptr;  // polytope states handed from the small EPA layout to the large one
@@ -381,7 +386,7 @@ int run_query(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_
     const int rc = collect_times(c);
     if (rc) return rc;
   }
-  if (prm.want_epa) FCLG_CUDA(c, cudaMemsetAsync(c->epa_count, 0, 4 * sizeof(uint32_t), st));
+  FCLG_CUDA(c, cudaMemsetAsync(c->epa_count, 0, kQueueCounters * sizeof(uint32_t), st));
   if (c->bucketing) {
     const int rc = ensure_bucket(c, n);
     if (rc) return rc;
@@ -401,9 +406,10 @@ int run_query(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_
                            c->bk_small + 2 * fclg::kBucketKeys};
     FCLG_CUDA(c, fclg::launch_bucketing(b, bs, (uint32_t)c->large_hull, st));
     const int blocks = c->num_sms * c->gjk_ctas_per_sm;
-    FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes, bs.order, bs.ranges, blocks, st, c->gjk_refill));
+    FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes, bs.order, bs.ranges, blocks, st, c->gjk_refill,
+                                  c->epa_count + 4));
     FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes_large, bs.order, bs.ranges + 2, blocks, st,
-                                  c->gjk_refill));
+                                  c->gjk_refill, c->epa_count + 5));
     c->launches += 5;
   } else {
     FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes, nullptr, nullptr, 0, st, c->gjk_refill));
@@ -461,7 +467,8 @@ int fclg_create(fclg_context** out, int device) {
   c->device = device;
   c->num_sms = prop.multiProcessorCount;
   if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaMalloc(&c->epa_count, 4 * sizeof(uint32_t)) != cudaSuccess || fclg::prepare_epa() != cudaSuccess) {
+      cudaMalloc(&c->epa_count, kQueueCounters * sizeof(uint32_t)) != cudaSuccess ||
+      fclg::prepare_epa() != cudaSuccess) {
     fclg_destroy(c);
     return FCLG_E_CUDA;
   }
@@ -1271,7 +1278,7 @@ extern "C" int fclg_distance_device_static(fclg_context* c, const fclg_pair* d_p
     const int prc = collect_times(c);
     if (prc) return prc;
   }
-  if (prm.want_epa) FCLG_CUDA(c, cudaMemsetAsync(counts, 0, 4 * sizeof(uint32_t), st));
+  if (prm.want_epa) FCLG_CUDA(c, cudaMemsetAsync(counts, 0, kQueueCounters * sizeof(uint32_t), st));
   if (c->profiling) FCLG_CUDA(c, cudaEventRecord(c->ev[0], st));
   FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes, nullptr, nullptr, 0, st, c->gjk_refill));
   c->launches += 1;

@@ -4,9 +4,12 @@
 // table (narrowphase/detail/collision_func_matrix-inl.h:585-858); on the GPU the
 // same role is played by sorting the batch so that every warp runs one support
 // routine pair: warps over mixed types would execute every support routine of
-// the mix in turn.  Shape classes: box, sphere, capsule, cylinder, and convex
-// hulls split at `big_nv` vertices; pairs with a hull above it sort last so a
-// second launch can give them more lanes per pair.
+// the mix in turn.  Shape classes: box, sphere, capsule, cylinder, convex hulls
+// up to `big_nv` vertices in five bins of vertex count (a lane's hull scan
+// takes as long as its vertex count, and a warp as long as its largest hull,
+// so the warps of a bin scan hulls within a factor of two of each other), and
+// hulls above `big_nv`; pairs with such a hull sort last so a second launch can
+// give them more lanes per pair.
 //
 //   classify  per pair: class key + block histogram, merged with one atomic
 //             per (block, key)
@@ -20,13 +23,20 @@ namespace fclg {
 
 namespace {
 
+constexpr uint32_t kBigHull = 4 + kHullBins;
+
 __device__ __forceinline__ uint32_t shape_class(int4 h, uint32_t big_nv) {
   switch (h.x) {
     case kBox: return 0;
     case kSphere: return 1;
     case kCapsule: return 2;
     case kCylinder: return 3;
-    default: return (uint32_t)h.z > big_nv ? 5u : 4u;
+    default: {
+      const uint32_t nv = (uint32_t)h.z;
+      if (nv > big_nv) return kBigHull;
+      const int lg = 31 - __clz((int)(nv | 1u));  // floor(log2(nv))
+      return 4u + (uint32_t)min(max(lg - 3, 0), kHullBins - 1);
+    }
   }
 }
 
@@ -46,7 +56,7 @@ __global__ void __launch_bounds__(256) classify_pairs(const float4* __restrict__
     if (a < n_shapes && b < n_shapes) {
       const uint32_t ca = shape_class(__ldg(shapes + 2 * (size_t)a), big_nv);
       const uint32_t cb = shape_class(__ldg(shapes + 2 * (size_t)b), big_nv);
-      const bool big = ca == 5 || cb == 5;
+      const bool big = ca == kBigHull || cb == kBigHull;
       key = (big ? kBucketSmallKeys : 0u) + ca * kShapeClasses + cb;
     }
     keys[pid] = (uint8_t)key;
@@ -107,7 +117,7 @@ cudaError_t launch_bucketing(const BatchArgs& b, const BucketScratch& s, uint32_
   if (b.n_pairs == 0) return cudaSuccess;
   const unsigned blocks = (b.n_pairs + 255) / 256;
   classify_pairs<<<blocks, 256, 0, st>>>(b.pairs, b.shapes, b.n_pairs, b.n_shapes, big_nv, s.keys, s.hist);
-  scan_buckets<<<1, 128, 0, st>>>(s.hist, s.cursor, s.ranges);
+  scan_buckets<<<1, 256, 0, st>>>(s.hist, s.cursor, s.ranges);
   scatter_pairs<<<blocks, 256, 0, st>>>(s.keys, b.n_pairs, s.cursor, s.order);
   return cudaGetLastError();
 }

@@ -110,12 +110,14 @@ __global__ void __launch_bounds__(128, FCLG_REFILL_MINB) gjk_refill(BatchArgs b,
 
 
 cudaError_t launch_gjk(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q, int lanes,
-                       const uint32_t* order, const uint32_t* range, int blocks, cudaStream_t st, bool refill) {
+                       const uint32_t* order, const uint32_t* range, int blocks, cudaStream_t st, bool refill,
+                       uint32_t* next) {
   if (b.n_pairs == 0) return cudaSuccess;
   const int threads = 128;
   if (blocks <= 0) {
     const uint64_t total = (uint64_t)b.n_pairs * (uint64_t)lanes;
     blocks = (int)((total + threads - 1) / threads);
+    next = nullptr;  // one CTA per 128 lanes of work: the block scheduler balances the grid
   }
   if (refill && lanes == 1 && !prm.use_mpr && !prm.analytic) {
     // a persistent grid: FCLG_REFILL_MINB CTAs on every SM
@@ -128,12 +130,12 @@ cudaError_t launch_gjk(const BatchArgs& b, const QueryParams& prm, const EpaQueu
     return cudaGetLastError();
   }
   switch (lanes) {
-    case 1: return launch_gjk_lanes<1>(b, prm, q, order, range, blocks, st);
-    case 2: return launch_gjk_lanes<2>(b, prm, q, order, range, blocks, st);
-    case 4: return launch_gjk_lanes<4>(b, prm, q, order, range, blocks, st);
-    case 8: return launch_gjk_lanes<8>(b, prm, q, order, range, blocks, st);
-    case 16: return launch_gjk_lanes<16>(b, prm, q, order, range, blocks, st);
-    case 32: return launch_gjk_lanes<32>(b, prm, q, order, range, blocks, st);
+    case 1: return launch_gjk_lanes<1>(b, prm, q, order, range, blocks, st, next);
+    case 2: return launch_gjk_lanes<2>(b, prm, q, order, range, blocks, st, next);
+    case 4: return launch_gjk_lanes<4>(b, prm, q, order, range, blocks, st, next);
+    case 8: return launch_gjk_lanes<8>(b, prm, q, order, range, blocks, st, next);
+    case 16: return launch_gjk_lanes<16>(b, prm, q, order, range, blocks, st, next);
+    case 32: return launch_gjk_lanes<32>(b, prm, q, order, range, blocks, st, next);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -112,15 +112,31 @@ enum : int { kPassPlain = 0, kPassFull = 1 };
 template <int LANES, int MODE>
 __global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_pass(BatchArgs b, QueryParams prm, EpaQueue q,
                                                    const uint32_t* __restrict__ order,
-                                                   const uint32_t* __restrict__ range) {
+                                                   const uint32_t* __restrict__ range, uint32_t* next) {
   uint32_t begin = 0, end = b.n_pairs;
   if (range) {
     begin = range[0];
     end = range[1];
   }
   const Group<LANES> g = Group<LANES>::make();
-  const uint32_t stride = gridDim.x * (blockDim.x / LANES);
-  for (uint32_t item = begin + (blockIdx.x * blockDim.x + threadIdx.x) / LANES; item < end; item += stride) {
+  // A warp runs 32 / LANES pairs at a time.  With a counter (next, zero
+  // before the launch) it takes its next pairs there as it finishes a round,
+  // so a persistent grid's warps end together; without one, warp w takes
+  // rounds w, w + W, ... (W warps in the grid).
+  constexpr uint32_t kPer = 32 / LANES;
+  const uint32_t slot = (threadIdx.x & 31u) / LANES;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
+  auto take = [&](uint32_t done) -> uint32_t {
+    if (!next) return done + n_warps * kPer;
+    uint32_t k = 0;
+    if ((threadIdx.x & 31u) == 0) k = atomicAdd(next, kPer);
+    return __shfl_sync(0xFFFFFFFFu, k, 0);
+  };
+  const uint32_t n_items = end > begin ? end - begin : 0u;
+  for (uint32_t round = next ? take(0) : warp * kPer; round < n_items; round = take(round)) {
+    const uint32_t item = begin + round + slot;
+    if (item >= end) continue;
     const uint32_t pid = order ? order[item] : item;
     const PairDev pr = load_pair(b.pairs, pid);
     if (pr.a >= b.n_shapes || pr.b >= b.n_shapes) {
@@ -206,16 +222,17 @@ __global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_pass(BatchArgs b, Quer
 // PLAIN variant when the query has no closed-form pairs, MPR or learned start.
 template <int LANES>
 cudaError_t launch_gjk_lanes(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q, const uint32_t* order,
-                             const uint32_t* range, int blocks, cudaStream_t st);
+                             const uint32_t* range, int blocks, cudaStream_t st, uint32_t* next);
 
 #define FCLG_GJK_INSTANTIATE(L)                                                                              \
   template <>                                                                                                \
   cudaError_t launch_gjk_lanes<L>(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q,             \
-                                  const uint32_t* order, const uint32_t* range, int blocks, cudaStream_t st) { \
+                                  const uint32_t* order, const uint32_t* range, int blocks, cudaStream_t st, \
+                                  uint32_t* next) {                                                          \
     if (FCLG_GJK_PLAIN_VARIANT && !prm.analytic && !prm.use_mpr && !b.guess)                                 \
-      gjk_pass<L, kPassPlain><<<blocks, 128, 0, st>>>(b, prm, q, order, range);                              \
+      gjk_pass<L, kPassPlain><<<blocks, 128, 0, st>>>(b, prm, q, order, range, next);                        \
     else                                                                                                     \
-      gjk_pass<L, kPassFull><<<blocks, 128, 0, st>>>(b, prm, q, order, range);                               \
+      gjk_pass<L, kPassFull><<<blocks, 128, 0, st>>>(b, prm, q, order, range, next);                         \
     return cudaGetLastError();                                                                               \
   }
 

@@ -37,9 +37,13 @@ constexpr size_t kEpaRecordBytes = 7 * sizeof(float4);
 constexpr size_t kEpaResumeBytes = 6688;
 
 // Scratch of the bucketing pass: pairs sorted by shape class (bucket.cu).
-constexpr int kShapeClasses = 6;  // box, sphere, capsule, cylinder, convex <= big_nv, convex > big_nv
+// box, sphere, capsule, cylinder, five bins of convex hulls up to big_nv vertices (by the
+// power of two of the vertex count: < 16, < 32, < 64, < 128, more), convex > big_nv
+constexpr int kHullBins = 5;
+constexpr int kShapeClasses = 4 + kHullBins + 1;
 constexpr int kBucketSmallKeys = kShapeClasses * kShapeClasses;
 constexpr int kBucketKeys = 2 * kBucketSmallKeys;
+static_assert(kBucketKeys <= 256, "bucket keys are bytes; the scan runs one thread per key");
 struct BucketScratch {
   uint8_t* keys;      // [n] class key per pair
   uint32_t* order;    // [n] pair indices sorted by key
@@ -55,9 +59,11 @@ cudaError_t launch_bucketing(const BatchArgs& b, const BucketScratch& s, uint32_
 // `blocks` CTAs (0: one CTA per 128 lanes of work, not persistent).  refill:
 // one-lane launches of queries without MPR or closed-form pairs run
 // gjk_refill (lanes take new pairs as theirs finish) instead of gjk_pass<1>.
+// next (optional, zero before the launch): the counter the persistent grid's
+// warps take their pairs from.
 cudaError_t launch_gjk(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q, int lanes,
                        const uint32_t* order, const uint32_t* range, int blocks, cudaStream_t st,
-                       bool refill = false);
+                       bool refill = false, uint32_t* next = nullptr);
 // fcl::collide with directed penetration along b.guess (directed_pass.cu).
 cudaError_t launch_directed(const BatchArgs& b, const QueryParams& prm, int blocks, cudaStream_t st);
 // GJKSolver<double>::shapeDistance per pair in FP64, one thread per pair, as a
