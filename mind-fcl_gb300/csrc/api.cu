@@ -21,8 +21,9 @@
 #include "warmstart.h"
 
 // Counters of a query (fclg_context::epa_count): EPA work list and overflow
-// list lengths, entries taken by the two EPA launches and by the two GJK launches.
-constexpr int kQueueCounters = 6;
+// list lengths, entries taken by the two EPA launches and by the two GJK
+// launches, then the separated-pair list's length and entries taken.
+constexpr int kQueueCounters = 8;
 
 struct fclg_context {
   int device = 0;
@@ -50,8 +51,7 @@ struct fclg_context {
   size_t bp_join_bytes = 0;
   bool gjk_refill = false;
   // scratch handed from the GJK pass to the EPA pass
-  uint32_t* epa_count = nullptr;  // [6]: work list, overflow list; entries taken by the two EPA launches,
-                                  // then by the two GJK launches
+  uint32_t* epa_count = nullptr;  // [kQueueCounters]
   uint32_t* epa_list = nullptr;
   uint32_t* epa_ovf = nullptr;
   unsigned char* epa_resume = nullptr;  // polytope states handed from the small EPA layout to the large one
@@ -67,6 +67,7 @@ struct fclg_context {
   uint8_t* bk_keys = nullptr;
   uint32_t* bk_order = nullptr;
   uint32_t* bk_small = nullptr;  // hist | cursor | ranges
+  float4* bk_dist = nullptr;     // separated pairs between the split GJK launches (fclg::DistList)
   size_t bk_cap = 0;
   // launch shape
   bool bucketing = true;
@@ -282,13 +283,16 @@ int ensure_bucket(fclg_context* c, size_t n) {
   if (n <= c->bk_cap) return FCLG_OK;
   if (c->bk_keys) cudaFree(c->bk_keys);
   if (c->bk_order) cudaFree(c->bk_order);
+  if (c->bk_dist) cudaFree(c->bk_dist);
   c->bk_keys = nullptr;
   c->bk_order = nullptr;
+  c->bk_dist = nullptr;
   c->bk_cap = 0;
   c->scratch_epoch += 1;
   const size_t cap = std::max<size_t>(n, 1024);
   FCLG_CUDA(c, cudaMalloc(&c->bk_keys, cap));
   FCLG_CUDA(c, cudaMalloc(&c->bk_order, cap * sizeof(uint32_t)));
+  FCLG_CUDA(c, cudaMalloc(&c->bk_dist, cap * fclg::kDistRecordBytes));
   c->bk_cap = cap;
   return FCLG_OK;
 }
@@ -406,11 +410,12 @@ int run_query(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_
                            c->bk_small + 2 * fclg::kBucketKeys};
     FCLG_CUDA(c, fclg::launch_bucketing(b, bs, (uint32_t)c->large_hull, st));
     const int blocks = c->num_sms * c->gjk_ctas_per_sm;
+    const fclg::DistList dl{c->epa_count + 6, c->bk_dist, c->epa_count + 7};
     FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes, bs.order, bs.ranges, blocks, st, c->gjk_refill,
-                                  c->epa_count + 4));
+                                  c->epa_count + 4, &dl));
     FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes_large, bs.order, bs.ranges + 2, blocks, st,
                                   c->gjk_refill, c->epa_count + 5));
-    c->launches += 5;
+    c->launches += fclg::gjk_split_applies(b, prm, c->gjk_lanes, blocks, c->gjk_refill) ? 6 : 5;
   } else {
     FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes, nullptr, nullptr, 0, st, c->gjk_refill));
     c->launches += 1;
@@ -490,6 +495,7 @@ void fclg_destroy(fclg_context* c) {
   if (c->bk_keys) cudaFree(c->bk_keys);
   if (c->bk_order) cudaFree(c->bk_order);
   if (c->bk_small) cudaFree(c->bk_small);
+  if (c->bk_dist) cudaFree(c->bk_dist);
   if (c->mesh_io) cudaFree(c->mesh_io);
   if (c->mesh_cbuf) cudaFree(c->mesh_cbuf);
   if (c->mesh_ctr) cudaFree(c->mesh_ctr);

@@ -585,18 +585,19 @@ __device__ __forceinline__ bool min_distance(const Sup& sup, Simplex& s, float t
   return false;
 }
 
-// gjk.hpp:10-140.  want_distance selects the MinSeparationDistanceOutput path.
-// probe > 0 (a learned start) allows the boolean phase that many support
-// evaluations to certify separation; past them the run ends with
-// kGjkIterLimit and no points (the pair is then redone from the plain start).
-// cert_gap: see min_distance.
+// Outcome of the boolean phase (gjk_boolean): the run is over (o.status set),
+// separation is certified (s holds the separating vertex as a rank-1 simplex:
+// the distance loop starts there), or the loop stopped undetermined (o.status
+// set; the witness points come from the simplex by extract_try_sub).
+enum : int { kBoolDone = 0, kBoolSeparated = 1, kBoolUndetermined = 2 };
+
+// The boolean phase of gjk.hpp:10-140.  probe > 0 (a learned start) allows it
+// that many support evaluations to certify separation; past them the run ends
+// with kGjkIterLimit and no points (the pair is then redone from the plain
+// start).  o.iterations counts its loop iterations.
 template <class Sup>
-__device__ __forceinline__ GjkOut gjk_evaluate(const Sup& sup, f3 guess, float tol, int max_iter, bool want_distance,
-                                               Simplex& s, int probe = 0, float cert_gap = 0.f) {
-  GjkOut o;
-  o.point_valid = false;
-  o.iterations = 0;
-  o.p0 = o.p1 = mk3(0, 0, 0);
+__device__ __forceinline__ int gjk_boolean(const Sup& sup, f3 guess, float tol, int max_iter, Simplex& s, GjkOut& o,
+                                           int probe = 0) {
   f3 d = guess;
   if (sqn(d) <= 0.f) d = mk3(1, 0, 0);
   d = normalized(d);
@@ -605,58 +606,58 @@ __device__ __forceinline__ GjkOut gjk_evaluate(const Sup& sup, f3 guess, float t
   sup(d, pa, pb);
   s.set(0, pa, pb);
   s.rank = 1;
-  if (sqn(s.w[0]) <= tol2) { o.status = kGjkIntersect; return o; }
-  bool separated = dot(s.w[0], d) < 0.f;
-  int undetermined = -1;
-  if (!separated) {
-    d = -d;
-    const int bool_iters = (probe > 0 && probe - 1 < max_iter) ? probe - 1 : max_iter;
-    int it = 0;
-    for (; it < bool_iters; ++it) {
-      o.iterations = it + 1;
-      sup(d, pa, pb);
-      const f3 w = pa - pb;
-      if (dot(w, d) < 0.f) {
-        s.set(0, pa, pb);  // the separating vertex seeds the distance simplex
-        s.rank = 1;
-        separated = true;
-        break;
-      }
-      bool dup = false;
+  if (sqn(s.w[0]) <= tol2) { o.status = kGjkIntersect; return kBoolDone; }
+  if (dot(s.w[0], d) < 0.f) return kBoolSeparated;
+  d = -d;
+  const int bool_iters = (probe > 0 && probe - 1 < max_iter) ? probe - 1 : max_iter;
+  for (int it = 0; it < bool_iters; ++it) {
+    o.iterations = it + 1;
+    sup(d, pa, pb);
+    const f3 w = pa - pb;
+    if (dot(w, d) < 0.f) {
+      s.set(0, pa, pb);  // the separating vertex seeds the distance simplex
+      s.rank = 1;
+      return kBoolSeparated;
+    }
+    bool dup = false;
 #pragma unroll
-      for (int j = 0; j < 4; ++j)
-        if (j < s.rank && sqn(s.w[j] - w) < tol2) dup = true;
-      if (dup) { undetermined = kGjkNoProgress; break; }
-      if (s.rank == 1) s.set(1, pa, pb);
-      else if (s.rank == 2) s.set(2, pa, pb);
-      else s.set(3, pa, pb);
-      s.rank += 1;
-      if (sqn(w) <= tol2) { o.status = kGjkIntersect; return o; }
-      Proj st;
-      if (s.rank == 2) st = project2(s, d);
-      else if (s.rank == 3) st = project3(s, d, tol);
-      else st = project4(s, d, tol);
-      if (st == Proj::Failed) { o.status = kGjkFailed; return o; }
-      if (st == Proj::Intersect) { o.status = kGjkIntersect; return o; }
-      if (st == Proj::ZeroVolume) { undetermined = kGjkNoProgress; break; }
-    }
-    if (!separated && undetermined < 0) {
-      if (bool_iters < max_iter) {  // the learned start's probe ran out
-        o.status = kGjkIterLimit;
-        return o;
-      }
-      undetermined = kGjkIterLimit;
-    }
-  } else {
-    s.rank = 1;
+    for (int j = 0; j < 4; ++j)
+      if (j < s.rank && sqn(s.w[j] - w) < tol2) dup = true;
+    if (dup) { o.status = kGjkNoProgress; return kBoolUndetermined; }
+    if (s.rank == 1) s.set(1, pa, pb);
+    else if (s.rank == 2) s.set(2, pa, pb);
+    else s.set(3, pa, pb);
+    s.rank += 1;
+    if (sqn(w) <= tol2) { o.status = kGjkIntersect; return kBoolDone; }
+    Proj st;
+    if (s.rank == 2) st = project2(s, d);
+    else if (s.rank == 3) st = project3(s, d, tol);
+    else st = project4(s, d, tol);
+    if (st == Proj::Failed) { o.status = kGjkFailed; return kBoolDone; }
+    if (st == Proj::Intersect) { o.status = kGjkIntersect; return kBoolDone; }
+    if (st == Proj::ZeroVolume) { o.status = kGjkNoProgress; return kBoolUndetermined; }
   }
-  if (separated) {
+  o.status = kGjkIterLimit;
+  // the learned start's probe ran out: no points
+  return bool_iters < max_iter ? kBoolDone : kBoolUndetermined;
+}
+
+// gjk.hpp:10-140.  want_distance selects the MinSeparationDistanceOutput path.
+// probe: see gjk_boolean; cert_gap: see min_distance.
+template <class Sup>
+__device__ __forceinline__ GjkOut gjk_evaluate(const Sup& sup, f3 guess, float tol, int max_iter, bool want_distance,
+                                               Simplex& s, int probe = 0, float cert_gap = 0.f) {
+  GjkOut o;
+  o.point_valid = false;
+  o.iterations = 0;
+  o.p0 = o.p1 = mk3(0, 0, 0);
+  const int k = gjk_boolean(sup, guess, tol, max_iter, s, o, probe);
+  if (k == kBoolSeparated) {
     o.status = kGjkSeparated;
     if (want_distance) o.point_valid = min_distance(sup, s, tol, max_iter, o.p0, o.p1, o.iterations, cert_gap);
-    return o;
+  } else if (k == kBoolUndetermined && want_distance) {
+    o.point_valid = extract_try_sub(s, o.p0, o.p1);
   }
-  o.status = undetermined;
-  if (want_distance) o.point_valid = extract_try_sub(s, o.p0, o.p1);
   return o;
 }
 

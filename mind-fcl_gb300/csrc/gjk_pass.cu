@@ -109,10 +109,22 @@ __global__ void __launch_bounds__(128, FCLG_REFILL_MINB) gjk_refill(BatchArgs b,
 }
 
 
+bool gjk_split_applies(const BatchArgs& b, const QueryParams& prm, int lanes, int blocks, bool refill) {
+  // the one-lane plain distance pass on a persistent grid (the distance
+  // launch sizes itself by a count on the device)
+  return FCLG_GJK_PLAIN_VARIANT && lanes == 1 && blocks > 0 && !refill && !prm.analytic && !prm.use_mpr &&
+         !b.guess && prm.want_distance;
+}
+
 cudaError_t launch_gjk(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q, int lanes,
                        const uint32_t* order, const uint32_t* range, int blocks, cudaStream_t st, bool refill,
-                       uint32_t* next) {
+                       uint32_t* next, const DistList* dl) {
   if (b.n_pairs == 0) return cudaSuccess;
+  if (dl && gjk_split_applies(b, prm, lanes, blocks, refill)) {
+    gjk_pass<1, kPassSplit><<<blocks, 128, 0, st>>>(b, prm, q, order, range, next, *dl);
+    gjk_dist_pass<1><<<blocks, 128, 0, st>>>(b, prm, q, *dl);
+    return cudaGetLastError();
+  }
   const int threads = 128;
   if (blocks <= 0) {
     const uint64_t total = (uint64_t)b.n_pairs * (uint64_t)lanes;

@@ -104,7 +104,9 @@ __device__ __forceinline__ void finish_pair(const BatchArgs& b, const QueryParam
 // entry points), which keeps the kernel's code small enough for the
 // instruction cache; FULL compiles every path and selects by prm / b.guess.
 // Both give the same results on the queries PLAIN serves.
-enum : int { kPassPlain = 0, kPassFull = 1 };
+// SPLIT is PLAIN's boolean phase alone: a separated pair goes to the
+// DistList for gjk_dist_pass (distance queries only).
+enum : int { kPassPlain = 0, kPassFull = 1, kPassSplit = 2 };
 #ifndef FCLG_GJK_PLAIN_VARIANT
 #define FCLG_GJK_PLAIN_VARIANT 1
 #endif
@@ -112,7 +114,8 @@ enum : int { kPassPlain = 0, kPassFull = 1 };
 template <int LANES, int MODE>
 __global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_pass(BatchArgs b, QueryParams prm, EpaQueue q,
                                                    const uint32_t* __restrict__ order,
-                                                   const uint32_t* __restrict__ range, uint32_t* next) {
+                                                   const uint32_t* __restrict__ range, uint32_t* next,
+                                                   DistList dl) {
   uint32_t begin = 0, end = b.n_pairs;
   if (range) {
     begin = range[0];
@@ -188,7 +191,22 @@ __global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_pass(BatchArgs b, Quer
     }
     Simplex s;
     GjkOut o;
-    if (MODE == kPassFull && b.guess) {
+    if (MODE == kPassSplit) {
+      // gjk_evaluate's boolean phase; the distance loop runs in gjk_dist_pass
+      o.point_valid = false;
+      o.iterations = 0;
+      o.p0 = o.p1 = mk3(0, 0, 0);
+      const int k = gjk_boolean(sup, -plain, prm.gjk_tol, prm.gjk_max_iter, s, o);
+      if (k == kBoolSeparated) {
+        if (g.lane == 0) {
+          const uint32_t r = aggregated_slot(dl.count);
+          dl.rec[2 * (size_t)r] = make_float4(__uint_as_float(pid), __int_as_float(o.iterations), s.a[0].x, s.a[0].y);
+          dl.rec[2 * (size_t)r + 1] = make_float4(s.a[0].z, s.b[0].x, s.b[0].y, s.b[0].z);
+        }
+        continue;
+      }
+      if (k == kBoolUndetermined) o.point_valid = extract_try_sub(s, o.p0, o.p1);
+    } else if (MODE == kPassFull && b.guess) {
       // Learned direction first, for a separation certificate within
       // warm_probe supports and a distance certified to warm_gap.  A pair it
       // does not settle (overlapping: its EPA must start from the plain
@@ -218,6 +236,47 @@ __global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_pass(BatchArgs b, Quer
 }
 
 
+// The distance loop of the separated pairs a SPLIT gjk_pass handed over
+// (gjk_distance.hpp:10-105 from the separating vertex), as a persistent grid
+// whose warps take 32 / LANES records at a time from dl.next.
+template <int LANES>
+__global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_dist_pass(BatchArgs b, QueryParams prm, EpaQueue q,
+                                                        DistList dl) {
+  const Group<LANES> g = Group<LANES>::make();
+  constexpr uint32_t kPer = 32 / LANES;
+  const uint32_t slot = (threadIdx.x & 31u) / LANES;
+  const uint32_t n = *dl.count;
+  auto take = [&]() -> uint32_t {
+    uint32_t k = 0;
+    if ((threadIdx.x & 31u) == 0) k = atomicAdd(dl.next, kPer);
+    return __shfl_sync(0xFFFFFFFFu, k, 0);
+  };
+  for (uint32_t round = take(); round < n; round = take()) {
+    const uint32_t item = round + slot;
+    if (item >= n) continue;
+    const float4 r0 = dl.rec[2 * (size_t)item], r1 = dl.rec[2 * (size_t)item + 1];
+    const uint32_t pid = __float_as_uint(r0.x);
+    const PairDev pr = load_pair(b.pairs, pid);
+    MinkowskiSupport<LANES> sup;
+    sup.A = load_shape(b.shapes, LANES == 1 ? b.walk : nullptr, pr.a);
+    sup.B = load_shape(b.shapes, LANES == 1 ? b.walk : nullptr, pr.b);
+    sup.pose = pr.pose;
+    sup.verts = b.verts;
+    sup.hull = b.hull;
+    sup.g = g;
+    Simplex s;
+    s.set(0, mk3(r0.z, r0.w, r1.x), mk3(r1.y, r1.z, r1.w));
+    s.rank = 1;
+    GjkOut o;
+    o.status = kGjkSeparated;
+    o.iterations = __float_as_int(r0.y);
+    o.p0 = o.p1 = mk3(0, 0, 0);
+    o.point_valid = min_distance(sup, s, prm.gjk_tol, prm.gjk_max_iter, o.p0, o.p1, o.iterations);
+    if (g.lane != 0) continue;
+    finish_pair(b, prm, q, pid, o, s);
+  }
+}
+
 // Launches gjk_pass<LANES, ...> (defined in the translation unit that instantiates LANES): the
 // PLAIN variant when the query has no closed-form pairs, MPR or learned start.
 template <int LANES>
@@ -230,9 +289,9 @@ cudaError_t launch_gjk_lanes(const BatchArgs& b, const QueryParams& prm, const E
                                   const uint32_t* order, const uint32_t* range, int blocks, cudaStream_t st, \
                                   uint32_t* next) {                                                          \
     if (FCLG_GJK_PLAIN_VARIANT && !prm.analytic && !prm.use_mpr && !b.guess)                                 \
-      gjk_pass<L, kPassPlain><<<blocks, 128, 0, st>>>(b, prm, q, order, range, next);                        \
+      gjk_pass<L, kPassPlain><<<blocks, 128, 0, st>>>(b, prm, q, order, range, next, DistList{});            \
     else                                                                                                     \
-      gjk_pass<L, kPassFull><<<blocks, 128, 0, st>>>(b, prm, q, order, range, next);                         \
+      gjk_pass<L, kPassFull><<<blocks, 128, 0, st>>>(b, prm, q, order, range, next, DistList{});             \
     return cudaGetLastError();                                                                               \
   }
 

@@ -33,6 +33,16 @@ struct EpaQueue {
                              // warp takes every (warps in the grid)-th entry
 };
 constexpr size_t kEpaRecordBytes = 7 * sizeof(float4);
+
+// Separated pairs handed from the boolean GJK pass to the distance pass (the
+// split one-lane launch, launch_gjk): each record is the pair and the
+// separating vertex the distance loop starts from.
+struct DistList {
+  uint32_t* count;  // [1] records written; zero before the boolean pass
+  float4* rec;      // [capacity][2]: {pid, iterations so far, pa.x, pa.y}, {pa.z, pb.x, pb.y, pb.z}
+  uint32_t* next;   // [1] records taken by the distance pass; zero before it
+};
+constexpr size_t kDistRecordBytes = 2 * sizeof(float4);
 // Bytes of one small-layout polytope state handed to the large layout (epa.cuh EpaResume).
 constexpr size_t kEpaResumeBytes = 6688;
 
@@ -60,10 +70,15 @@ cudaError_t launch_bucketing(const BatchArgs& b, const BucketScratch& s, uint32_
 // one-lane launches of queries without MPR or closed-form pairs run
 // gjk_refill (lanes take new pairs as theirs finish) instead of gjk_pass<1>.
 // next (optional, zero before the launch): the counter the persistent grid's
-// warps take their pairs from.
+// warps take their pairs from.  dl (optional, capacity = the batch): where
+// gjk_split_applies, the pass runs as two launches -- the boolean phase for
+// every pair, which hands its separated pairs to dl, then the distance loop
+// over dl -- so that no warp interleaves the two phases' code (same results).
 cudaError_t launch_gjk(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q, int lanes,
                        const uint32_t* order, const uint32_t* range, int blocks, cudaStream_t st,
-                       bool refill = false, uint32_t* next = nullptr);
+                       bool refill = false, uint32_t* next = nullptr, const DistList* dl = nullptr);
+// Whether launch_gjk with these arguments and a DistList runs the split pair of launches.
+bool gjk_split_applies(const BatchArgs& b, const QueryParams& prm, int lanes, int blocks, bool refill);
 // fcl::collide with directed penetration along b.guess (directed_pass.cu).
 cudaError_t launch_directed(const BatchArgs& b, const QueryParams& prm, int blocks, cudaStream_t st);
 // GJKSolver<double>::shapeDistance per pair in FP64, one thread per pair, as a

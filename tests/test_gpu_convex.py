@@ -446,3 +446,25 @@ def test_epa_resume_equals_restart(gpu_ctx):
     assert resumed.tobytes() == restarted.tobytes()
     # the batch does reach the large layout (about 64 expansions fill 128 faces)
     assert np.sum((resumed["distance"] < 0) & (resumed["iterations"] > 90)) > 100
+
+
+@pytest.mark.parametrize("workload", ["mixed", "pareto"])
+def test_split_gjk_launches_equal_one_pass(gpu_ctx, workload):
+    """The bucketed one-lane distance query runs GJK as two launches (boolean
+    phase, then the distance loop over the separated pairs it hands over);
+    the results equal the single-pass launch's (bucketing off) byte for byte,
+    with and without EPA."""
+    from fclg.api import FCLG_REQ_NO_EPA, make_request
+    b = getattr(workloads, workload)(100_000, seed=workloads.SEED_BASE + 43)
+    keep = gpu_ctx.get_tuning()
+    gpu_ctx.set_batch(b)
+    try:
+        for req in (None, make_request(flags=FCLG_REQ_NO_EPA)):
+            out = []
+            for bucketing in (True, False):
+                gpu_ctx.set_tuning(bucketing=bucketing, gjk_lanes_small=1, gjk_lanes_large=1, gjk_refill=False,
+                                   large_hull_vertices=1024)
+                out.append(gpu_ctx.distance(b.pairs, req))
+            assert np.array_equal(out[0].view(np.uint8), out[1].view(np.uint8))
+    finally:
+        gpu_ctx.set_tuning(**keep)
