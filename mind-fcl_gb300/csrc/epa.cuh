@@ -221,39 +221,40 @@ struct EpaWarp {
   }
 
   // Initial polytope from faces (index triples into the vertices already
-  // pushed), oriented away from the vertex centroid; lane 0 only.  Returns
+  // pushed), oriented away from the vertex centroid: a lane per face, then a
+  // lane per (face, edge) finding the neighbour across it (nf <= 8).  Returns
   // false when the faces do not close up.
   __device__ bool build_faces(const int (*tri)[3], int nf) {
-    bool ok = true;
-    if (lane == 0) {
+    if ((int)lane < nf) {
       f3 c = mk3(0, 0, 0);
       for (int i = 0; i < nv; ++i) c = c + W(i);
       c = c * (1.f / (float)nv);
-      for (int f = 0; f < nf; ++f) {
-        int i = tri[f][0], j = tri[f][1], k = tri[f][2];
-        const f3 n = cross(W(j) - W(i), W(k) - W(i));
-        if (dot(n, W(i) - c) < 0.f) { const int t = j; j = k; k = t; }
-        write_face(f, i, j, k);
-        P.fmark[f] = 0;
-      }
-      for (int f = 0; f < nf && ok; ++f) {
-        for (int e = 0; e < 3 && ok; ++e) {
-          const uint32_t u = fvert(P.fv[f], e), v = fvert(P.fv[f], (e + 1) % 3);
-          int found = -1;
-          for (int g = 0; g < nf && found < 0; ++g) {
-            if (g == f) continue;
-            for (int h = 0; h < 3; ++h)
-              if (fvert(P.fv[g], h) == v && fvert(P.fv[g], (h + 1) % 3) == u) { found = g; break; }
-          }
-          if (found < 0) ok = false;
-          else P.fadj[f][e] = (uint16_t)found;
-        }
-      }
+      const int f = (int)lane;
+      int i = tri[f][0], j = tri[f][1], k = tri[f][2];
+      const f3 n = cross(W(j) - W(i), W(k) - W(i));
+      if (dot(n, W(i) - c) < 0.f) { const int t = j; j = k; k = t; }
+      write_face(f, i, j, k);
+      P.fmark[f] = 0;
     }
+    __syncwarp();
+    bool ok = true;
+    if ((int)lane < 3 * nf) {
+      const int f = (int)lane / 3, e = (int)lane % 3;
+      const uint32_t u = fvert(P.fv[f], e), v = fvert(P.fv[f], (e + 1) % 3);
+      int found = -1;
+      for (int g = 0; g < nf && found < 0; ++g) {
+        if (g == f) continue;
+        for (int h = 0; h < 3; ++h)
+          if (fvert(P.fv[g], h) == v && fvert(P.fv[g], (h + 1) % 3) == u) { found = g; break; }
+      }
+      if (found < 0) ok = false;
+      else P.fadj[f][e] = (uint16_t)found;
+    }
+    __syncwarp();
     hw = nf;
     live = nf;
     fs_top = 0;
-    return __shfl_sync(0xFFFFFFFFu, (int)ok, 0) != 0;
+    return __all_sync(0xFFFFFFFFu, ok);
   }
 
   // formNewTetrahedronPolytope, epa_simplex2polytope.hpp:143-174
@@ -270,7 +271,9 @@ struct EpaWarp {
   // edge / vertex feature).  Depth is that point's distance from the origin
   // (the reference's min_distance_square).  A degenerate triangle falls back
   // to the last support pair like assignPenetrationPair (epa.hpp:340-365).
+  // Lane 0 only (the lane that reports the result): the FP64 pipe is narrow.
   __device__ void finalize(uint32_t fvp, f3 cand_pa, f3 cand_pb, EpaResult& r) const {
+    if (lane != 0) return;
     const uint32_t ia = fvert(fvp, 0), ib = fvert(fvp, 1), ic = fvert(fvp, 2);
     const d3 a = tod(W(ia)), b = tod(W(ib)), c = tod(W(ic));
     const d3 ab = b - a, ac = c - a;
