@@ -18,9 +18,14 @@
 #endif
 
 // Inline policy of the simplex routines that run at most once per pair or
-// only at rank 4 (kept out of line by a build that defines it so).
+// only at rank 4 (kept out of line by a build that defines
+// FCLG_GJK_COLD_OUTLINED, or FCLG_GJK_COLD itself).
 #ifndef FCLG_GJK_COLD
+#ifdef FCLG_GJK_COLD_OUTLINED
+#define FCLG_GJK_COLD static __noinline__
+#else
 #define FCLG_GJK_COLD __forceinline__
+#endif
 #endif
 
 namespace fclg {
@@ -153,7 +158,10 @@ __device__ __forceinline__ void update2(Simplex& s, f3& out, float tol) {
   }
 }
 
-// gjk_distance.hpp:155-286 (slot 2 newest)
+// gjk_distance.hpp:155-286 (slot 2 newest).  The segment candidates --
+// (s2, s1), (s3, s1), (s3, s2), in that order, the first of equal distances
+// kept -- run through one update2 call site in a loop, so the routine holds a
+// single copy of update2's code.
 __device__ __forceinline__ void update3(Simplex& s, f3& out, float tol) {
   const f3 s1 = s.w[2], s2 = s.w[1], s3 = s.w[0];
   const f3 s1_to_s2 = s2 - s1, s1_to_s3 = s3 - s1;
@@ -169,82 +177,82 @@ __device__ __forceinline__ void update3(Simplex& s, f3& out, float tol) {
   const float area2 = sqn(n);
   const bool zero_area = area2 <= 0.f;
   const bool s12_sep = dot(s1, cross(n, s1_to_s2)) > 0.f;
+  unsigned cand;
   if (!sep2 && s12_sep) {
+    cand = 1u;  // segment s1 s2 alone
+  } else {
+    const bool s13_sep = dot(s1, cross(n, s1_to_s3)) < 0.f;
+    if (!sep3 && s13_sep) {
+      cand = 2u;  // segment s1 s3 alone
+    } else {
+      const bool s23_sep = dot(s2, cross(n, s3 - s2)) > 0.f;
+      cand = ((zero_area || s12_sep) ? 1u : 0u) | ((zero_area || s13_sep) ? 2u : 0u) |
+             ((zero_area || s23_sep) ? 4u : 0u);
+    }
+  }
+  // the winner is run once more on s itself (the same result) instead of
+  // keeping a copy of its simplex
+  float best = -1.f;
+  int bk = -1;
+#pragma unroll 1
+  for (int k = 0; k < 3; ++k) {
+    if (!(cand & (1u << k))) continue;
+    Simplex c = s;
+    if (k == 0) {
+      c.copy(0, 1);
+      c.copy(1, 2);
+    } else if (k == 1) {
+      c.copy(1, 2);
+    }
+    c.rank = 2;
+    f3 pt;
+    update2(c, pt, tol);
+    const float dd = sqn(pt);
+    if (best < 0.f || dd < best) { best = dd; bk = k; }
+  }
+  if (bk < 0) {
+    out = n * (dot(s1, n) / area2);
+    return;
+  }
+  if (bk == 0) {
     s.copy(0, 1);
     s.copy(1, 2);
-    s.rank = 2;
-    update2(s, out, tol);
-    return;
-  }
-  const bool s13_sep = dot(s1, cross(n, s1_to_s3)) < 0.f;
-  if (!sep3 && s13_sep) {
+  } else if (bk == 1) {
     s.copy(1, 2);
-    s.rank = 2;
-    update2(s, out, tol);
-    return;
   }
-  float best = -1.f;
-  f3 best_pt = mk3(0, 0, 0), pt;
-  Simplex best_s = s, c;
-  if (zero_area || s12_sep) {
-    c = s;
-    c.copy(0, 1);
-    c.copy(1, 2);
-    c.rank = 2;
-    update2(c, pt, tol);
-    const float dd = sqn(pt);
-    if (best < 0.f || dd < best) { best = dd; best_s = c; best_pt = pt; }
-  }
-  if (zero_area || s13_sep) {
-    c = s;
-    c.copy(1, 2);
-    c.rank = 2;
-    update2(c, pt, tol);
-    const float dd = sqn(pt);
-    if (best < 0.f || dd < best) { best = dd; best_s = c; best_pt = pt; }
-  }
-  const bool s23_sep = dot(s2, cross(n, s3 - s2)) > 0.f;
-  if (zero_area || s23_sep) {
-    c = s;
-    c.rank = 2;
-    update2(c, pt, tol);
-    const float dd = sqn(pt);
-    if (best < 0.f || dd < best) { best = dd; best_s = c; best_pt = pt; }
-  }
-  if (best < 0.f) {
-    out = n * (dot(s1, n) / area2);
-  } else {
-    s = best_s;
-    out = best_pt;
-  }
+  s.rank = 2;
+  update2(s, out, tol);
 }
 
-// gjk_distance.hpp:288-373 (slot 3 newest): best of faces (3,2,1), (3,2,0), (3,1,0).
+// gjk_distance.hpp:288-373 (slot 3 newest): best of faces (3,2,1), (3,2,0),
+// (3,1,0), through one update3 call site.
 __device__ FCLG_GJK_COLD Upd update4(Simplex& s, f3& out, float tol) {
+  // k = 0..2 the three faces, k = 3 the winner once more on s itself (the
+  // same result; no copy of its simplex is kept)
   float best = -1.f;
-  f3 best_pt = mk3(0, 0, 0), pt;
-  Simplex best_s = s, c;
-  c = s;
-  c.copy(0, 1); c.copy(1, 2); c.copy(2, 3);
-  c.rank = 3;
-  update3(c, pt, tol);
-  float dd = sqn(pt);
-  if (best < 0.f || dd < best) { best = dd; best_pt = pt; best_s = c; }
-  c = s;
-  c.copy(1, 2); c.copy(2, 3);
-  c.rank = 3;
-  update3(c, pt, tol);
-  dd = sqn(pt);
-  if (best < 0.f || dd < best) { best = dd; best_pt = pt; best_s = c; }
-  c = s;
-  c.copy(2, 3);
-  c.rank = 3;
-  update3(c, pt, tol);
-  dd = sqn(pt);
-  if (best < 0.f || dd < best) { best = dd; best_pt = pt; best_s = c; }
-  if (best < 0.f) return Upd::NoImprovement;
-  s = best_s;
-  out = best_pt;
+  int bk = 0;
+#pragma unroll 1
+  for (int k = 0; k < 4; ++k) {
+    const int f = k < 3 ? k : bk;
+    Simplex c = s;
+    if (f == 0) {
+      c.copy(0, 1); c.copy(1, 2); c.copy(2, 3);
+    } else if (f == 1) {
+      c.copy(1, 2); c.copy(2, 3);
+    } else {
+      c.copy(2, 3);
+    }
+    c.rank = 3;
+    f3 pt;
+    update3(c, pt, tol);
+    if (k == 3) {
+      s = c;
+      out = pt;
+      break;
+    }
+    const float dd = sqn(pt);
+    if (best < 0.f || dd < best) { best = dd; bk = k; }
+  }
   return Upd::OK;
 }
 
@@ -545,44 +553,48 @@ struct GjkRun {
 template <class Sup>
 __device__ __forceinline__ bool min_distance(const Sup& sup, Simplex& s, float tol, int max_iter, f3& p0, f3& p1,
                                              int& iters, float cert_gap = 0.f) {
-  f3 cur;
-  if (update_simplex(s, cur, tol) != Upd::OK) return false;
+  // every stop that extracts the witness points leaves the loop to the one
+  // extract_no_sub call at the end (one copy of its code)
+  if (s.rank != 1) return false;
+  f3 cur = s.w[0];
   float book = nrm(cur);
-  if (book <= tol) return extract_no_sub(s, p0, p1);
-  f3 next = cur * (-1.f / book);
-  const float tol2 = tol * tol;
-  for (int it = 0; it < max_iter; ++it) {
-    ++iters;
-    f3 pa, pb;
-    sup(next, pa, pb);
-    const f3 w = pa - pb;
-    const float gap = dot(next, w - cur);
-    FCLG_GJK_TRACE(it, -1, gap, 0.f);
-    if (gap < tol) return extract_no_sub(s, p0, p1);
-    bool dup = false;
+  bool extract = book <= tol;
+  if (!extract) {
+    f3 next = cur * (-1.f / book);
+    const float tol2 = tol * tol;
+    for (int it = 0; it < max_iter; ++it) {
+      ++iters;
+      f3 pa, pb;
+      sup(next, pa, pb);
+      const f3 w = pa - pb;
+      const float gap = dot(next, w - cur);
+      FCLG_GJK_TRACE(it, -1, gap, 0.f);
+      if (gap < tol) { extract = true; break; }
+      bool dup = false;
 #pragma unroll
-    for (int j = 0; j < 4; ++j)
-      if (j < s.rank && sqn(s.w[j] - w) < tol2) dup = true;
-    if (dup) return extract_no_sub(s, p0, p1);
-    // s.rank is 1..3 here
-    if (s.rank == 1) s.set(1, pa, pb);
-    else if (s.rank == 2) s.set(2, pa, pb);
-    else s.set(3, pa, pb);
-    s.rank += 1;
-    const Upd st = update_simplex(s, cur, tol);
-    if (st == Upd::NoImprovement) return extract_no_sub(s, p0, p1);
-    if (st != Upd::OK) return false;
-    const float nd = nrm(cur);
-    FCLG_GJK_TRACE(it, s.rank, nd, book - nd);
-    if (book - nd < tol) {
-      if (!(cert_gap > 0.f) || gap <= cert_gap) return extract_no_sub(s, p0, p1);
-      if (!(book - nd > 0.f)) return false;
+      for (int j = 0; j < 4; ++j)
+        if (j < s.rank && sqn(s.w[j] - w) < tol2) dup = true;
+      if (dup) { extract = true; break; }
+      // s.rank is 1..3 here
+      if (s.rank == 1) s.set(1, pa, pb);
+      else if (s.rank == 2) s.set(2, pa, pb);
+      else s.set(3, pa, pb);
+      s.rank += 1;
+      const Upd st = update_simplex(s, cur, tol);
+      if (st == Upd::NoImprovement) { extract = true; break; }
+      if (st != Upd::OK) break;
+      const float nd = nrm(cur);
+      FCLG_GJK_TRACE(it, s.rank, nd, book - nd);
+      if (book - nd < tol) {
+        if (!(cert_gap > 0.f) || gap <= cert_gap) { extract = true; break; }
+        if (!(book - nd > 0.f)) break;
+      }
+      if (nd < tol) { extract = true; break; }
+      book = nd;
+      next = cur * (-1.f / book);
     }
-    if (nd < tol) return extract_no_sub(s, p0, p1);
-    book = nd;
-    next = cur * (-1.f / book);
   }
-  return false;
+  return extract && extract_no_sub(s, p0, p1);
 }
 
 // Outcome of the boolean phase (gjk_boolean): the run is over (o.status set),
