@@ -22,8 +22,9 @@
 
 // Counters of a query (fclg_context::epa_count): EPA work list and overflow
 // list lengths, entries taken by the two EPA launches and by the two GJK
-// launches, then the separated-pair list's length and entries taken.
-constexpr int kQueueCounters = 8;
+// launches, then the separated-pair list's and the redo list's lengths and
+// entries taken.
+constexpr int kQueueCounters = 10;
 
 struct fclg_context {
   int device = 0;
@@ -68,6 +69,7 @@ struct fclg_context {
   uint32_t* bk_order = nullptr;
   uint32_t* bk_small = nullptr;  // hist | cursor | ranges
   float4* bk_dist = nullptr;     // separated pairs between the split GJK launches (fclg::DistList)
+  uint2* bk_redo = nullptr;      // learned-start pairs rerun from the plain direction (fclg::DistList)
   size_t bk_cap = 0;
   // launch shape
   bool bucketing = true;
@@ -284,15 +286,18 @@ int ensure_bucket(fclg_context* c, size_t n) {
   if (c->bk_keys) cudaFree(c->bk_keys);
   if (c->bk_order) cudaFree(c->bk_order);
   if (c->bk_dist) cudaFree(c->bk_dist);
+  if (c->bk_redo) cudaFree(c->bk_redo);
   c->bk_keys = nullptr;
   c->bk_order = nullptr;
   c->bk_dist = nullptr;
+  c->bk_redo = nullptr;
   c->bk_cap = 0;
   c->scratch_epoch += 1;
   const size_t cap = std::max<size_t>(n, 1024);
   FCLG_CUDA(c, cudaMalloc(&c->bk_keys, cap));
   FCLG_CUDA(c, cudaMalloc(&c->bk_order, cap * sizeof(uint32_t)));
   FCLG_CUDA(c, cudaMalloc(&c->bk_dist, cap * fclg::kDistRecordBytes));
+  FCLG_CUDA(c, cudaMalloc(&c->bk_redo, cap * sizeof(uint2)));
   c->bk_cap = cap;
   return FCLG_OK;
 }
@@ -410,12 +415,13 @@ int run_query(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_
                            c->bk_small + 2 * fclg::kBucketKeys};
     FCLG_CUDA(c, fclg::launch_bucketing(b, bs, (uint32_t)c->large_hull, st));
     const int blocks = c->num_sms * c->gjk_ctas_per_sm;
-    const fclg::DistList dl{c->epa_count + 6, c->bk_dist, c->epa_count + 7};
+    const fclg::DistList dl{c->epa_count + 6, c->bk_dist, c->epa_count + 7,
+                            c->epa_count + 8, c->bk_redo, c->epa_count + 9};
     FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes, bs.order, bs.ranges, blocks, st, c->gjk_refill,
                                   c->epa_count + 4, &dl));
     FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes_large, bs.order, bs.ranges + 2, blocks, st,
                                   c->gjk_refill, c->epa_count + 5));
-    c->launches += fclg::gjk_split_applies(b, prm, c->gjk_lanes, blocks, c->gjk_refill) ? 6 : 5;
+    c->launches += 4 + fclg::gjk_split_launches(b, prm, c->gjk_lanes, blocks, c->gjk_refill);
   } else {
     FCLG_CUDA(c, fclg::launch_gjk(b, prm, q, c->gjk_lanes, nullptr, nullptr, 0, st, c->gjk_refill));
     c->launches += 1;
@@ -496,6 +502,7 @@ void fclg_destroy(fclg_context* c) {
   if (c->bk_order) cudaFree(c->bk_order);
   if (c->bk_small) cudaFree(c->bk_small);
   if (c->bk_dist) cudaFree(c->bk_dist);
+  if (c->bk_redo) cudaFree(c->bk_redo);
   if (c->mesh_io) cudaFree(c->mesh_io);
   if (c->mesh_cbuf) cudaFree(c->mesh_cbuf);
   if (c->mesh_ctr) cudaFree(c->mesh_ctr);

@@ -113,7 +113,12 @@ bool gjk_split_applies(const BatchArgs& b, const QueryParams& prm, int lanes, in
   // the one-lane plain distance pass on a persistent grid (the distance
   // launch sizes itself by a count on the device)
   return FCLG_GJK_PLAIN_VARIANT && lanes == 1 && blocks > 0 && !refill && !prm.analytic && !prm.use_mpr &&
-         !b.guess && prm.want_distance;
+         prm.want_distance;
+}
+
+int gjk_split_launches(const BatchArgs& b, const QueryParams& prm, int lanes, int blocks, bool refill) {
+  if (!gjk_split_applies(b, prm, lanes, blocks, refill)) return 1;
+  return b.guess ? 3 : 2;
 }
 
 cudaError_t launch_gjk(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q, int lanes,
@@ -121,8 +126,10 @@ cudaError_t launch_gjk(const BatchArgs& b, const QueryParams& prm, const EpaQueu
                        uint32_t* next, const DistList* dl) {
   if (b.n_pairs == 0) return cudaSuccess;
   if (dl && gjk_split_applies(b, prm, lanes, blocks, refill)) {
-    gjk_pass<1, kPassSplit><<<blocks, 128, 0, st>>>(b, prm, q, order, range, next, *dl);
+    if (b.guess) gjk_pass<1, kPassSplitWarm><<<blocks, 128, 0, st>>>(b, prm, q, order, range, next, *dl);
+    else gjk_pass<1, kPassSplit><<<blocks, 128, 0, st>>>(b, prm, q, order, range, next, *dl);
     gjk_dist_pass<1><<<blocks, 128, 0, st>>>(b, prm, q, *dl);
+    if (b.guess) gjk_redo_pass<1><<<blocks, 128, 0, st>>>(b, prm, q, *dl);
     return cudaGetLastError();
   }
   const int threads = 128;

@@ -105,8 +105,22 @@ __device__ __forceinline__ void finish_pair(const BatchArgs& b, const QueryParam
 // instruction cache; FULL compiles every path and selects by prm / b.guess.
 // Both give the same results on the queries PLAIN serves.
 // SPLIT is PLAIN's boolean phase alone: a separated pair goes to the
-// DistList for gjk_dist_pass (distance queries only).
-enum : int { kPassPlain = 0, kPassFull = 1, kPassSplit = 2 };
+// DistList for gjk_dist_pass (distance queries only).  SPLIT_WARM is the
+// boolean phase of FULL's learned-start runs (the learned direction, then the
+// plain one for a pair it does not separate), handing separated pairs over
+// the same way.
+enum : int { kPassPlain = 0, kPassFull = 1, kPassSplit = 2, kPassSplitWarm = 3 };
+// DistList record stages
+enum : int { kStagePlain = 0, kStageLearned = 1, kStagePlainCertified = 2 };
+
+__device__ __forceinline__ void push_dist(const DistList& dl, uint32_t pid, const Simplex& s, int before,
+                                          int bool_iters, int stage) {
+  const uint32_t r = aggregated_slot(dl.count);
+  float4* o = dl.rec + 3 * (size_t)r;
+  o[0] = make_float4(__uint_as_float(pid), __int_as_float(before), __int_as_float(bool_iters), __int_as_float(stage));
+  o[1] = make_float4(s.a[0].x, s.a[0].y, s.a[0].z, s.b[0].x);
+  o[2] = make_float4(s.b[0].y, s.b[0].z, 0.f, 0.f);
+}
 #ifndef FCLG_GJK_PLAIN_VARIANT
 #define FCLG_GJK_PLAIN_VARIANT 1
 #endif
@@ -198,14 +212,32 @@ __global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_pass(BatchArgs b, Quer
       o.p0 = o.p1 = mk3(0, 0, 0);
       const int k = gjk_boolean(sup, -plain, prm.gjk_tol, prm.gjk_max_iter, s, o);
       if (k == kBoolSeparated) {
-        if (g.lane == 0) {
-          const uint32_t r = aggregated_slot(dl.count);
-          dl.rec[2 * (size_t)r] = make_float4(__uint_as_float(pid), __int_as_float(o.iterations), s.a[0].x, s.a[0].y);
-          dl.rec[2 * (size_t)r + 1] = make_float4(s.a[0].z, s.b[0].x, s.b[0].y, s.b[0].z);
-        }
+        if (g.lane == 0) push_dist(dl, pid, s, 0, o.iterations, kStagePlain);
         continue;
       }
       if (k == kBoolUndetermined) o.point_valid = extract_try_sub(s, o.p0, o.p1);
+    } else if (MODE == kPassSplitWarm) {
+      // the boolean phases of FULL's runs below: the learned direction (a
+      // separation certificate within warm_probe supports), else the plain one
+      o.point_valid = false;
+      o.iterations = 0;
+      o.p0 = o.p1 = mk3(0, 0, 0);
+      const f3 guess = mk3(__ldg(b.guess + 3 * (size_t)pid), __ldg(b.guess + 3 * (size_t)pid + 1),
+                           __ldg(b.guess + 3 * (size_t)pid + 2));
+      int k = gjk_boolean(sup, -guess, prm.gjk_tol, prm.gjk_max_iter, s, o, prm.warm_probe);
+      int stage = kStageLearned, before = 0;
+      if (k != kBoolSeparated && !(o.status == kGjkIntersect && !prm.want_epa)) {
+        before = o.iterations;
+        o.iterations = 0;
+        k = gjk_boolean(sup, -plain, prm.gjk_tol, prm.gjk_max_iter, s, o);
+        stage = kStagePlainCertified;
+      }
+      if (k == kBoolSeparated) {
+        if (g.lane == 0) push_dist(dl, pid, s, before, o.iterations, stage);
+        continue;
+      }
+      if (k == kBoolUndetermined) o.point_valid = extract_try_sub(s, o.p0, o.p1);
+      o.iterations += before;
     } else if (MODE == kPassFull && b.guess) {
       // Learned direction first, for a separation certificate within
       // warm_probe supports and a distance certified to warm_gap.  A pair it
@@ -236,9 +268,13 @@ __global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_pass(BatchArgs b, Quer
 }
 
 
-// The distance loop of the separated pairs a SPLIT gjk_pass handed over
-// (gjk_distance.hpp:10-105 from the separating vertex), as a persistent grid
-// whose warps take 32 / LANES records at a time from dl.next.
+// The distance loop of the separated pairs a SPLIT or SPLIT_WARM gjk_pass
+// handed over (gjk_distance.hpp:10-105 from the separating vertex), as a
+// persistent grid whose warps take 32 / LANES records at a time from dl.next.
+// The stop per record stage, as FULL's runs: the reference's (plain run); the
+// certified one (learned start: an uncertified pair goes to the redo list);
+// the certified one, then the reference's from the same vertex (plain run of
+// a learned-start query).
 template <int LANES>
 __global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_dist_pass(BatchArgs b, QueryParams prm, EpaQueue q,
                                                         DistList dl) {
@@ -254,8 +290,9 @@ __global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_dist_pass(BatchArgs b,
   for (uint32_t round = take(); round < n; round = take()) {
     const uint32_t item = round + slot;
     if (item >= n) continue;
-    const float4 r0 = dl.rec[2 * (size_t)item], r1 = dl.rec[2 * (size_t)item + 1];
+    const float4 r0 = dl.rec[3 * (size_t)item], r1 = dl.rec[3 * (size_t)item + 1], r2 = dl.rec[3 * (size_t)item + 2];
     const uint32_t pid = __float_as_uint(r0.x);
+    const int stage = __float_as_int(r0.w);
     const PairDev pr = load_pair(b.pairs, pid);
     MinkowskiSupport<LANES> sup;
     sup.A = load_shape(b.shapes, LANES == 1 ? b.walk : nullptr, pr.a);
@@ -265,13 +302,73 @@ __global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_dist_pass(BatchArgs b,
     sup.hull = b.hull;
     sup.g = g;
     Simplex s;
-    s.set(0, mk3(r0.z, r0.w, r1.x), mk3(r1.y, r1.z, r1.w));
-    s.rank = 1;
     GjkOut o;
     o.status = kGjkSeparated;
-    o.iterations = __float_as_int(r0.y);
     o.p0 = o.p1 = mk3(0, 0, 0);
-    o.point_valid = min_distance(sup, s, prm.gjk_tol, prm.gjk_max_iter, o.p0, o.p1, o.iterations);
+    int before = __float_as_int(r0.y);
+    float cert = stage == kStagePlain ? 0.f : prm.warm_gap;
+    for (int attempt = 0;; ++attempt) {
+      s.set(0, mk3(r1.x, r1.y, r1.z), mk3(r1.w, r2.x, r2.y));
+      s.rank = 1;
+      o.iterations = __float_as_int(r0.z);
+      o.point_valid = min_distance(sup, s, prm.gjk_tol, prm.gjk_max_iter, o.p0, o.p1, o.iterations, cert);
+      if (o.point_valid || stage != kStagePlainCertified || attempt > 0) break;
+      // not certified: the same run under the reference's stop
+      before += o.iterations;
+      cert = 0.f;
+    }
+    if (stage == kStageLearned && !o.point_valid) {
+      if (g.lane == 0) {
+        const uint32_t r = aggregated_slot(dl.redo_count);
+        dl.redo[r] = make_uint2(pid, (uint32_t)o.iterations);
+      }
+      continue;
+    }
+    o.iterations += before;
+    if (g.lane != 0) continue;
+    finish_pair(b, prm, q, pid, o, s);
+  }
+}
+
+// Learned-start pairs whose distance the learned start did not certify: the
+// plain run with the certified stop, then (not certified) with the
+// reference's, as FULL runs them; iterations count every run.
+template <int LANES>
+__global__ void __launch_bounds__(128, FCLG_GJK_MINB) gjk_redo_pass(BatchArgs b, QueryParams prm, EpaQueue q,
+                                                        DistList dl) {
+  const Group<LANES> g = Group<LANES>::make();
+  constexpr uint32_t kPer = 32 / LANES;
+  const uint32_t slot = (threadIdx.x & 31u) / LANES;
+  const uint32_t n = *dl.redo_count;
+  auto take = [&]() -> uint32_t {
+    uint32_t k = 0;
+    if ((threadIdx.x & 31u) == 0) k = atomicAdd(dl.redo_next, kPer);
+    return __shfl_sync(0xFFFFFFFFu, k, 0);
+  };
+  const f3 plain = mk3(1.f, 0.f, 0.f);
+  for (uint32_t round = take(); round < n; round = take()) {
+    const uint32_t item = round + slot;
+    if (item >= n) continue;
+    const uint2 rr = dl.redo[item];
+    const uint32_t pid = rr.x;
+    const PairDev pr = load_pair(b.pairs, pid);
+    MinkowskiSupport<LANES> sup;
+    sup.A = load_shape(b.shapes, LANES == 1 ? b.walk : nullptr, pr.a);
+    sup.B = load_shape(b.shapes, LANES == 1 ? b.walk : nullptr, pr.b);
+    sup.pose = pr.pose;
+    sup.verts = b.verts;
+    sup.hull = b.hull;
+    sup.g = g;
+    Simplex s;
+    GjkOut o;
+    int done_iters = (int)rr.y;
+    for (int attempt = 0;; ++attempt) {
+      o = gjk_evaluate(sup, -plain, prm.gjk_tol, prm.gjk_max_iter, prm.want_distance != 0, s, 0,
+                       attempt == 0 ? prm.warm_gap : 0.f);
+      if (attempt > 0 || !uncertified(o, prm)) break;
+      done_iters += o.iterations;
+    }
+    o.iterations += done_iters;
     if (g.lane != 0) continue;
     finish_pair(b, prm, q, pid, o, s);
   }

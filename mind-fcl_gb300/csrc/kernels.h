@@ -35,14 +35,21 @@ struct EpaQueue {
 constexpr size_t kEpaRecordBytes = 7 * sizeof(float4);
 
 // Separated pairs handed from the boolean GJK pass to the distance pass (the
-// split one-lane launch, launch_gjk): each record is the pair and the
-// separating vertex the distance loop starts from.
+// split one-lane launch, launch_gjk): each record is the pair, the separating
+// vertex the distance loop starts from and the run it belongs to.  With a
+// learned start, pairs whose distance from it is not certified go on to the
+// redo list, which a third launch reruns from the plain direction.
 struct DistList {
-  uint32_t* count;  // [1] records written; zero before the boolean pass
-  float4* rec;      // [capacity][2]: {pid, iterations so far, pa.x, pa.y}, {pa.z, pb.x, pb.y, pb.z}
-  uint32_t* next;   // [1] records taken by the distance pass; zero before it
+  uint32_t* count;       // [1] records written; zero before the boolean pass
+  float4* rec;           // [capacity][3]: {pid, iterations of earlier runs, boolean iterations, stage},
+                         // {pa.xyz, pb.x}, {pb.y, pb.z, 0, 0}; stage 0: plain run (the reference's stop),
+                         // 1: learned start, 2: plain run with the certified stop
+  uint32_t* next;        // [1] records taken by the distance pass; zero before it
+  uint32_t* redo_count;  // [1] redo records written; zero before the boolean pass
+  uint2* redo;           // [capacity] {pid, iterations of the learned-start run}
+  uint32_t* redo_next;   // [1] redo records taken; zero before the redo pass
 };
-constexpr size_t kDistRecordBytes = 2 * sizeof(float4);
+constexpr size_t kDistRecordBytes = 3 * sizeof(float4);
 // Bytes of one small-layout polytope state handed to the large layout (epa.cuh EpaResume).
 constexpr size_t kEpaResumeBytes = 6688;
 
@@ -77,8 +84,11 @@ cudaError_t launch_bucketing(const BatchArgs& b, const BucketScratch& s, uint32_
 cudaError_t launch_gjk(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q, int lanes,
                        const uint32_t* order, const uint32_t* range, int blocks, cudaStream_t st,
                        bool refill = false, uint32_t* next = nullptr, const DistList* dl = nullptr);
-// Whether launch_gjk with these arguments and a DistList runs the split pair of launches.
+// Whether launch_gjk with these arguments and a DistList runs the split launches
+// (boolean, distance, and with a learned start the redo launch), and how many
+// kernels that launch_gjk call then launches.
 bool gjk_split_applies(const BatchArgs& b, const QueryParams& prm, int lanes, int blocks, bool refill);
+int gjk_split_launches(const BatchArgs& b, const QueryParams& prm, int lanes, int blocks, bool refill);
 // fcl::collide with directed penetration along b.guess (directed_pass.cu).
 cudaError_t launch_directed(const BatchArgs& b, const QueryParams& prm, int blocks, cudaStream_t st);
 // GJKSolver<double>::shapeDistance per pair in FP64, one thread per pair, as a

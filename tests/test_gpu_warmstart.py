@@ -169,14 +169,19 @@ def test_trained_model_cuts_iterations_and_keeps_answers(torch):
         it_p = plain["iterations"][sep].astype(np.float64).mean()
         it_w = warm["iterations"][sep].astype(np.float64).mean()
         assert it_w <= 0.75 * it_p, (it_p, it_w)
-        # the refilling GJK pass takes the same warm starts and answers bit for bit as the group pass
+        # the refilling GJK pass and the one-pass kernel (bucketing off) take the
+        # same warm starts and answer bit for bit as the split launches
+        # (bucketed: boolean, distance and redo launches)
         keep_t = ctx.get_tuning()
-        ctx.set_tuning(gjk_lanes_small=1, gjk_lanes_large=1, gjk_refill=False)
+        ctx.set_tuning(bucketing=True, gjk_lanes_small=1, gjk_lanes_large=1, gjk_refill=False)
         w_group = _query(torch, ctx, d_te, test.n_pairs, WARM)
         ctx.set_tuning(gjk_refill=True)
         w_refill = _query(torch, ctx, d_te, test.n_pairs, WARM)
+        ctx.set_tuning(bucketing=False, gjk_refill=False)
+        w_one = _query(torch, ctx, d_te, test.n_pairs, WARM)
         ctx.set_tuning(**keep_t)
         assert np.array_equal(w_group.view(np.uint8), w_refill.view(np.uint8))
+        assert np.array_equal(w_group.view(np.uint8), w_one.view(np.uint8))
         ctx.set_warmstart(None)
         ws.close()
     finally:
