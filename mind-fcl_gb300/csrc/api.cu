@@ -94,6 +94,7 @@ struct fclg_context {
   size_t mesh_cbuf_bytes = 0;
   // mesh-mesh traffic counters while profiling: node pairs and triangle pairs tested
   unsigned long long* mesh_ctr = nullptr;
+  uint32_t* mesh_take = nullptr;  // poses / queries taken by a mesh launch's warps
   // learned warm start: the model and its per-pair directions
   fclg_warmstart* ws = nullptr;
   float* guess = nullptr;
@@ -506,6 +507,7 @@ void fclg_destroy(fclg_context* c) {
   if (c->mesh_io) cudaFree(c->mesh_io);
   if (c->mesh_cbuf) cudaFree(c->mesh_cbuf);
   if (c->mesh_ctr) cudaFree(c->mesh_ctr);
+  if (c->mesh_take) cudaFree(c->mesh_take);
   if (c->guess) cudaFree(c->guess);
   if (c->bp_scratch) cudaFree(c->bp_scratch);
   if (c->bp_io) cudaFree(c->bp_io);
@@ -800,11 +802,14 @@ int fclg_mesh_collide_device(fclg_context* c, const fclg_mesh* a, const fclg_mes
   m.counts = d_counts;
   m.pairs = d_pairs;
   m.status = d_status;
-  int blocks = c->num_sms * 8;
+  // a persistent grid whose warps take poses from a counter
+  const int blocks = fclg::mesh_collide_resident_blocks(c->num_sms);
+  if (!c->mesh_take) FCLG_CUDA(c, cudaMalloc(&c->mesh_take, sizeof(uint32_t)));
+  FCLG_CUDA(c, cudaMemsetAsync(c->mesh_take, 0, sizeof(uint32_t), static_cast<cudaStream_t>(stream)));
+  m.next = c->mesh_take;
   const int cbuf_len = fclg::mesh_contact_buffer_len(max_contacts);
   if (cbuf_len > 0) {
-    // contact buffers in device memory, one per warp of a grid that fits at once
-    blocks = fclg::mesh_collide_resident_blocks(c->num_sms);
+    // contact buffers in device memory, one per warp of the grid
     const size_t need = (size_t)fclg::mesh_collide_warps(blocks) * cbuf_len * (8 + 8);
     if (need > ((size_t)8 << 30))
       return fail(c, FCLG_E_TOO_LARGE, "max_contacts too large for the ordered contact buffers (8 GiB)");
@@ -913,11 +918,14 @@ static int run_mesh_shape(fclg_context* c, const fclg_mesh* mesh, const uint32_t
   m.tri_ids = d_tri_ids;
   m.status = d_status;
   m.contacts = d_contacts;
-  int blocks = c->num_sms * 8;
+  // a persistent grid whose warps take queries from a counter
+  const int blocks = fclg::mesh_shape_resident_blocks(c->num_sms, d_contacts != nullptr);
+  if (!c->mesh_take) FCLG_CUDA(c, cudaMalloc(&c->mesh_take, sizeof(uint32_t)));
+  FCLG_CUDA(c, cudaMemsetAsync(c->mesh_take, 0, sizeof(uint32_t), static_cast<cudaStream_t>(stream)));
+  m.next = c->mesh_take;
   const int cbuf_len = fclg::mesh_contact_buffer_len(max_contacts);
   if (cbuf_len > 0) {
-    // contact buffers in device memory, one per warp of a grid that fits at once
-    blocks = fclg::mesh_shape_resident_blocks(c->num_sms, d_contacts != nullptr);
+    // contact buffers in device memory, one per warp of the grid
     const size_t n_entries = (size_t)fclg::mesh_shape_warps(blocks) * cbuf_len;
     if (n_entries * 16 > ((size_t)8 << 30))
       return fail(c, FCLG_E_TOO_LARGE, "max_contacts too large for the ordered contact buffers (8 GiB)");

@@ -30,6 +30,10 @@ struct MeshArgs {
   // optional traffic counters (profiling): [0] node pairs whose boxes were
   // tested, [1] triangle pairs tested
   unsigned long long* counters = nullptr;
+  // optional, zero before the launch: poses taken so far; each warp takes its
+  // next pose there as it finishes one (a persistent grid), else warp w takes
+  // poses w, w + W, ...
+  uint32_t* next = nullptr;
 };
 
 cudaError_t launch_mesh_collide(const MeshArgs& m, int blocks, cudaStream_t st);
@@ -68,6 +72,8 @@ struct MeshShapeArgs {
   unsigned long long* cbuf_key = nullptr;
   int2* cbuf_val = nullptr;
   uint32_t cbuf_len = 0;
+  // optional, zero before the launch: queries taken so far (as MeshArgs::next)
+  uint32_t* next = nullptr;
 };
 
 cudaError_t launch_mesh_shape(const MeshShapeArgs& m, int blocks, cudaStream_t st);

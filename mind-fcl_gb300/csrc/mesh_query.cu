@@ -165,7 +165,15 @@ __global__ void __launch_bounds__(kMeshWarps * 32) mesh_collide_kernel(MeshArgs 
     ckey = m.cbuf_key + (size_t)gw * m.cbuf_len;
     cpair = m.cbuf_pair + (size_t)gw * m.cbuf_len;
   }
-  for (uint32_t pose_i = gw; pose_i < m.n_poses; pose_i += nw) {
+  // poses differ in traversal work by orders of magnitude: with m.next each
+  // warp takes its next pose as it finishes one
+  auto take = [&](uint32_t done) -> uint32_t {
+    if (!m.next) return done + nw;
+    uint32_t k = 0;
+    if (lane == 0) k = atomicAdd(m.next, 1u);
+    return __shfl_sync(0xFFFFFFFFu, k, 0);
+  };
+  for (uint32_t pose_i = m.next ? take(0) : gw; pose_i < m.n_poses; pose_i = take(pose_i)) {
     Pose P;
     {
       const float4 q0 = __ldg(m.poses + 3 * (size_t)pose_i);

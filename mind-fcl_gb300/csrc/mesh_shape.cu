@@ -260,7 +260,14 @@ __global__ void __launch_bounds__(kMsWarps * 32, FCLG_MESH_SHAPE_MINB) mesh_shap
     ckey = m.cbuf_key + (size_t)gw * m.cbuf_len;
     cval = m.cbuf_val + (size_t)gw * m.cbuf_len;
   }
-  for (uint32_t q = gw; q < m.n; q += nw) {
+  // with m.next each warp takes its next query as it finishes one
+  auto take = [&](uint32_t done) -> uint32_t {
+    if (!m.next) return done + nw;
+    uint32_t k = 0;
+    if (lane == 0) k = atomicAdd(m.next, 1u);
+    return __shfl_sync(0xFFFFFFFFu, k, 0);
+  };
+  for (uint32_t q = m.next ? take(0) : gw; q < m.n; q = take(q)) {
     Pose X;  // the shape in the mesh frame
     {
       const float4 q0 = __ldg(m.poses + 3 * (size_t)q);
