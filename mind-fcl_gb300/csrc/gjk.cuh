@@ -111,19 +111,59 @@ __device__ __forceinline__ Proj project3(Simplex& s, f3& d, float tol) {
   return Proj::Continue;
 }
 
-// gjk.hpp:280-360; orientation tests in FP64.
+// Triple product u . (v x w) in FP32 with a bound on its error: the inputs are
+// differences of FP32 points rounded once (or exact), so the computed value is
+// within 8 eps of |u| . (|v| x+ |w|) of the exact one (eps = 2^-24; the bound
+// below keeps a factor of four in hand).  certain: the sign is the exact one.
+__device__ __forceinline__ float triple_filtered(f3 u, f3 v, f3 w, bool& certain) {
+  const float t = dot(u, cross(v, w));
+  const f3 au = mk3(fabsf(u.x), fabsf(u.y), fabsf(u.z));
+  const f3 av = mk3(fabsf(v.x), fabsf(v.y), fabsf(v.z));
+  const f3 aw = mk3(fabsf(w.x), fabsf(w.y), fabsf(w.z));
+  const float mag = au.x * (av.y * aw.z + av.z * aw.y) + au.y * (av.z * aw.x + av.x * aw.z) +
+                    au.z * (av.x * aw.y + av.y * aw.x);
+  // 32 * 2^-24; below 1e-30 the products may be subnormal: no certainty
+  certain = certain && mag > 1e-30f && fabsf(t) > 1.9073486e-06f * mag;
+  return t;
+}
+
+// gjk.hpp:280-360.  The orientation tests decide the branch by their signs
+// alone: they run in FP32 with an error bound (triple_filtered) and again in
+// FP64 only when a sign is within the bound (near-degenerate tetrahedra), so
+// the decisions are the FP64 tests' everywhere.
 __device__ FCLG_GJK_COLD Proj project4(Simplex& s, f3& dir, float tol) {
-  const d3 a = tod(s.w[3]), b = tod(s.w[2]), c = tod(s.w[1]), dd = tod(s.w[0]);
-  const d3 ab = b - a, ac = c - a, ad = dd - a;
-  d3 abc = cross(ab, ac), acd = cross(ac, ad), abd = cross(ab, ad);
-  const double abc_ad = dot(abc, ad), acd_ab = dot(acd, ab), abd_ac = dot(abd, ac);
-  if (fabs(abc_ad) <= 0.0) return Proj::ZeroVolume;
-  if (abc_ad > 0) abc = abc * -1.0;
-  if (acd_ab > 0) acd = acd * -1.0;
-  if (abd_ac > 0) abd = abd * -1.0;
-  const bool d_side = dot(a, abc) > 0;
-  const bool c_side = dot(a, abd) > 0;
-  const bool b_side = dot(a, acd) > 0;
+  bool zero_volume, d_side, c_side, b_side;
+  {
+    const f3 a = s.w[3], b = s.w[2], c = s.w[1], dd = s.w[0];
+    const f3 ab = b - a, ac = c - a, ad = dd - a;
+    bool certain = true;
+    // abc . ad = ad . (ab x ac), acd . ab = ab . (ac x ad), abd . ac = ac . (ab x ad)
+    const float abc_ad = triple_filtered(ad, ab, ac, certain);
+    const float acd_ab = triple_filtered(ab, ac, ad, certain);
+    const float abd_ac = triple_filtered(ac, ab, ad, certain);
+    // the side tests a . n with each normal turned away from the fourth vertex
+    const float sd = triple_filtered(a, ab, ac, certain);
+    const float sc = triple_filtered(a, ab, ad, certain);
+    const float sb = triple_filtered(a, ac, ad, certain);
+    zero_volume = false;
+    d_side = abc_ad > 0.f ? sd < 0.f : sd > 0.f;
+    c_side = abd_ac > 0.f ? sc < 0.f : sc > 0.f;
+    b_side = acd_ab > 0.f ? sb < 0.f : sb > 0.f;
+    if (!certain) {
+      const d3 a = tod(s.w[3]), b = tod(s.w[2]), c = tod(s.w[1]), dd = tod(s.w[0]);
+      const d3 ab = b - a, ac = c - a, ad = dd - a;
+      d3 abc = cross(ab, ac), acd = cross(ac, ad), abd = cross(ab, ad);
+      const double abc_ad = dot(abc, ad), acd_ab = dot(acd, ab), abd_ac = dot(abd, ac);
+      zero_volume = fabs(abc_ad) <= 0.0;
+      if (abc_ad > 0) abc = abc * -1.0;
+      if (acd_ab > 0) acd = acd * -1.0;
+      if (abd_ac > 0) abd = abd * -1.0;
+      d_side = dot(a, abc) > 0;
+      c_side = dot(a, abd) > 0;
+      b_side = dot(a, acd) > 0;
+    }
+  }
+  if (zero_volume) return Proj::ZeroVolume;
   if (d_side && c_side && b_side) return Proj::Intersect;
   if (!b_side) {
     s.copy(2, 3);
