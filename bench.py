@@ -176,8 +176,9 @@ CONVEX_WORKLOADS = {
 }
 MLP_FLOP_PER_PAIR = 2.0 * (28 * 256 + 2 * 256 * 256 + 256 * 3)
 # DRAM bytes (read + write) of the two EPA launches of one mixed-workload query
-# at 10^6 pairs, from one ncu capture (profiles/epa_pass_mixed_1M.md)
-EPA_TRAFFIC_MIXED_1M = (367.640320 + 40.247040 + 15.708416 + 0.013824) * 1e6
+# at 10^6 pairs: one ncu capture at 400 k pairs (profiles/epa_pass_mixed_400k.md),
+# scaled by the pairs (the traffic is per overlapping pair)
+EPA_TRAFFIC_MIXED_1M = (144.232960 + 72.651776 + 59.215616 + 0.439808) * 1e6 * (1_000_000 / 400_000)
 
 
 def _to_dev(torch, arr, dev):
@@ -1135,7 +1136,8 @@ def main():
                          "traffic": (EPA_TRAFFIC_MIXED_1M if args.workload == "mixed" and n == 1_000_000
                                      and dominant == "epa_pass" else None),
                          "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of both EPA "
-                                           "launches, profiles/epa_pass_mixed_1M.md",
+                                           "launches at 400 k pairs scaled by the pairs to 10^6, "
+                                           "profiles/epa_pass_mixed_400k.md",
                          "kernel": dominant + " (all launches of the pass)",
                          "peak_source": peak_kind,
                          "algorithmic_bytes": "%d B/query x %d queries per launch" % (algo_bytes, n)},
