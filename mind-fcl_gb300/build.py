@@ -65,7 +65,7 @@ def build(force=False, verbose_ptxas=False, jobs=None):
     todo = [s for s in srcs if force or verbose_ptxas or _stale(_obj(s), [s] + hdrs)]
     logs = {}
     if todo:
-        with concurrent.futures.ThreadPoolExecutor(max_workers=jobs or min(8, len(todo))) as ex:
+        with concurrent.futures.ThreadPoolExecutor(max_workers=jobs or min(os.cpu_count() or 8, len(todo))) as ex:
             for s, log in zip(todo, ex.map(lambda s: compile_one(s, verbose_ptxas), todo)):
                 logs[s] = log
     objs = [_obj(s) for s in srcs]
