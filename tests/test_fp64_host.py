@@ -76,3 +76,23 @@ def test_host_build_is_the_oracle_on_plain(g64, oracle_lib):
     sep = (rs == GJK_SEPARATED) & (ref["ok"] == 1)
     assert sep.mean() > 0.3
     assert np.array_equal(got["distance"][sep], ref["distance"][sep])
+
+
+def test_host_build_invalid_and_limits(g64):
+    """A pair whose shape index is out of range gets GJK_Failed, ok = 0 and
+    distance -1; an iteration limit of 1 leaves pairs undecided or decided
+    without a certified distance, never with a wrong flag."""
+    batch = workloads.plain_small(256)
+    bad = batch.pairs.copy()
+    bad["shape_b"][::7] = len(batch.shapes) + 5
+    b2 = workloads.Batch("bad", batch.shapes, batch.vertices, bad)
+    got = g64(b2)
+    sel = np.arange(len(bad)) % 7 == 0
+    assert np.all(got["status"][sel] == 4) and np.all(got["ok"][sel] == 0)
+    assert np.all(got["distance"][sel] == -1.0)
+    full = g64(batch)
+    short = g64(batch, 1e-6, 1)
+    sep_short = (short["status"] == GJK_SEPARATED) & (short["ok"] == 1)
+    # a separation certificate found within one iteration is a true separation
+    assert np.all(full["status"][sep_short] == GJK_SEPARATED)
+    assert np.all(short["distance"][sep_short] >= full["distance"][sep_short] - 1e-9)

@@ -82,3 +82,19 @@ def test_distance64_matches_oracle_full_plain(gpu_ctx, oracle_lib):
     assert sep.mean() > 0.3
     assert np.abs(got["distance"][sep] - ref["distance"][sep]).max() <= TOL
     assert np.array_equal(got["status"] & 0xFF, rs)
+
+
+def test_distance64_invalid_indices_and_empty(gpu_ctx):
+    """Out-of-range shape indices give GJK_Failed, ok = 0, distance -1 (no
+    fault); an empty batch is a no-op."""
+    batch = workloads.plain_small(512)
+    bad = batch.pairs.copy()
+    bad["shape_a"][::5] = len(batch.shapes) + 3
+    gpu_ctx.set_batch(batch)
+    got = gpu_ctx.distance64(bad)
+    sel = np.arange(len(bad)) % 5 == 0
+    assert np.all((got["status"][sel] & 0xFF) == 4) and np.all(got["ok"][sel] == 0)
+    assert np.all(got["distance"][sel] == -1.0)
+    ref = gpu_ctx.distance64(batch.pairs)
+    assert np.array_equal(got[~sel].view(np.uint8), ref[~sel].view(np.uint8))
+    assert len(gpu_ctx.distance64(batch.pairs[:0])) == 0
