@@ -94,7 +94,8 @@ struct fclg_context {
   size_t mesh_cbuf_bytes = 0;
   // mesh-mesh traffic counters while profiling: node pairs and triangle pairs tested
   unsigned long long* mesh_ctr = nullptr;
-  uint32_t* mesh_take = nullptr;  // poses / queries taken by a mesh launch's warps
+  uint32_t* mesh_take = nullptr;  // work taken by a persistent launch's warps (mesh, mesh-shape, CCD)
+  uint32_t* contact_take = nullptr;  // contact slots taken by the mesh-shape contact launch's warps
   // learned warm start: the model and its per-pair directions
   fclg_warmstart* ws = nullptr;
   float* guess = nullptr;
@@ -508,6 +509,7 @@ void fclg_destroy(fclg_context* c) {
   if (c->mesh_cbuf) cudaFree(c->mesh_cbuf);
   if (c->mesh_ctr) cudaFree(c->mesh_ctr);
   if (c->mesh_take) cudaFree(c->mesh_take);
+  if (c->contact_take) cudaFree(c->contact_take);
   if (c->guess) cudaFree(c->guess);
   if (c->bp_scratch) cudaFree(c->bp_scratch);
   if (c->bp_io) cudaFree(c->bp_io);
@@ -944,6 +946,9 @@ static int run_mesh_shape(fclg_context* c, const fclg_mesh* mesh, const uint32_t
   FCLG_CUDA(c, fclg::launch_mesh_shape(m, blocks, static_cast<cudaStream_t>(stream)));
   c->launches += 1;
   if (d_contacts) {
+    if (!c->contact_take) FCLG_CUDA(c, cudaMalloc(&c->contact_take, sizeof(uint32_t)));
+    FCLG_CUDA(c, cudaMemsetAsync(c->contact_take, 0, sizeof(uint32_t), static_cast<cudaStream_t>(stream)));
+    m.contact_next = c->contact_take;
     FCLG_CUDA(c, fclg::launch_mesh_contacts(m, c->num_sms, static_cast<cudaStream_t>(stream)));
     c->launches += 1;
   }
@@ -1603,8 +1608,10 @@ int run_ccd(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_di
     c->launches += 3;
     order = bs.order;
   }
+  if (!c->mesh_take) FCLG_CUDA(c, cudaMalloc(&c->mesh_take, sizeof(uint32_t)));
+  FCLG_CUDA(c, cudaMemsetAsync(c->mesh_take, 0, sizeof(uint32_t), st));
   FCLG_CUDA(c, fclg::launch_ccd(b, reinterpret_cast<const float4*>(d_disp), c->hull_aabb, prm, order,
-                                reinterpret_cast<float4*>(d_results), c->num_sms, st));
+                                reinterpret_cast<float4*>(d_results), c->num_sms, st, c->mesh_take));
   c->launches += 1;
   return FCLG_OK;
 }

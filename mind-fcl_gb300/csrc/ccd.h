@@ -27,8 +27,10 @@ cudaError_t launch_hull_aabbs(const int4* shapes, const float4* verts, uint32_t 
                               cudaStream_t st);
 // One pass over b's pairs: disp[i] = (unit axis in a's frame, distance),
 // aabb = the hull boxes (read by the approximate request), order = the pairs
-// in shape-class order (or null: index order), out[i] = fclg_ccd_result.
+// in shape-class order (or null: index order), out[i] = fclg_ccd_result;
+// next (optional, zero before the launch): the counter the persistent grid's
+// warps take their pairs from.
 cudaError_t launch_ccd(const BatchArgs& b, const float4* disp, const float4* aabb, const CcdParams& prm,
-                       const uint32_t* order, float4* out, int num_sms, cudaStream_t st);
+                       const uint32_t* order, float4* out, int num_sms, cudaStream_t st, uint32_t* next = nullptr);
 
 }  // namespace fclg

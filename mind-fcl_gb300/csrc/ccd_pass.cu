@@ -239,9 +239,23 @@ __device__ float toc_sample(const MprPortal& P, f3 sweep) {
 
 __global__ void __launch_bounds__(128, FCLG_CCD_MINB) ccd_pass(BatchArgs b, const float4* __restrict__ disp,
                                                    const float4* __restrict__ aabb, CcdParams prm,
-                                                   const uint32_t* __restrict__ order, float4* __restrict__ out) {
-  const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < b.n_pairs; k += stride) {
+                                                   const uint32_t* __restrict__ order, float4* __restrict__ out,
+                                                   uint32_t* next) {
+  // a warp runs 32 pairs at a time; with a counter (next, zero before the
+  // launch) it takes its next 32 there as it finishes, so the persistent
+  // grid's warps end together
+  const unsigned lane = threadIdx.x & 31u;
+  const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
+  auto take = [&](uint32_t done) -> uint32_t {
+    if (!next) return done + n_warps * 32u;
+    uint32_t r = 0;
+    if (lane == 0) r = atomicAdd(next, 32u);
+    return __shfl_sync(0xFFFFFFFFu, r, 0);
+  };
+  const uint32_t first = next ? take(0) : ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32u;
+  for (uint32_t round = first; round < b.n_pairs; round = take(round)) {
+    const uint32_t k = round + lane;
+    if (k >= b.n_pairs) continue;
     const uint32_t pid = order ? __ldg(order + k) : k;
     const PairDev pr = load_pair(b.pairs, pid);
     uint32_t st = kCcdNoMpr;
@@ -327,10 +341,10 @@ cudaError_t launch_hull_aabbs(const int4* shapes, const float4* verts, uint32_t 
 }
 
 cudaError_t launch_ccd(const BatchArgs& b, const float4* disp, const float4* aabb, const CcdParams& prm,
-                       const uint32_t* order, float4* out, int num_sms, cudaStream_t st) {
+                       const uint32_t* order, float4* out, int num_sms, cudaStream_t st, uint32_t* next) {
   if (b.n_pairs == 0) return cudaSuccess;
   // persistent: FCLG_CCD_MINB CTAs on every SM
-  ccd_pass<<<num_sms * FCLG_CCD_MINB, 128, 0, st>>>(b, disp, aabb, prm, order, out);
+  ccd_pass<<<num_sms * FCLG_CCD_MINB, 128, 0, st>>>(b, disp, aabb, prm, order, out, next);
   return cudaGetLastError();
 }
 

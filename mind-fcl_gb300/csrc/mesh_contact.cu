@@ -132,7 +132,18 @@ __global__ void __launch_bounds__(kMcWarps * 32) mesh_contact_kernel(MeshShapeAr
   const unsigned lane = threadIdx.x & 31u;
   const uint64_t total = (uint64_t)m.n * m.max_contacts;
   const uint64_t nw = (uint64_t)gridDim.x * kMcWarps;
-  for (uint64_t item = (uint64_t)blockIdx.x * kMcWarps + (threadIdx.x >> 5); item < total; item += nw) {
+  // contacts differ in EPA work: with m.contact_next a warp takes its next
+  // kMcTake slots as it finishes (empty slots cost a count check each)
+  constexpr uint32_t kMcTake = 4;
+  auto take = [&](uint64_t done) -> uint64_t {
+    if (!m.contact_next) return done + nw;
+    if ((done + 1) % kMcTake != 0) return done + 1;
+    uint32_t k = 0;
+    if (lane == 0) k = atomicAdd(m.contact_next, kMcTake);
+    return (uint64_t)__shfl_sync(0xFFFFFFFFu, k, 0);
+  };
+  const uint64_t first = m.contact_next ? take(kMcTake - 1) : (uint64_t)blockIdx.x * kMcWarps + (threadIdx.x >> 5);
+  for (uint64_t item = first; item < total; item = take(item)) {
     const uint32_t q = (uint32_t)(item / m.max_contacts), slot = (uint32_t)(item % m.max_contacts);
     if (slot >= __ldg(m.counts + q)) continue;  // warp-uniform
     float* out = m.contacts + 8 * item;

@@ -74,6 +74,9 @@ struct MeshShapeArgs {
   uint32_t cbuf_len = 0;
   // optional, zero before the launch: queries taken so far (as MeshArgs::next)
   uint32_t* next = nullptr;
+  // optional, zero before the contact launch: contact slots taken so far by
+  // its warps (launch_mesh_contacts)
+  uint32_t* contact_next = nullptr;
 };
 
 cudaError_t launch_mesh_shape(const MeshShapeArgs& m, int blocks, cudaStream_t st);
