@@ -384,13 +384,14 @@ struct EpaWarp {
       const float k = P.fkey[s];
       if (k < bk) { bk = k; bs = s; }
     }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      const float ok = __shfl_xor_sync(0xFFFFFFFFu, bk, off);
-      const int os = __shfl_xor_sync(0xFFFFFFFFu, bs, off);
-      if (ok < bk || (ok == bk && os < bs)) { bk = ok; bs = os; }
-    }
-    best_slot = __shfl_sync(0xFFFFFFFFu, bs, 0);
+    // warp minimum of the key by two reductions: the smallest key (an
+    // order-preserving map to unsigned, -0 taken as +0), then the lowest slot
+    // holding it
+    bk += 0.f;
+    const uint32_t kb = __float_as_uint(bk);
+    const uint32_t u = (kb & 0x80000000u) ? ~kb : (kb | 0x80000000u);
+    const uint32_t umin = __reduce_min_sync(0xFFFFFFFFu, u);
+    best_slot = (int)__reduce_min_sync(0xFFFFFFFFu, u == umin ? (uint32_t)bs : 0xFFFFFFFFu);
     best_d = (best_slot != 0x7FFFFFFF) ? P.fn[best_slot].w : INFINITY;
   }
 
