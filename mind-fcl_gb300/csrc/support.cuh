@@ -50,7 +50,16 @@ __device__ __forceinline__ f3 convex_support(const float4* __restrict__ v, uint3
       bi = i;
     }
   }
-  if (LANES > 1) {
+  if constexpr (LANES == 32) {
+    // warp argmax by two reductions: the largest value (an order-preserving
+    // map to unsigned; -0 taken as +0, NaN below everything), then the
+    // lowest index holding it
+    best += 0.f;
+    const uint32_t vb = __float_as_uint(best);
+    const uint32_t u = (best != best) ? 0u : ((vb & 0x80000000u) ? ~vb : (vb | 0x80000000u));
+    const uint32_t umax = __reduce_max_sync(0xFFFFFFFFu, u);
+    bi = __reduce_min_sync(0xFFFFFFFFu, u == umax ? bi : 0xFFFFFFFFu);
+  } else if (LANES > 1) {
 #pragma unroll
     for (int off = LANES / 2; off > 0; off >>= 1) {
       const float ov = __shfl_xor_sync(g.mask, best, off);
