@@ -401,13 +401,10 @@ __global__ void __launch_bounds__(kMsWarps * 32, FCLG_MESH_SHAPE_MINB) mesh_shap
         // Children go back above the entries that follow their parent (lane j's
         // below those of lanes < j), the second child on top: the reference
         // pushes the first child, then the second, and pops the second first.
-        int incl = push;
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-          const int t = __shfl_down_sync(0xFFFFFFFFu, incl, off);
-          if ((int)lane + off < 32) incl += t;
-        }
-        const int total = __shfl_sync(0xFFFFFFFFu, incl, 0);
+        // (every push is two entries: the suffix sum is twice a population count)
+        const unsigned pm = __ballot_sync(0xFFFFFFFFu, push != 0);
+        const int incl = 2 * __popc(pm >> lane);
+        const int total = 2 * __popc(pm);
         if (push) {
           const int o = size + incl - push;
           S.node[o + 1] = child + 1;
