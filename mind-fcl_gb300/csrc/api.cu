@@ -77,7 +77,7 @@ struct fclg_context {
   int gjk_lanes_large = 4;
   int large_hull = 128;
   int gjk_ctas_per_sm = 4;
-  int epa_ctas_per_sm = 6;
+  int epa_ctas_per_sm = fclg::epa_default_ctas_per_sm();
   uint64_t launches = 0;
   // optional per-pass timing
   bool profiling = false;

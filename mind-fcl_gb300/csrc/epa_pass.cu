@@ -6,16 +6,22 @@
 namespace fclg {
 
 // Small layout: 128 faces / 72 vertices (~8.4 KB of shared memory per warp,
-// six 4-warp CTAs per SM; a polytope of 128 faces has about 66 vertices);
+// five 5-warp CTAs per SM: 25 warps, one more than six 4-warp CTAs, at 72
+// registers -- an SM sub-partition then holds seven warps; a polytope of 128
+// faces has about 66 vertices);
 // large layout: the reference's 256 faces (~18 KB per warp, three 4-warp CTAs
 // per SM).
 #ifndef FCLG_EPA_SMALL_V
 #define FCLG_EPA_SMALL_V 72
 #endif
 #ifndef FCLG_EPA_SMALL_MINB
-#define FCLG_EPA_SMALL_MINB 6
+#define FCLG_EPA_SMALL_MINB 5
 #endif
-constexpr int kSmallF = 128, kSmallV = FCLG_EPA_SMALL_V, kSmallWarps = 4, kSmallMinB = FCLG_EPA_SMALL_MINB;
+#ifndef FCLG_EPA_SMALL_WARPS
+#define FCLG_EPA_SMALL_WARPS 5
+#endif
+constexpr int kSmallF = 128, kSmallV = FCLG_EPA_SMALL_V, kSmallWarps = FCLG_EPA_SMALL_WARPS,
+              kSmallMinB = FCLG_EPA_SMALL_MINB;
 #ifndef FCLG_EPA_LARGE_MINB
 #define FCLG_EPA_LARGE_MINB 3
 #endif
@@ -142,5 +148,7 @@ cudaError_t launch_epa(const BatchArgs& b, const QueryParams& prm, const EpaQueu
 }
 
 int epa_max_faces_supported() { return kLargeF; }
+
+int epa_default_ctas_per_sm() { return kSmallMinB; }
 
 }  // namespace fclg

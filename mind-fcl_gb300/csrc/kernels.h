@@ -103,5 +103,7 @@ cudaError_t launch_epa(const BatchArgs& b, const QueryParams& prm, const EpaQueu
 size_t epa_smem_bytes();
 size_t epa_smem_bytes_large();
 int epa_max_faces_supported();
+// CTAs per SM the small-layout EPA kernel is compiled for (the default launch).
+int epa_default_ctas_per_sm();
 
 }  // namespace fclg
