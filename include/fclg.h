@@ -373,7 +373,7 @@ typedef struct fclg_tuning {
   int32_t gjk_lanes_large;
   int32_t large_hull_vertices;
   int32_t gjk_ctas_per_sm;
-  int32_t epa_ctas_per_sm;      /* small-layout EPA CTAs per SM (five 5-warp CTAs by default) */
+  int32_t epa_ctas_per_sm;      /* small-layout EPA CTAs per SM (two 13-warp CTAs by default) */
   int32_t support_walk;         /* 1 on, -1 off, 0 unchanged */
   int32_t gjk_refill;           /* 1 on, -1 off, 0 unchanged */
   int32_t epa_resume;           /* 1 on (default), -1 off, 0 unchanged: a pair whose EPA polytope

@@ -6,19 +6,20 @@
 namespace fclg {
 
 // Small layout: 128 faces / 72 vertices (~8.4 KB of shared memory per warp,
-// five 5-warp CTAs per SM: 25 warps, one more than six 4-warp CTAs, at 72
-// registers -- an SM sub-partition then holds seven warps; a polytope of 128
-// faces has about 66 vertices);
+// two 13-warp CTAs per SM: 26 warps, the most the SM's shared memory holds,
+// at 72 registers -- an SM sub-partition then holds seven warps; measured
+// against six 4-warp and five 5-warp CTAs: 9.26 / 9.03 / 8.97 ms on 10^6
+// mixed pairs; a polytope of 128 faces has about 66 vertices);
 // large layout: the reference's 256 faces (~18 KB per warp, three 4-warp CTAs
 // per SM).
 #ifndef FCLG_EPA_SMALL_V
 #define FCLG_EPA_SMALL_V 72
 #endif
 #ifndef FCLG_EPA_SMALL_MINB
-#define FCLG_EPA_SMALL_MINB 5
+#define FCLG_EPA_SMALL_MINB 2
 #endif
 #ifndef FCLG_EPA_SMALL_WARPS
-#define FCLG_EPA_SMALL_WARPS 5
+#define FCLG_EPA_SMALL_WARPS 13
 #endif
 constexpr int kSmallF = 128, kSmallV = FCLG_EPA_SMALL_V, kSmallWarps = FCLG_EPA_SMALL_WARPS,
               kSmallMinB = FCLG_EPA_SMALL_MINB;
