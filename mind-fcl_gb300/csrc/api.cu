@@ -76,7 +76,7 @@ struct fclg_context {
   int gjk_lanes = 1;
   int gjk_lanes_large = 4;
   int large_hull = 128;
-  int gjk_ctas_per_sm = 4;
+  int gjk_ctas_per_sm = fclg::gjk_default_ctas_per_sm();
   int epa_ctas_per_sm = fclg::epa_default_ctas_per_sm();
   uint64_t launches = 0;
   // optional per-pass timing

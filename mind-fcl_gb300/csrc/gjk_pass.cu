@@ -109,6 +109,8 @@ __global__ void __launch_bounds__(128, FCLG_REFILL_MINB) gjk_refill(BatchArgs b,
 }
 
 
+int gjk_default_ctas_per_sm() { return FCLG_GJK_MINB; }
+
 bool gjk_split_applies(const BatchArgs& b, const QueryParams& prm, int lanes, int blocks, bool refill) {
   // the one-lane plain distance pass on a persistent grid (the distance
   // launch sizes itself by a count on the device)

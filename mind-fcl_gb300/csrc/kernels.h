@@ -84,6 +84,8 @@ cudaError_t launch_bucketing(const BatchArgs& b, const BucketScratch& s, uint32_
 cudaError_t launch_gjk(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q, int lanes,
                        const uint32_t* order, const uint32_t* range, int blocks, cudaStream_t st,
                        bool refill = false, uint32_t* next = nullptr, const DistList* dl = nullptr);
+// CTAs per SM the persistent GJK passes are compiled for (the default launch).
+int gjk_default_ctas_per_sm();
 // Whether launch_gjk with these arguments and a DistList runs the split launches
 // (boolean, distance, and with a learned start the redo launch), and how many
 // kernels that launch_gjk call then launches.
