@@ -178,7 +178,7 @@ MLP_FLOP_PER_PAIR = 2.0 * (28 * 256 + 2 * 256 * 256 + 256 * 3)
 # DRAM bytes (read + write) of the two EPA launches of one mixed-workload query
 # at 10^6 pairs: one ncu capture at 400 k pairs (profiles/epa_pass_mixed_400k.md),
 # scaled by the pairs (the traffic is per overlapping pair)
-EPA_TRAFFIC_MIXED_1M = (144.232960 + 72.651776 + 59.215616 + 0.439808) * 1e6 * (1_000_000 / 400_000)
+EPA_TRAFFIC_MIXED_1M = (144.364544 + 82.854912 + 59.217664 + 0.432896) * 1e6 * (1_000_000 / 400_000)
 
 
 def _to_dev(torch, arr, dev):
