@@ -175,10 +175,12 @@ CONVEX_WORKLOADS = {
                           "(64 vertices), 100k joint configurations = 22.4M link-obstacle pairs; GJK distance + EPA"),
 }
 MLP_FLOP_PER_PAIR = 2.0 * (28 * 256 + 2 * 256 * 256 + 256 * 3)
-# DRAM bytes (read + write) of the two EPA launches of one mixed-workload query
-# at 10^6 pairs: one ncu capture at 400 k pairs (profiles/epa_pass_mixed_400k.md),
-# scaled by the pairs (the traffic is per overlapping pair)
-EPA_TRAFFIC_MIXED_1M = (144.364544 + 82.854912 + 59.217664 + 0.432896) * 1e6 * (1_000_000 / 400_000)
+# DRAM bytes (read + write) of the three EPA launches (128-face pass, 256-face
+# pass, final solves) of one mixed-workload query at 10^6 pairs: one ncu capture
+# at 400 k pairs (profiles/epa_pass_mixed_400k.md), scaled by the pairs (the
+# traffic is per overlapping pair)
+EPA_TRAFFIC_MIXED_1M = ((141.391104 + 94.594304) + (59.201024 + 0.594176) + (18.391296 + 0.365824)) * 1e6 \
+    * (1_000_000 / 400_000)
 
 
 def _to_dev(torch, arr, dev):
@@ -1135,8 +1137,8 @@ def main():
                          "frac": achieved / peak,
                          "traffic": (EPA_TRAFFIC_MIXED_1M if args.workload == "mixed" and n == 1_000_000
                                      and dominant == "epa_pass" else None),
-                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of both EPA "
-                                           "launches at 400 k pairs scaled by the pairs to 10^6, "
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the three "
+                                           "EPA launches at 400 k pairs scaled by the pairs to 10^6, "
                                            "profiles/epa_pass_mixed_400k.md",
                          "kernel": dominant + " (all launches of the pass)",
                          "peak_source": peak_kind,

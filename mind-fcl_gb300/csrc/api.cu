@@ -433,7 +433,7 @@ int run_query(fclg_context* c, const fclg_pair* d_pairs, uint32_t n, const fclg_
     fclg::EpaQueue ovf{c->epa_count + 1, c->epa_ovf, reinterpret_cast<float4*>(c->epa_resume),
                        c->epa_resume_on ? c->epa_resume_cap : 0u, c->epa_count + 3};
     FCLG_CUDA(c, fclg::launch_epa(b, prm, q, ovf, c->num_sms, c->epa_ctas_per_sm, st));
-    c->launches += prm.epa_max_faces > 128 ? 2 : 1;
+    c->launches += (uint64_t)fclg::epa_launches(prm);
     if (c->profiling) FCLG_CUDA(c, cudaEventRecord(c->ev[2], st));
   }
   if (c->profiling) {
@@ -1216,7 +1216,7 @@ int fclg_pass_times(fclg_context* c, double* gjk_ms, double* epa_ms, uint64_t* q
 //   [0, 256)                         counts[2]: EPA work list, overflow list
 //   [256, +4 * kStaticMax)           work list (pair indices)
 //   [.., +4 * kStaticMax)            overflow list (work-list items)
-//   [.., +kEpaRecordBytes * kStaticMax)  final GJK simplex per work-list item
+//   [.., +kEpaRecordBytes * kStaticMax)  final GJK simplex per work-list item (then its final-solve record)
 // counts must be zero before the GJK pass; each call zeroes them with
 // cudaMemsetAsync on its stream (the lists and records are written before
 // they are read and need no clearing).
@@ -1312,7 +1312,7 @@ extern "C" int fclg_distance_device_static(fclg_context* c, const fclg_pair* d_p
   if (prm.want_epa) {
     fclg::EpaQueue ovf{counts + 1, reinterpret_cast<uint32_t*>(base + kStaticOvfOffset), nullptr, 0u, counts + 3};
     FCLG_CUDA(c, fclg::launch_epa(b, prm, q, ovf, c->num_sms, c->epa_ctas_per_sm, st));
-    c->launches += prm.epa_max_faces > 128 ? 2 : 1;
+    c->launches += (uint64_t)fclg::epa_launches(prm);
     if (c->profiling) FCLG_CUDA(c, cudaEventRecord(c->ev[2], st));
   }
   if (c->profiling) {

@@ -28,7 +28,9 @@
 // slot: one shared-memory load per lane per 32 slots.  Face planes are FP32
 // unit normals and distances whose cross products are compensated (see
 // face_plane); the final closest-face solve (depth, barycentric witness
-// points) runs in FP64.
+// points) runs in FP64 (epa_final_solve), in the batched query a thread per
+// pair after the EPA launches (epa_pass.cu) rather than on one lane of the
+// warp that ran the pair.
 //
 // Initial polytope from the GJK simplex: epa_simplex2polytope.hpp:41-376
 // (touching detection, triangle blown up along +-normal, segment search over
@@ -150,7 +152,45 @@ struct EpaResult {
   f3 p0, p1;
   int iterations;
   int resume_nv;  // kEpaOverflow: vertices of the polytope state to continue from
+  // A warp that defers the final solve (EpaWarp<..., true>) leaves here the
+  // final face's vertex indices (packed as EpaSmem::fv; kNoSlot when the
+  // result needs no solve) and in p0 / p1 the fallback support pair; the
+  // caller runs epa_final_solve on that face's vertices.
+  uint32_t fin_fv;
 };
+
+// Final closest-face solve in FP64: the point of the face's triangle nearest
+// the origin (Ericson, Real-Time Collision Detection, 5.1.5) and its
+// barycentric weights, which interpolate the support points into the witness
+// pair (epa.hpp:425-498; when the origin projects into the triangle this is
+// the reference's face parameterisation, otherwise its edge / vertex feature).
+// Depth is that point's distance from the origin (the reference's
+// min_distance_square).  A degenerate triangle falls back to the last support
+// pair (cand_pa, cand_pb) like assignPenetrationPair (epa.hpp:340-365).
+// wa..wc are the face's Minkowski vertices, pa_a..pa_c their support points on
+// shape a.
+__device__ __forceinline__ void epa_final_solve(f3 wa, f3 wb, f3 wc, f3 pa_a, f3 pa_b, f3 pa_c, f3 cand_pa,
+                                                f3 cand_pb, EpaResult& r) {
+  const d3 a = tod(wa), b = tod(wb), c = tod(wc);
+  const d3 ab = b - a, ac = c - a;
+  const d3 n = cross(ab, ac);
+  if (!(dot(n, n) > 0.0)) {
+    r.p0 = cand_pa;
+    r.p1 = cand_pb;
+    r.depth = nrm(cand_pa - cand_pb);
+    return;
+  }
+  double u, v, w;
+  closest_bary_origin(a, b, c, u, v, w);
+  const d3 q = (a * u + b * v) + c * w;
+  const d3 pa0 = tod(pa_a), pa1 = tod(pa_b), pa2 = tod(pa_c);
+  const d3 pb0 = pa0 - a, pb1 = pa1 - b, pb2 = pa2 - c;
+  const d3 x0 = (pa0 * u + pa1 * v) + pa2 * w;
+  const d3 x1 = (pb0 * u + pb1 * v) + pb2 * w;
+  r.p0 = mk3((float)x0.x, (float)x0.y, (float)x0.z);
+  r.p1 = mk3((float)x1.x, (float)x1.y, (float)x1.z);
+  r.depth = (float)sqrt(dot(q, q));
+}
 
 // Byte offsets of a polytope state written by a layout of F faces / V
 // vertices when it runs out of slots (the state before the iteration that
@@ -185,7 +225,9 @@ __device__ __forceinline__ float point_to_plane(f3 p, f3 a, f3 b, f3 c) {
   return fabsf(dot(n * (1.f / nl), a - p));
 }
 
-template <int FMAX, int VMAX, class Sup = MinkowskiSupport<32>>
+// DEFER: the final closest-face solve is left to the caller (EpaResult::fin_fv)
+// instead of running on lane 0 inside the warp.
+template <int FMAX, int VMAX, class Sup = MinkowskiSupport<32>, bool DEFER = false>
 struct EpaWarp {
   EpaSmem<FMAX, VMAX>& P;
   const Sup& sup;
@@ -263,37 +305,19 @@ struct EpaWarp {
     return build_faces(tri, 4);
   }
 
-  // Final closest-face solve in FP64: the point of the face's triangle
-  // nearest the origin (Ericson, Real-Time Collision Detection, 5.1.5) and its
-  // barycentric weights, which interpolate the support points into the
-  // witness pair (epa.hpp:425-498; when the origin projects into the
-  // triangle this is the reference's face parameterisation, otherwise its
-  // edge / vertex feature).  Depth is that point's distance from the origin
-  // (the reference's min_distance_square).  A degenerate triangle falls back
-  // to the last support pair like assignPenetrationPair (epa.hpp:340-365).
-  // Lane 0 only (the lane that reports the result): the FP64 pipe is narrow.
+  // The final solve on the face with vertices fvp (epa_final_solve), on lane 0
+  // only (the lane that reports the result: the FP64 pipe is narrow), or,
+  // deferred, the face and the fallback pair recorded for the caller.
   __device__ void finalize(uint32_t fvp, f3 cand_pa, f3 cand_pb, EpaResult& r) const {
-    if (lane != 0) return;
-    const uint32_t ia = fvert(fvp, 0), ib = fvert(fvp, 1), ic = fvert(fvp, 2);
-    const d3 a = tod(W(ia)), b = tod(W(ib)), c = tod(W(ic));
-    const d3 ab = b - a, ac = c - a;
-    const d3 n = cross(ab, ac);
-    if (!(dot(n, n) > 0.0)) {
+    if constexpr (DEFER) {
+      r.fin_fv = fvp;
       r.p0 = cand_pa;
       r.p1 = cand_pb;
-      r.depth = nrm(cand_pa - cand_pb);
       return;
     }
-    double u, v, w;
-    closest_bary_origin(a, b, c, u, v, w);
-    const d3 q = (a * u + b * v) + c * w;
-    const d3 pa0 = tod(ld3(P.vpa[ia])), pa1 = tod(ld3(P.vpa[ib])), pa2 = tod(ld3(P.vpa[ic]));
-    const d3 pb0 = pa0 - a, pb1 = pa1 - b, pb2 = pa2 - c;
-    const d3 x0 = (pa0 * u + pa1 * v) + pa2 * w;
-    const d3 x1 = (pb0 * u + pb1 * v) + pb2 * w;
-    r.p0 = mk3((float)x0.x, (float)x0.y, (float)x0.z);
-    r.p1 = mk3((float)x1.x, (float)x1.y, (float)x1.z);
-    r.depth = (float)sqrt(dot(q, q));
+    if (lane != 0) return;
+    const uint32_t ia = fvert(fvp, 0), ib = fvert(fvp, 1), ic = fvert(fvp, 2);
+    epa_final_solve(W(ia), W(ib), W(ic), ld3(P.vpa[ia]), ld3(P.vpa[ib]), ld3(P.vpa[ic]), cand_pa, cand_pb, r);
   }
 
   __device__ void touching(f3 pa, f3 pb, EpaResult& r) const {
@@ -645,6 +669,7 @@ struct EpaWarp {
     r.p0 = r.p1 = mk3(0, 0, 0);
     r.iterations = it0;
     r.resume_nv = 0;
+    r.fin_fv = kNoSlot;
     iterate(it0, max_iter, max_faces, overflow_is_final, r);
     return r;
   }
@@ -660,6 +685,7 @@ struct EpaWarp {
     r.p0 = r.p1 = mk3(0, 0, 0);
     r.iterations = 0;
     r.resume_nv = 0;
+    r.fin_fv = kNoSlot;
     nv = 0;
     hw = 0;
     live = 0;

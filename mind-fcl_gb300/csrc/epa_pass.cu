@@ -1,5 +1,9 @@
 // EPA pass of a convex query batch: persistent grid, one warp per overlapping
-// pair listed by the GJK pass (gjk_pass.cu), polytope in shared memory.
+// pair listed by the GJK pass (gjk_pass.cu), polytope in shared memory.  The
+// warps leave the final FP64 closest-face solve of each pair to a third
+// launch that runs it a thread per pair (epa_finalize): on one lane of the
+// warp it held the warp for hundreds of FP64 instructions, each of which
+// occupies the narrow FP64 pipe as long as a full warp's would.
 #include "epa.cuh"
 #include "kernels.h"
 
@@ -28,6 +32,15 @@ constexpr int kSmallF = 128, kSmallV = FCLG_EPA_SMALL_V, kSmallWarps = FCLG_EPA_
 #endif
 constexpr int kLargeF = 256, kLargeV = 192, kLargeWarps = 4, kLargeMinB = FCLG_EPA_LARGE_MINB;
 static_assert(EpaResume<kSmallF, kSmallV>::kBytes <= kEpaResumeBytes, "resume record size");
+
+// Final-solve record of a work-list entry, written over the entry's GJK
+// simplex record (q.rec, 7 float4) once the entry is done:
+//   {wa, pid} {wb, status} {wc, iterations} {pa_a, fb.x} {pa_b, fb.y}
+//   {pa_c, fb.z} {fa, pending}
+// w* the final face's Minkowski vertices, pa_* their support points on shape
+// a, (fa, fb) the fallback support pair; pending 1: epa_finalize solves and
+// stores the result, 0: the pass stored it.
+constexpr int kFinPending = 6;
 
 // EPA over the work list.  The small layout runs every listed pair and hands
 // the pairs whose polytope outgrows it to `ovf` (indices into the work list),
@@ -86,7 +99,7 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) epa_pass(BatchArgs b, QueryP
     }
     __syncwarp();
     const SharedSupport32 sup{&P.pair};
-    EpaWarp<FMAX, VMAX, SharedSupport32> E{P, sup, prm.epa_tol, lane, 0, 0, 0, 0, 0u};
+    EpaWarp<FMAX, VMAX, SharedSupport32, true> E{P, sup, prm.epa_tol, lane, 0, 0, 0, 0, 0u};
     EpaResult er;
     if (large && k < ovf.resume_cap && FMAX >= kSmallF && VMAX >= kSmallV) {
       er = E.template resume<kSmallF, kSmallV>(reinterpret_cast<const unsigned char*>(ovf.rec) +
@@ -108,9 +121,21 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) epa_pass(BatchArgs b, QueryP
                                             er);
       }
     } else if (lane == 0) {
-      {
-        const int32_t status = kGjkIntersect | ((er.status + 1) << 8);
-        const uint32_t iters = (uint32_t)(gjk_iters + er.iterations);
+      const int32_t status = kGjkIntersect | ((er.status + 1) << 8);
+      const uint32_t iters = (uint32_t)(gjk_iters + er.iterations);
+      float4* fin = q.rec + 7 * (size_t)item;
+      if (er.status != kEpaFailed && er.fin_fv != kNoSlot) {
+        const uint32_t ia = fvert(er.fin_fv, 0), ib = fvert(er.fin_fv, 1), ic = fvert(er.fin_fv, 2);
+        const float4 wa = P.vw[ia], wb = P.vw[ib], wc = P.vw[ic];
+        const float4 qa = P.vpa[ia], qb = P.vpa[ib], qc = P.vpa[ic];
+        fin[0] = make_float4(wa.x, wa.y, wa.z, __uint_as_float(pid));
+        fin[1] = make_float4(wb.x, wb.y, wb.z, __int_as_float(status));
+        fin[2] = make_float4(wc.x, wc.y, wc.z, __uint_as_float(iters));
+        fin[3] = make_float4(qa.x, qa.y, qa.z, er.p1.x);
+        fin[4] = make_float4(qb.x, qb.y, qb.z, er.p1.y);
+        fin[5] = make_float4(qc.x, qc.y, qc.z, er.p1.z);
+        fin[kFinPending] = make_float4(er.p0.x, er.p0.y, er.p0.z, __int_as_float(1));
+      } else {
         if (er.status != kEpaFailed) {
           f3 nv = er.p0 - er.p1;
           nv = (sqn(nv) > 0.f) ? normalized(nv) : mk3(0, 0, 1);
@@ -118,9 +143,28 @@ __global__ void __launch_bounds__(WARPS * 32, MINB) epa_pass(BatchArgs b, QueryP
         } else {
           store_result(b.results, pid, -1.f, mk3(0, 0, 1), mk3(0, 0, 0), mk3(0, 0, 0), status, iters, true, false);
         }
+        fin[kFinPending] = make_float4(0.f, 0.f, 0.f, __int_as_float(0));
       }
     }
     __syncwarp();
+  }
+}
+
+// The final solves the EPA launches left, a thread per work-list entry
+// (epa_final_solve, then the result record as the pass writes it).
+__global__ void __launch_bounds__(256) epa_finalize(BatchArgs b, EpaQueue q) {
+  const uint32_t n = *q.count;
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const float4* fin = q.rec + 7 * (size_t)k;
+    const float4 f6 = fin[kFinPending];
+    if (__float_as_int(f6.w) != 1) continue;
+    const float4 f0 = fin[0], f1 = fin[1], f2 = fin[2], f3r = fin[3], f4 = fin[4], f5 = fin[5];
+    EpaResult er;
+    epa_final_solve(ld3(f0), ld3(f1), ld3(f2), ld3(f3r), ld3(f4), ld3(f5), ld3(f6), mk3(f3r.w, f4.w, f5.w), er);
+    f3 nv = er.p0 - er.p1;
+    nv = (sqn(nv) > 0.f) ? normalized(nv) : mk3(0, 0, 1);
+    store_result(b.results, __float_as_uint(f0.w), -er.depth, nv, er.p0, er.p1, __float_as_int(f1.w),
+                 __float_as_uint(f2.w), true, true);
   }
 }
 
@@ -142,11 +186,17 @@ cudaError_t launch_epa(const BatchArgs& b, const QueryParams& prm, const EpaQueu
   epa_pass<kSmallF, kSmallV, kSmallWarps, kSmallMinB>
       <<<small_blocks, kSmallWarps * 32, epa_smem_bytes(), st>>>(b, prm, q, ovf, 0);
   cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess || prm.epa_max_faces <= kSmallF) return e;
-  epa_pass<kLargeF, kLargeV, kLargeWarps, kLargeMinB>
-      <<<num_sms * kLargeMinB, kLargeWarps * 32, epa_smem_bytes_large(), st>>>(b, prm, q, ovf, 1);
+  if (e == cudaSuccess && prm.epa_max_faces > kSmallF) {
+    epa_pass<kLargeF, kLargeV, kLargeWarps, kLargeMinB>
+        <<<num_sms * kLargeMinB, kLargeWarps * 32, epa_smem_bytes_large(), st>>>(b, prm, q, ovf, 1);
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess) return e;
+  epa_finalize<<<num_sms * 4, 256, 0, st>>>(b, q);
   return cudaGetLastError();
 }
+
+int epa_launches(const QueryParams& prm) { return prm.epa_max_faces > kSmallF ? 3 : 2; }
 
 int epa_max_faces_supported() { return kLargeF; }
 

@@ -25,8 +25,9 @@ struct BatchArgs {
 struct EpaQueue {
   uint32_t* count;        // [1]
   uint32_t* list;         // [capacity] pair indices
-  float4* rec;            // [capacity][7] final GJK simplex (rank, support points); for the overflow
-                          // list: [resume_cap] polytope states (kEpaResumeBytes each) or null
+  float4* rec;            // [capacity][7] final GJK simplex (rank, support points), which the EPA pass
+                          // replaces by the entry's final-solve record; for the overflow list:
+                          // [resume_cap] polytope states (kEpaResumeBytes each) or null
   uint32_t resume_cap = 0;  // overflow list: states the pool holds (the rest restart from the simplex)
   uint32_t* next = nullptr;  // zero before the EPA pass over this list: the count of entries its warps have
                              // taken (each warp takes its next entry there as it finishes one); null: each
@@ -98,10 +99,13 @@ cudaError_t launch_directed(const BatchArgs& b, const QueryParams& prm, int bloc
 cudaError_t launch_gjk64(const BatchArgs& b, double tol, int max_iter, double* out, int blocks, cudaStream_t st);
 cudaError_t prepare_epa();
 // EPA over q's list: the small-polytope pass, then (when max_faces exceeds it)
-// the large pass over the pairs ovf collected.  ovf.count must be zero and
-// ovf.list hold q's capacity; ovf.rec is unused.
+// the large pass over the pairs ovf collected, then the final FP64 solves a
+// thread per pair.  ovf.count must be zero and ovf.list hold q's capacity.
+// q.rec's records are consumed (overwritten by the final-solve records).
 cudaError_t launch_epa(const BatchArgs& b, const QueryParams& prm, const EpaQueue& q, const EpaQueue& ovf,
                        int num_sms, int ctas_per_sm, cudaStream_t st);
+// Kernel launches launch_epa makes.
+int epa_launches(const QueryParams& prm);
 size_t epa_smem_bytes();
 size_t epa_smem_bytes_large();
 int epa_max_faces_supported();
