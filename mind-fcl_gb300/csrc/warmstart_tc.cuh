@@ -8,11 +8,14 @@
 //              by tcgen05.mma kind::f16 issued by one thread, operands read
 //              from shared memory through matrix descriptors
 //   epilogue:  tcgen05.ld of 64 columns of the thread's row (four warps per
-//              TMEM lane quarter), + bias, GELU, BF16 -> act
+//              TMEM lane quarter), + bias (staged in shared memory once),
+//              GELU, BF16 -> act
 // Weights stream from global memory (already in the MMA's K-major
 // core-matrix layout, see tc_slot) into two 64 KB buffers with cp.async.bulk
 // on mbarrier transaction counts: W1 | W2 (two N halves) | W3 (two halves) |
-// W4, the next chunk loading while the current one multiplies.
+// W4.  A chunk loads as soon as its buffer is free -- right after the MMAs
+// that read the buffer complete -- so the loads run under the epilogues and
+// under the other buffer's MMAs.
 //
 // Shared-memory operand layout (K-major, no swizzle): 8 x 16-byte core
 // matrices (8 rows x 8 BF16 along K, 128 contiguous bytes); along K the core
@@ -32,7 +35,8 @@ constexpr uint32_t kTcCols = 256;                      // TMEM columns: one 128 
 constexpr uint32_t kActBytes = 128u * kH * 2u;         // 64 KB
 constexpr uint32_t kBufBytes = 65536u;
 constexpr uint32_t kGroupStride = 4096u;               // 32 core matrices of 128 bytes along K
-constexpr size_t kTcSmem = (size_t)kActBytes + 2 * kBufBytes + 128;
+constexpr size_t kTcBiasOffset = (size_t)kActBytes + 2 * kBufBytes + 128;  // b1 | b2 | b3, FP32
+constexpr size_t kTcSmem = kTcBiasOffset + 3 * (size_t)kH * 4;
 constexpr long long kWaitCycles = 1ll << 31;           // about one second per wait
 
 // tc-layout weight copy (BF16 elements): W1 [256][32] | W2 [256][256] | W3 | W4 padded to 16 rows
@@ -137,23 +141,33 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
 }
 
 // Columns [cbeg, cbeg + 64) of row r of a 128 x 256 FP32 accumulator (TMEM
-// row address trow) -> + bias, GELU, BF16 -> act in the operand layout.
-__device__ __forceinline__ void tc_epilogue_hidden(uint32_t trow, const float* __restrict__ bias, unsigned char* act,
-                                                   int r, int cbeg) {
+// row address trow) -> + bias (shared memory), GELU, BF16 -> act in the
+// operand layout.
+__device__ __forceinline__ void tc_epilogue_hidden(uint32_t trow, const float* bias, unsigned char* act, int r,
+                                                   int cbeg) {
   unsigned char* row = act + (size_t)(r >> 3) * kGroupStride + (size_t)(r & 7) * 16;
 #pragma unroll 1
   for (int c0 = cbeg; c0 < cbeg + 64; c0 += 32) {
     uint32_t v0[16], v1[16];
     tmem_ld16(trow + (uint32_t)c0, v0);
     tmem_ld16(trow + (uint32_t)c0 + 16u, v1);
+    float bv[32];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const float4 t = reinterpret_cast<const float4*>(bias + c0)[q];
+      bv[4 * q] = t.x;
+      bv[4 * q + 1] = t.y;
+      bv[4 * q + 2] = t.z;
+      bv[4 * q + 3] = t.w;
+    }
     tmem_wait_ld();
     uint32_t p[16];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
-      p[j] = pack_bf16(gelu_fast(__uint_as_float(v0[2 * j]) + __ldg(bias + c0 + 2 * j)),
-                       gelu_fast(__uint_as_float(v0[2 * j + 1]) + __ldg(bias + c0 + 2 * j + 1)));
-      p[8 + j] = pack_bf16(gelu_fast(__uint_as_float(v1[2 * j]) + __ldg(bias + c0 + 16 + 2 * j)),
-                           gelu_fast(__uint_as_float(v1[2 * j + 1]) + __ldg(bias + c0 + 16 + 2 * j + 1)));
+      p[j] = pack_bf16(gelu_fast(__uint_as_float(v0[2 * j]) + bv[2 * j]),
+                       gelu_fast(__uint_as_float(v0[2 * j + 1]) + bv[2 * j + 1]));
+      p[8 + j] = pack_bf16(gelu_fast(__uint_as_float(v1[2 * j]) + bv[16 + 2 * j]),
+                           gelu_fast(__uint_as_float(v1[2 * j + 1]) + bv[16 + 2 * j + 1]));
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q)
@@ -173,6 +187,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   uint64_t* bars = reinterpret_cast<uint64_t*>(buf1 + kBufBytes);  // full0, full1, mma, half, drain
   uint32_t* s_taddr = reinterpret_cast<uint32_t*>(bars + 5);
   volatile int* s_abort = reinterpret_cast<volatile int*>(bars + 6);
+  float* s_bias = reinterpret_cast<float*>(tc_smem + kTcBiasOffset);
   const int tid = threadIdx.x, warp = tid >> 5;
   const bool leader = tid == 0;
   const int row = (warp & 3) * 32 + (tid & 31);  // TMEM lane (tile row) this thread reads
@@ -185,6 +200,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     for (int i = 0; i < 5; ++i) mbar_init(smem_u32(&bars[i]), 1);
     *s_abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  for (int i = tid; i < 3 * kH; i += kTcThreads) {
+    const size_t base = i < kH ? oB1 : (i < 2 * kH ? oB2 : oB3);
+    s_bias[i] = params[base + (size_t)(i % kH)];
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(s_taddr)),
@@ -238,8 +257,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   };
 
   const uint32_t n_tiles = (n + 127) / 128;
-  if (leader && blockIdx.x < n_tiles) load(0, srcW1, (uint32_t)(kH * kIn * 2));
+  if (leader && blockIdx.x < n_tiles) {
+    load(0, srcW1, (uint32_t)(kH * kIn * 2));
+    load(1, srcW2, kBufBytes);
+  }
   for (uint32_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    const bool more = tile + gridDim.x < n_tiles;
     // features: four threads per row, one 8-column chunk each
     {
       const int fr = tid >> 2, chunk = tid & 3;
@@ -271,24 +294,21 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     end_stage();
     if (*s_abort) break;
 
-    // layer 1: K = 32, N = 256 (W1 in buffer 0); W2's first half loads into buffer 1
-    if (leader) {
-      load(1, srcW2, kBufBytes);
-      if (wait_full(0)) {
-        tc_fence_after();
-        mma_layer(0, 0, kIn / 16, 512u, id256);
-        umma_commit(bar_mma);
-      }
+    // layer 1: K = 32, N = 256 (W1 in buffer 0; W2's first half is in or on its way to buffer 1)
+    if (leader && wait_full(0)) {
+      tc_fence_after();
+      mma_layer(0, 0, kIn / 16, 512u, id256);
+      umma_commit(bar_mma);
     }
-    if (all_wait_mma()) tc_epilogue_hidden(trow, params + oB1, act, row, cbeg);
+    const bool ok1 = all_wait_mma();
+    if (leader && ok1) load(0, srcW2 + kBufBytes, kBufBytes);  // buffer 0 is free: W2's second half
+    if (ok1) tc_epilogue_hidden(trow, s_bias, act, row, cbeg);
     end_stage();
     if (*s_abort) break;
 
     // layers 2 and 3: two N halves each, weights double-buffered
     for (int layer = 2; layer <= 3; ++layer) {
-      const char* srcW = layer == 2 ? srcW2 : srcW3;
       if (leader) {
-        load(0, srcW + kBufBytes, kBufBytes);  // second half into buffer 0 (free: its MMAs completed)
         if (wait_full(1)) {
           mma_layer(0, 1, kH / 16, kGroupStride, id128);
           umma_commit(bar_half);
@@ -304,21 +324,26 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           else load(1, srcW4, (uint32_t)(16 * kH * 2));
         }
       }
-      if (all_wait_mma()) tc_epilogue_hidden(trow, params + (layer == 2 ? oB2 : oB3), act, row, cbeg);
+      const bool okl = all_wait_mma();
+      // buffer 0 is free (the layer's MMAs completed): W3's second half, or the next tile's W1
+      if (leader && okl) {
+        if (layer == 2) load(0, srcW3 + kBufBytes, kBufBytes);
+        else if (more) load(0, srcW1, (uint32_t)(kH * kIn * 2));
+      }
+      if (okl) tc_epilogue_hidden(trow, s_bias + (layer - 1) * kH, act, row, cbeg);
       end_stage();
       if (*s_abort) break;
     }
     if (*s_abort) break;
 
-    // layer 4: N = 16 (rows 3..15 of W4 are zero); the next tile's W1 loads into buffer 0
-    if (leader) {
-      if (tile + gridDim.x < n_tiles) load(0, srcW1, (uint32_t)(kH * kIn * 2));
-      if (wait_full(1)) {
-        mma_layer(0, 1, kH / 16, kGroupStride, id16);
-        umma_commit(bar_mma);
-      }
+    // layer 4: N = 16 (rows 3..15 of W4 are zero)
+    if (leader && wait_full(1)) {
+      mma_layer(0, 1, kH / 16, kGroupStride, id16);
+      umma_commit(bar_mma);
     }
-    if (all_wait_mma() && warp < 4) {
+    const bool ok4 = all_wait_mma();
+    if (leader && ok4 && more) load(1, srcW2, kBufBytes);  // buffer 1 is free: the next tile's W2 first half
+    if (ok4 && warp < 4) {
       uint32_t v[16];
       tmem_ld16(trow, v);
       tmem_wait_ld();

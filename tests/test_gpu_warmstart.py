@@ -76,6 +76,16 @@ def test_forward_matches_oracle(torch):
     ws.predict(d_pairs.data_ptr(), m, d_y.data_ptr(), normalize=False)
     ws.status()
     assert np.array_equal(d_y.cpu().numpy().reshape(m, 3), outs["tcgen05"][:m])
+    # a batch of 70 copies (980 tiles of 128 pairs: every CTA runs several,
+    # with the next tile's weights loading under the current one's
+    # epilogues) gives every copy the same outputs, bit for bit
+    big = np.tile(b.pairs, 70)
+    d_big = _dev(torch, big)
+    d_y = torch.zeros(len(big) * 3, dtype=torch.float32, device="cuda")
+    ws.predict(d_big.data_ptr(), len(big), d_y.data_ptr(), normalize=False)
+    ws.status()
+    yb = d_y.cpu().numpy().reshape(70, n, 3)
+    assert all(np.array_equal(yb[i], outs["tcgen05"]) for i in range(70))
     # normalised output is the unit direction of the raw one
     d_u = torch.zeros(n * 3, dtype=torch.float32, device="cuda")
     ws.predict(d_pairs.data_ptr(), n, d_u.data_ptr(), normalize=True)
