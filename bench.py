@@ -40,7 +40,7 @@ sys.path.insert(0, os.path.join(ROOT, "mind-fcl_gb300"))
 
 import numpy as np  # noqa: E402
 
-BASELINE_METRIC = "convex pair queries/s (GJK+EPA) & BVH collides/s, warm-start vs plain, 1 GB300"
+METRIC = "convex pair queries/s (GJK+EPA) & BVH collides/s, warm-start vs plain, 1 GB300"
 UNIT = "pair queries/s"
 N_PAIRS = 1_000_000
 # compulsory bytes per query of this workload: hull vertices (12 B each) of the
@@ -423,7 +423,7 @@ def run_reference(args):
         total += secs
     value = batch.n_pairs * args.steps / total
     line = {
-        "impl": "reference", "metric": BASELINE_METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": WORKLOAD, "pairs_per_gpu": batch.n_pairs, "seed": batch.meta["seed"]},
@@ -566,7 +566,7 @@ def run_mesh(args):
     with ClockSampler(local) as clk:
         m = mesh_block(args, torch, dev, stream, local)
     fc = m["first_contact"]
-    line = {"metric": BASELINE_METRIC, "value": fc["value"], "unit": "BVH collides/s", "n_gpus": 1,
+    line = {"metric": METRIC, "value": fc["value"], "unit": "BVH collides/s", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": fc["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 (FP64 triangle fallback)", "data": "synthetic",
@@ -1122,7 +1122,7 @@ def main():
         threads = os.cpu_count() or 1
         cpu_v, cpu_n, cpu_s = cpu_baseline(batch, threads)
         line = {
-            "metric": BASELINE_METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (FP64 EPA closest-face solve and GJK tetrahedron tests)",
             "data": "synthetic",
