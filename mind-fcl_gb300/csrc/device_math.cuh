@@ -3,23 +3,27 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+// The vector helpers below and the FP64 final solve (epa_final_solve) also
+// build for the host, where the CPU tests run them.
+#define FCLG_HD __host__ __device__ __forceinline__
+
 namespace fclg {
 
 struct f3 {
   float x, y, z;
 };
-__device__ __forceinline__ f3 mk3(float x, float y, float z) { return f3{x, y, z}; }
-__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
-__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
-__device__ __forceinline__ f3 operator-(f3 a) { return mk3(-a.x, -a.y, -a.z); }
-__device__ __forceinline__ f3 operator*(f3 a, float s) { return mk3(a.x * s, a.y * s, a.z * s); }
-__device__ __forceinline__ f3 operator*(float s, f3 a) { return mk3(a.x * s, a.y * s, a.z * s); }
-__device__ __forceinline__ float dot(f3 a, f3 b) { return fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)); }
-__device__ __forceinline__ f3 cross(f3 a, f3 b) {
+FCLG_HD f3 mk3(float x, float y, float z) { return f3{x, y, z}; }
+FCLG_HD f3 operator+(f3 a, f3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
+FCLG_HD f3 operator-(f3 a, f3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
+FCLG_HD f3 operator-(f3 a) { return mk3(-a.x, -a.y, -a.z); }
+FCLG_HD f3 operator*(f3 a, float s) { return mk3(a.x * s, a.y * s, a.z * s); }
+FCLG_HD f3 operator*(float s, f3 a) { return mk3(a.x * s, a.y * s, a.z * s); }
+FCLG_HD float dot(f3 a, f3 b) { return fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)); }
+FCLG_HD f3 cross(f3 a, f3 b) {
   return mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
-__device__ __forceinline__ float sqn(f3 a) { return dot(a, a); }
-__device__ __forceinline__ float nrm(f3 a) { return sqrtf(sqn(a)); }
+FCLG_HD float sqn(f3 a) { return dot(a, a); }
+FCLG_HD float nrm(f3 a) { return sqrtf(sqn(a)); }
 // Leaves a zero vector unchanged (the reference's Eigen normalize()).
 __device__ __forceinline__ f3 normalized(f3 a) {
   const float n2 = sqn(a);
@@ -29,18 +33,18 @@ __device__ __forceinline__ f3 normalized(f3 a) {
 struct d3 {
   double x, y, z;
 };
-__device__ __forceinline__ d3 tod(f3 a) { return d3{(double)a.x, (double)a.y, (double)a.z}; }
-__device__ __forceinline__ d3 operator-(d3 a, d3 b) { return d3{a.x - b.x, a.y - b.y, a.z - b.z}; }
-__device__ __forceinline__ d3 operator+(d3 a, d3 b) { return d3{a.x + b.x, a.y + b.y, a.z + b.z}; }
-__device__ __forceinline__ d3 operator*(d3 a, double s) { return d3{a.x * s, a.y * s, a.z * s}; }
-__device__ __forceinline__ double dot(d3 a, d3 b) { return fma(a.z, b.z, fma(a.y, b.y, a.x * b.x)); }
-__device__ __forceinline__ d3 cross(d3 a, d3 b) {
+FCLG_HD d3 tod(f3 a) { return d3{(double)a.x, (double)a.y, (double)a.z}; }
+FCLG_HD d3 operator-(d3 a, d3 b) { return d3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+FCLG_HD d3 operator+(d3 a, d3 b) { return d3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+FCLG_HD d3 operator*(d3 a, double s) { return d3{a.x * s, a.y * s, a.z * s}; }
+FCLG_HD double dot(d3 a, d3 b) { return fma(a.z, b.z, fma(a.y, b.y, a.x * b.x)); }
+FCLG_HD d3 cross(d3 a, d3 b) {
   return d3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
 
 // Barycentric weights (u, v, w) of the point of triangle (a, b, c) nearest the
 // origin (Ericson, Real-Time Collision Detection, 5.1.5), in FP64.
-__device__ __forceinline__ void closest_bary_origin(d3 a, d3 b, d3 c, double& u, double& v, double& w) {
+FCLG_HD void closest_bary_origin(d3 a, d3 b, d3 c, double& u, double& v, double& w) {
   const d3 ab = b - a, ac = c - a;
   const d3 ap = a * -1.0, bp = b * -1.0, cp = c * -1.0;
   const double d1 = dot(ab, ap), d2 = dot(ac, ap);
@@ -62,6 +66,39 @@ __device__ __forceinline__ void closest_bary_origin(d3 a, d3 b, d3 c, double& u,
     w = vc * inv;
     u = 1.0 - v - w;
   }
+}
+
+// EPA's final closest-face solve in FP64: the point of the final face's
+// triangle nearest the origin (closest_bary_origin) and its barycentric
+// weights, which interpolate the support points into the witness pair
+// (epa.hpp:425-498; when the origin projects into the triangle this is the
+// reference's face parameterisation, otherwise its edge / vertex feature).
+// Depth is that point's distance from the origin (the reference's
+// min_distance_square).  A degenerate triangle falls back to the last support
+// pair (cand_pa, cand_pb) like assignPenetrationPair (epa.hpp:340-365).
+// wa..wc are the face's Minkowski vertices, pa_a..pa_c their support points on
+// shape a.
+FCLG_HD void epa_final_solve(f3 wa, f3 wb, f3 wc, f3 pa_a, f3 pa_b, f3 pa_c, f3 cand_pa, f3 cand_pb, f3& p0,
+                             f3& p1, float& depth) {
+  const d3 a = tod(wa), b = tod(wb), c = tod(wc);
+  const d3 ab = b - a, ac = c - a;
+  const d3 n = cross(ab, ac);
+  if (!(dot(n, n) > 0.0)) {
+    p0 = cand_pa;
+    p1 = cand_pb;
+    depth = nrm(cand_pa - cand_pb);
+    return;
+  }
+  double u, v, w;
+  closest_bary_origin(a, b, c, u, v, w);
+  const d3 q = (a * u + b * v) + c * w;
+  const d3 pa0 = tod(pa_a), pa1 = tod(pa_b), pa2 = tod(pa_c);
+  const d3 pb0 = pa0 - a, pb1 = pa1 - b, pb2 = pa2 - c;
+  const d3 x0 = (pa0 * u + pa1 * v) + pa2 * w;
+  const d3 x1 = (pb0 * u + pb1 * v) + pb2 * w;
+  p0 = mk3((float)x0.x, (float)x0.y, (float)x0.z);
+  p1 = mk3((float)x1.x, (float)x1.y, (float)x1.z);
+  depth = (float)sqrt(dot(q, q));
 }
 
 // Shape types: the reference's GJKShapeType values (gjk_shape.h:9-28).

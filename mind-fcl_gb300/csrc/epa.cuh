@@ -159,39 +159,6 @@ struct EpaResult {
   uint32_t fin_fv;
 };
 
-// Final closest-face solve in FP64: the point of the face's triangle nearest
-// the origin (Ericson, Real-Time Collision Detection, 5.1.5) and its
-// barycentric weights, which interpolate the support points into the witness
-// pair (epa.hpp:425-498; when the origin projects into the triangle this is
-// the reference's face parameterisation, otherwise its edge / vertex feature).
-// Depth is that point's distance from the origin (the reference's
-// min_distance_square).  A degenerate triangle falls back to the last support
-// pair (cand_pa, cand_pb) like assignPenetrationPair (epa.hpp:340-365).
-// wa..wc are the face's Minkowski vertices, pa_a..pa_c their support points on
-// shape a.
-__device__ __forceinline__ void epa_final_solve(f3 wa, f3 wb, f3 wc, f3 pa_a, f3 pa_b, f3 pa_c, f3 cand_pa,
-                                                f3 cand_pb, EpaResult& r) {
-  const d3 a = tod(wa), b = tod(wb), c = tod(wc);
-  const d3 ab = b - a, ac = c - a;
-  const d3 n = cross(ab, ac);
-  if (!(dot(n, n) > 0.0)) {
-    r.p0 = cand_pa;
-    r.p1 = cand_pb;
-    r.depth = nrm(cand_pa - cand_pb);
-    return;
-  }
-  double u, v, w;
-  closest_bary_origin(a, b, c, u, v, w);
-  const d3 q = (a * u + b * v) + c * w;
-  const d3 pa0 = tod(pa_a), pa1 = tod(pa_b), pa2 = tod(pa_c);
-  const d3 pb0 = pa0 - a, pb1 = pa1 - b, pb2 = pa2 - c;
-  const d3 x0 = (pa0 * u + pa1 * v) + pa2 * w;
-  const d3 x1 = (pb0 * u + pb1 * v) + pb2 * w;
-  r.p0 = mk3((float)x0.x, (float)x0.y, (float)x0.z);
-  r.p1 = mk3((float)x1.x, (float)x1.y, (float)x1.z);
-  r.depth = (float)sqrt(dot(q, q));
-}
-
 // Byte offsets of a polytope state written by a layout of F faces / V
 // vertices when it runs out of slots (the state before the iteration that
 // did not fit), read back by a larger layout, which continues from it: a
@@ -317,7 +284,8 @@ struct EpaWarp {
     }
     if (lane != 0) return;
     const uint32_t ia = fvert(fvp, 0), ib = fvert(fvp, 1), ic = fvert(fvp, 2);
-    epa_final_solve(W(ia), W(ib), W(ic), ld3(P.vpa[ia]), ld3(P.vpa[ib]), ld3(P.vpa[ic]), cand_pa, cand_pb, r);
+    epa_final_solve(W(ia), W(ib), W(ic), ld3(P.vpa[ia]), ld3(P.vpa[ib]), ld3(P.vpa[ic]), cand_pa, cand_pb, r.p0,
+                    r.p1, r.depth);
   }
 
   __device__ void touching(f3 pa, f3 pb, EpaResult& r) const {

@@ -160,7 +160,8 @@ __global__ void __launch_bounds__(256) epa_finalize(BatchArgs b, EpaQueue q) {
     if (__float_as_int(f6.w) != 1) continue;
     const float4 f0 = fin[0], f1 = fin[1], f2 = fin[2], f3r = fin[3], f4 = fin[4], f5 = fin[5];
     EpaResult er;
-    epa_final_solve(ld3(f0), ld3(f1), ld3(f2), ld3(f3r), ld3(f4), ld3(f5), ld3(f6), mk3(f3r.w, f4.w, f5.w), er);
+    epa_final_solve(ld3(f0), ld3(f1), ld3(f2), ld3(f3r), ld3(f4), ld3(f5), ld3(f6), mk3(f3r.w, f4.w, f5.w), er.p0,
+                    er.p1, er.depth);
     f3 nv = er.p0 - er.p1;
     nv = (sqn(nv) > 0.f) ? normalized(nv) : mk3(0, 0, 1);
     store_result(b.results, __float_as_uint(f0.w), -er.depth, nv, er.p0, er.p1, __float_as_int(f1.w),
